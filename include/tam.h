@@ -1,0 +1,252 @@
+/*
+ * tam.h -- C ABI of the GB300-native hot paths of Tissue-Ablation-MC.
+ *
+ * The reference (lewisfish/Tissue-Ablation-MC, Fortran + MPI) has no plugin or
+ * FFI: its "API" is the set of Fortran subroutines called from the driver
+ * loop in src/mcpolar.f90:148-186, communicating through module globals.  A
+ * per-photon FFI call is not viable, so this ABI replaces whole blocks of that
+ * loop:
+ *   - the photon loop + MPI_Allreduce + normalisation (src/mcpolar.f90:151-174)
+ *     -> tam_mc_pass
+ *   - heat_sim_3D (src/mcpolar.f90:178)            -> tam_heat_steps
+ *   - Arrhenius (src/mcpolar.f90:180)              -> tam_arrhenius
+ *   - setupThermalCoeff (src/mcpolar.f90:182)      -> tam_update_props
+ *   - one whole outer iteration / the whole loop   -> tam_step_coupled / tam_run
+ *
+ * Conventions
+ *   - Plain C types only; every call returns an int status (TAM_OK == 0);
+ *     tam_last_error() gives a one-line message.  Nothing aborts the process:
+ *     the reference's `error stop` / `mpi_abort` sites become status codes.
+ *   - Arrays exchanged with the host use the reference layout: FP64,
+ *     Fortran column-major (x fastest), with the reference's halo where the
+ *     reference allocates one (start index 0, src/subs.f90:62-73,
+ *     src/3dFD.f90:254-260).
+ *   - A context owns its device state, which stays resident across calls.
+ *     A context is not thread-safe; use one per host thread.  All work of a
+ *     context is issued on one CUDA stream (its own, or one set with
+ *     tam_set_stream) and each hot call returns after that work completes.
+ *   - No CPU fallback: tam_create fails with TAM_E_NODEV without a GPU.
+ */
+#ifndef TAM_H
+#define TAM_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TAM_ABI_VERSION 1
+
+/* ---- status codes ---- */
+enum tam_status {
+    TAM_OK = 0,
+    TAM_E_INVALID = 1,   /* bad argument or parameter value */
+    TAM_E_CUDA = 2,      /* CUDA runtime error */
+    TAM_E_NOMEM = 3,     /* device allocation failed */
+    TAM_E_IO = 4,        /* file could not be opened / written */
+    TAM_E_PARSE = 5,     /* input.params could not be parsed */
+    TAM_E_STATE = 6,     /* call not valid in this mode / state */
+    TAM_E_DEVICE = 7,    /* a kernel raised its error word (see tam_device_errors) */
+    TAM_E_NODEV = 8      /* no CUDA device */
+};
+
+enum tam_mode { TAM_MODE_REFERENCE = 0, TAM_MODE_CONFIG = 1 };
+enum tam_precision { TAM_FP64 = 0, TAM_FP32 = 1 };
+enum tam_pulse { TAM_PULSE_GAUSSIAN = 0, TAM_PULSE_TOPHAT = 1, TAM_PULSE_TRIANGULAR = 2 };
+enum tam_source { TAM_SRC_DISK = 0, TAM_SRC_GAUSSIAN = 1 };
+enum tam_bc { TAM_BC_DIRICHLET = 0, TAM_BC_ROBIN = 1 };
+
+/* Device error-word bits returned by tam_device_errors. */
+#define TAM_DEVERR_STEP_CAP 0x1u  /* a packet hit its step cap and was killed */
+#define TAM_DEVERR_NAN 0x2u       /* NaN direction or temperature */
+#define TAM_DEVERR_NEG_T 0x4u     /* negative kelvin (src/3dFD.f90:179-182) */
+
+/*
+ * Run parameters.  The first block is res/input.params in file order, as read
+ * by src/mcpolar.f90:79-94.  The grid is compile-time in the reference
+ * (src/constants.f90:12) and a run-time field here; numproc reproduces the
+ * nphotons*numproc divisor of src/mcpolar.f90:174.
+ */
+typedef struct tam_params {
+    int64_t nphotons;            /* packets per MC pass */
+    double xmax, ymax, zmax;     /* half-widths, cm */
+    double n1, n2;               /* refractive indices (ambient, tissue) */
+    double total_time;           /* s */
+    int32_t loops;               /* heat steps per outer iteration */
+    double repetition_rate_1;    /* s, pulse repetition period */
+    double power;                /* W */
+    double energy_per_pixel;     /* mJ */
+    double ablate_temp;          /* deg C */
+    int32_t pulses_to_do;
+    int32_t pulse_type;          /* enum tam_pulse */
+    int32_t nxg, nyg, nzg;       /* grid */
+    int32_t numproc;             /* normalisation divisor, >= 1 */
+    int32_t mode;                /* enum tam_mode */
+    int32_t precision;           /* enum tam_precision: transport and fused heat step */
+    int32_t device;              /* CUDA device ordinal */
+} tam_params;
+
+#define TAM_MAX_MATERIALS 16
+
+/* Optical + thermal properties of one material.  Material 0 is the
+ * ablated state ("air"): its optics are used for ablated voxels. */
+typedef struct tam_material {
+    double mua, mus, g, n;       /* /cm, /cm, HG anisotropy, refractive index */
+    double k, rho, c;            /* W/m/K, kg/m^3, J/kg/K */
+} tam_material;
+
+/*
+ * Config-mode extension (no slot in the reference's input.params): material
+ * table, beam, boundaries, Arrhenius constants.  Ignored in reference mode.
+ */
+typedef struct tam_config {
+    int32_t nmat;
+    tam_material mat[TAM_MAX_MATERIALS];
+    double n_ambient;
+    int32_t source;              /* enum tam_source */
+    double source_radius;        /* disk radius or Gaussian 1/e^2 radius, cm */
+    int32_t fresnel;             /* specular entry + Fresnel at the outer faces */
+    int32_t roulette;
+    double roulette_w, roulette_m;
+    double T0;                   /* initial tissue temperature, K */
+    int32_t bc_type[6];          /* faces x-, x+, y-, y+, z- (bottom), z+ (top, beam side) */
+    double bc_T[6], bc_h[6], bc_Tamb[6];
+    double dt_factor;            /* dt = dt_factor * stability limit */
+    double dt;                   /* if > 0, overrides dt_factor */
+    double opscale;              /* 1 = physical operator */
+    int32_t boil;
+    double T_boil, lw;
+    double T_abl;                /* K */
+    int32_t arrhenius;
+    double A, Ea, Rgas, T_lo, T_hi;
+    double thr[3];
+    double retrace_fraction;     /* re-run MC when newly ablated > fraction of grid; <=0 never */
+    int32_t retrace_check;       /* heat steps between re-trace checks */
+    int64_t max_steps;           /* per-packet loop cap */
+} tam_config;
+
+/* Mutable module scalars of the reference (module Heat, src/3dFD.f90:7-12). */
+typedef struct tam_state {
+    double time, delt, total_time, pulse_count, repetition_count, laser_on;
+    double pulse_length, real_pulse_length, volume_voxel, mass_voxel, qvapor;
+    double dx, dy, dz;
+    int32_t laser_flag, pulse_flag, pulses_done, counter;
+    int64_t n_ablated;           /* config mode: voxels ablated so far */
+    int64_t mc_passes;
+} tam_state;
+
+/* Fields for tam_upload / tam_download / tam_field_bytes. */
+enum tam_field {
+    TAM_F_TEMP = 0,        /* (0:nx+1,0:ny+1,0:nz+1) K            src/iarray.f90:10 */
+    TAM_F_RHOKAP = 1,      /* (0:nx+1,...) /cm, halo 0             src/iarray.f90:9 */
+    TAM_F_JMEAN = 2,       /* (1:nx,1:ny,1:nz) packet units        src/iarray.f90:10 */
+    TAM_F_JMEAN_GLOBAL = 3,/* (1:nx,...) W/m^3 (config: per W)     src/mcpolar.f90:174 */
+    TAM_F_TISSUE = 4,      /* (1:nx,...) Omega                     src/3dFD.f90:451 */
+    TAM_F_THRESTIME = 5,   /* (1:nx,...,3) s                       src/3dFD.f90:455-461 */
+    TAM_F_KAPPA = 6,       /* (0:nx+1,...) W/m/K                   src/3dFD.f90:256 */
+    TAM_F_DENSITY = 7,     /* (0:nx+1,...) kg/m^3 */
+    TAM_F_HEATCAP = 8,     /* (0:nx+1,...) J/kg/K */
+    TAM_F_COEFF = 9,       /* (0:nx+1,...) reference mode only */
+    TAM_F_ALPHA = 10,      /* (0:nx+1,...) reference mode only */
+    TAM_F_Q = 11,          /* (1:nx,...) J latent heat */
+    TAM_F_WATER = 12,      /* (1:nx,...) reference mode only */
+    TAM_F_MATERIAL = 13,   /* (1:nx,...) uint8 material id, config mode only */
+    TAM_NFIELDS = 14
+};
+
+/* Library identification. */
+const char *tam_version(void);
+int tam_abi_version(void);
+/* sizeof the ABI structs, for FFI layout checks: 0 tam_params, 1 tam_config,
+ * 2 tam_state, 3 tam_material; -1 otherwise. */
+int64_t tam_struct_size(int32_t which);
+
+/* The shipped res/input.params values on the 80^3 grid, reference mode, FP64. */
+int tam_params_default(tam_params *p);
+/* Config-mode defaults (homogeneous tissue, Gaussian beam, Robin top face). */
+int tam_config_default(tam_config *c);
+
+/*
+ * Parse res/input.params with Fortran list-directed semantics: one value per
+ * line in the order of src/mcpolar.f90:79-94; the rest of each line is
+ * ignored; ',' '/' and blanks end a value; 'd'/'D' exponents accepted.
+ * Fields not in the file (grid, mode, ...) are left untouched.
+ */
+int tam_read_input_params(const char *path, tam_params *p);
+
+/*
+ * Create a context: allocates the device state and runs the initialisation
+ * of src/mcpolar.f90:55-140 (alloc_array, zarray, init_opt1, gridset,
+ * temperature init, initThermalCoeff, total_time override) in reference
+ * mode, or the material/thermal set-up in config mode (cfg != NULL).
+ */
+int tam_create(const tam_params *p, const tam_config *cfg, struct tam_ctx **out);
+int tam_destroy(struct tam_ctx *ctx);
+/* Last error message of ctx (or of this thread when ctx is NULL). */
+const char *tam_last_error(const struct tam_ctx *ctx);
+/* Issue all further work of ctx on the given cudaStream_t (NULL: own stream). */
+int tam_set_stream(struct tam_ctx *ctx, void *cuda_stream);
+/* Bits of the device error word accumulated since creation. */
+int tam_device_errors(struct tam_ctx *ctx, uint32_t *bits);
+
+/* Re-run the set-up subroutines (tam_create already ran them).
+ *   init_opt1 (src/ch_opt.f90:7-25), gridset (src/gridset.f90:6-46),
+ *   initThermalCoeff (src/3dFD.f90:233-309). */
+int tam_init_opt(struct tam_ctx *ctx);
+int tam_gridset(struct tam_ctx *ctx, double xmax, double ymax, double zmax);
+int tam_init_thermal(struct tam_ctx *ctx, double *delt);
+
+/* Host <-> device copies of one field in the reference layout. */
+int tam_field_bytes(struct tam_ctx *ctx, int field, int64_t *nbytes);
+int tam_upload(struct tam_ctx *ctx, int field, const void *host, int64_t nbytes);
+int tam_download(struct tam_ctx *ctx, int field, void *host, int64_t nbytes);
+
+/*
+ * One MC pass of nphotons packets (packet ids 0..nphotons-1, Philox stream
+ * `stream` under `seed`): sourcephCO2 + tauint1 (+ stokes in config mode)
+ * for every packet (src/mcpolar.f90:151-170), the tally reduction
+ * (src/mcpolar.f90:173) and the normalisation (src/mcpolar.f90:174):
+ *   reference mode: jmeanGLOBAL = jmean * (getPwr()/81)/(nphotons*numproc*Vvox)
+ *   config mode:    jmeanGLOBAL = jmean / (nphotons * Vvox)   [W/m^3 per W]
+ * jmean_out (nullable) receives jmeanGLOBAL, nx*ny*nz doubles.
+ */
+int tam_mc_pass(struct tam_ctx *ctx, int64_t nphotons, uint64_t seed, uint32_t stream, double *jmean_out);
+
+/*
+ * Heat steps.  Reference mode: heat_sim_3D with `nsteps` loops
+ * (src/3dFD.f90:21-230), including the pulse state machine.  Config mode:
+ * nsteps fused steps (stencil + latent-heat clamp + Arrhenius + ablation).
+ * temp_out (nullable) receives the (nx+2)(ny+2)(nz+2) temperature.
+ */
+int tam_heat_steps(struct tam_ctx *ctx, int32_t nsteps, double *temp_out);
+/* Arrhenius (src/3dFD.f90:424-466), reference mode. */
+int tam_arrhenius(struct tam_ctx *ctx);
+/* setupThermalCoeff (src/3dFD.f90:312-361), reference mode. */
+int tam_update_props(struct tam_ctx *ctx, double ablate_temp);
+/* n iterations of the outer loop of src/mcpolar.f90:148-186. */
+int tam_step_coupled(struct tam_ctx *ctx, int32_t n, uint64_t seed);
+/* The whole outer loop while time <= total_time (at most max_iters, <=0 no cap). */
+int tam_run(struct tam_ctx *ctx, uint64_t seed, int64_t max_iters, int64_t *iters);
+/* tissue(rhokap <= 0.1) = -1 (src/mcpolar.f90:196-204). */
+int tam_finalize(struct tam_ctx *ctx);
+
+/* Tallies of the last MC pass, as fractions of launched packets.
+ * The reference never records escapes (src/inttau2.f90:58-61). */
+int tam_get_tallies(struct tam_ctx *ctx, double *absorbed, double *reflected, double *transmitted);
+/* All tally slots of the last pass: absorbed, specular, reflected,
+ * transmitted, side, roulette_net, missed, voxel_steps, scatters, overflow. */
+int tam_get_tallies_ex(struct tam_ctx *ctx, double *out, int32_t n);
+int tam_get_state(struct tam_ctx *ctx, tam_state *st);
+
+/* writer (src/writer.f90:6-81): stream-unformatted FP64 files in `dir`. */
+int tam_write_output(struct tam_ctx *ctx, const char *dir);
+
+/* Self-test: Philox4x32-10 of this library against cuRAND's device Philox on
+ * n inputs of 6 words {c0,c1,c2,c3,k0,k1}; outputs 4 words each. */
+int tam_selftest_philox(const uint32_t *in, uint32_t *out_mine, uint32_t *out_curand, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* TAM_H */

@@ -1,0 +1,379 @@
+"""Parity of the CUDA library (through its C ABI) with the CPU oracle.
+
+Tolerances, stated per test:
+  * reference-mode FP64 heat path (stencil, Arrhenius, property update):
+    1e-12 relative (the kernels evaluate the reference's operations in its
+    order with explicit round-to-nearest, so most values are bit-identical);
+  * FP64 transport vs the oracle on identical Philox streams: 1e-9 relative
+    per voxel (summation order of the tally differs; the reference's
+    absolute-coordinate arithmetic differs from the cell-relative DDA in the
+    last bits);
+  * FP32 transport vs FP64 / oracle: statistical, |diff| < 4 combined batch
+    standard errors for >= 99% of voxels with signal, totals within 4 SE;
+  * FP32 + Kahan fused heat vs FP64 fused heat: max |dT| <= 1e-3 K.
+"""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+F = None  # set by the fixture below
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _fields(tam):
+    global F
+    F = tam._abi
+
+
+def ref_pair(tam, orc, nx, ny, nz, precision=0, **kw):
+    p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, precision=precision, **kw)
+    okw = {k: v for k, v in kw.items()}
+    o = orc.RefOracle(orc.ref_params(nx=nx, ny=ny, nz=nz, **okw))
+    return tam.Context(p), o
+
+
+# ------------------------------------------------------------------ RNG --
+def test_philox_matches_curand_and_oracle(tam, orc):
+    rng = np.random.default_rng(0)
+    w = rng.integers(0, 2 ** 32, size=(4096, 6), dtype=np.uint64).astype(np.uint32)
+    w[0] = 0
+    w[1] = 0xFFFFFFFF
+    mine, ref = tam.selftest_philox(w)
+    assert np.array_equal(mine, ref)
+    for q in range(0, 4096, 97):
+        assert orc.philox(list(map(int, w[q, :4])), list(map(int, w[q, 4:]))) == list(map(int, mine[q]))
+
+
+# ------------------------------------------------- reference heat path --
+def _randomise_ref(o, ctx, rng, hot=True):
+    nx, ny, nz = o.nx, o.ny, o.nz
+    inter = (slice(1, nx + 1), slice(1, ny + 1), slice(1, nz + 1))
+    T = o.arr("temp")
+    T[inter] = rng.uniform(300.0, 380.0 if hot else 360.0, (nx, ny, nz))
+    for name, lo, hi in (("kappa", 0.3, 0.7), ("density", 900.0, 1200.0), ("heatcap", 2500.0, 4000.0)):
+        a = o.arr(name)
+        a[inter] = rng.uniform(lo, hi, (nx, ny, nz))
+    o.arr("coeff")[inter] = o.st.delt / (o.arr("density")[inter] * o.arr("heatcap")[inter])
+    o.arr("jmeanGLOBAL")[...] = rng.uniform(0.0, 5e9, (nx, ny, nz))
+    o.arr("Q")[...] = rng.uniform(0.0, o.st.QVapor * 1.1, (nx, ny, nz))
+    for f, name in ((F.TAM_F_TEMP, "temp"), (F.TAM_F_KAPPA, "kappa"), (F.TAM_F_DENSITY, "density"),
+                    (F.TAM_F_HEATCAP, "heatcap"), (F.TAM_F_COEFF, "coeff"), (F.TAM_F_JMEAN_GLOBAL, "jmeanGLOBAL"),
+                    (F.TAM_F_Q, "Q")):
+        ctx.upload(f, o.arr(name))
+
+
+def test_ref_stencil_fp64_matches_oracle(tam, orc):
+    ctx, o = ref_pair(tam, orc, 20, 16, 12)
+    rng = np.random.default_rng(1)
+    _randomise_ref(o, ctx, rng)
+    n = 6
+    o.st.p.loops = n
+    assert o.heat_sim(nthreads=1) == 0
+    T = ctx.heat_steps(n, want=True)
+    To = o.arr("temp")
+    np.testing.assert_allclose(T, To, rtol=1e-12, atol=0)
+    np.testing.assert_allclose(ctx.download(F.TAM_F_Q), o.arr("Q"), rtol=1e-12, atol=0)
+    assert (o.arr("Q") > 0).any()
+    exact = np.mean(T == To)
+    assert exact > 0.99, f"bit-identical fraction {exact}"
+    st = ctx.state()
+    assert st.time == o.st.time and st.delt == o.st.delt and st.laser_flag == o.st.laser_flag
+    ctx.close()
+    o.close()
+
+
+def test_ref_arrhenius_fp64_matches_oracle(tam, orc):
+    ctx, o = ref_pair(tam, orc, 11, 9, 7)
+    rng = np.random.default_rng(2)
+    inter = (slice(1, 12), slice(1, 10), slice(1, 8))
+    for it in range(30):
+        o.arr("temp")[inter] = rng.uniform(320.0, 372.0, (11, 9, 7))
+        ctx.upload(F.TAM_F_TEMP, o.arr("temp"))
+        o.st.p.loops = 1
+        assert o.heat_sim(nthreads=1) == 0
+        ctx.heat_steps(1)
+        ctx.upload(F.TAM_F_TEMP, o.arr("temp"))
+        o.arrhenius()
+        ctx.arrhenius()
+    np.testing.assert_allclose(ctx.download(F.TAM_F_TISSUE), o.arr("tissue"), rtol=1e-13, atol=0)
+    np.testing.assert_array_equal(ctx.download(F.TAM_F_THRESTIME), o.arr("thres"))
+    assert (o.arr("thres")[..., 0] > 0).any()
+    ctx.close()
+    o.close()
+
+
+@pytest.mark.parametrize("zero_p", [0.2, 0.6, 0.85])
+def test_ref_props_fp64_matches_sequential_sweep(tam, orc, zero_p):
+    nx, ny, nz = 13, 10, 9
+    ctx, o = ref_pair(tam, orc, nx, ny, nz, ablate_temp=100.0)
+    rng = np.random.default_rng(int(zero_p * 100))
+    inter = (slice(1, nx + 1), slice(1, ny + 1), slice(1, nz + 1))
+    rk = o.arr("rhokap")
+    rk[inter] = np.where(rng.random((nx, ny, nz)) < zero_p, 0.0, rng.uniform(170, 550, (nx, ny, nz)))
+    o.arr("temp")[inter] = rng.uniform(300, 400, (nx, ny, nz))
+    o.arr("Q")[...] = rng.uniform(0, o.st.QVapor * 1.2, (nx, ny, nz))
+    o.arr("water")[...] = rng.uniform(0, 0.75, (nx, ny, nz))
+    for f, name in ((F.TAM_F_RHOKAP, "rhokap"), (F.TAM_F_TEMP, "temp"), (F.TAM_F_Q, "Q"), (F.TAM_F_WATER, "water")):
+        ctx.upload(f, o.arr(name))
+    o.setup_thermal()
+    ctx.update_props(100.0)
+    np.testing.assert_array_equal(ctx.download(F.TAM_F_RHOKAP) == 0, o.arr("rhokap") == 0)
+    for f, name in ((F.TAM_F_RHOKAP, "rhokap"), (F.TAM_F_WATER, "water"), (F.TAM_F_KAPPA, "kappa"),
+                    (F.TAM_F_DENSITY, "density"), (F.TAM_F_HEATCAP, "heatcap"), (F.TAM_F_COEFF, "coeff"),
+                    (F.TAM_F_ALPHA, "alpha")):
+        np.testing.assert_allclose(ctx.download(f), o.arr(name), rtol=1e-13, atol=0, err_msg=name)
+    ctx.close()
+    o.close()
+
+
+# --------------------------------------------------- reference transport --
+def test_ref_mc_fp64_matches_oracle_same_streams(tam, orc):
+    ctx, o = ref_pair(tam, orc, 80, 80, 80)
+    n = 60000
+    J = ctx.mc_pass(n, seed=12345, stream=3, want=True)
+    o.photons(n, seed=12345, stream=3, nthreads=0)
+    o.normalise()
+    Jo = o.arr("jmeanGLOBAL")
+    assert Jo.max() > 0
+    np.testing.assert_allclose(J, Jo, rtol=1e-9, atol=1e-9 * Jo.max())
+    np.testing.assert_allclose(ctx.download(F.TAM_F_JMEAN), o.arr("jmean"), rtol=1e-9, atol=1e-9 * o.arr("jmean").max())
+    t = ctx.tallies()
+    assert t["absorbed"] == pytest.approx(o.arr("jmean").sum() / n, rel=1e-12)
+    assert t["scatters"] == 0 and t["overflow"] == 0
+    ctx.close()
+    o.close()
+
+
+def _batches_gpu(ctx, n, nb, seed, stream0=0):
+    out = []
+    for b in range(nb):
+        ctx.mc_pass(n, seed=seed, stream=stream0 + b)
+        out.append(ctx.download(F.TAM_F_JMEAN) / n)
+    return np.array(out)
+
+
+def _stat_compare(a, b, thresh=4.0, frac=0.99, min_signal=None):
+    ma, mb = a.mean(0), b.mean(0)
+    sa = a.std(0, ddof=1) / math.sqrt(a.shape[0])
+    sb = b.std(0, ddof=1) / math.sqrt(b.shape[0])
+    se = np.sqrt(sa ** 2 + sb ** 2)
+    sig = se > 0 if min_signal is None else (np.maximum(ma, mb) > min_signal) & (se > 0)
+    z = np.abs(ma - mb)[sig] / se[sig]
+    return (z < thresh).mean(), int(sig.sum()), ma, mb
+
+
+def test_ref_mc_fp32_statistical_vs_oracle(tam, orc):
+    ctx, o = ref_pair(tam, orc, 80, 80, 80, precision=1)
+    nb, n = 16, 20000
+    g = _batches_gpu(ctx, n, nb, seed=77)
+    ob = []
+    jm = o.arr("jmean")
+    for b in range(nb):
+        jm[...] = 0.0
+        o.photons(n, seed=999, stream=b, nthreads=0)
+        ob.append(jm / n)
+    ob = np.array(ob)
+    ok, nsig, ma, mb = _stat_compare(g, ob, min_signal=1e-4)
+    assert nsig > 500
+    assert ok >= 0.99, ok
+    assert abs(ma.sum() - mb.sum()) / mb.sum() < 0.02
+    ctx.close()
+    o.close()
+
+
+# ----------------------------------------------------- config transport --
+def cfg_pair(tam, orc, nx, ny, nz, half, precision=0, mats=None, radius=0.1, fresnel=1, roulette=1,
+             max_steps=10_000_000):
+    mats = mats or [(0.0, 0.0, 0.0, 1.0), (0.3, 100.0, 0.9, 1.38)]
+    p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half, zmax=half, mode=1, precision=precision,
+                           pulse_type=1, power=1.0, energy_per_pixel=1000.0, total_time=1.0)
+    c = tam.default_config(nmat=len(mats), source_radius=radius, fresnel=fresnel, roulette=roulette,
+                           max_steps=max_steps)
+    for i, (mua, mus, g, nn) in enumerate(mats):
+        tam.set_material(c, i, mua, mus, g, nn, 0.56, 1070.0, 3400.0)
+    d = orc.mc_desc(nx, ny, nz, half, half, half, materials=mats, source_radius=radius, fresnel=fresnel,
+                    roulette=roulette, max_steps=max_steps)
+    return tam.Context(p, c), d
+
+
+def test_config_mc_fp64_matches_oracle_same_streams(tam, orc):
+    ctx, d = cfg_pair(tam, orc, 24, 24, 24, 0.5)
+    n = 4000
+    ctx.mc_pass(n, seed=31, stream=5)
+    J = ctx.download(F.TAM_F_JMEAN)
+    grid = np.ones((24, 24, 24), dtype=np.uint8, order="F")
+    Jo, to = orc.mc_transport(d, grid, n, seed=31, stream=5, nthreads=0)
+    t = ctx.tallies()
+    for k in ("specular", "reflected", "transmitted", "side", "roulette_net"):
+        assert t[k] == pytest.approx(to[k] / n, rel=1e-9, abs=1e-12), k
+    assert t["scatters"] == to["scatters"] and t["voxel_steps"] == to["voxel_steps"]
+    rel = np.abs(J - Jo).sum() / np.abs(Jo).sum()
+    assert rel < 1e-9, rel
+    ctx.close()
+
+
+def test_config_mc_layers_and_ablated_material(tam, orc):
+    # three-layer slab with an ablated (air) pocket: material table + id grid
+    mats = [(0.0, 0.0, 0.0, 1.0), (1.0, 200.0, 0.8, 1.4), (0.3, 120.0, 0.9, 1.4), (0.1, 80.0, 0.9, 1.4)]
+    nx = ny = 20
+    nz = 16
+    ctx, d = cfg_pair(tam, orc, nx, ny, nz, 0.25, mats=mats, radius=0.08)
+    grid = np.ones((nx, ny, nz), dtype=np.uint8, order="F") * 3
+    grid[:, :, nz - 2:] = 1
+    grid[:, :, 6:nz - 2] = 2
+    grid[8:12, 8:12, nz - 3:] = 0
+    ctx.upload(F.TAM_F_MATERIAL, grid)
+    n = 3000
+    ctx.mc_pass(n, seed=5, stream=1)
+    J = ctx.download(F.TAM_F_JMEAN)
+    Jo, to = orc.mc_transport(d, grid, n, seed=5, stream=1, nthreads=0)
+    assert np.abs(J - Jo).sum() / np.abs(Jo).sum() < 1e-9
+    assert J[9, 9, nz - 1] == 0.0  # air absorbs nothing
+    rk = ctx.download(F.TAM_F_RHOKAP)
+    assert rk[10, 10, nz] == 0.0 and rk[1, 1, nz] == 201.0
+    ctx.close()
+
+
+def test_config_mc_fp32_vs_fp64_statistical(tam, orc):
+    c64, _ = cfg_pair(tam, orc, 24, 24, 24, 0.5, precision=0)
+    c32, _ = cfg_pair(tam, orc, 24, 24, 24, 0.5, precision=1)
+    nb, n = 16, 2000
+    a = _batches_gpu(c64, n, nb, seed=3)
+    b = _batches_gpu(c32, n, nb, seed=3, stream0=100)
+    ok, nsig, ma, mb = _stat_compare(a, b, min_signal=1e-5)
+    assert nsig > 300
+    assert ok >= 0.99, ok
+    assert abs(ma.sum() - mb.sum()) / mb.sum() < 0.03
+    t64, t32 = c64.tallies(), c32.tallies()
+    assert abs(t64["reflected"] - t32["reflected"]) < 0.03
+    c64.close()
+    c32.close()
+
+
+# --------------------------------------------------------- fused heat ----
+def fused_setup(tam, orc, nx, ny, nz, half, precision, dt, rng, jscale):
+    p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half, zmax=half, mode=1, precision=precision,
+                           pulse_type=1, power=1.0, energy_per_pixel=1e6, total_time=10.0)
+    c = tam.default_config(dt=dt)
+    ctx = tam.Context(p, c)
+    d = 2 * half * 1e-2 / nx
+    h = orc.heat_desc(nx, ny, nz, d, 2 * half * 1e-2 / ny, 2 * half * 1e-2 / nz, dt=dt)
+    J = np.asfortranarray(rng.uniform(0, 1, (nx, ny, nz)) ** 2 * jscale)
+    ctx.upload(F.TAM_F_JMEAN_GLOBAL, J)
+    return ctx, h, J
+
+
+def test_fused_fp64_matches_oracle(tam, orc):
+    nx, ny, nz = 24, 20, 16
+    rng = np.random.default_rng(4)
+    dt = 2e-3
+    ctx, h, J = fused_setup(tam, orc, nx, ny, nz, 0.12, 0, dt, rng, 2e9)
+    st = dict(T=np.full((nx, ny, nz), 310.15, order="F"), k=np.full((nx, ny, nz), 0.56, order="F"),
+              rho=np.full((nx, ny, nz), 1070.0, order="F"), c=np.full((nx, ny, nz), 3400.0, order="F"),
+              Q=np.zeros((nx, ny, nz), order="F"), omega=np.zeros((nx, ny, nz), order="F"),
+              thres=np.zeros((nx, ny, nz, 3), order="F"), mat=np.ones((nx, ny, nz), dtype=np.uint8, order="F"))
+    Jo = J.copy(order="F")
+    T = st["T"]
+    nsteps = 40
+    for s in range(nsteps):
+        T, _ = orc.fused_step(h, 1.0, (s + 1) * dt, T, st["k"], st["rho"], st["c"], Jo, st["Q"], st["omega"],
+                              st["thres"], st["mat"])
+    Tg = ctx.heat_steps(nsteps, want=True)
+    np.testing.assert_allclose(Tg[1:-1, 1:-1, 1:-1], T, rtol=1e-12, atol=0)
+    assert T.max() > 320.0
+    np.testing.assert_allclose(ctx.download(F.TAM_F_TISSUE), st["omega"], rtol=1e-10, atol=1e-300)
+    assert st["omega"].max() > 0
+    np.testing.assert_array_equal(ctx.download(F.TAM_F_MATERIAL), st["mat"])
+    ctx.close()
+
+
+def test_fused_fp32_kahan_within_1mK_of_fp64(tam, orc):
+    nx = ny = nz = 48
+    rng = np.random.default_rng(5)
+    half = 0.24
+    d = 2 * half * 1e-2 / nx
+    alpha = 0.56 / (1070 * 3400)
+    dt = 0.9 / (2 * alpha * 3 / d ** 2)
+    c64, _, J = fused_setup(tam, orc, nx, ny, nz, half, 0, dt, rng, 1e8)
+    c32, _, _ = fused_setup(tam, orc, nx, ny, nz, half, 1, dt, np.random.default_rng(5), 1e8)
+    nsteps = 400
+    T64 = c64.heat_steps(nsteps, want=True)
+    T32 = c32.heat_steps(nsteps, want=True)
+    rise = (T64 - 310.15).max()
+    assert rise > 20.0, rise
+    err = np.abs(T32 - T64).max()
+    assert err <= 1e-3, err
+    om64, om32 = c64.download(F.TAM_F_TISSUE), c32.download(F.TAM_F_TISSUE)
+    assert np.abs(om32 - om64).max() <= 1e-3 * max(om64.max(), 1e-30) + 1e-30
+    c64.close()
+    c32.close()
+
+
+# ------------------------------------------------------- coupled driver --
+def test_coupled_reference_matches_oracle(tam, orc):
+    kw = dict(nphotons=3000, power=70.0, ablate_temp=60.0, pulse_type=1)
+    ctx, o = ref_pair(tam, orc, 16, 16, 16, **kw)
+    for it in range(6):
+        ctx.step_coupled(1, seed=2024)
+        assert o.outer_iteration(2024, nthreads=0) == 0
+    np.testing.assert_allclose(ctx.download(F.TAM_F_JMEAN_GLOBAL), o.arr("jmeanGLOBAL"), rtol=1e-9,
+                               atol=1e-9 * o.arr("jmeanGLOBAL").max())
+    To = o.arr("temp")
+    np.testing.assert_allclose(ctx.download(F.TAM_F_TEMP), To, rtol=1e-10, atol=0)
+    np.testing.assert_allclose(ctx.download(F.TAM_F_TISSUE), o.arr("tissue"), rtol=1e-8, atol=1e-300)
+    np.testing.assert_array_equal(ctx.download(F.TAM_F_RHOKAP) == 0, o.arr("rhokap") == 0)
+    st = ctx.state()
+    assert st.counter == o.st.counter and st.time == o.st.time
+    ctx.close()
+    o.close()
+
+
+# --------------------------------------------------------- error paths --
+def test_error_paths_and_recovery(tam, orc):
+    ctx, d = cfg_pair(tam, orc, 12, 12, 12, 0.3, max_steps=3)
+    with pytest.raises(tam.TamError) as e:
+        ctx.mc_pass(500, seed=1)
+    assert e.value.code == F.TAM_E_DEVICE
+    assert ctx.device_errors() & F.TAM_DEVERR_STEP_CAP
+    assert ctx.tallies()["overflow"] > 0
+    with pytest.raises(tam.TamError) as e:
+        ctx.arrhenius()
+    assert e.value.code == F.TAM_E_STATE
+    with pytest.raises(tam.TamError) as e:
+        ctx.download(F.TAM_F_WATER)
+    assert e.value.code == F.TAM_E_STATE
+    # the context stays usable after a device-reported error
+    ctx.heat_steps(2)
+    ctx.close()
+    p = tam.default_params(nxg=8, nyg=8, nzg=8)
+    with tam.Context(p) as c2:
+        bad = np.ones((10, 10, 10), order="F")
+        bad[3, 3, 3] = -1.0
+        with pytest.raises(tam.TamError) as e:
+            c2.upload(F.TAM_F_RHOKAP, bad)
+        assert e.value.code == F.TAM_E_INVALID
+        import ctypes as C
+
+        buf = np.zeros(5)
+        rc = c2._lib.tam_download(c2._h, F.TAM_F_TEMP, buf.ctypes.data_as(C.c_void_p), buf.nbytes)
+        assert rc == F.TAM_E_INVALID
+
+
+def test_writer_files(tam, orc, tmp_path):
+    p = tam.default_params(nxg=8, nyg=8, nzg=8)
+    with tam.Context(p) as ctx:
+        ctx.step_coupled(2, seed=1)
+        ctx.finalize()
+        ctx.write_output(str(tmp_path))
+    names = sorted(x.name for x in tmp_path.iterdir())
+    tail = "70w-8-500-400-0.030-0.030-0.060.dat"
+    want = sorted([f"{k}-t{tail}" for k in ("jmean", "rhokap", "temp", "water", "tissue")] +
+                  [f"time-t-{q}-{tail}" for q in (1, 2, 3)])
+    assert names == want
+    assert (tmp_path / f"temp-t{tail}").stat().st_size == 10 ** 3 * 8
+    assert (tmp_path / f"jmean-t{tail}").stat().st_size == 8 ** 3 * 8
+    t = np.fromfile(tmp_path / f"temp-t{tail}").reshape((10, 10, 10), order="F")
+    assert t[0, 5, 5] == 5.0 and t[5, 5, 0] == 25.0

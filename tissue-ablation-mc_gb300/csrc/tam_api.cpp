@@ -1,0 +1,1376 @@
+// tam_api.cpp -- the C ABI of include/tam.h.
+//
+// Host side of the drop-in boundary: context and device memory, the
+// reference's set-up (src/mcpolar.f90:55-140, src/ch_opt.f90:7-25,
+// src/gridset.f90:6-46, src/3dFD.f90:233-309), its outer driver loop and
+// pulse state machine (src/mcpolar.f90:148-186, src/3dFD.f90:199-214), the
+// res/input.params reader (src/mcpolar.f90:79-94) and the writer
+// (src/writer.f90:6-81).  All grid work runs in the sm_103a kernels; there
+// is no CPU fallback.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <sstream>
+#include <string>
+#include <type_traits>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/tam.h"
+#include "tam_kernels.h"
+#include "tam_util.h"
+
+#define TAM_VERSION_STRING "tam-gb300 0.1.0 (sm_103a)"
+
+namespace {
+
+thread_local std::string g_thread_err;
+
+// Reference constants (src/constants.f90:12-13, src/thermalConst_mod.f90:5-6).
+constexpr double WATER_INIT = 0.75;
+constexpr double PROTEIN = 1.0 - WATER_INIT;
+constexpr double AIR_HEAT_CAP = 1.006e3;
+constexpr double LW = 2256.e3;
+constexpr int SPOTS = 9 * 9;
+
+double air_cond(double T) { return -0.188521 * std::exp(-(0.000367259 * (T - 273.15))) + 0.212453; }
+double air_dens(double T) { return 101.325e3 / (287.058 * T); }
+double skin_dens(double w) { return 1000.0 / (w + 0.649 * PROTEIN); }
+double skin_cap(double w) { return 1000.0 * (4.2 * w + 1.09 * PROTEIN); }
+double skin_cond(double w, double rho) { return rho * (6.28e-4 * w + 1.17e-4 * PROTEIN); }
+
+}  // namespace
+
+struct tam_ctx {
+    tam_params p{};
+    tam_config cfg{};
+    bool config = false;
+    bool fp64 = true;  // precision of transport and of the fused heat step
+    int device = 0;
+    int sm_count = 152;
+    cudaStream_t stream = nullptr;
+    bool own_stream = false;
+    std::string err;
+
+    int nx = 0, ny = 0, nz = 0;
+    int64_t ni = 0, nh = 0;
+
+    // module scalars (opt_prop, Heat)
+    double hgg = 0, g2 = 0, mua = 0, mus = 0, kappa_opt = 0, albedo = 0, mu_water = 0, mu_protein = 0, delta = 0;
+    double delt = 0, dx = 0, dy = 0, dz = 0, volumeVoxel = 0, massVoxel = 0, QVapor = 0;
+    double pulseLength = 0, realPulseLength = 0, total_time = 0;
+    double time = 0, pulseCount = 0, repetitionCount = 0, laserOn = 1;
+    int laser_flag = 1, pulseFlag = 0, pulsesDone = 0, loops_left = 0, counter = 0;
+
+    // device buffers
+    std::vector<void *> allocs;
+    unsigned *d_err = nullptr;
+    double *d_tally = nullptr;
+    unsigned long long *d_work = nullptr, *d_nabl = nullptr, *d_cnt = nullptr;
+    double *d_jmean = nullptr, *d_jglob = nullptr, *d_sum = nullptr;
+    // reference mode
+    double *d_T[2] = {nullptr, nullptr};
+    int tcur = 0;
+    double *d_rk[2] = {nullptr, nullptr};
+    int rcur = 0;
+    double *d_kappa = nullptr, *d_density = nullptr, *d_heatcap = nullptr, *d_coeff = nullptr, *d_alpha = nullptr;
+    double *d_Q = nullptr, *d_water = nullptr, *d_tissue = nullptr, *d_thres = nullptr;
+    // config mode
+    void *d_Tf[2] = {nullptr, nullptr};
+    float *d_Tc[2] = {nullptr, nullptr};
+    int fcur = 0;
+    void *d_k = nullptr, *d_rho = nullptr, *d_c = nullptr, *d_J = nullptr, *d_Qf = nullptr;
+    uint8_t *d_mat = nullptr;
+    double *d_halo = nullptr;  // scratch in the reference halo layout
+    tam::MatThermal lut{};
+    double cdt = 0;            // config-mode step
+    bool need_trace = true;
+    long long nabl_at_trace = 0;
+
+    // last pass
+    double tally[tam::N_TALLY] = {0};
+    int64_t last_n = 0;
+    int64_t mc_passes = 0;
+    unsigned errbits_seen = 0;
+};
+
+namespace {
+
+int fail(tam_ctx *c, int code, const std::string &msg)
+{
+    if (c) c->err = msg;
+    g_thread_err = msg;
+    return code;
+}
+
+#define CK(expr)                                                                                         \
+    do {                                                                                                 \
+        cudaError_t e_ = (expr);                                                                         \
+        if (e_ != cudaSuccess) return fail(ctx, TAM_E_CUDA, std::string(#expr) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+#define RC(expr)                      \
+    do {                              \
+        int r_ = (expr);              \
+        if (r_ != TAM_OK) return r_;  \
+    } while (0)
+
+int dalloc(tam_ctx *ctx, void **p, size_t bytes)
+{
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        (void)cudaGetLastError();
+        return fail(ctx, TAM_E_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
+                                           cudaGetErrorString(e));
+    }
+    ctx->allocs.push_back(*p);
+    return TAM_OK;
+}
+
+template <typename T> int dalloc_t(tam_ctx *ctx, T **p, int64_t n)
+{
+    void *v = nullptr;
+    int r = dalloc(ctx, &v, (size_t)n * sizeof(T));
+    *p = (T *)v;
+    return r;
+}
+
+// Wait for the stream, then fold the device error word into the status.
+int finish(tam_ctx *ctx, const char *what)
+{
+    CK(cudaGetLastError());
+    CK(cudaStreamSynchronize(ctx->stream));
+    unsigned bits = 0;
+    CK(cudaMemcpy(&bits, ctx->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    const unsigned fresh = bits & ~ctx->errbits_seen;
+    ctx->errbits_seen |= bits;
+    if (fresh) {
+        std::string m = std::string(what) + ": device error word 0x";
+        char buf[16];
+        std::snprintf(buf, sizeof buf, "%x", fresh);
+        m += buf;
+        if (fresh & TAM_DEVERR_STEP_CAP) m += " (packet step cap reached)";
+        if (fresh & TAM_DEVERR_NAN) m += " (NaN)";
+        if (fresh & TAM_DEVERR_NEG_T) m += " (negative temperature in kelvin)";
+        return fail(ctx, TAM_E_DEVICE, m);
+    }
+    return TAM_OK;
+}
+
+// ----------------------------------------------------- pulse / getPwr --
+// src/3dFD.f90:365-421 (procedure pointer selected in initThermalCoeff)
+double get_pwr(tam_ctx *c)
+{
+    const double P = c->p.power;
+    switch (c->p.pulse_type) {
+    case TAM_PULSE_GAUSSIAN: {
+        const double fact = 2. * std::sqrt(2. * std::log(2.));
+        const double mu = fact * c->pulseLength, sig = c->pulseLength / fact;
+        const double tm = c->time - mu;
+        return P * std::exp(-((tm * tm) / (2.0 * (sig * sig))));
+    }
+    case TAM_PULSE_TOPHAT: return c->laser_flag ? P : 0.0;
+    default: {
+        const double m = P / c->pulseLength, cc = 2.0 * P;
+        if (!c->laser_flag) return 0.0;
+        double v;
+        if (c->pulseFlag) {
+            v = -m * c->time + cc;
+        } else if (c->time >= c->pulseLength) {
+            c->pulseFlag = 1;
+            v = -m * c->time + cc;
+        } else {
+            return m * c->time;
+        }
+        return v < 0.0 ? 0.0 : v;
+    }
+    }
+}
+
+// src/3dFD.f90:199-214; returns true when this update switched the laser on
+bool pulse_update(tam_ctx *c, double dt)
+{
+    bool on = false;
+    if (c->pulseCount >= c->realPulseLength && c->laser_flag) {
+        c->laser_flag = 0;
+        c->laserOn = 0.;
+        c->pulseCount = 0.;
+        c->pulsesDone += 1;
+        c->repetitionCount = 0.;
+    } else if (c->repetitionCount >= c->p.repetition_rate_1 && !c->laser_flag && c->pulsesDone < c->p.pulses_to_do) {
+        c->laser_flag = 1;
+        c->laserOn = 1.;
+        c->pulseCount = 0.;
+        c->repetitionCount = 0.;
+        on = true;
+    }
+    c->pulseCount += dt;
+    c->repetitionCount += dt;
+    c->time += dt;
+    return on;
+}
+
+int validate_params(const tam_params *p, std::string &why)
+{
+    if (p->nxg < 1 || p->nyg < 1 || p->nzg < 1) { why = "grid sizes must be >= 1"; return 0; }
+    if ((int64_t)p->nxg * p->nyg * p->nzg > (int64_t)1 << 34) { why = "grid too large"; return 0; }
+    if (!(p->xmax > 0) || !(p->ymax > 0) || !(p->zmax > 0)) { why = "xmax, ymax, zmax must be > 0"; return 0; }
+    if (p->nphotons < 0) { why = "nphotons must be >= 0"; return 0; }
+    if (p->loops < 1) { why = "loops must be >= 1"; return 0; }
+    if (p->numproc < 1) { why = "numproc must be >= 1"; return 0; }
+    if (!(p->power > 0)) { why = "power must be > 0"; return 0; }
+    if (p->pulse_type < 0 || p->pulse_type > 2) { why = "no pulse type"; return 0; }
+    if (p->mode != TAM_MODE_REFERENCE && p->mode != TAM_MODE_CONFIG) { why = "bad mode"; return 0; }
+    if (p->precision != TAM_FP64 && p->precision != TAM_FP32) { why = "bad precision"; return 0; }
+    return 1;
+}
+
+// ---------------------------------------------------- reference set-up --
+int ref_setup(tam_ctx *ctx)
+{
+    const tam_params &p = ctx->p;
+    const int nx = ctx->nx, ny = ctx->ny, nz = ctx->nz;
+    cudaStream_t s = ctx->stream;
+    // init_opt1 (src/ch_opt.f90:15-22)
+    ctx->hgg = 0.9;
+    ctx->g2 = ctx->hgg * ctx->hgg;
+    ctx->mu_water = 510.0;
+    ctx->mu_protein = 170.0;
+    ctx->mua = ctx->mu_water + ctx->mu_protein;
+    ctx->mus = 0.;
+    ctx->kappa_opt = ctx->mus + ctx->mua;
+    ctx->albedo = ctx->mus / ctx->kappa_opt;
+    // gridset: rhokap = kappa inside, 0 on the halo (src/gridset.f90:34-45)
+    for (int b = 0; b < 2; ++b) CK(tam::launch_fill_halo(ctx->d_rk[b], nx, ny, nz, ctx->kappa_opt, 0.0, 0.0, false, s));
+    ctx->rcur = 0;
+    ctx->delta = 1.e-8 * (2. * p.zmax / nz);  // src/mcpolar.f90:112
+    // temperature (src/mcpolar.f90:123-129)
+    for (int b = 0; b < 2; ++b) CK(tam::launch_ref_init_temp(ctx->d_T[b], nx, ny, nz, s));
+    ctx->tcur = 0;
+    // initThermalCoeff (src/3dFD.f90:249-307)
+    ctx->dx = (2.0 * p.xmax * 1.e-2) / (nx + 2.0);
+    ctx->dy = (2.0 * p.ymax * 1.e-2) / (ny + 2.0);
+    ctx->dz = (2.0 * p.zmax * 1.e-2) / (nz + 2.0);
+    const double heatCaptmp = skin_cap(WATER_INIT);
+    const double densitytmp = skin_dens(WATER_INIT);
+    const double kappatmp = skin_cond(WATER_INIT, densitytmp);
+    const double alphatmp = kappatmp / (densitytmp * skin_cap(WATER_INIT));
+    const double alpha_air = air_cond(25.0 + 273.0) / (air_dens(25.0 + 273.0) * AIR_HEAT_CAP);
+    CK(cudaMemsetAsync(ctx->d_Q, 0, ctx->ni * sizeof(double), s));
+    CK(tam::launch_fill_f64(ctx->d_water, WATER_INIT, ctx->ni, s));
+    CK(tam::launch_fill_halo(ctx->d_alpha, nx, ny, nz, alphatmp, alphatmp, alpha_air, true, s));
+    CK(tam::launch_fill_halo(ctx->d_kappa, nx, ny, nz, skin_cond(WATER_INIT, densitytmp), air_cond(25. + 273.), 0.0,
+                             false, s));
+    CK(tam::launch_fill_f64(ctx->d_density, densitytmp, ctx->nh, s));
+    CK(tam::launch_fill_f64(ctx->d_heatcap, heatCaptmp, ctx->nh, s));
+    const double constd = (1.0 / (ctx->dx * ctx->dx)) + (1.0 / (ctx->dy * ctx->dy)) + (1.0 / (ctx->dz * ctx->dz));
+    ctx->delt = 1.0 / (1.0 * alphatmp * constd);
+    CK(tam::launch_fill_halo(ctx->d_coeff, nx, ny, nz, alphatmp * ctx->delt / kappatmp, 0.0, 0.0, false, s));
+    ctx->pulseLength = (p.energy_per_pixel * 1.e-3 * (double)SPOTS) / p.power;
+    ctx->volumeVoxel = (2.0 * p.xmax * 1.e-2 / nx) * (2.0 * p.ymax * 1.e-2 / ny) * (2.0 * p.zmax * 1.e-2 / nz);
+    ctx->massVoxel = densitytmp * ctx->volumeVoxel;
+    ctx->QVapor = LW * ctx->massVoxel;
+    switch (p.pulse_type) {
+    case TAM_PULSE_TOPHAT: ctx->realPulseLength = ctx->pulseLength; break;
+    case TAM_PULSE_GAUSSIAN: ctx->realPulseLength = 20000.0 * ctx->pulseLength; break;
+    default: ctx->realPulseLength = 2.0 * ctx->pulseLength; break;
+    }
+    // total_time override (src/mcpolar.f90:134-140)
+    ctx->total_time = p.total_time;
+    if (p.pulse_type == TAM_PULSE_GAUSSIAN) {
+        ctx->total_time = 2. * ctx->pulseLength * (2. * std::sqrt(2. * std::log(2.)));
+        ctx->realPulseLength = ctx->total_time;
+    } else if ((int64_t)(ctx->total_time / ctx->delt) <= (int64_t)(ctx->realPulseLength / ctx->delt)) {
+        ctx->total_time = ctx->delt * (ctx->realPulseLength / ctx->delt + 2000.);
+    }
+    return TAM_OK;
+}
+
+// -------------------------------------------------------- config set-up --
+int cfg_setup(tam_ctx *ctx)
+{
+    const tam_params &p = ctx->p;
+    const tam_config &c = ctx->cfg;
+    const int nx = ctx->nx, ny = ctx->ny, nz = ctx->nz;
+    cudaStream_t s = ctx->stream;
+    for (int m = 0; m < TAM_MAX_MATERIALS; ++m) {
+        const tam_material &mm = c.mat[m < c.nmat ? m : 0];
+        ctx->lut.k[m] = mm.k;
+        ctx->lut.rho[m] = mm.rho;
+        ctx->lut.c[m] = mm.c;
+        ctx->lut.mut[m] = mm.mua + mm.mus;
+    }
+    ctx->dx = 2.0 * p.xmax * 1.e-2 / nx;
+    ctx->dy = 2.0 * p.ymax * 1.e-2 / ny;
+    ctx->dz = 2.0 * p.zmax * 1.e-2 / nz;
+    ctx->volumeVoxel = ctx->dx * ctx->dy * ctx->dz;
+    double amax = 0.0;
+    for (int m = 1; m < c.nmat; ++m) {
+        const double a = c.mat[m].k / (c.mat[m].rho * c.mat[m].c);
+        if (a > amax) amax = a;
+    }
+    if (c.nmat == 1) amax = c.mat[0].k / (c.mat[0].rho * c.mat[0].c);
+    if (c.dt > 0) {
+        ctx->cdt = c.dt;
+    } else {
+        const double sum = 1.0 / (ctx->dx * ctx->dx) + 1.0 / (ctx->dy * ctx->dy) + 1.0 / (ctx->dz * ctx->dz);
+        ctx->cdt = c.dt_factor / (2.0 * c.opscale * amax * sum);
+    }
+    ctx->delt = ctx->cdt;
+    // pulse: energy (mJ) over power (no 81-spot factor in config mode)
+    ctx->pulseLength = p.energy_per_pixel * 1.e-3 / p.power;
+    switch (p.pulse_type) {
+    case TAM_PULSE_TOPHAT: ctx->realPulseLength = ctx->pulseLength; break;
+    case TAM_PULSE_GAUSSIAN: ctx->realPulseLength = 2. * ctx->pulseLength * (2. * std::sqrt(2. * std::log(2.))); break;
+    default: ctx->realPulseLength = 2.0 * ctx->pulseLength; break;
+    }
+    ctx->total_time = p.total_time;
+    const uint8_t m0 = (uint8_t)(c.nmat > 1 ? 1 : 0);
+    CK(tam::launch_fill_u8(ctx->d_mat, m0, ctx->ni, s));
+    CK(tam::launch_props_from_mat(ctx->d_mat, c.nmat, ctx->lut, ctx->d_k, ctx->d_rho, ctx->d_c, ctx->fp64, ctx->ni, s));
+    for (int b = 0; b < 2; ++b) {
+        CK(tam::launch_fill_real(ctx->d_Tf[b], ctx->fp64, c.T0, ctx->ni, s));
+        if (!ctx->fp64) CK(cudaMemsetAsync(ctx->d_Tc[b], 0, ctx->ni * sizeof(float), s));
+    }
+    ctx->fcur = 0;
+    CK(cudaMemsetAsync(ctx->d_J, 0, ctx->ni * (ctx->fp64 ? 8 : 4), s));
+    CK(cudaMemsetAsync(ctx->d_Qf, 0, ctx->ni * (ctx->fp64 ? 8 : 4), s));
+    CK(cudaMemsetAsync(ctx->d_tissue, 0, ctx->ni * sizeof(double), s));
+    CK(cudaMemsetAsync(ctx->d_thres, 0, 3 * ctx->ni * sizeof(double), s));
+    CK(cudaMemsetAsync(ctx->d_nabl, 0, sizeof(unsigned long long), s));
+    ctx->need_trace = true;
+    ctx->nabl_at_trace = 0;
+    return TAM_OK;
+}
+
+tam::FusedArgs fused_args(tam_ctx *ctx)
+{
+    const tam_config &c = ctx->cfg;
+    tam::FusedArgs a{};
+    a.nx = ctx->nx;
+    a.ny = ctx->ny;
+    a.nz = ctx->nz;
+    a.dx = ctx->dx;
+    a.dy = ctx->dy;
+    a.dz = ctx->dz;
+    a.opscale = c.opscale;
+    a.dt = ctx->cdt;
+    a.vvox = ctx->volumeVoxel;
+    a.boil = c.boil;
+    a.T_boil = c.T_boil;
+    a.lw = c.lw;
+    a.T_abl = c.T_abl;
+    a.arrhenius = c.arrhenius;
+    a.lnA = std::log(c.A);
+    a.Ea = c.Ea;
+    a.Rgas = c.Rgas;
+    a.T_lo = c.T_lo;
+    a.T_hi = c.T_hi;
+    for (int t = 0; t < 3; ++t) a.thr[t] = c.thr[t];
+    for (int f = 0; f < 6; ++f) {
+        a.bc_type[f] = c.bc_type[f];
+        a.bc_T[f] = c.bc_T[f];
+        a.bc_h[f] = c.bc_h[f];
+        a.bc_Tamb[f] = c.bc_Tamb[f];
+    }
+    a.T_in = ctx->d_Tf[ctx->fcur];
+    a.T_out = ctx->d_Tf[1 - ctx->fcur];
+    a.Tc_in = ctx->fp64 ? nullptr : ctx->d_Tc[ctx->fcur];
+    a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[1 - ctx->fcur];
+    a.k = ctx->d_k;
+    a.rho = ctx->d_rho;
+    a.c = ctx->d_c;
+    a.J = ctx->d_J;
+    a.Q = ctx->d_Qf;
+    a.omega = ctx->d_tissue;
+    a.thres = ctx->d_thres;
+    a.mat = ctx->d_mat;
+    a.n_ablated = ctx->d_nabl;
+    a.err = ctx->d_err;
+    return a;
+}
+
+// ------------------------------------------------------------ MC pass --
+int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream)
+{
+    cudaStream_t s = ctx->stream;
+    tam::TransportArgs a{};
+    a.nx = ctx->nx;
+    a.ny = ctx->ny;
+    a.nz = ctx->nz;
+    a.xmax = ctx->p.xmax;
+    a.ymax = ctx->p.ymax;
+    a.zmax = ctx->p.zmax;
+    if (ctx->config) {
+        const tam_config &c = ctx->cfg;
+        a.medium = tam::MED_MATERIAL;
+        a.mat = ctx->d_mat;
+        a.nmat = c.nmat;
+        for (int m = 0; m < tam::MAX_MAT; ++m) {
+            const tam_material &mm = c.mat[m < c.nmat ? m : 0];
+            a.lut[m] = tam::OptMat{mm.mua, mm.mus, mm.g, mm.n};
+        }
+        a.n_ambient = c.n_ambient;
+        a.source = c.source;
+        a.source_radius = c.source_radius;
+        a.fresnel = c.fresnel;
+        a.roulette = c.roulette;
+        a.roulette_w = c.roulette_w;
+        a.roulette_m = c.roulette_m;
+        a.max_steps = c.max_steps;
+        a.nudge = 0.0;
+    } else {
+        // sourcephCO2: uniform disk of diameter 250 um, no Fresnel, no roulette
+        a.medium = tam::MED_RHOKAP;
+        a.rhokap = ctx->d_rk[ctx->rcur];
+        a.rhokap_n = ctx->p.n2;
+        a.n_ambient = ctx->p.n1;
+        a.source = tam::SRC_DISK;
+        a.source_radius = 250e-4 / 2.;
+        a.fresnel = 0;
+        a.roulette = 0;
+        a.roulette_w = 0.0;
+        a.roulette_m = 1.0;
+        a.max_steps = (int64_t)1 << 40;
+        a.nudge = ctx->delta;  // src/mcpolar.f90:112
+    }
+    a.seed = seed;
+    a.stream = stream;
+    a.p0 = 0;
+    a.n = n;
+    a.jmean = ctx->d_jmean;
+    a.tally = ctx->d_tally;
+    a.work = ctx->d_work;
+    a.err = ctx->d_err;
+    CK(cudaMemsetAsync(ctx->d_jmean, 0, ctx->ni * sizeof(double), s));
+    CK(cudaMemsetAsync(ctx->d_tally, 0, tam::N_TALLY * sizeof(double), s));
+    CK(tam::launch_transport(a, ctx->fp64, ctx->sm_count, s));
+    CK(tam::launch_sum_f64(ctx->d_jmean, ctx->ni, ctx->d_tally + tam::T_ABSORBED, s));
+    ctx->last_n = n;
+    ctx->mc_passes += 1;
+    // normalisation (src/mcpolar.f90:174)
+    if (ctx->config) {
+        const double f = n > 0 ? 1.0 / ((double)n * ctx->volumeVoxel) : 0.0;
+        if (ctx->fp64) CK(tam::launch_scale_f64((double *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s));
+        else CK(tam::launch_scale_to_f32((float *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s));
+    } else {
+        const tam_params &p = ctx->p;
+        const double pw = get_pwr(ctx);
+        const double den = (double)n * (2. * p.xmax * 1.e-2 / p.nxg) * (2. * p.ymax * 1.e-2 / p.nyg) *
+                           (2. * p.zmax * 1.e-2 / p.nzg);
+        const double f = n > 0 ? (pw / 81.0) / den : 0.0;
+        CK(tam::launch_scale_f64(ctx->d_jglob, ctx->d_jmean, f, ctx->ni, false, s));
+    }
+    CK(cudaMemcpyAsync(ctx->tally, ctx->d_tally, sizeof(ctx->tally), cudaMemcpyDeviceToHost, s));
+    return finish(ctx, "tam_mc_pass");
+}
+
+// ------------------------------------------------------ heat (reference) --
+int ref_heat(tam_ctx *ctx, int32_t loops)
+{
+    if (ctx->pulseLength < ctx->delt) ctx->delt = ctx->pulseLength / 100.;  // src/3dFD.f90:102-105
+    ctx->loops_left = (int)(ctx->total_time / ((double)loops * ctx->delt)) - ctx->counter;
+    tam::RefHeatArgs a{};
+    a.nx = ctx->nx;
+    a.ny = ctx->ny;
+    a.nz = ctx->nz;
+    a.idx2 = 1.0 / (ctx->dx * ctx->dx);
+    a.idy2 = 1.0 / (ctx->dy * ctx->dy);
+    a.idz2 = 1.0 / (ctx->dz * ctx->dz);
+    a.vvox = ctx->volumeVoxel;
+    a.mvox = ctx->massVoxel;
+    a.qvapor = ctx->QVapor;
+    a.kappa = ctx->d_kappa;
+    a.density = ctx->d_density;
+    a.heatcap = ctx->d_heatcap;
+    a.coeff = ctx->d_coeff;
+    a.J = ctx->d_jglob;
+    a.Q = ctx->d_Q;
+    a.err = ctx->d_err;
+    for (int32_t it = 0; it < loops; ++it) {
+        a.delt = ctx->delt;
+        a.laserOn = ctx->laserOn;
+        a.t0 = ctx->d_T[ctx->tcur];
+        a.tn = ctx->d_T[1 - ctx->tcur];
+        CK(tam::launch_ref_stencil(a, ctx->stream));
+        ctx->tcur = 1 - ctx->tcur;  // t0 = tn (src/3dFD.f90:187)
+        pulse_update(ctx, ctx->delt);
+    }
+    return TAM_OK;
+}
+
+int ref_arrhenius(tam_ctx *ctx)
+{
+    tam::RefArrheniusArgs a{};
+    a.nx = ctx->nx;
+    a.ny = ctx->ny;
+    a.nz = ctx->nz;
+    a.delt = ctx->delt;
+    a.time = ctx->time;
+    a.temp = ctx->d_T[ctx->tcur];
+    a.rhokap = ctx->d_rk[ctx->rcur];
+    a.tissue = ctx->d_tissue;
+    a.thres = ctx->d_thres;
+    CK(tam::launch_ref_arrhenius(a, ctx->stream));
+    return TAM_OK;
+}
+
+int ref_props(tam_ctx *ctx, double ablate_temp)
+{
+    tam::RefPropsArgs a{};
+    a.nx = ctx->nx;
+    a.ny = ctx->ny;
+    a.nz = ctx->nz;
+    a.ablate_temp = ablate_temp;
+    a.delt = ctx->delt;
+    a.qvapor = ctx->QVapor;
+    a.mu_water = ctx->mu_water;
+    a.mu_protein = ctx->mu_protein;
+    a.temp = ctx->d_T[ctx->tcur];
+    a.rk_old = ctx->d_rk[ctx->rcur];
+    a.rk_new = ctx->d_rk[1 - ctx->rcur];
+    a.kappa = ctx->d_kappa;
+    a.density = ctx->d_density;
+    a.heatcap = ctx->d_heatcap;
+    a.coeff = ctx->d_coeff;
+    a.alpha = ctx->d_alpha;
+    a.Q = ctx->d_Q;
+    a.water = ctx->d_water;
+    a.err = ctx->d_err;
+    CK(tam::launch_ref_props(a, ctx->stream));
+    ctx->rcur = 1 - ctx->rcur;
+    return TAM_OK;
+}
+
+// --------------------------------------------------------- heat (config) --
+int cfg_heat(tam_ctx *ctx, int32_t nsteps)
+{
+    tam::FusedArgs a = fused_args(ctx);
+    const int check = ctx->cfg.retrace_check > 0 ? ctx->cfg.retrace_check : 0;
+    for (int32_t it = 0; it < nsteps; ++it) {
+        a.T_in = ctx->d_Tf[ctx->fcur];
+        a.T_out = ctx->d_Tf[1 - ctx->fcur];
+        a.Tc_in = ctx->fp64 ? nullptr : ctx->d_Tc[ctx->fcur];
+        a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[1 - ctx->fcur];
+        a.P = ctx->laserOn * get_pwr(ctx);
+        a.t_new = ctx->time + ctx->cdt;
+        CK(tam::launch_fused_step(a, ctx->fp64, ctx->stream));
+        ctx->fcur = 1 - ctx->fcur;
+        const bool on = pulse_update(ctx, ctx->cdt);
+        const bool last = it + 1 == nsteps;
+        if (ctx->cfg.retrace_fraction > 0 && ((check && (it + 1) % check == 0) || last || on)) {
+            unsigned long long n = 0;
+            CK(cudaMemcpyAsync(&n, ctx->d_nabl, sizeof n, cudaMemcpyDeviceToHost, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+            const long long fresh = (long long)n - ctx->nabl_at_trace;
+            if ((double)fresh > ctx->cfg.retrace_fraction * (double)ctx->ni || (on && fresh > 0))
+                ctx->need_trace = true;
+        }
+    }
+    return TAM_OK;
+}
+
+int outer_iteration(tam_ctx *ctx, uint64_t seed)
+{
+    const int64_t n = ctx->p.nphotons * (int64_t)ctx->p.numproc;
+    if (ctx->config) {
+        if (ctx->need_trace) {
+            RC(mc_pass(ctx, n, seed, (uint32_t)ctx->mc_passes));
+            unsigned long long nab = 0;
+            CK(cudaMemcpy(&nab, ctx->d_nabl, sizeof nab, cudaMemcpyDeviceToHost));
+            ctx->nabl_at_trace = (long long)nab;
+            ctx->need_trace = false;
+        }
+        RC(cfg_heat(ctx, ctx->p.loops));
+    } else {
+        // src/mcpolar.f90:149-185
+        if (ctx->laser_flag) RC(mc_pass(ctx, n, seed, (uint32_t)ctx->counter));
+        RC(ref_heat(ctx, ctx->p.loops));
+        RC(ref_arrhenius(ctx));
+        RC(ref_props(ctx, ctx->p.ablate_temp));
+    }
+    ctx->counter += 1;
+    return finish(ctx, "tam_step_coupled");
+}
+
+// ------------------------------------------------------ field exchange --
+struct FieldInfo {
+    int64_t count;
+    int esize;
+    bool ok;
+};
+
+FieldInfo field_info(const tam_ctx *ctx, int f)
+{
+    const int64_t nh = ctx->nh, ni = ctx->ni;
+    switch (f) {
+    case TAM_F_TEMP:
+    case TAM_F_RHOKAP:
+    case TAM_F_KAPPA:
+    case TAM_F_DENSITY:
+    case TAM_F_HEATCAP: return {nh, 8, true};
+    case TAM_F_COEFF:
+    case TAM_F_ALPHA: return {nh, 8, !ctx->config};
+    case TAM_F_JMEAN:
+    case TAM_F_JMEAN_GLOBAL:
+    case TAM_F_TISSUE:
+    case TAM_F_Q: return {ni, 8, true};
+    case TAM_F_WATER: return {ni, 8, !ctx->config};
+    case TAM_F_THRESTIME: return {3 * ni, 8, true};
+    case TAM_F_MATERIAL: return {ni, 1, ctx->config};
+    default: return {0, 0, false};
+    }
+}
+
+int halo_scratch(tam_ctx *ctx)
+{
+    if (!ctx->d_halo) RC(dalloc_t(ctx, &ctx->d_halo, ctx->nh));
+    return TAM_OK;
+}
+
+}  // namespace
+
+// =====================================================================
+extern "C" {
+
+const char *tam_version(void) { return TAM_VERSION_STRING; }
+int tam_abi_version(void) { return TAM_ABI_VERSION; }
+
+int64_t tam_struct_size(int32_t which)
+{
+    switch (which) {
+    case 0: return (int64_t)sizeof(tam_params);
+    case 1: return (int64_t)sizeof(tam_config);
+    case 2: return (int64_t)sizeof(tam_state);
+    case 3: return (int64_t)sizeof(tam_material);
+    default: return -1;
+    }
+}
+
+int tam_params_default(tam_params *p)
+{
+    if (!p) return fail(nullptr, TAM_E_INVALID, "null params");
+    std::memset(p, 0, sizeof *p);
+    // res/input.params as shipped
+    p->nphotons = 125000;
+    p->xmax = 0.03;
+    p->ymax = 0.03;
+    p->zmax = 0.06;
+    p->n1 = 1.0;
+    p->n2 = 1.38;
+    p->total_time = 2.;
+    p->loops = 1;
+    p->repetition_rate_1 = 10000000.;
+    p->power = 70;
+    p->energy_per_pixel = 400;
+    p->ablate_temp = 500;
+    p->pulses_to_do = 1;
+    p->pulse_type = TAM_PULSE_GAUSSIAN;
+    p->nxg = p->nyg = p->nzg = 80;  // src/constants.f90:12
+    p->numproc = 1;
+    p->mode = TAM_MODE_REFERENCE;
+    p->precision = TAM_FP64;
+    p->device = 0;
+    return TAM_OK;
+}
+
+int tam_config_default(tam_config *c)
+{
+    if (!c) return fail(nullptr, TAM_E_INVALID, "null config");
+    std::memset(c, 0, sizeof *c);
+    c->nmat = 2;
+    c->mat[0] = tam_material{0.0, 0.0, 0.0, 1.0, 0.56, 1070.0, 3400.0};   // ablated: optics of air
+    c->mat[1] = tam_material{0.3, 100.0, 0.9, 1.38, 0.56, 1070.0, 3400.0};
+    c->n_ambient = 1.0;
+    c->source = TAM_SRC_GAUSSIAN;
+    c->source_radius = 0.1;
+    c->fresnel = 1;
+    c->roulette = 1;
+    c->roulette_w = 1e-4;
+    c->roulette_m = 10.0;
+    c->T0 = 310.15;
+    for (int f = 0; f < 6; ++f) {
+        c->bc_type[f] = TAM_BC_DIRICHLET;
+        c->bc_T[f] = 310.15;
+        c->bc_h[f] = 0.0;
+        c->bc_Tamb[f] = 298.15;
+    }
+    c->bc_type[5] = TAM_BC_ROBIN;  // beam face: convective, h = 10 W/m^2/K
+    c->bc_h[5] = 10.0;
+    c->dt_factor = 0.9;
+    c->dt = 0.0;
+    c->opscale = 1.0;
+    c->boil = 1;
+    c->T_boil = 373.15;
+    c->lw = LW;
+    c->T_abl = 373.15;
+    c->arrhenius = 1;
+    c->A = 3.1e98;
+    c->Ea = 6.28e5;
+    c->Rgas = 8.314;
+    c->T_lo = 43.0 + 273.15;
+    c->T_hi = 100.0 + 273.15;
+    c->thr[0] = 0.53;
+    c->thr[1] = 1.0;
+    c->thr[2] = 1.0e4;
+    c->retrace_fraction = 1e-3;
+    c->retrace_check = 50;
+    c->max_steps = 10000000;
+    return TAM_OK;
+}
+
+int tam_read_input_params(const char *path, tam_params *p)
+{
+    if (!path || !p) return fail(nullptr, TAM_E_INVALID, "null argument");
+    std::ifstream in(path);
+    if (!in) return fail(nullptr, TAM_E_IO, std::string("cannot open ") + path);
+    std::vector<std::string> toks;
+    std::string line;
+    while (toks.size() < 14 && std::getline(in, line)) {
+        size_t i = 0;
+        while (i < line.size() && (line[i] == ' ' || line[i] == '\t' || line[i] == '\r')) ++i;
+        if (i >= line.size()) continue;  // blank record: list-directed read moves on
+        if (line[i] == '/') { toks.push_back(""); continue; }  // slash: value left unchanged
+        size_t j = i;
+        if (line[i] == '\'' || line[i] == '"') {
+            const char q = line[i];
+            j = line.find(q, i + 1);
+            if (j == std::string::npos) j = line.size();
+            toks.push_back(line.substr(i + 1, j - i - 1));
+            continue;
+        }
+        while (j < line.size() && line[j] != ' ' && line[j] != '\t' && line[j] != ',' && line[j] != '/' &&
+               line[j] != '\r')
+            ++j;
+        toks.push_back(line.substr(i, j - i));
+    }
+    if (toks.size() < 14) return fail(nullptr, TAM_E_PARSE, "input.params: expected 14 values");
+    auto rd = [](const std::string &t, double &v) -> bool {
+        if (t.empty()) return true;
+        std::string s = t;
+        for (char &ch : s)
+            if (ch == 'd' || ch == 'D') ch = 'e';
+        char *end = nullptr;
+        const double x = std::strtod(s.c_str(), &end);
+        if (end == s.c_str() || *end != '\0') return false;
+        v = x;
+        return true;
+    };
+    auto ri = [](const std::string &t, auto &v) -> bool {
+        if (t.empty()) return true;
+        char *end = nullptr;
+        const long long x = std::strtoll(t.c_str(), &end, 10);
+        if (end == t.c_str() || *end != '\0') return false;
+        v = (std::remove_reference_t<decltype(v)>)x;
+        return true;
+    };
+    tam_params q = *p;
+    bool ok = ri(toks[0], q.nphotons) && rd(toks[1], q.xmax) && rd(toks[2], q.ymax) && rd(toks[3], q.zmax) &&
+              rd(toks[4], q.n1) && rd(toks[5], q.n2) && rd(toks[6], q.total_time) && ri(toks[7], q.loops) &&
+              rd(toks[8], q.repetition_rate_1) && rd(toks[9], q.power) && rd(toks[10], q.energy_per_pixel) &&
+              rd(toks[11], q.ablate_temp) && ri(toks[12], q.pulses_to_do);
+    if (!ok) return fail(nullptr, TAM_E_PARSE, "input.params: malformed numeric value");
+    std::string pt = toks[13];
+    for (char &ch : pt) ch = (char)std::tolower((unsigned char)ch);
+    if (pt == "gaussian") q.pulse_type = TAM_PULSE_GAUSSIAN;
+    else if (pt == "tophat") q.pulse_type = TAM_PULSE_TOPHAT;
+    else if (pt == "triangular") q.pulse_type = TAM_PULSE_TRIANGULAR;
+    else if (!pt.empty()) return fail(nullptr, TAM_E_PARSE, "input.params: no pulse type '" + toks[13] + "'");
+    *p = q;
+    return TAM_OK;
+}
+
+int tam_create(const tam_params *p, const tam_config *cfg, tam_ctx **out)
+{
+    if (!p || !out) return fail(nullptr, TAM_E_INVALID, "null argument");
+    *out = nullptr;
+    std::string why;
+    if (!validate_params(p, why)) return fail(nullptr, TAM_E_INVALID, why);
+    if (p->mode == TAM_MODE_CONFIG && !cfg) return fail(nullptr, TAM_E_INVALID, "config mode needs a tam_config");
+    if (cfg && p->mode == TAM_MODE_CONFIG) {
+        if (cfg->nmat < 1 || cfg->nmat > TAM_MAX_MATERIALS) return fail(nullptr, TAM_E_INVALID, "nmat out of range");
+        for (int m = 0; m < cfg->nmat; ++m) {
+            const tam_material &mm = cfg->mat[m];
+            if (mm.mua < 0 || mm.mus < 0 || !(mm.n > 0) || mm.g <= -1.0 || mm.g >= 1.0 || !(mm.k > 0) ||
+                !(mm.rho > 0) || !(mm.c > 0))
+                return fail(nullptr, TAM_E_INVALID, "material " + std::to_string(m) + " out of range");
+        }
+        if (!(cfg->n_ambient > 0) || !(cfg->source_radius > 0) || !(cfg->opscale > 0) ||
+            (cfg->dt <= 0 && !(cfg->dt_factor > 0)) || (cfg->roulette && !(cfg->roulette_m > 1.0)) ||
+            cfg->max_steps < 1 || (cfg->arrhenius && (!(cfg->A > 0) || !(cfg->Rgas > 0))))
+            return fail(nullptr, TAM_E_INVALID, "config value out of range");
+    }
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        (void)cudaGetLastError();
+        return fail(nullptr, TAM_E_NODEV, "no CUDA device");
+    }
+    if (p->device < 0 || p->device >= ndev) return fail(nullptr, TAM_E_INVALID, "device ordinal out of range");
+
+    tam_ctx *ctx = new tam_ctx();
+    ctx->p = *p;
+    ctx->config = p->mode == TAM_MODE_CONFIG;
+    if (ctx->config) ctx->cfg = *cfg;
+    ctx->fp64 = p->precision == TAM_FP64;
+    ctx->device = p->device;
+    ctx->nx = p->nxg;
+    ctx->ny = p->nyg;
+    ctx->nz = p->nzg;
+    ctx->ni = (int64_t)ctx->nx * ctx->ny * ctx->nz;
+    ctx->nh = (int64_t)(ctx->nx + 2) * (ctx->ny + 2) * (ctx->nz + 2);
+    auto bail = [&](int code) {
+        tam_destroy(ctx);
+        return code;
+    };
+    if (cudaSetDevice(ctx->device) != cudaSuccess) return bail(fail(nullptr, TAM_E_CUDA, "cudaSetDevice failed"));
+    cudaDeviceGetAttribute(&ctx->sm_count, cudaDevAttrMultiProcessorCount, ctx->device);
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+        return bail(fail(nullptr, TAM_E_CUDA, "cudaStreamCreate failed"));
+    ctx->own_stream = true;
+
+    int r = TAM_OK;
+#define AL(ptr, n) \
+    if (r == TAM_OK) r = dalloc_t(ctx, &(ptr), (n))
+    AL(ctx->d_err, 1);
+    AL(ctx->d_tally, tam::N_TALLY);
+    AL(ctx->d_work, 1);
+    AL(ctx->d_nabl, 1);
+    AL(ctx->d_cnt, 1);
+    AL(ctx->d_jmean, ctx->ni);
+    AL(ctx->d_sum, 1);
+    AL(ctx->d_tissue, ctx->ni);
+    AL(ctx->d_thres, 3 * ctx->ni);
+    if (!ctx->config) {
+        AL(ctx->d_jglob, ctx->ni);
+        AL(ctx->d_T[0], ctx->nh);
+        AL(ctx->d_T[1], ctx->nh);
+        AL(ctx->d_rk[0], ctx->nh);
+        AL(ctx->d_rk[1], ctx->nh);
+        AL(ctx->d_kappa, ctx->nh);
+        AL(ctx->d_density, ctx->nh);
+        AL(ctx->d_heatcap, ctx->nh);
+        AL(ctx->d_coeff, ctx->nh);
+        AL(ctx->d_alpha, ctx->nh);
+        AL(ctx->d_Q, ctx->ni);
+        AL(ctx->d_water, ctx->ni);
+    } else {
+        const size_t rs = ctx->fp64 ? 8 : 4;
+        for (int b = 0; b < 2 && r == TAM_OK; ++b) {
+            r = dalloc(ctx, &ctx->d_Tf[b], ctx->ni * rs);
+            if (r == TAM_OK && !ctx->fp64) r = dalloc_t(ctx, &ctx->d_Tc[b], ctx->ni);
+        }
+        if (r == TAM_OK) r = dalloc(ctx, &ctx->d_k, ctx->ni * rs);
+        if (r == TAM_OK) r = dalloc(ctx, &ctx->d_rho, ctx->ni * rs);
+        if (r == TAM_OK) r = dalloc(ctx, &ctx->d_c, ctx->ni * rs);
+        if (r == TAM_OK) r = dalloc(ctx, &ctx->d_J, ctx->ni * rs);
+        if (r == TAM_OK) r = dalloc(ctx, &ctx->d_Qf, ctx->ni * rs);
+        AL(ctx->d_mat, ctx->ni);
+    }
+#undef AL
+    if (r != TAM_OK) return bail(r);
+    if (cudaMemsetAsync(ctx->d_err, 0, sizeof(unsigned), ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(ctx->d_jmean, 0, ctx->ni * 8, ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(ctx->d_tissue, 0, ctx->ni * 8, ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(ctx->d_thres, 0, 3 * ctx->ni * 8, ctx->stream) != cudaSuccess ||
+        cudaMemsetAsync(ctx->d_tally, 0, tam::N_TALLY * 8, ctx->stream) != cudaSuccess)
+        return bail(fail(nullptr, TAM_E_CUDA, "initial memset failed"));
+    if (!ctx->config && cudaMemsetAsync(ctx->d_jglob, 0, ctx->ni * 8, ctx->stream) != cudaSuccess)
+        return bail(fail(nullptr, TAM_E_CUDA, "initial memset failed"));
+    // module Heat initial scalars (src/mcpolar.f90:66-73)
+    ctx->time = 0.;
+    ctx->pulseCount = 0.;
+    ctx->repetitionCount = 0.;
+    ctx->laserOn = 1.;
+    ctx->laser_flag = 1;
+    ctx->pulseFlag = 0;
+    ctx->pulsesDone = 0;
+    ctx->counter = 0;
+    r = ctx->config ? cfg_setup(ctx) : ref_setup(ctx);
+    if (r == TAM_OK) r = finish(ctx, "tam_create");
+    if (r != TAM_OK) {
+        g_thread_err = ctx->err;
+        return bail(r);
+    }
+    *out = ctx;
+    return TAM_OK;
+}
+
+int tam_destroy(tam_ctx *ctx)
+{
+    if (!ctx) return TAM_OK;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    for (void *p : ctx->allocs) cudaFree(p);
+    if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return TAM_OK;
+}
+
+const char *tam_last_error(const tam_ctx *ctx) { return ctx ? ctx->err.c_str() : g_thread_err.c_str(); }
+
+int tam_set_stream(tam_ctx *ctx, void *stream)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (stream) {
+        if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+        ctx->own_stream = false;
+        ctx->stream = (cudaStream_t)stream;
+    } else if (!ctx->own_stream) {
+        CK(cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking));
+        ctx->own_stream = true;
+    }
+    return TAM_OK;
+}
+
+int tam_device_errors(tam_ctx *ctx, uint32_t *bits)
+{
+    if (!ctx || !bits) return fail(ctx, TAM_E_INVALID, "null argument");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    unsigned b = 0;
+    CK(cudaMemcpy(&b, ctx->d_err, sizeof b, cudaMemcpyDeviceToHost));
+    *bits = b;
+    return TAM_OK;
+}
+
+int tam_init_opt(tam_ctx *ctx)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    if (ctx->config) return fail(ctx, TAM_E_STATE, "init_opt1 applies to reference mode");
+    ctx->hgg = 0.9;
+    ctx->g2 = ctx->hgg * ctx->hgg;
+    ctx->mu_water = 510.0;
+    ctx->mu_protein = 170.0;
+    ctx->mua = ctx->mu_water + ctx->mu_protein;
+    ctx->mus = 0.;
+    ctx->kappa_opt = ctx->mus + ctx->mua;
+    ctx->albedo = ctx->mus / ctx->kappa_opt;
+    return TAM_OK;
+}
+
+int tam_gridset(tam_ctx *ctx, double xmax, double ymax, double zmax)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    if (!(xmax > 0) || !(ymax > 0) || !(zmax > 0)) return fail(ctx, TAM_E_INVALID, "half-widths must be > 0");
+    CK(cudaSetDevice(ctx->device));
+    ctx->p.xmax = xmax;
+    ctx->p.ymax = ymax;
+    ctx->p.zmax = zmax;
+    if (ctx->config) {
+        RC(cfg_setup(ctx));
+    } else {
+        RC(tam_init_opt(ctx));
+        for (int b = 0; b < 2; ++b)
+            CK(tam::launch_fill_halo(ctx->d_rk[b], ctx->nx, ctx->ny, ctx->nz, ctx->kappa_opt, 0.0, 0.0, false,
+                                     ctx->stream));
+        ctx->rcur = 0;
+        ctx->delta = 1.e-8 * (2. * zmax / ctx->nz);
+    }
+    return finish(ctx, "tam_gridset");
+}
+
+int tam_init_thermal(tam_ctx *ctx, double *delt)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    CK(cudaSetDevice(ctx->device));
+    RC(ctx->config ? cfg_setup(ctx) : ref_setup(ctx));
+    RC(finish(ctx, "tam_init_thermal"));
+    if (delt) *delt = ctx->config ? ctx->cdt : ctx->delt;
+    return TAM_OK;
+}
+
+int tam_field_bytes(tam_ctx *ctx, int field, int64_t *nbytes)
+{
+    if (!ctx || !nbytes) return fail(ctx, TAM_E_INVALID, "null argument");
+    const FieldInfo fi = field_info(ctx, field);
+    if (!fi.ok) return fail(ctx, TAM_E_STATE, "field " + std::to_string(field) + " not available in this mode");
+    *nbytes = fi.count * fi.esize;
+    return TAM_OK;
+}
+
+int tam_upload(tam_ctx *ctx, int field, const void *host, int64_t nbytes)
+{
+    if (!ctx || !host) return fail(ctx, TAM_E_INVALID, "null argument");
+    const FieldInfo fi = field_info(ctx, field);
+    if (!fi.ok) return fail(ctx, TAM_E_STATE, "field " + std::to_string(field) + " not available in this mode");
+    if (nbytes != fi.count * fi.esize) return fail(ctx, TAM_E_INVALID, "size mismatch for field " + std::to_string(field));
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const size_t b = (size_t)nbytes;
+    auto h2d = [&](void *d) { return cudaMemcpyAsync(d, host, b, cudaMemcpyHostToDevice, s); };
+    if (!ctx->config) {
+        switch (field) {
+        case TAM_F_TEMP:
+            CK(h2d(ctx->d_T[0]));
+            CK(h2d(ctx->d_T[1]));
+            break;
+        case TAM_F_RHOKAP: {
+            // extinction is 0 or positive (the 6-neighbour test of src/3dFD.f90:347-349 relies on it)
+            const double *h = (const double *)host;
+            for (int64_t q = 0; q < ctx->nh; ++q)
+                if (!(h[q] >= 0.0) || !std::isfinite(h[q]))
+                    return fail(ctx, TAM_E_INVALID, "rhokap must be finite and >= 0");
+            CK(h2d(ctx->d_rk[0]));
+            CK(h2d(ctx->d_rk[1]));
+            break;
+        }
+        case TAM_F_JMEAN: CK(h2d(ctx->d_jmean)); break;
+        case TAM_F_JMEAN_GLOBAL: CK(h2d(ctx->d_jglob)); break;
+        case TAM_F_TISSUE: CK(h2d(ctx->d_tissue)); break;
+        case TAM_F_THRESTIME: CK(h2d(ctx->d_thres)); break;
+        case TAM_F_KAPPA: CK(h2d(ctx->d_kappa)); break;
+        case TAM_F_DENSITY: CK(h2d(ctx->d_density)); break;
+        case TAM_F_HEATCAP: CK(h2d(ctx->d_heatcap)); break;
+        case TAM_F_COEFF: CK(h2d(ctx->d_coeff)); break;
+        case TAM_F_ALPHA: CK(h2d(ctx->d_alpha)); break;
+        case TAM_F_Q: CK(h2d(ctx->d_Q)); break;
+        case TAM_F_WATER: CK(h2d(ctx->d_water)); break;
+        default: return fail(ctx, TAM_E_STATE, "field not uploadable");
+        }
+        return finish(ctx, "tam_upload");
+    }
+    // config mode: convert from the reference layout into the interior state
+    tam::FusedArgs a = fused_args(ctx);
+    switch (field) {
+    case TAM_F_TEMP:
+        RC(halo_scratch(ctx));
+        CK(cudaMemcpyAsync(ctx->d_halo, host, b, cudaMemcpyHostToDevice, s));
+        for (int q = 0; q < 2; ++q) {
+            a.T_out = ctx->d_Tf[q];
+            a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[q];
+            CK(tam::launch_fused_from_halo(a, ctx->fp64, ctx->d_halo, s));
+        }
+        break;
+    case TAM_F_KAPPA:
+    case TAM_F_DENSITY:
+    case TAM_F_HEATCAP: {
+        RC(halo_scratch(ctx));
+        CK(cudaMemcpyAsync(ctx->d_halo, host, b, cudaMemcpyHostToDevice, s));
+        void *dst = field == TAM_F_KAPPA ? ctx->d_k : (field == TAM_F_DENSITY ? ctx->d_rho : ctx->d_c);
+        CK(tam::launch_halo_to_interior(ctx->d_halo, dst, ctx->fp64, ctx->nx, ctx->ny, ctx->nz, s));
+        break;
+    }
+    case TAM_F_JMEAN: CK(h2d(ctx->d_jmean)); break;
+    case TAM_F_JMEAN_GLOBAL:
+    case TAM_F_Q: {
+        RC(halo_scratch(ctx));
+        CK(cudaMemcpyAsync(ctx->d_halo, host, b, cudaMemcpyHostToDevice, s));
+        CK(tam::launch_from_f64(ctx->d_halo, field == TAM_F_Q ? ctx->d_Qf : ctx->d_J, ctx->fp64, ctx->ni, s));
+        if (field == TAM_F_JMEAN_GLOBAL) ctx->need_trace = false;
+        break;
+    }
+    case TAM_F_TISSUE: CK(h2d(ctx->d_tissue)); break;
+    case TAM_F_THRESTIME: CK(h2d(ctx->d_thres)); break;
+    case TAM_F_MATERIAL:
+        CK(h2d(ctx->d_mat));
+        CK(tam::launch_props_from_mat(ctx->d_mat, ctx->cfg.nmat, ctx->lut, ctx->d_k, ctx->d_rho, ctx->d_c, ctx->fp64,
+                                      ctx->ni, s));
+        ctx->need_trace = true;
+        break;
+    default: return fail(ctx, TAM_E_STATE, "field not uploadable in config mode");
+    }
+    return finish(ctx, "tam_upload");
+}
+
+int tam_download(tam_ctx *ctx, int field, void *host, int64_t nbytes)
+{
+    if (!ctx || !host) return fail(ctx, TAM_E_INVALID, "null argument");
+    const FieldInfo fi = field_info(ctx, field);
+    if (!fi.ok) return fail(ctx, TAM_E_STATE, "field " + std::to_string(field) + " not available in this mode");
+    if (nbytes != fi.count * fi.esize) return fail(ctx, TAM_E_INVALID, "size mismatch for field " + std::to_string(field));
+    CK(cudaSetDevice(ctx->device));
+    cudaStream_t s = ctx->stream;
+    const size_t b = (size_t)nbytes;
+    auto d2h = [&](const void *d) { return cudaMemcpyAsync(host, d, b, cudaMemcpyDeviceToHost, s); };
+    if (!ctx->config) {
+        const void *src = nullptr;
+        switch (field) {
+        case TAM_F_TEMP: src = ctx->d_T[ctx->tcur]; break;
+        case TAM_F_RHOKAP: src = ctx->d_rk[ctx->rcur]; break;
+        case TAM_F_JMEAN: src = ctx->d_jmean; break;
+        case TAM_F_JMEAN_GLOBAL: src = ctx->d_jglob; break;
+        case TAM_F_TISSUE: src = ctx->d_tissue; break;
+        case TAM_F_THRESTIME: src = ctx->d_thres; break;
+        case TAM_F_KAPPA: src = ctx->d_kappa; break;
+        case TAM_F_DENSITY: src = ctx->d_density; break;
+        case TAM_F_HEATCAP: src = ctx->d_heatcap; break;
+        case TAM_F_COEFF: src = ctx->d_coeff; break;
+        case TAM_F_ALPHA: src = ctx->d_alpha; break;
+        case TAM_F_Q: src = ctx->d_Q; break;
+        case TAM_F_WATER: src = ctx->d_water; break;
+        default: return fail(ctx, TAM_E_STATE, "field not downloadable");
+        }
+        CK(d2h(src));
+        return finish(ctx, "tam_download");
+    }
+    tam::FusedArgs a = fused_args(ctx);
+    switch (field) {
+    case TAM_F_TEMP:
+        RC(halo_scratch(ctx));
+        CK(tam::launch_fused_to_halo(a, ctx->fp64, ctx->d_halo, s));
+        CK(d2h(ctx->d_halo));
+        break;
+    case TAM_F_RHOKAP:
+        RC(halo_scratch(ctx));
+        CK(tam::launch_rhokap_from_mat(ctx->d_mat, ctx->cfg.nmat, ctx->lut, ctx->d_halo, ctx->nx, ctx->ny, ctx->nz, s));
+        CK(d2h(ctx->d_halo));
+        break;
+    case TAM_F_KAPPA:
+    case TAM_F_DENSITY:
+    case TAM_F_HEATCAP: {
+        RC(halo_scratch(ctx));
+        const void *src = field == TAM_F_KAPPA ? ctx->d_k : (field == TAM_F_DENSITY ? ctx->d_rho : ctx->d_c);
+        CK(tam::launch_interior_to_halo(src, ctx->fp64, ctx->d_halo, ctx->nx, ctx->ny, ctx->nz, s));
+        CK(d2h(ctx->d_halo));
+        break;
+    }
+    case TAM_F_JMEAN: CK(d2h(ctx->d_jmean)); break;
+    case TAM_F_JMEAN_GLOBAL:
+    case TAM_F_Q:
+        RC(halo_scratch(ctx));
+        CK(tam::launch_to_f64(field == TAM_F_Q ? ctx->d_Qf : ctx->d_J, ctx->fp64, ctx->d_halo, ctx->ni, s));
+        CK(d2h(ctx->d_halo));
+        break;
+    case TAM_F_TISSUE: CK(d2h(ctx->d_tissue)); break;
+    case TAM_F_THRESTIME: CK(d2h(ctx->d_thres)); break;
+    case TAM_F_MATERIAL: CK(d2h(ctx->d_mat)); break;
+    default: return fail(ctx, TAM_E_STATE, "field not downloadable in config mode");
+    }
+    return finish(ctx, "tam_download");
+}
+
+int tam_mc_pass(tam_ctx *ctx, int64_t nphotons, uint64_t seed, uint32_t stream, double *jmean_out)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    if (nphotons < 0) return fail(ctx, TAM_E_INVALID, "nphotons must be >= 0");
+    CK(cudaSetDevice(ctx->device));
+    RC(mc_pass(ctx, nphotons, seed, stream));
+    if (ctx->config) {
+        unsigned long long nab = 0;
+        CK(cudaMemcpy(&nab, ctx->d_nabl, sizeof nab, cudaMemcpyDeviceToHost));
+        ctx->nabl_at_trace = (long long)nab;
+        ctx->need_trace = false;
+    }
+    if (jmean_out) return tam_download(ctx, TAM_F_JMEAN_GLOBAL, jmean_out, ctx->ni * 8);
+    return TAM_OK;
+}
+
+int tam_heat_steps(tam_ctx *ctx, int32_t nsteps, double *temp_out)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    if (nsteps < 0) return fail(ctx, TAM_E_INVALID, "nsteps must be >= 0");
+    CK(cudaSetDevice(ctx->device));
+    RC(ctx->config ? cfg_heat(ctx, nsteps) : ref_heat(ctx, nsteps));
+    RC(finish(ctx, "tam_heat_steps"));
+    if (temp_out) return tam_download(ctx, TAM_F_TEMP, temp_out, ctx->nh * 8);
+    return TAM_OK;
+}
+
+int tam_arrhenius(tam_ctx *ctx)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    if (ctx->config) return fail(ctx, TAM_E_STATE, "config mode fuses Arrhenius into tam_heat_steps");
+    CK(cudaSetDevice(ctx->device));
+    RC(ref_arrhenius(ctx));
+    return finish(ctx, "tam_arrhenius");
+}
+
+int tam_update_props(tam_ctx *ctx, double ablate_temp)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    if (ctx->config) return fail(ctx, TAM_E_STATE, "config mode fuses ablation into tam_heat_steps");
+    CK(cudaSetDevice(ctx->device));
+    RC(ref_props(ctx, ablate_temp));
+    return finish(ctx, "tam_update_props");
+}
+
+int tam_step_coupled(tam_ctx *ctx, int32_t n, uint64_t seed)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    if (n < 0) return fail(ctx, TAM_E_INVALID, "n must be >= 0");
+    CK(cudaSetDevice(ctx->device));
+    for (int32_t i = 0; i < n; ++i) RC(outer_iteration(ctx, seed));
+    return TAM_OK;
+}
+
+int tam_run(tam_ctx *ctx, uint64_t seed, int64_t max_iters, int64_t *iters)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    CK(cudaSetDevice(ctx->device));
+    int64_t it = 0;
+    while (ctx->time <= ctx->total_time) {
+        if (max_iters > 0 && it >= max_iters) break;
+        RC(outer_iteration(ctx, seed));
+        ++it;
+    }
+    if (iters) *iters = it;
+    return TAM_OK;
+}
+
+int tam_finalize(tam_ctx *ctx)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    CK(cudaSetDevice(ctx->device));
+    if (ctx->config) {
+        RC(halo_scratch(ctx));
+        CK(tam::launch_rhokap_from_mat(ctx->d_mat, ctx->cfg.nmat, ctx->lut, ctx->d_halo, ctx->nx, ctx->ny, ctx->nz,
+                                       ctx->stream));
+        CK(tam::launch_ref_finalize(ctx->nx, ctx->ny, ctx->nz, ctx->d_halo, ctx->d_tissue, ctx->stream));
+    } else {
+        CK(tam::launch_ref_finalize(ctx->nx, ctx->ny, ctx->nz, ctx->d_rk[ctx->rcur], ctx->d_tissue, ctx->stream));
+    }
+    return finish(ctx, "tam_finalize");
+}
+
+int tam_get_tallies(tam_ctx *ctx, double *absorbed, double *reflected, double *transmitted)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    const double n = ctx->last_n > 0 ? (double)ctx->last_n : 1.0;
+    if (absorbed) *absorbed = ctx->tally[tam::T_ABSORBED] / n;
+    if (reflected) *reflected = (ctx->tally[tam::T_SPECULAR] + ctx->tally[tam::T_REFLECTED]) / n;
+    if (transmitted) *transmitted = ctx->tally[tam::T_TRANSMITTED] / n;
+    return TAM_OK;
+}
+
+int tam_get_tallies_ex(tam_ctx *ctx, double *out, int32_t n)
+{
+    if (!ctx || !out || n < 0) return fail(ctx, TAM_E_INVALID, "bad argument");
+    const double np = ctx->last_n > 0 ? (double)ctx->last_n : 1.0;
+    for (int i = 0; i < n && i < tam::N_TALLY; ++i) {
+        const bool count = i == tam::T_STEPS || i == tam::T_SCATTERS || i == tam::T_OVERFLOW;
+        out[i] = count ? ctx->tally[i] : ctx->tally[i] / np;
+    }
+    return TAM_OK;
+}
+
+int tam_get_state(tam_ctx *ctx, tam_state *st)
+{
+    if (!ctx || !st) return fail(ctx, TAM_E_INVALID, "null argument");
+    std::memset(st, 0, sizeof *st);
+    st->time = ctx->time;
+    st->delt = ctx->config ? ctx->cdt : ctx->delt;
+    st->total_time = ctx->total_time;
+    st->pulse_count = ctx->pulseCount;
+    st->repetition_count = ctx->repetitionCount;
+    st->laser_on = ctx->laserOn;
+    st->pulse_length = ctx->pulseLength;
+    st->real_pulse_length = ctx->realPulseLength;
+    st->volume_voxel = ctx->volumeVoxel;
+    st->mass_voxel = ctx->massVoxel;
+    st->qvapor = ctx->QVapor;
+    st->dx = ctx->dx;
+    st->dy = ctx->dy;
+    st->dz = ctx->dz;
+    st->laser_flag = ctx->laser_flag;
+    st->pulse_flag = ctx->pulseFlag;
+    st->pulses_done = ctx->pulsesDone;
+    st->counter = ctx->counter;
+    st->mc_passes = ctx->mc_passes;
+    if (ctx->config) {
+        CK(cudaSetDevice(ctx->device));
+        CK(cudaStreamSynchronize(ctx->stream));
+        unsigned long long nab = 0;
+        CK(cudaMemcpy(&nab, ctx->d_nabl, sizeof nab, cudaMemcpyDeviceToHost));
+        st->n_ablated = (int64_t)nab;
+    }
+    return TAM_OK;
+}
+
+namespace {
+// str() of src/utils.f90:109-207: integers optionally zero-padded to len;
+// reals written with f100.16 and cut to their first len characters.
+std::string fstr_int(long long v, int len = 0)
+{
+    std::string s = std::to_string(v);
+    if (len > 0 && (int)s.size() < len) s = std::string(len - s.size(), '0') + s;
+    else if (len > 0 && (int)s.size() > len) s = s.substr(0, len);
+    return s;
+}
+std::string fstr_real(double v, int len)
+{
+    char buf[160];
+    std::snprintf(buf, sizeof buf, "%.16f", v);
+    std::string s(buf);
+    if ((int)s.size() > len) s = s.substr(0, len);
+    while (!s.empty() && s.back() == ' ') s.pop_back();
+    return s;
+}
+}  // namespace
+
+int tam_write_output(tam_ctx *ctx, const char *dir)
+{
+    if (!ctx || !dir) return fail(ctx, TAM_E_INVALID, "null argument");
+    const tam_params &p = ctx->p;
+    const std::string tail = fstr_int((long long)p.power) + "w-" + fstr_int(ctx->nz) + "-" +
+                             fstr_real(p.ablate_temp, 3) + "-" + fstr_int((long long)p.energy_per_pixel, 3) + "-" +
+                             fstr_real(p.xmax, 5) + "-" + fstr_real(p.ymax, 5) + "-" + fstr_real(p.zmax, 5) + ".dat";
+    std::string base(dir);
+    if (!base.empty() && base.back() != '/') base += '/';
+    auto put = [&](const std::string &name, const std::vector<double> &v) -> int {
+        FILE *f = std::fopen((base + name).c_str(), "wb");
+        if (!f) return fail(ctx, TAM_E_IO, "cannot write " + base + name);
+        const size_t w = std::fwrite(v.data(), sizeof(double), v.size(), f);
+        std::fclose(f);
+        if (w != v.size()) return fail(ctx, TAM_E_IO, "short write " + base + name);
+        return TAM_OK;
+    };
+    const int64_t ni = ctx->ni, nh = ctx->nh;
+    std::vector<double> a((size_t)nh), b((size_t)ni);
+    RC(tam_download(ctx, TAM_F_JMEAN_GLOBAL, b.data(), ni * 8));
+    RC(put("jmean-t" + tail, b));
+    RC(tam_download(ctx, TAM_F_RHOKAP, a.data(), nh * 8));
+    for (int k = 1; k <= ctx->nz; ++k)
+        for (int j = 1; j <= ctx->ny; ++j)
+            for (int i = 1; i <= ctx->nx; ++i)
+                b[(size_t)((i - 1) + (int64_t)ctx->nx * ((j - 1) + (int64_t)ctx->ny * (k - 1)))] =
+                    a[(size_t)(i + (int64_t)(ctx->nx + 2) * (j + (int64_t)(ctx->ny + 2) * k))];
+    RC(put("rhokap-t" + tail, b));
+    RC(tam_download(ctx, TAM_F_TEMP, a.data(), nh * 8));
+    for (auto &x : a) x -= 273.0;
+    RC(put("temp-t" + tail, a));
+    if (ctx->config) std::fill(b.begin(), b.end(), 0.0);
+    else RC(tam_download(ctx, TAM_F_WATER, b.data(), ni * 8));
+    RC(put("water-t" + tail, b));
+    RC(tam_download(ctx, TAM_F_TISSUE, b.data(), ni * 8));
+    RC(put("tissue-t" + tail, b));
+    std::vector<double> t3((size_t)(3 * ni));
+    RC(tam_download(ctx, TAM_F_THRESTIME, t3.data(), 3 * ni * 8));
+    for (int q = 0; q < 3; ++q) {
+        std::vector<double> t(t3.begin() + q * ni, t3.begin() + (q + 1) * ni);
+        RC(put("time-t-" + std::to_string(q + 1) + "-" + tail, t));
+    }
+    return TAM_OK;
+}
+
+int tam_selftest_philox(const uint32_t *in, uint32_t *out_mine, uint32_t *out_curand, int64_t n)
+{
+    tam_ctx *ctx = nullptr;
+    if (!in || !out_mine || !out_curand || n < 0) return fail(nullptr, TAM_E_INVALID, "bad argument");
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        (void)cudaGetLastError();
+        return fail(nullptr, TAM_E_NODEV, "no CUDA device");
+    }
+    if (n == 0) return TAM_OK;
+    uint32_t *d_in = nullptr, *d_a = nullptr, *d_b = nullptr;
+    CK(cudaMalloc(&d_in, n * 6 * sizeof(uint32_t)));
+    cudaError_t e = cudaMalloc(&d_a, n * 4 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&d_b, n * 4 * sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMemcpy(d_in, in, n * 6 * sizeof(uint32_t), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = tam::launch_philox_selftest(d_in, d_a, d_b, n, nullptr);
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e == cudaSuccess) e = cudaMemcpy(out_mine, d_a, n * 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(out_curand, d_b, n * 4 * sizeof(uint32_t), cudaMemcpyDeviceToHost);
+    cudaFree(d_in);
+    cudaFree(d_a);
+    cudaFree(d_b);
+    if (e != cudaSuccess) return fail(nullptr, TAM_E_CUDA, cudaGetErrorString(e));
+    return TAM_OK;
+}
+
+}  // extern "C"

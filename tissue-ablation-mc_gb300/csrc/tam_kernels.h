@@ -1,0 +1,137 @@
+// tam_kernels.h -- argument blocks and launchers of the sm_103a kernels.
+// Host-only declarations (no device code), included by the C-ABI layer.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace tam {
+
+constexpr int MAX_MAT = 16;
+
+enum Medium : int32_t { MED_RHOKAP = 0, MED_MATERIAL = 1 };
+enum Source : int32_t { SRC_DISK = 0, SRC_GAUSSIAN = 1 };
+
+// Tally slots (double), same order as the oracle's ORC_T_*.
+enum Tally : int {
+    T_ABSORBED = 0, T_SPECULAR, T_REFLECTED, T_TRANSMITTED, T_SIDE, T_ROULETTE_NET, T_MISSED,
+    T_STEPS, T_SCATTERS, T_OVERFLOW, N_TALLY
+};
+
+struct OptMat {
+    double mua, mus, g, n;
+};
+
+// One transport pass (packets [p0, p0 + n)).
+struct TransportArgs {
+    int32_t nx, ny, nz;
+    double xmax, ymax, zmax;          // half-widths, cm
+    int32_t medium;                   // Medium
+    const double *rhokap;             // halo (nx+2)(ny+2)(nz+2), MED_RHOKAP
+    const uint8_t *mat;               // interior nx*ny*nz, MED_MATERIAL
+    int32_t nmat;
+    OptMat lut[MAX_MAT];
+    double rhokap_n;                  // refractive index of the rhokap medium
+    double n_ambient;
+    int32_t source;                   // Source
+    double source_radius;             // cm
+    int32_t fresnel, roulette;
+    double roulette_w, roulette_m;
+    uint64_t seed;
+    uint32_t stream;
+    int64_t p0, n;
+    int64_t max_steps;
+    double nudge;                     // offset past a crossed face (reference delta), 0 in config mode
+    double *jmean;                    // interior, packet units (sum of w*d*mua)
+    double *tally;                    // N_TALLY doubles
+    unsigned long long *work;         // dynamic packet counter (zeroed by the launcher)
+    unsigned *err;                    // device error word
+};
+
+// Launch the transport kernel in FP32 (fp64 == false) or FP64.
+cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cudaStream_t s);
+
+// out[q] = in[q] * f for q < n; in is then zeroed when zero_in is set.
+cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s);
+cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s);
+
+// Philox self-test: out_mine / out_curand hold 4 words per input; in holds 6
+// words per input {c0, c1, c2, c3, k0, k1}.
+cudaError_t launch_philox_selftest(const uint32_t *in, uint32_t *out_mine, uint32_t *out_curand, int64_t n,
+                                   cudaStream_t s);
+
+// ---------------------------------------------- reference-mode heat path --
+// Scalars of module Heat (src/3dFD.f90:7-12) needed on the device.
+struct RefHeatArgs {
+    int32_t nx, ny, nz;
+    double idx2, idy2, idz2;          // 1/dx^2 etc (dx = 2 max 1e-2 / (n+2))
+    double delt, laserOn, vvox, mvox, qvapor;
+    const double *t0;                 // halo, read
+    double *tn;                       // halo, written (interior)
+    const double *kappa, *density, *heatcap, *coeff; // halo
+    const double *J;                  // interior jmeanGLOBAL
+    double *Q;                        // interior
+    unsigned *err;
+};
+cudaError_t launch_ref_stencil(const RefHeatArgs &a, cudaStream_t s);
+
+struct RefArrheniusArgs {
+    int32_t nx, ny, nz;
+    double delt, time;
+    const double *temp, *rhokap;      // halo
+    double *tissue, *thres;           // interior, interior x 3
+};
+cudaError_t launch_ref_arrhenius(const RefArrheniusArgs &a, cudaStream_t s);
+
+struct RefPropsArgs {
+    int32_t nx, ny, nz;
+    double ablate_temp, delt, qvapor, mu_water, mu_protein;
+    const double *temp;               // halo
+    const double *rk_old;             // halo
+    double *rk_new;                   // halo (interior written)
+    double *kappa, *density, *heatcap, *coeff, *alpha; // halo
+    const double *Q;                  // interior
+    double *water;                    // interior
+    unsigned *err;
+};
+cudaError_t launch_ref_props(const RefPropsArgs &a, cudaStream_t s);
+
+// tissue(rhokap <= 0.1) = -1 (src/mcpolar.f90:196-204)
+cudaError_t launch_ref_finalize(int nx, int ny, int nz, const double *rhokap, double *tissue, cudaStream_t s);
+
+// --------------------------------------------------- fused config-mode step --
+enum Bc : int32_t { BC_DIRICHLET = 0, BC_ROBIN = 1 };
+
+struct FusedArgs {
+    int32_t nx, ny, nz;
+    double dx, dy, dz;                // m
+    double opscale, dt, vvox;
+    int32_t boil;
+    double T_boil, lw, T_abl;
+    int32_t arrhenius;
+    double lnA, Ea, Rgas, T_lo, T_hi, thr[3];
+    int32_t bc_type[6];
+    double bc_T[6], bc_h[6], bc_Tamb[6];
+    double P;                         // source multiplier for this step
+    double t_new;                     // time stamp of this step's end
+    const void *T_in;                 // interior, Real
+    void *T_out;
+    const float *Tc_in;               // Kahan compensation (FP32 form only)
+    float *Tc_out;
+    const void *k, *rho, *c;          // Real
+    void *J, *Q;                      // Real
+    double *omega, *thres;
+    uint8_t *mat;
+    unsigned long long *n_ablated;    // running count
+    unsigned *err;
+};
+// fp64 == false: FP32 storage with Kahan compensation; true: plain FP64.
+cudaError_t launch_fused_step(const FusedArgs &a, bool fp64, cudaStream_t s);
+
+// Halo (reference-layout) FP64 temperature from the interior state, with
+// ghosts filled from the boundary conditions.
+cudaError_t launch_fused_to_halo(const FusedArgs &a, bool fp64, double *halo, cudaStream_t s);
+// Interior Real state from a halo FP64 temperature (Tc zeroed).
+cudaError_t launch_fused_from_halo(const FusedArgs &a, bool fp64, const double *halo, cudaStream_t s);
+
+}  // namespace tam
