@@ -131,8 +131,8 @@ def test_ref_props_fp64_matches_sequential_sweep(tam, orc, zero_p):
 
 # --------------------------------------------------- reference transport --
 def test_ref_mc_fp64_matches_oracle_same_streams(tam, orc):
-    ctx, o = ref_pair(tam, orc, 80, 80, 80)
     n = 60000
+    ctx, o = ref_pair(tam, orc, 80, 80, 80, nphotons=n)  # normalisation divides by nphotons*numproc
     J = ctx.mc_pass(n, seed=12345, stream=3, want=True)
     o.photons(n, seed=12345, stream=3, nthreads=0)
     o.normalise()
@@ -147,11 +147,13 @@ def test_ref_mc_fp64_matches_oracle_same_streams(tam, orc):
     o.close()
 
 
-def _batches_gpu(ctx, n, nb, seed, stream0=0):
+def _batches_gpu(ctx, n, nb, seed, stream0=0, tallies=None):
     out = []
     for b in range(nb):
         ctx.mc_pass(n, seed=seed, stream=stream0 + b)
         out.append(ctx.download(F.TAM_F_JMEAN) / n)
+        if tallies is not None:
+            tallies.append(ctx.tallies())
     return np.array(out)
 
 
@@ -241,14 +243,17 @@ def test_config_mc_fp32_vs_fp64_statistical(tam, orc):
     c64, _ = cfg_pair(tam, orc, 24, 24, 24, 0.5, precision=0)
     c32, _ = cfg_pair(tam, orc, 24, 24, 24, 0.5, precision=1)
     nb, n = 16, 2000
-    a = _batches_gpu(c64, n, nb, seed=3)
-    b = _batches_gpu(c32, n, nb, seed=3, stream0=100)
+    ta, tb = [], []
+    a = _batches_gpu(c64, n, nb, seed=3, tallies=ta)
+    b = _batches_gpu(c32, n, nb, seed=3, stream0=100, tallies=tb)
     ok, nsig, ma, mb = _stat_compare(a, b, min_signal=1e-5)
     assert nsig > 300
     assert ok >= 0.99, ok
-    assert abs(ma.sum() - mb.sum()) / mb.sum() < 0.03
-    t64, t32 = c64.tallies(), c32.tallies()
-    assert abs(t64["reflected"] - t32["reflected"]) < 0.03
+    for k in ("absorbed", "reflected", "transmitted", "side"):
+        xa = np.array([t[k] for t in ta])
+        xb = np.array([t[k] for t in tb])
+        se = math.hypot(xa.std(ddof=1), xb.std(ddof=1)) / math.sqrt(nb)
+        assert abs(xa.mean() - xb.mean()) < 4 * se + 1e-6, (k, xa.mean(), xb.mean(), se)
     c64.close()
     c32.close()
 
@@ -314,9 +319,11 @@ def test_fused_fp32_kahan_within_1mK_of_fp64(tam, orc):
 
 # ------------------------------------------------------- coupled driver --
 def test_coupled_reference_matches_oracle(tam, orc):
-    kw = dict(nphotons=3000, power=70.0, ablate_temp=60.0, pulse_type=1)
+    # tophat at 8 W heats the beam column to the 100 C latent-heat clamp within a
+    # few iterations, so Q, water content, rhokap and the MC source all feed back
+    kw = dict(nphotons=3000, power=8.0, pulse_type=1)
     ctx, o = ref_pair(tam, orc, 16, 16, 16, **kw)
-    for it in range(6):
+    for it in range(12):
         ctx.step_coupled(1, seed=2024)
         assert o.outer_iteration(2024, nthreads=0) == 0
     np.testing.assert_allclose(ctx.download(F.TAM_F_JMEAN_GLOBAL), o.arr("jmeanGLOBAL"), rtol=1e-9,
@@ -325,6 +332,9 @@ def test_coupled_reference_matches_oracle(tam, orc):
     np.testing.assert_allclose(ctx.download(F.TAM_F_TEMP), To, rtol=1e-10, atol=0)
     np.testing.assert_allclose(ctx.download(F.TAM_F_TISSUE), o.arr("tissue"), rtol=1e-8, atol=1e-300)
     np.testing.assert_array_equal(ctx.download(F.TAM_F_RHOKAP) == 0, o.arr("rhokap") == 0)
+    np.testing.assert_allclose(ctx.download(F.TAM_F_RHOKAP), o.arr("rhokap"), rtol=1e-10)
+    np.testing.assert_allclose(ctx.download(F.TAM_F_Q), o.arr("Q"), rtol=1e-9, atol=1e-9 * o.st.QVapor)
+    assert o.arr("Q").max() > 0 and o.arr("temp").max() >= 373.0
     st = ctx.state()
     assert st.counter == o.st.counter and st.time == o.st.time
     ctx.close()
