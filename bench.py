@@ -1,0 +1,480 @@
+#!/usr/bin/env python3
+"""Benchmark of the two hot paths on the 200^3 precision-form workload.
+
+Workload (one "step"): a homogeneous 1 x 1 x 1 cm tissue cube on a 200^3
+grid (mua 0.3 /cm, mus 100 /cm, g 0.9, n 1.38 in air), a collimated Gaussian
+beam of 1/e^2 radius 0.1 cm with Fresnel faces and Russian roulette at 1e-4:
+one MC pass of 1e8 packets (FP32 transport, FP64 tally), then 2 s of heating
+at 2 W as 821 fused FP32 + Kahan heat steps (dt = 0.9 x the stability limit,
+convective beam face h = 10 W/m^2/K, other faces at 37 C, Arrhenius damage
+A = 3.1e98 /s, Ea = 6.28e5 J/mol, optics ablated above 100 C).  Inputs are
+synthetic (built from these parameters); the working set (~0.4 GB) is larger
+than L2, so no L2 flush is needed between steps.
+
+value   : photons/s of transport + heat (packets per step / step time),
+          inputs resident on the device, CUDA events on the library's stream.
+e2e     : the same through the C ABI with pinned host buffers: every step
+          uploads the material grid and the initial temperature and reads back
+          temperature, damage and the absorbed-power field.
+roofline: the dominant kernel (transport): 12 B per voxel step (rhokap /
+          material read + FP64 tally read-modify-write) against the measured
+          HBM copy bandwidth; the stencil's 36 B per voxel update likewise.
+
+--impl reference runs the CPU oracle (the C restatement of the reference,
+OpenMP on all host cores) on a bounded sample of the same workload, scaled to
+the same metric.  With --gpus N > 1 every rank runs an independent replica
+(the path has no exchange step on one instance).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "tissue-ablation-mc_gb300"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+METRIC = "photons/s & voxel-updates/s, FP32 vs FP64 GPU at stated error; %HBM roofline"
+GRID = 200
+HALF = 0.5
+PACKETS = 100_000_000
+POWER = 2.0
+SIM_TIME = 2.0
+B_TRANSPORT = 12.0   # bytes per voxel step
+B_STENCIL32 = 36.0   # bytes per voxel update, FP32 + Kahan
+B_STENCIL64 = 56.0   # bytes per voxel update, FP64 plain
+SEED = 20251203
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def make_ctx(tam, precision, grid=GRID, packets=PACKETS, device=0):
+    p = tam.default_params(nxg=grid, nyg=grid, nzg=grid, xmax=HALF, ymax=HALF, zmax=HALF, mode=1,
+                           precision=precision, nphotons=packets, pulse_type=1, power=POWER,
+                           energy_per_pixel=POWER * SIM_TIME * 1e3, total_time=SIM_TIME, loops=1, device=device)
+    c = tam.default_config()  # the tissue, beam and boundary values above are the config defaults
+    c.retrace_fraction = 0.0  # one MC pass per step (no ablation re-trace inside the timed step)
+    return tam.Context(p, c)
+
+
+def heat_steps_for(ctx):
+    dt = ctx.state().delt
+    return int(math.ceil(SIM_TIME / dt - 1e-9))
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", str(self.device)], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for ln in self.proc.stdout:
+            self.lines.append(ln.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[4:8]):
+                if v.lower() in ("active", "0x1", "1"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ------------------------------------------------------------ GPU arm --
+def run_gpu(args):
+    import numpy as np
+    import torch
+
+    import tam_gb300 as tam
+
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    packets = args.packets
+    ctx = make_ctx(tam, tam._abi.TAM_FP32, packets=packets, device=local)
+    stream = torch.cuda.Stream(device=local)
+    ctx.set_stream(stream.cuda_stream)
+    nsteps = args.heat_steps if args.heat_steps > 0 else heat_steps_for(ctx)
+    nvox = GRID ** 3
+
+    def one_step(i):
+        ctx.init_thermal()                          # device-side reset of the instance
+        ctx.mc_pass(packets, seed=SEED, stream=i)   # transport + normalisation
+        ctx.heat_steps(nsteps)                      # fused stencil + Arrhenius + ablation
+
+    for i in range(args.warmup):
+        one_step(1000 + i)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    l0 = tam.kernel_launches()
+    t_tr, t_heat, vsteps = [], [], []
+    with Clocks(local) as clk:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for i in range(args.steps):
+            one_step(i)
+            tr, hm, _ = ctx.timing()
+            t_tr.append(tr)
+            t_heat.append(hm)
+            vsteps.append(ctx.tallies()["voxel_steps"])
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    launches = tam.kernel_launches() - l0
+    ms = ev0.elapsed_time(ev1)
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * packets * args.steps / (ms * 1e-3)
+    tr_ms = statistics.mean(t_tr)
+    heat_ms = statistics.mean(t_heat)
+    vs = statistics.mean(vsteps)
+    hbm, peak_kind = peaks()
+
+    # ---- end to end through the C ABI with pinned host buffers ----
+    mat_h = torch.ones((nvox,), dtype=torch.uint8).pin_memory().numpy()
+    temp_h = torch.full(((GRID + 2) ** 3,), 310.15, dtype=torch.float64).pin_memory().numpy()
+    out_T = torch.empty(((GRID + 2) ** 3,), dtype=torch.float64).pin_memory().numpy()
+    out_O = torch.empty((nvox,), dtype=torch.float64).pin_memory().numpy()
+    out_J = torch.empty((nvox,), dtype=torch.float64).pin_memory().numpy()
+    import ctypes as C
+
+    L = tam._abi.load()
+    h = ctx._h
+
+    def vp(a):
+        return a.ctypes.data_as(C.c_void_p)
+
+    def e2e_step(i):
+        tam.api.check(L.tam_init_thermal(h, None), h)
+        tam.api.check(L.tam_upload(h, tam.TAM_F_MATERIAL, vp(mat_h), mat_h.nbytes), h)
+        tam.api.check(L.tam_upload(h, tam.TAM_F_TEMP, vp(temp_h), temp_h.nbytes), h)
+        tam.api.check(L.tam_mc_pass(h, packets, SEED, i, None), h)
+        tam.api.check(L.tam_heat_steps(h, nsteps, None), h)
+        tam.api.check(L.tam_download(h, tam.TAM_F_TEMP, vp(out_T), out_T.nbytes), h)
+        tam.api.check(L.tam_download(h, tam.TAM_F_TISSUE, vp(out_O), out_O.nbytes), h)
+        tam.api.check(L.tam_download(h, tam.TAM_F_JMEAN_GLOBAL, vp(out_J), out_J.nbytes), h)
+
+    e2e_step(2000)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    w0 = time.perf_counter()
+    ev0.record(stream)
+    for i in range(args.steps):
+        e2e_step(i)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = ev0.elapsed_time(ev1)
+    e2e_wall = (time.perf_counter() - w0) * 1e3
+    e2e_ms = max(e2e_ms, e2e_wall)
+    if dist:
+        t = torch.tensor([e2e_ms], device=f"cuda:{local}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_ms = float(t.item())
+    e2e_val = world * packets * args.steps / (e2e_ms * 1e-3)
+    h2d = mat_h.nbytes + temp_h.nbytes
+    d2h = out_T.nbytes + out_O.nbytes + out_J.nbytes
+
+    # ---- FP64 GPU form on identical Philox streams + stated error ----
+    fp64 = None
+    if rank == 0 and not args.no_fp64:
+        n64 = args.fp64_packets
+        c64 = make_ctx(tam, tam._abi.TAM_FP64, packets=n64, device=local)
+        c64.set_stream(stream.cuda_stream)
+        c64.mc_pass(n64, seed=SEED, stream=7)     # warm-up
+        c64.mc_pass(n64, seed=SEED, stream=7)
+        tr64, _, _ = c64.timing()
+        J64 = c64.download(tam.TAM_F_JMEAN_GLOBAL)
+        ctx.init_thermal()
+        ctx.mc_pass(n64, seed=SEED, stream=7)
+        J32 = ctx.download(tam.TAM_F_JMEAN_GLOBAL)
+        fl_err = float(np.abs(J32 - J64).sum() / np.abs(J64).sum())
+        # identical source for the heat comparison
+        c64.init_thermal()
+        c64.upload(tam.TAM_F_JMEAN_GLOBAL, J64)
+        c64.heat_steps(nsteps)
+        _, heat64_ms, _ = c64.timing()
+        T64 = c64.download(tam.TAM_F_TEMP)
+        O64 = c64.download(tam.TAM_F_TISSUE)
+        ctx.init_thermal()
+        ctx.upload(tam.TAM_F_JMEAN_GLOBAL, J64)
+        ctx.heat_steps(nsteps)
+        T32 = ctx.download(tam.TAM_F_TEMP)
+        O32 = ctx.download(tam.TAM_F_TISSUE)
+        c64.close()
+        t_fp64_step = tr64 * (packets / n64) + heat64_ms
+        fp64 = {
+            "photons_per_s": packets / (t_fp64_step * 1e-3),
+            "transport_photons_per_s": n64 / (tr64 * 1e-3),
+            "voxel_updates_per_s": nvox * nsteps / (heat64_ms * 1e-3),
+            "sample": f"{n64} packets timed, scaled to {packets}; full {nsteps} heat steps",
+            "fp32_speedup": value / (packets / (t_fp64_step * 1e-3)),
+            "error_fp32_vs_fp64": {
+                "relative_fluence_l1": fl_err,
+                "max_abs_dT_K": float(np.abs(T32 - T64).max()),
+                "max_T_rise_K": float(T64.max() - 310.15),
+                "max_abs_dOmega": float(np.abs(O32 - O64).max()),
+                "max_Omega": float(O64.max()),
+            },
+        }
+
+    # ---- CPU baseline (oracle port, all host cores) ----
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        cpu = cpu_measure(args.cpu_seconds)
+
+    ctx.close()
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    clk_s = clk.summary()
+    line = {
+        "metric": METRIC,
+        "value": value,
+        "unit": "photons/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": ms / args.steps,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32 transport + f64 tally; f32+Kahan stencil, f64 Arrhenius exponent",
+        "data": "synthetic (homogeneous tissue cube built from the workload parameters)",
+        "config": {
+            "workload": f"precision form: {GRID}^3 homogeneous cube 1x1x1 cm, {packets:.0e} packets "
+                        f"(Gaussian beam w=0.1 cm, Fresnel, roulette 1e-4) + {nsteps} fused FP32 heat steps "
+                        f"(2 W for 2 s, Arrhenius, ablation at 100 C)",
+            "grid": [GRID, GRID, GRID],
+            "packets_per_step": packets,
+            "heat_steps_per_step": nsteps,
+            "l2": "inputs larger than L2 (working set ~0.4 GB); no flush",
+            "parallelism": f"replicas x{world}",
+        },
+        "voxel_updates_per_s": world * nvox * nsteps / (heat_ms * 1e-3),
+        "transport": {
+            "photons_per_s": world * packets / (tr_ms * 1e-3),
+            "voxel_steps_per_packet": vs / packets,
+            "voxel_steps_per_s": world * vs / (tr_ms * 1e-3),
+            "kernel_ms": tr_ms,
+        },
+        "heat": {"ms_per_step_segment": heat_ms, "ms_per_heat_step": heat_ms / nsteps},
+        "roofline": {
+            "bound": "hbm",
+            "kernel": "transport_kernel<float, material>",
+            "achieved": B_TRANSPORT * vs / (tr_ms * 1e-3) / 1e9,
+            "peak": hbm,
+            "unit": "GB/s",
+            "frac": B_TRANSPORT * vs / (tr_ms * 1e-3) / 1e9 / hbm,
+            "traffic": None,
+            "bytes_per_unit": f"{B_TRANSPORT:g} B per voxel step; {vs / packets:.1f} voxel steps per packet",
+            "peak_kind": peak_kind,
+            "note": "transport is issue/latency bound (divergent random walks, L2-resident atomics), not HBM bound",
+        },
+        "roofline_stencil": {
+            "bound": "hbm",
+            "kernel": "fused_kernel<float, kahan>",
+            "achieved": B_STENCIL32 * nvox * nsteps / (heat_ms * 1e-3) / 1e9,
+            "peak": hbm,
+            "unit": "GB/s",
+            "frac": B_STENCIL32 * nvox * nsteps / (heat_ms * 1e-3) / 1e9 / hbm,
+            "bytes_per_unit": f"{B_STENCIL32:g} B per voxel update",
+            "peak_kind": peak_kind,
+        },
+        "e2e": {"value": e2e_val, "unit": "photons/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": launches,
+        "clocks": clk_s,
+        "fp64": fp64,
+        "cpu_baseline": cpu,
+    }
+    traffic = profile_traffic(vs)
+    if traffic is not None:
+        line["roofline"]["traffic"] = traffic
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def profile_traffic(voxel_steps):
+    """DRAM bytes of one full transport launch, scaled from the committed ncu summary."""
+    path = os.path.join(ROOT, "profiles", "transport_c2.txt")
+    try:
+        for ln in open(path):
+            if ln.startswith("dram_bytes_per_voxel_step:"):
+                return float(ln.split(":")[1]) * voxel_steps
+    except OSError:
+        pass
+    return None
+
+
+# ------------------------------------------------------- CPU (oracle) --
+def cpu_measure(seconds, threads=0):
+    """Oracle port (C, FP64, OpenMP) on a bounded sample of the workload,
+    scaled to photons/s of transport + heat for the full step."""
+    import numpy as np
+
+    import build_oracle
+
+    build_oracle.build()
+    import oracle as orc
+
+    ncores = threads or os.cpu_count() or 1
+    mats = [(0.0, 0.0, 0.0, 1.0), (0.3, 100.0, 0.9, 1.38)]
+    d = orc.mc_desc(GRID, GRID, GRID, HALF, HALF, HALF, materials=mats, source_radius=0.1)
+    grid = np.ones((GRID, GRID, GRID), dtype=np.uint8, order="F")
+    # calibrate the packet sample to about half the budget
+    n = 2000
+    t0 = time.perf_counter()
+    orc.mc_transport(d, grid, n, seed=SEED, nthreads=ncores)
+    t_cal = time.perf_counter() - t0
+    n_mc = max(2000, int(n * (0.5 * seconds) / max(t_cal, 1e-3)))
+    t0 = time.perf_counter()
+    _, tal = orc.mc_transport(d, grid, n_mc, seed=SEED, stream=1, nthreads=ncores)
+    t_mc = time.perf_counter() - t0
+    dxm = 2 * HALF * 1e-2 / GRID
+    alpha = 0.56 / (1070 * 3400)
+    h = orc.heat_desc(GRID, GRID, GRID, dxm, dxm, dxm, dt=0.9 * dxm * dxm / (6 * alpha))
+    nsteps = int(math.ceil(SIM_TIME / h.dt - 1e-9))
+    sh = (GRID, GRID, GRID)
+    T = np.full(sh, 310.15, order="F")
+    k = np.full(sh, 0.56, order="F")
+    rho = np.full(sh, 1070.0, order="F")
+    c = np.full(sh, 3400.0, order="F")
+    J = np.asfortranarray(np.random.default_rng(0).uniform(0, 1e6, sh))
+    Q = np.zeros(sh, order="F")
+    om = np.zeros(sh, order="F")
+    thr = np.zeros(sh + (3,), order="F")
+    mat = np.ones(sh, dtype=np.uint8, order="F")
+    t0 = time.perf_counter()
+    s = 0
+    while s < 2 or (time.perf_counter() - t0) < 0.4 * seconds:
+        T, _ = orc.fused_step(h, POWER, (s + 1) * h.dt, T, k, rho, c, J, Q, om, thr, mat, nthreads=ncores)
+        s += 1
+    t_heat = time.perf_counter() - t0
+    t_step = t_mc * (PACKETS / n_mc) + t_heat * (nsteps / s)
+    return {
+        "value": PACKETS / t_step,
+        "unit": "photons/s",
+        "cores": ncores,
+        "kind": "port",
+        "sample": f"{n_mc} packets ({t_mc:.1f} s) and {s} of {nsteps} heat steps ({t_heat:.1f} s) of the "
+                  f"{GRID}^3 workload, FP64 oracle on {ncores} threads, scaled linearly to {PACKETS:.0e} packets "
+                  f"+ {nsteps} steps",
+        "transport_photons_per_s": n_mc / t_mc,
+        "voxel_updates_per_s": GRID ** 3 * s / t_heat,
+        "voxel_steps_per_packet": tal["voxel_steps"] / n_mc,
+    }
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    vals = []
+    last = None
+    for i in range(args.warmup + args.steps):
+        r = cpu_measure(args.cpu_seconds)
+        if i >= args.warmup:
+            vals.append(r["value"])
+            last = r
+    v = statistics.mean(vals)
+    line = {
+        "metric": METRIC, "value": v, "unit": "photons/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * PACKETS / v, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "impl": "reference",
+        "config": {"workload": f"precision form: {GRID}^3 homogeneous cube, {PACKETS:.0e} packets + 2 s of heat steps"},
+        "cpu_baseline": {"value": v, "unit": "photons/s", "cores": last["cores"], "kind": "port",
+                         "sample": last["sample"]},
+        "e2e": {"value": v, "unit": "photons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference is Fortran + MPI and no Fortran compiler exists on either machine; "
+                "its C restatement (oracle/) is timed instead",
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--packets", type=int, default=PACKETS, help="profiling only: packets per step")
+    ap.add_argument("--heat-steps", type=int, default=0, help="profiling only: heat steps per step")
+    ap.add_argument("--fp64-packets", type=int, default=2_000_000)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        args.cpu_seconds = min(args.cpu_seconds, 8.0)
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

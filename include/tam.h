@@ -239,6 +239,14 @@ int tam_get_tallies(struct tam_ctx *ctx, double *absorbed, double *reflected, do
 int tam_get_tallies_ex(struct tam_ctx *ctx, double *out, int32_t n);
 int tam_get_state(struct tam_ctx *ctx, tam_state *st);
 
+/* Device time of the last hot calls, from CUDA events recorded on the
+ * context's stream: the transport kernel of the last tam_mc_pass, and the
+ * span of the last tam_heat_steps from its first to its last kernel, with the
+ * number of heat kernels it launched. */
+int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, int64_t *heat_launches);
+/* Kernels this library has launched in this process (all contexts). */
+int64_t tam_kernel_launches(void);
+
 /* writer (src/writer.f90:6-81): stream-unformatted FP64 files in `dir`. */
 int tam_write_output(struct tam_ctx *ctx, const char *dir);
 

@@ -387,6 +387,7 @@ cudaError_t launch_fused_t(const FusedArgs &a, cudaStream_t s)
     if (chunks > a.nz) chunks = a.nz;
     const int zchunk = (a.nz + chunks - 1) / chunks;
     chunks = (a.nz + zchunk - 1) / zchunk;
+    count_launch();
     fused_kernel<Real, KAHAN><<<dim3(bx, by, chunks), dim3(FX, FY), 0, s>>>(a, zchunk);
     return cudaGetLastError();
 }
@@ -447,24 +448,28 @@ __global__ void from_halo_kernel(const FusedArgs a, const double *halo)
 
 cudaError_t launch_ref_stencil(const RefHeatArgs &a, cudaStream_t s)
 {
+    count_launch();
     ref_stencil_kernel<<<ref_grid(a.nx, a.ny, a.nz), dim3(32, 8), 0, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ref_arrhenius(const RefArrheniusArgs &a, cudaStream_t s)
 {
+    count_launch();
     ref_arrhenius_kernel<<<ref_grid(a.nx, a.ny, a.nz), dim3(32, 8), 0, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ref_props(const RefPropsArgs &a, cudaStream_t s)
 {
+    count_launch();
     ref_props_kernel<<<ref_grid(a.nx, a.ny, a.nz), dim3(32, 8), 0, s>>>(a);
     return cudaGetLastError();
 }
 
 cudaError_t launch_ref_finalize(int nx, int ny, int nz, const double *rhokap, double *tissue, cudaStream_t s)
 {
+    count_launch();
     ref_finalize_kernel<<<ref_grid(nx, ny, nz), dim3(32, 8), 0, s>>>(nx, ny, nz, rhokap, tissue);
     return cudaGetLastError();
 }
@@ -477,6 +482,7 @@ cudaError_t launch_fused_step(const FusedArgs &a, bool fp64, cudaStream_t s)
 cudaError_t launch_fused_to_halo(const FusedArgs &a, bool fp64, double *halo, cudaStream_t s)
 {
     const dim3 g((a.nx + 2 + 31) / 32, (a.ny + 2 + 7) / 8, a.nz + 2);
+    count_launch();
     if (fp64) to_halo_kernel<double><<<g, dim3(32, 8), 0, s>>>(a, halo);
     else to_halo_kernel<float><<<g, dim3(32, 8), 0, s>>>(a, halo);
     return cudaGetLastError();
@@ -485,6 +491,7 @@ cudaError_t launch_fused_to_halo(const FusedArgs &a, bool fp64, double *halo, cu
 cudaError_t launch_fused_from_halo(const FusedArgs &a, bool fp64, const double *halo, cudaStream_t s)
 {
     const dim3 g((a.nx + 31) / 32, (a.ny + 7) / 8, a.nz);
+    count_launch();
     if (fp64) from_halo_kernel<double><<<g, dim3(32, 8), 0, s>>>(a, halo);
     else from_halo_kernel<float><<<g, dim3(32, 8), 0, s>>>(a, halo);
     return cudaGetLastError();

@@ -89,6 +89,11 @@ struct tam_ctx {
     bool need_trace = true;
     long long nabl_at_trace = 0;
 
+    // CUDA events around the transport kernel and the heat loop
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    bool have_mc_time = false, have_heat_time = false;
+    int64_t heat_launches = 0;
+
     // last pass
     double tally[tam::N_TALLY] = {0};
     int64_t last_n = 0;
@@ -229,9 +234,23 @@ int validate_params(const tam_params *p, std::string &why)
     return 1;
 }
 
+// module Heat initial scalars (src/mcpolar.f90:66-73)
+void reset_scalars(tam_ctx *ctx)
+{
+    ctx->time = 0.;
+    ctx->pulseCount = 0.;
+    ctx->repetitionCount = 0.;
+    ctx->laserOn = 1.;
+    ctx->laser_flag = 1;
+    ctx->pulseFlag = 0;
+    ctx->pulsesDone = 0;
+    ctx->counter = 0;
+}
+
 // ---------------------------------------------------- reference set-up --
 int ref_setup(tam_ctx *ctx)
 {
+    reset_scalars(ctx);
     const tam_params &p = ctx->p;
     const int nx = ctx->nx, ny = ctx->ny, nz = ctx->nz;
     cudaStream_t s = ctx->stream;
@@ -293,6 +312,7 @@ int ref_setup(tam_ctx *ctx)
 // -------------------------------------------------------- config set-up --
 int cfg_setup(tam_ctx *ctx)
 {
+    reset_scalars(ctx);
     const tam_params &p = ctx->p;
     const tam_config &c = ctx->cfg;
     const int nx = ctx->nx, ny = ctx->ny, nz = ctx->nz;
@@ -448,7 +468,10 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream)
     a.err = ctx->d_err;
     CK(cudaMemsetAsync(ctx->d_jmean, 0, ctx->ni * sizeof(double), s));
     CK(cudaMemsetAsync(ctx->d_tally, 0, tam::N_TALLY * sizeof(double), s));
+    CK(cudaEventRecord(ctx->ev[0], s));
     CK(tam::launch_transport(a, ctx->fp64, ctx->sm_count, s));
+    CK(cudaEventRecord(ctx->ev[1], s));
+    ctx->have_mc_time = true;
     CK(tam::launch_sum_f64(ctx->d_jmean, ctx->ni, ctx->d_tally + tam::T_ABSORBED, s));
     ctx->last_n = n;
     ctx->mc_passes += 1;
@@ -472,6 +495,7 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream)
 // ------------------------------------------------------ heat (reference) --
 int ref_heat(tam_ctx *ctx, int32_t loops)
 {
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
     if (ctx->pulseLength < ctx->delt) ctx->delt = ctx->pulseLength / 100.;  // src/3dFD.f90:102-105
     ctx->loops_left = (int)(ctx->total_time / ((double)loops * ctx->delt)) - ctx->counter;
     tam::RefHeatArgs a{};
@@ -500,6 +524,9 @@ int ref_heat(tam_ctx *ctx, int32_t loops)
         ctx->tcur = 1 - ctx->tcur;  // t0 = tn (src/3dFD.f90:187)
         pulse_update(ctx, ctx->delt);
     }
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    ctx->have_heat_time = true;
+    ctx->heat_launches = loops;
     return TAM_OK;
 }
 
@@ -551,6 +578,7 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
 {
     tam::FusedArgs a = fused_args(ctx);
     const int check = ctx->cfg.retrace_check > 0 ? ctx->cfg.retrace_check : 0;
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
     for (int32_t it = 0; it < nsteps; ++it) {
         a.T_in = ctx->d_Tf[ctx->fcur];
         a.T_out = ctx->d_Tf[1 - ctx->fcur];
@@ -571,6 +599,9 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
                 ctx->need_trace = true;
         }
     }
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    ctx->have_heat_time = true;
+    ctx->heat_launches = nsteps;
     return TAM_OK;
 }
 
@@ -831,6 +862,8 @@ int tam_create(const tam_params *p, const tam_config *cfg, tam_ctx **out)
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
         return bail(fail(nullptr, TAM_E_CUDA, "cudaStreamCreate failed"));
     ctx->own_stream = true;
+    for (int e = 0; e < 4; ++e)
+        if (cudaEventCreate(&ctx->ev[e]) != cudaSuccess) return bail(fail(nullptr, TAM_E_CUDA, "cudaEventCreate failed"));
 
     int r = TAM_OK;
 #define AL(ptr, n) \
@@ -880,15 +913,6 @@ int tam_create(const tam_params *p, const tam_config *cfg, tam_ctx **out)
         return bail(fail(nullptr, TAM_E_CUDA, "initial memset failed"));
     if (!ctx->config && cudaMemsetAsync(ctx->d_jglob, 0, ctx->ni * 8, ctx->stream) != cudaSuccess)
         return bail(fail(nullptr, TAM_E_CUDA, "initial memset failed"));
-    // module Heat initial scalars (src/mcpolar.f90:66-73)
-    ctx->time = 0.;
-    ctx->pulseCount = 0.;
-    ctx->repetitionCount = 0.;
-    ctx->laserOn = 1.;
-    ctx->laser_flag = 1;
-    ctx->pulseFlag = 0;
-    ctx->pulsesDone = 0;
-    ctx->counter = 0;
     r = ctx->config ? cfg_setup(ctx) : ref_setup(ctx);
     if (r == TAM_OK) r = finish(ctx, "tam_create");
     if (r != TAM_OK) {
@@ -905,6 +929,8 @@ int tam_destroy(tam_ctx *ctx)
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     for (void *p : ctx->allocs) cudaFree(p);
+    for (cudaEvent_t e : ctx->ev)
+        if (e) cudaEventDestroy(e);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return TAM_OK;
@@ -1280,6 +1306,22 @@ int tam_get_state(tam_ctx *ctx, tam_state *st)
     }
     return TAM_OK;
 }
+
+int tam_get_timing(tam_ctx *ctx, double *transport_ms, double *heat_ms, int64_t *heat_launches)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float t = 0.f, h = 0.f;
+    if (ctx->have_mc_time) CK(cudaEventElapsedTime(&t, ctx->ev[0], ctx->ev[1]));
+    if (ctx->have_heat_time) CK(cudaEventElapsedTime(&h, ctx->ev[2], ctx->ev[3]));
+    if (transport_ms) *transport_ms = t;
+    if (heat_ms) *heat_ms = h;
+    if (heat_launches) *heat_launches = ctx->heat_launches;
+    return TAM_OK;
+}
+
+int64_t tam_kernel_launches(void) { return tam::launch_count(); }
 
 namespace {
 // str() of src/utils.f90:109-207: integers optionally zero-padded to len;

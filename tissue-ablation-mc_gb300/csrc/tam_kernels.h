@@ -7,6 +7,10 @@
 
 namespace tam {
 
+// Kernel launches issued by this library (process-wide).
+void count_launch(int n = 1);
+int64_t launch_count();
+
 constexpr int MAX_MAT = 16;
 
 enum Medium : int32_t { MED_RHOKAP = 0, MED_MATERIAL = 1 };

@@ -463,6 +463,7 @@ template <typename Real, int MED> cudaError_t launch_t(const TransportArgs &a, i
     const int64_t need = (a.n + TPB - 1) / TPB;
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
+    count_launch();
     transport_kernel<Real, MED><<<(unsigned)blocks, TPB, 0, s>>>(a);
     return cudaGetLastError();
 }
@@ -485,6 +486,7 @@ cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cu
 cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    count_launch();
     scale_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0);
     return cudaGetLastError();
 }
@@ -492,6 +494,7 @@ cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool 
 cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    count_launch();
     scale_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0);
     return cudaGetLastError();
 }
@@ -499,6 +502,7 @@ cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, boo
 cudaError_t launch_philox_selftest(const uint32_t *in, uint32_t *mine, uint32_t *ref, int64_t n, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    count_launch();
     philox_selftest_kernel<<<grid_for(n, 256), 256, 0, s>>>(in, mine, ref, n);
     return cudaGetLastError();
 }

@@ -3,7 +3,18 @@
 #include "tam_device.cuh"
 #include "tam_util.h"
 
+#include <atomic>
+
+#include "tam_kernels.h"
+
 namespace tam {
+
+namespace {
+std::atomic<int64_t> g_launches{0};
+}  // namespace
+
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+int64_t launch_count() { return g_launches.load(std::memory_order_relaxed); }
 
 namespace {
 
@@ -154,12 +165,14 @@ __global__ void count_negative_kernel(const double *p, int64_t n, unsigned long 
 cudaError_t launch_fill_f64(double *p, double v, int64_t n, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    count_launch();
     fill_f64_kernel<<<blocks_for(n, 256), 256, 0, s>>>(p, v, n);
     return cudaGetLastError();
 }
 cudaError_t launch_fill_real(void *p, bool fp64, double v, int64_t n, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    count_launch();
     if (fp64) fill_f64_kernel<<<blocks_for(n, 256), 256, 0, s>>>((double *)p, v, n);
     else fill_f32_kernel<<<blocks_for(n, 256), 256, 0, s>>>((float *)p, (float)v, n);
     return cudaGetLastError();
@@ -167,6 +180,7 @@ cudaError_t launch_fill_real(void *p, bool fp64, double v, int64_t n, cudaStream
 cudaError_t launch_fill_u8(uint8_t *p, uint8_t v, int64_t n, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    count_launch();
     fill_u8_kernel<<<blocks_for(n, 256), 256, 0, s>>>(p, v, n);
     return cudaGetLastError();
 }
@@ -174,12 +188,14 @@ cudaError_t launch_fill_halo(double *p, int nx, int ny, int nz, double vin, doub
                              cudaStream_t s)
 {
     const int64_t n = (int64_t)(nx + 2) * (ny + 2) * (nz + 2);
+    count_launch();
     fill_halo_kernel<<<blocks_for(n, 256), 256, 0, s>>>(p, nx, ny, nz, vin, vhalo, vtop, has_top ? 1 : 0);
     return cudaGetLastError();
 }
 cudaError_t launch_ref_init_temp(double *p, int nx, int ny, int nz, cudaStream_t s)
 {
     const int64_t n = (int64_t)(nx + 2) * (ny + 2) * (nz + 2);
+    count_launch();
     ref_init_temp_kernel<<<blocks_for(n, 256), 256, 0, s>>>(p, nx, ny, nz);
     return cudaGetLastError();
 }
@@ -187,6 +203,7 @@ cudaError_t launch_props_from_mat(const uint8_t *mat, int nmat, const MatThermal
                                   bool fp64, int64_t n, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;
+    count_launch();
     if (fp64)
         props_from_mat_kernel<double>
             <<<blocks_for(n, 256), 256, 0, s>>>(mat, nmat, lut, (double *)k, (double *)r, (double *)c, n);
@@ -199,6 +216,7 @@ cudaError_t launch_to_f64(const void *src, bool fp64, double *dst, int64_t n, cu
 {
     if (n <= 0) return cudaSuccess;
     if (fp64) return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    count_launch();
     to_f64_kernel<float><<<blocks_for(n, 256), 256, 0, s>>>((const float *)src, dst, n);
     return cudaGetLastError();
 }
@@ -206,12 +224,14 @@ cudaError_t launch_from_f64(const double *src, void *dst, bool fp64, int64_t n, 
 {
     if (n <= 0) return cudaSuccess;
     if (fp64) return cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    count_launch();
     from_f64_kernel<float><<<blocks_for(n, 256), 256, 0, s>>>(src, (float *)dst, n);
     return cudaGetLastError();
 }
 cudaError_t launch_interior_to_halo(const void *src, bool fp64, double *halo, int nx, int ny, int nz, cudaStream_t s)
 {
     const int64_t n = (int64_t)(nx + 2) * (ny + 2) * (nz + 2);
+    count_launch();
     if (fp64) interior_to_halo_kernel<double><<<blocks_for(n, 256), 256, 0, s>>>((const double *)src, halo, nx, ny, nz);
     else interior_to_halo_kernel<float><<<blocks_for(n, 256), 256, 0, s>>>((const float *)src, halo, nx, ny, nz);
     return cudaGetLastError();
@@ -219,6 +239,7 @@ cudaError_t launch_interior_to_halo(const void *src, bool fp64, double *halo, in
 cudaError_t launch_halo_to_interior(const double *halo, void *dst, bool fp64, int nx, int ny, int nz, cudaStream_t s)
 {
     const int64_t n = (int64_t)nx * ny * nz;
+    count_launch();
     if (fp64) halo_to_interior_kernel<double><<<blocks_for(n, 256), 256, 0, s>>>(halo, (double *)dst, nx, ny, nz);
     else halo_to_interior_kernel<float><<<blocks_for(n, 256), 256, 0, s>>>(halo, (float *)dst, nx, ny, nz);
     return cudaGetLastError();
@@ -227,6 +248,7 @@ cudaError_t launch_rhokap_from_mat(const uint8_t *mat, int nmat, const MatTherma
                                    int nz, cudaStream_t s)
 {
     const int64_t n = (int64_t)(nx + 2) * (ny + 2) * (nz + 2);
+    count_launch();
     rhokap_from_mat_kernel<<<blocks_for(n, 256), 256, 0, s>>>(mat, nmat, lut, halo, nx, ny, nz);
     return cudaGetLastError();
 }
@@ -234,6 +256,7 @@ cudaError_t launch_sum_f64(const double *p, int64_t n, double *out, cudaStream_t
 {
     cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
     if (e != cudaSuccess || n <= 0) return e;
+    count_launch();
     sum_f64_kernel<<<blocks_for(n, 256), 256, 0, s>>>(p, n, out);
     return cudaGetLastError();
 }
@@ -241,6 +264,7 @@ cudaError_t launch_count_negative(const double *p, int64_t n, unsigned long long
 {
     cudaError_t e = cudaMemsetAsync(out, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess || n <= 0) return e;
+    count_launch();
     count_negative_kernel<<<blocks_for(n, 256), 256, 0, s>>>(p, n, out);
     return cudaGetLastError();
 }

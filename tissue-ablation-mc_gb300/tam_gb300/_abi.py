@@ -125,6 +125,8 @@ SIGNATURES = [
     ("tam_get_tallies", C.c_int, [_P, _D, _D, _D]),
     ("tam_get_tallies_ex", C.c_int, [_P, _D, C.c_int32]),
     ("tam_get_state", C.c_int, [_P, C.POINTER(State)]),
+    ("tam_get_timing", C.c_int, [_P, _D, _D, C.POINTER(C.c_int64)]),
+    ("tam_kernel_launches", C.c_int64, []),
     ("tam_write_output", C.c_int, [_P, C.c_char_p]),
     ("tam_selftest_philox", C.c_int, [_U32, _U32, _U32, C.c_int64]),
 ]

@@ -173,8 +173,19 @@ class Context:
         self._ck(self._lib.tam_device_errors(self._h, C.byref(b)))
         return b.value
 
+    def timing(self):
+        t = C.c_double(0)
+        h = C.c_double(0)
+        n = C.c_int64(0)
+        self._ck(self._lib.tam_get_timing(self._h, C.byref(t), C.byref(h), C.byref(n)))
+        return t.value, h.value, n.value
+
     def write_output(self, directory: str) -> None:
         self._ck(self._lib.tam_write_output(self._h, directory.encode()))
+
+
+def kernel_launches() -> int:
+    return int(lib().tam_kernel_launches())
 
 
 def selftest_philox(words: np.ndarray):
