@@ -244,6 +244,12 @@ int tam_get_state(struct tam_ctx *ctx, tam_state *st);
  * span of the last tam_heat_steps from its first to its last kernel, with the
  * number of heat kernels it launched. */
 int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, int64_t *heat_launches);
+/* Kernel tuning knobs (no reference counterpart; defaults are tuned for
+ * GB300).  Keys: "transport.scat_min" (lanes of a warp that wait at an
+ * interaction before the warp scatters, 1..32), "heat.zchunk" (z planes per
+ * thread column of the fused step, 0 = automatic), "heat.tma" (1: stage the
+ * FP32 fused step's planes with TMA where the row pitch allows, 0: cp.async). */
+int tam_set_tuning(struct tam_ctx *ctx, const char *key, int64_t value);
 /* Kernels this library has launched in this process (all contexts). */
 int64_t tam_kernel_launches(void);
 

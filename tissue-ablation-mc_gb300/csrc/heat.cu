@@ -10,10 +10,11 @@
 //    exponent ln A - Ea/RT) + ablation in one pass, with FP32 storage and a
 //    Kahan-compensated temperature, or plain FP64.  Each thread marches a
 //    (x, y) column through a z-chunk keeping the z-neighbours in registers.
+#include <algorithm>
+#include <atomic>
 #include <cstdio>
 
-#include "tam_device.cuh"
-#include "tam_kernels.h"
+#include "heat_common.cuh"
 
 namespace tam {
 
@@ -214,57 +215,68 @@ __global__ void ref_finalize_kernel(int nx, int ny, int nz, const double *rk, do
 dim3 ref_grid(int nx, int ny, int nz) { return dim3((nx + 31) / 32, (ny + 7) / 8, nz); }
 
 // --------------------------------------------------------- fused path --
-constexpr int FX = 32, FY = 8;
+// cp.async (LDGSTS) of one 4- or 8-byte element into shared memory.
+template <int BYTES> __device__ __forceinline__ void cp_async(void *smem, const void *gmem)
+{
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2;\n" ::"r"(sa), "l"(gmem), "n"(BYTES));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+template <int N> __device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N)); }
 
-template <typename Real> struct Pt {
-    Real T, e, k, r, h;  // temperature, Kahan compensation (true T = T - e), k, rho, c
+// One z level of the block's tile in shared memory: FX x FY voxels plus a
+// one-cell halo in x and y (the 7-point stencil never reads the corners).
+constexpr int NSTAGE = 4;
+template <typename Real> struct Plane {
+    Real T[FY + 2][FX + 2];
+    float e[FY + 2][FX + 2];
+    Real k[FY + 2][FX + 2];
+    Real r[FY + 2][FX + 2];
+    Real h[FY + 2][FX + 2];
+    Real J[FY][FX];
 };
 
+template <typename Real, bool KAHAN> __device__ __forceinline__ Pt<Real> get(const Plane<Real> &P, int i, int j)
+{
+    Pt<Real> q;
+    q.T = P.T[i][j];
+    q.e = KAHAN ? (Real)P.e[i][j] : (Real)0;
+    q.k = P.k[i][j];
+    q.r = P.r[i][j];
+    q.h = P.h[i][j];
+    return q;
+}
+
+// Issue the asynchronous copies of one voxel's T, Kahan term, k, rho, c.
 template <typename Real, bool KAHAN>
-__device__ __forceinline__ Pt<Real> ld(const Real *T, const float *E, const Real *K, const Real *R, const Real *C,
-                                       int64_t v)
+__device__ __forceinline__ void stage_cell(Plane<Real> &P, int i, int j, const Real *T, const float *E,
+                                           const Real *K, const Real *R, const Real *C, int64_t v)
 {
-    Pt<Real> p;
-    p.T = __ldg(T + v);
-    p.e = KAHAN ? (Real)__ldg(E + v) : (Real)0;
-    p.k = __ldg(K + v);
-    p.r = __ldg(R + v);
-    p.h = __ldg(C + v);
-    return p;
+    cp_async<sizeof(Real)>(&P.T[i][j], T + v);
+    if (KAHAN) cp_async<4>(&P.e[i][j], E + v);
+    cp_async<sizeof(Real)>(&P.k[i][j], K + v);
+    cp_async<sizeof(Real)>(&P.r[i][j], R + v);
+    cp_async<sizeof(Real)>(&P.h[i][j], C + v);
 }
 
-// face diffusivity k_f / (rho_f c_f) with arithmetic face means
-template <typename Real> __device__ __forceinline__ Real falpha(const Pt<Real> &a, const Pt<Real> &b)
-{
-    const Real kf = (Real)0.5 * (a.k + b.k), rf = (Real)0.5 * (a.r + b.r), cf = (Real)0.5 * (a.h + b.h);
-    return M<Real>::div(kf, rf * cf);
-}
-
-// (true neighbour - true centre) for an interior neighbour
-template <typename Real> __device__ __forceinline__ Real tdiff(const Pt<Real> &n, const Pt<Real> &c)
-{
-    return (n.T - c.T) - (n.e - c.e);
-}
-
-// (ghost - true centre) for a boundary face
-template <typename Real>
-__device__ __forceinline__ Real gdiff(const FusedArgs &a, int f, Real d, const Pt<Real> &c)
-{
-    if (a.bc_type[f] == BC_ROBIN) {
-        const Real beta = (Real)a.bc_h[f] * d / c.k;
-        return -beta * ((c.T - (Real)a.bc_Tamb[f]) - c.e);
-    }
-    return ((Real)a.bc_T[f] - c.T) + c.e;
-}
-
+// 2.5-D blocking: a block owns an FX x FY column of the grid for zchunk
+// planes.  Planes stream through a ring of NSTAGE shared-memory stages filled
+// with cp.async two planes ahead of the one being updated (own voxels, the
+// x/y halo staged by the edge threads, and J), so HBM latency overlaps the
+// compute of earlier planes; one barrier per plane.  Per voxel the kernel
+// reads T, the Kahan term, k, rho, c and J once from HBM and writes T and the
+// Kahan term once.  Interior voxels take a branch-free path; faces on the
+// grid boundary are handled by ghost_term.
 template <typename Real, bool KAHAN>
-__global__ void __launch_bounds__(FX *FY) fused_kernel(const FusedArgs a, int zchunk)
+__global__ void __launch_bounds__(FX *FY, KAHAN ? 4 : 2) fused_kernel(const FusedArgs a, int zchunk)
 {
-    const int x = blockIdx.x * FX + threadIdx.x, y = blockIdx.y * FY + threadIdx.y;
-    if (x >= a.nx || y >= a.ny) return;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    Plane<Real> *S = reinterpret_cast<Plane<Real> *>(smem_raw);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = blockIdx.x * FX + tx, y = blockIdx.y * FY + ty;
+    const bool in = x < a.nx && y < a.ny;
     const int z0 = blockIdx.z * zchunk;
     const int z1 = min(a.nz, z0 + zchunk);
-    if (z0 >= z1) return;
     const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, ni = sz * a.nz;
     const Real *T = (const Real *)a.T_in, *K = (const Real *)a.k, *R = (const Real *)a.rho,
                *C = (const Real *)a.c;
@@ -272,123 +284,210 @@ __global__ void __launch_bounds__(FX *FY) fused_kernel(const FusedArgs a, int zc
     Real *J = (Real *)a.J, *Q = (Real *)a.Q;
     const float *E = a.Tc_in;
     float *Eo = a.Tc_out;
-    const Real dx = (Real)a.dx, dy = (Real)a.dy, dz = (Real)a.dz;
-    const Real cx = (Real)(a.opscale / (a.dx * a.dx)), cy = (Real)(a.opscale / (a.dy * a.dy)),
-               cz = (Real)(a.opscale / (a.dz * a.dz));
-    const Real dt = (Real)a.dt, P = (Real)a.P, vvox = (Real)a.vvox;
-    const Real Tboil = (Real)a.T_boil, lw = (Real)a.lw;
+    const Real cx = cst<Real>(a, FC_CX), cy = cst<Real>(a, FC_CY), cz = cst<Real>(a, FC_CZ);
+    const Real dt = cst<Real>(a, FC_DT), Pdt = cst<Real>(a, FC_PDT);
+    const bool src_on = Pdt != (Real)0;
+    // halo cells this thread stages for every plane
+    const bool hL = tx == 0 && x >= 1 && y < a.ny;
+    const bool hR = tx == FX - 1 && x + 1 < a.nx && y < a.ny;
+    const bool hB = ty == 0 && y >= 1 && x < a.nx;
+    const bool hT = ty == FY - 1 && y + 1 < a.ny && x < a.nx;
+    const bool xy_inner = x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1;
+    const int64_t vxy = (int64_t)x + sy * y;
 
-    int64_t v = x + sy * y + sz * z0;
-    Pt<Real> cur = ld<Real, KAHAN>(T, E, K, R, C, v);
-    Pt<Real> prv;
-    if (z0 > 0) prv = ld<Real, KAHAN>(T, E, K, R, C, v - sz);
-    Real am_z = z0 > 0 ? falpha(cur, prv) : M<Real>::div(cur.k, cur.r * cur.h);
+    // copies of plane zz into its stage (no-op outside the grid)
+    auto stage = [&](int zz) {
+        if (zz >= 0 && zz < a.nz) {
+            Plane<Real> &P = S[(zz + NSTAGE) % NSTAGE];
+            const int64_t v = vxy + sz * zz;
+            if (in) {
+                stage_cell<Real, KAHAN>(P, ty + 1, tx + 1, T, E, K, R, C, v);
+                if (src_on) cp_async<sizeof(Real)>(&P.J[ty][tx], J + v);
+            }
+            if (hL) stage_cell<Real, KAHAN>(P, ty + 1, 0, T, E, K, R, C, v - 1);
+            if (hR) stage_cell<Real, KAHAN>(P, ty + 1, FX + 1, T, E, K, R, C, v + 1);
+            if (hB) stage_cell<Real, KAHAN>(P, 0, tx + 1, T, E, K, R, C, v - sy);
+            if (hT) stage_cell<Real, KAHAN>(P, FY + 1, tx + 1, T, E, K, R, C, v + sy);
+        }
+        cp_async_commit();
+    };
+
+    // prologue: planes z0-1, z0, z0+1 in flight
+    stage(z0 - 1);
+    stage(z0);
+    stage(z0 + 1);
+    cp_async_wait<1>();  // z0-1 and z0 have landed
+    __syncthreads();
+    Pt<Real> prv{}, cur{};
+    Real am_z = 0;
+    if (in) {
+        cur = get<Real, KAHAN>(S[(z0 + NSTAGE) % NSTAGE], ty + 1, tx + 1);
+        if (z0 > 0) {
+            prv = get<Real, KAHAN>(S[(z0 - 1 + NSTAGE) % NSTAGE], ty + 1, tx + 1);
+            am_z = falpha(cur, prv);
+        }
+    }
     unsigned errbits = 0;
-    for (int z = z0; z < z1; ++z, v += sz) {
-        Pt<Real> nxt;
+    for (int z = z0; z < z1; ++z) {
+        const int64_t v = vxy + sz * z;
         const bool has_n = z + 1 < a.nz;
-        if (has_n) nxt = ld<Real, KAHAN>(T, E, K, R, C, v + sz);
-        const Real aself = M<Real>::div(cur.k, cur.r * cur.h);
-        // z axis
-        const Real dzm = z > 0 ? tdiff(prv, cur) : gdiff<Real>(a, 4, dz, cur);
-        const Real ap_z = has_n ? falpha(cur, nxt) : aself;
-        const Real dzp = has_n ? tdiff(nxt, cur) : gdiff<Real>(a, 5, dz, cur);
-        Real lap = cz * (am_z * dzm + ap_z * dzp);
-        // y axis
-        if (y > 0) {
-            const Pt<Real> nb = ld<Real, KAHAN>(T, E, K, R, C, v - sy);
-            lap += cy * falpha(cur, nb) * tdiff(nb, cur);
-        } else {
-            lap += cy * aself * gdiff<Real>(a, 2, dy, cur);
-        }
-        if (y < a.ny - 1) {
-            const Pt<Real> nb = ld<Real, KAHAN>(T, E, K, R, C, v + sy);
-            lap += cy * falpha(cur, nb) * tdiff(nb, cur);
-        } else {
-            lap += cy * aself * gdiff<Real>(a, 3, dy, cur);
-        }
-        // x axis
-        if (x > 0) {
-            const Pt<Real> nb = ld<Real, KAHAN>(T, E, K, R, C, v - 1);
-            lap += cx * falpha(cur, nb) * tdiff(nb, cur);
-        } else {
-            lap += cx * aself * gdiff<Real>(a, 0, dx, cur);
-        }
-        if (x < a.nx - 1) {
-            const Pt<Real> nb = ld<Real, KAHAN>(T, E, K, R, C, v + 1);
-            lap += cx * falpha(cur, nb) * tdiff(nb, cur);
-        } else {
-            lap += cx * aself * gdiff<Real>(a, 1, dx, cur);
-        }
-
-        const Real dT = dt * lap;
-        const Real Jv = P != (Real)0 ? J[v] : (Real)0;
-        const Real rc = cur.r * cur.h;
-        const Real src = M<Real>::div(P * Jv * dt, rc);
-        Real Tn, En = (Real)0;
-        bool clamped = false;
-        if (a.boil && cur.T >= Tboil) {
-            const Real qv = lw * cur.r * vvox;
-            const Real Qv = Q[v];
-            if (Qv < qv) {
-                const Real Ein = (P * Jv * dt + rc * dT) * vvox;
-                if (Ein > (Real)0) {
-                    const Real qn = Qv + Ein;
-                    Q[v] = qn < qv ? qn : qv;
-                    Tn = Tboil;
-                    clamped = true;
+        stage(z + 2);        // two planes ahead
+        cp_async_wait<1>();  // plane z+1 has landed (for this thread's copies)
+        __syncthreads();     // ... and for every thread's copies
+        const Plane<Real> &P = S[z % NSTAGE];
+        Pt<Real> nxt{};
+        if (in && has_n) nxt = get<Real, KAHAN>(S[(z + 1) % NSTAGE], ty + 1, tx + 1);
+        Real ap_z = am_z;
+        if (in) {
+            const Real Jv = src_on ? P.J[ty][tx] : (Real)0;
+            Real lap;
+            if (xy_inner && z > 0 && has_n) {
+                ap_z = falpha(cur, nxt);
+                const Pt<Real> ym = get<Real, KAHAN>(P, ty, tx + 1), yp = get<Real, KAHAN>(P, ty + 2, tx + 1);
+                const Pt<Real> xm = get<Real, KAHAN>(P, ty + 1, tx), xp = get<Real, KAHAN>(P, ty + 1, tx + 2);
+                lap = cz * (am_z * tdiff(prv, cur) + ap_z * tdiff(nxt, cur)) +
+                      cy * (falpha(cur, ym) * tdiff(ym, cur) + falpha(cur, yp) * tdiff(yp, cur)) +
+                      cx * (falpha(cur, xm) * tdiff(xm, cur) + falpha(cur, xp) * tdiff(xp, cur));
+            } else {
+                // a face of this voxel lies on the grid boundary
+                lap = (Real)0;
+                if (z > 0) lap += cz * am_z * tdiff(prv, cur);
+                else lap += ghost_term<Real>(a, 4, cur.T, cur.e, cur.k, cur.r, cur.h);
+                if (has_n) {
+                    ap_z = falpha(cur, nxt);
+                    lap += cz * ap_z * tdiff(nxt, cur);
+                } else {
+                    lap += ghost_term<Real>(a, 5, cur.T, cur.e, cur.k, cur.r, cur.h);
+                }
+                if (y > 0) {
+                    const Pt<Real> nb = get<Real, KAHAN>(P, ty, tx + 1);
+                    lap += cy * falpha(cur, nb) * tdiff(nb, cur);
+                } else {
+                    lap += ghost_term<Real>(a, 2, cur.T, cur.e, cur.k, cur.r, cur.h);
+                }
+                if (y < a.ny - 1) {
+                    const Pt<Real> nb = get<Real, KAHAN>(P, ty + 2, tx + 1);
+                    lap += cy * falpha(cur, nb) * tdiff(nb, cur);
+                } else {
+                    lap += ghost_term<Real>(a, 3, cur.T, cur.e, cur.k, cur.r, cur.h);
+                }
+                if (x > 0) {
+                    const Pt<Real> nb = get<Real, KAHAN>(P, ty + 1, tx);
+                    lap += cx * falpha(cur, nb) * tdiff(nb, cur);
+                } else {
+                    lap += ghost_term<Real>(a, 0, cur.T, cur.e, cur.k, cur.r, cur.h);
+                }
+                if (x < a.nx - 1) {
+                    const Pt<Real> nb = get<Real, KAHAN>(P, ty + 1, tx + 2);
+                    lap += cx * falpha(cur, nb) * tdiff(nb, cur);
+                } else {
+                    lap += ghost_term<Real>(a, 1, cur.T, cur.e, cur.k, cur.r, cur.h);
                 }
             }
-        }
-        if (!clamped) {
-            const Real inc = dT + src;
-            if (KAHAN) {
-                const Real yk = inc - cur.e;
-                const Real t = cur.T + yk;
-                En = (t - cur.T) - yk;
-                Tn = t;
-            } else {
-                Tn = cur.T + inc;
+
+            const Real dT = dt * lap;
+            const Real rc = cur.r * cur.h;
+            const Real sPJ = Pdt * Jv;  // P J dt
+            const Real src = src_on ? M<Real>::div(sPJ, rc) : (Real)0;
+            Real Tn, En = (Real)0;
+            bool clamped = false;
+            if (a.boil && cur.T >= cst<Real>(a, FC_TBOIL)) {
+                const Real qv = cst<Real>(a, FC_LW) * cur.r * cst<Real>(a, FC_VVOX);
+                const Real Qv = Q[v];
+                if (Qv < qv) {
+                    const Real Ein = (sPJ + rc * dT) * cst<Real>(a, FC_VVOX);
+                    if (Ein > (Real)0) {
+                        const Real qn = Qv + Ein;
+                        Q[v] = qn < qv ? qn : qv;
+                        Tn = cst<Real>(a, FC_TBOIL);
+                        clamped = true;
+                    }
+                }
             }
-        }
-        To[v] = Tn;
-        if (KAHAN) Eo[v] = (float)En;
-        const double Tt = (double)Tn - (double)En;
-        if (!(Tt == Tt)) errbits |= DEVERR_NAN;
-        else if (Tt < 0.0) errbits |= DEVERR_NEG_T;
-        if (a.arrhenius && Tt >= a.T_lo && Tt < a.T_hi) {
-            const double o = a.omega[v];
-            const double on = o + a.dt * exp(a.lnA - a.Ea / (a.Rgas * Tt));
-            a.omega[v] = on;
-#pragma unroll
-            for (int t = 0; t < 3; ++t)
-                if (o < a.thr[t] && on >= a.thr[t]) a.thres[v + t * ni] = a.t_new;
-        }
-        if (Tt >= a.T_abl && a.mat[v] != 0) {
-            a.mat[v] = 0;  // optics -> air
-            J[v] = (Real)0;
-            atomicAdd(a.n_ablated, 1ull);
+            if (!clamped) {
+                const Real inc = dT + src;
+                if (KAHAN) {
+                    const Real yk = inc - cur.e;
+                    const Real t = cur.T + yk;
+                    En = (t - cur.T) - yk;
+                    Tn = t;
+                } else {
+                    Tn = cur.T + inc;
+                }
+            }
+            To[v] = Tn;
+            if (KAHAN) Eo[v] = (float)En;
+            // screen in the storage precision; FP64 only for voxels inside the
+            // damage window or at the ablation threshold
+            const Real Ts = Tn - En;
+            if (!(Ts == Ts)) errbits |= DEVERR_NAN;
+            else if (Ts < (Real)0) errbits |= DEVERR_NEG_T;
+            if (Ts >= cst<Real>(a, FC_SCREEN)) rare_update<Real>(a, v, ni, (double)Tn - (double)En);
         }
         prv = cur;
+        cur = nxt;
         am_z = ap_z;
-        if (has_n) cur = nxt;
     }
+    cp_async_wait<0>();
     if (errbits) atomicOr(a.err, errbits);
 }
 
-template <typename Real, bool KAHAN>
-cudaError_t launch_fused_t(const FusedArgs &a, cudaStream_t s)
+}  // namespace
+
+void fill_fused_consts(FusedArgs &a)
 {
+    double *d = a.dc;
+    d[FC_CX] = a.opscale / (a.dx * a.dx);
+    d[FC_CY] = a.opscale / (a.dy * a.dy);
+    d[FC_CZ] = a.opscale / (a.dz * a.dz);
+    d[FC_DT] = a.dt;
+    d[FC_PDT] = a.P * a.dt;
+    d[FC_VVOX] = a.vvox;
+    d[FC_TBOIL] = a.T_boil;
+    d[FC_LW] = a.lw;
+    // screening thresholds a little below the exact ones (|T - true T| <= a few ulp)
+    d[FC_TLO_S] = a.T_lo - 0.01;
+    d[FC_TABL_S] = a.T_abl - 0.01;
+    d[FC_SCREEN] = a.arrhenius ? std::min(d[FC_TLO_S], d[FC_TABL_S]) : d[FC_TABL_S];
+    for (int f = 0; f < 6; ++f) {
+        d[FC_BCT + f] = a.bc_T[f];
+        d[FC_BCHD + f] = a.bc_h[f] * (f < 2 ? a.dx : (f < 4 ? a.dy : a.dz));
+        d[FC_BCTA + f] = a.bc_Tamb[f];
+    }
+    for (int i = 0; i < FC_N; ++i) a.fc[i] = (float)d[i];
+}
+
+namespace {
+
+template <typename Real, bool KAHAN>
+cudaError_t launch_fused_t(const FusedArgs &a0, cudaStream_t s)
+{
+    FusedArgs a = a0;
+    fill_fused_consts(a);
     const int bx = (a.nx + FX - 1) / FX, by = (a.ny + FY - 1) / FY;
     // enough z-chunks to fill every SM several times over
     int64_t want = 152 * 8;
     int chunks = (int)((want + (int64_t)bx * by - 1) / ((int64_t)bx * by));
     if (chunks < 1) chunks = 1;
     if (chunks > a.nz) chunks = a.nz;
-    const int zchunk = (a.nz + chunks - 1) / chunks;
+    int zchunk = (a.nz + chunks - 1) / chunks;
+    if (zchunk > 16) zchunk = 16;
+    if (a.zchunk > 0) zchunk = a.zchunk;
     chunks = (a.nz + zchunk - 1) / zchunk;
+    const size_t smem = NSTAGE * sizeof(Plane<Real>);
+    // the dynamic shared-memory opt-in is per device; remember it per ordinal
+    static std::atomic<unsigned long long> attr_set{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(attr_set.load() & bit)) {
+        e = cudaFuncSetAttribute(fused_kernel<Real, KAHAN>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr_set.fetch_or(bit);
+    }
     count_launch();
-    fused_kernel<Real, KAHAN><<<dim3(bx, by, chunks), dim3(FX, FY), 0, s>>>(a, zchunk);
+    fused_kernel<Real, KAHAN><<<dim3(bx, by, chunks), dim3(FX, FY), smem, s>>>(a, zchunk);
     return cudaGetLastError();
 }
 

@@ -1,0 +1,83 @@
+// heat_common.cuh -- device helpers shared by the fused heat-step kernels
+// (heat.cu: cp.async form; heat_tma.cu: TMA form).
+#pragma once
+
+#include "tam_device.cuh"
+#include "tam_kernels.h"
+
+namespace tam {
+namespace {
+
+constexpr int FX = 32, FY = 8;
+
+template <typename Real> struct Pt {
+    Real T, e, k, r, h;  // temperature, Kahan compensation (true T = T - e), k, rho, c
+};
+
+template <typename Real, bool KAHAN>
+__device__ __forceinline__ Pt<Real> ld(const Real *T, const float *E, const Real *K, const Real *R, const Real *C,
+                                       int64_t v)
+{
+    Pt<Real> p;
+    p.T = __ldg(T + v);
+    p.e = KAHAN ? (Real)__ldg(E + v) : (Real)0;
+    p.k = __ldg(K + v);
+    p.r = __ldg(R + v);
+    p.h = __ldg(C + v);
+    return p;
+}
+
+// face diffusivity k_f / (rho_f c_f) with arithmetic face means
+template <typename Real> __device__ __forceinline__ Real falpha(const Pt<Real> &a, const Pt<Real> &b)
+{
+    const Real kf = (Real)0.5 * (a.k + b.k), rf = (Real)0.5 * (a.r + b.r), cf = (Real)0.5 * (a.h + b.h);
+    return M<Real>::div(kf, rf * cf);
+}
+
+// (true neighbour - true centre) for an interior neighbour
+template <typename Real> __device__ __forceinline__ Real tdiff(const Pt<Real> &n, const Pt<Real> &c)
+{
+    return (n.T - c.T) - (n.e - c.e);
+}
+
+template <typename Real> __device__ __forceinline__ Real cst(const FusedArgs &a, int i);
+template <> __device__ __forceinline__ float cst<float>(const FusedArgs &a, int i) { return a.fc[i]; }
+template <> __device__ __forceinline__ double cst<double>(const FusedArgs &a, int i) { return a.dc[i]; }
+
+// Laplacian term of one boundary face f (x-, x+, y-, y+, z-, z+): the ghost
+// carries the voxel's own properties, so the face diffusivity is k/(rho c);
+// (ghost - true centre) is the Dirichlet value minus the true temperature, or
+// -h d / k (T - T_amb) for a convective (Robin) face.
+template <typename Real>
+__device__ __noinline__ Real ghost_term(const FusedArgs &a, int f, Real T, Real e, Real k, Real r, Real h)
+{
+    Real d;
+    if (a.bc_type[f] == BC_ROBIN) d = -(cst<Real>(a, FC_BCHD + f) / k) * ((T - cst<Real>(a, FC_BCTA + f)) - e);
+    else d = (cst<Real>(a, FC_BCT + f) - T) + e;
+    return cst<Real>(a, f < 2 ? FC_CX : (f < 4 ? FC_CY : FC_CZ)) * (k / (r * h)) * d;
+}
+
+// Arrhenius damage (FP64 exponent ln A - Ea/RT, src/3dFD.f90:450-461 with
+// every crossed threshold stamped) and ablation of the optics for one voxel
+// whose new true temperature is Tt.  Kept out of line so that no FP64 work is
+// scheduled for the voxels that never reach it.
+template <typename Real> __device__ __noinline__ void rare_update(const FusedArgs &a, int64_t v, int64_t ni, double Tt)
+{
+    if (a.arrhenius && Tt >= a.T_lo && Tt < a.T_hi) {
+        const double o = a.omega[v];
+        const double on = o + a.dt * exp(a.lnA - a.Ea / (a.Rgas * Tt));
+        a.omega[v] = on;
+#pragma unroll
+        for (int t = 0; t < 3; ++t)
+            if (o < a.thr[t] && on >= a.thr[t]) a.thres[v + t * ni] = a.t_new;
+    }
+    if (Tt >= a.T_abl && a.mat[v] != 0) {
+        a.mat[v] = 0;  // optics -> air
+        ((Real *)a.J)[v] = (Real)0;
+        atomicAdd(a.n_ablated, 1ull);
+    }
+}
+
+
+}  // namespace
+}  // namespace tam

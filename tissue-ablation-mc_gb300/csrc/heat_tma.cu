@@ -1,0 +1,389 @@
+// heat_tma.cu -- the FP32 + Kahan fused heat step with TMA plane staging.
+//
+// The physics of fused_kernel<float, true> (heat.cu) with two changes made
+// for GB300: the face diffusivities k_f/(rho_f c_f) and 1/(rho c), which only
+// change when the properties do, are precomputed per voxel (face_coeff_kernel),
+// and the planes are staged by TMA.  One elected thread streams each z-plane
+// of the block's tile -- T, the Kahan term and the x / y face coefficients
+// with a one-cell x/y halo; the z face coefficient, 1/(rho c) and J --
+// into a ring of shared-memory stages with cp.async.bulk.tensor, three planes
+// ahead of the plane being updated; completion is tracked by one mbarrier per
+// stage (transaction bytes), and every wait is bounded.  The x origin of a
+// tile is rounded down to a 16-byte boundary (bx*32 - 4), so the x halo sits
+// in columns 3 and 36 of a 40-wide row; out-of-range rows, columns and planes
+// read as zeros and are never used (those faces take the boundary path).
+#include <cuda.h>
+
+#include <atomic>
+
+#include "heat_common.cuh"
+
+namespace tam {
+
+struct FusedTma {
+    CUtensorMap T[2], E[2], ax, ay, az, irc, J;
+};
+
+namespace {
+
+constexpr int TS = 4;                                  // shared-memory stages
+constexpr int TPITCH = FX + 8;                         // 40 floats per staged row
+constexpr int TROWS = FY + 2;                          // 10 rows
+constexpr int ARR_BYTES = ((TROWS * TPITCH * 4 + 127) / 128) * 128;  // 1664: T, E, Ax, Ay (with halo)
+constexpr int OWN_BYTES = FY * FX * 4;                 // 1024: Az, 1/(rho c), J (own voxels)
+constexpr int STAGE_BYTES = 4 * ARR_BYTES + 3 * OWN_BYTES;  // 9728
+constexpr uint32_t TX_BYTES = 4u * TROWS * TPITCH * 4 + 3u * FY * FX * 4;  // bytes landed per plane
+constexpr int SMEM_BYTES = TS * STAGE_BYTES + TS * 8 + 128;
+constexpr long long WAIT_CYCLES = 4000000000ll;        // ~2 s at 2 GHz: give up and flag
+
+static_assert(STAGE_BYTES % 128 == 0, "stage alignment");
+
+struct Maps {  // the seven maps of one launch
+    CUtensorMap T, E, ax, ay, az, irc, J;
+};
+
+__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(su32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
+{
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(su32(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
+{
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(ok)
+        : "r"(su32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait for phase `parity` of a stage barrier; false on time-out.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
+{
+    if (mbar_try_wait(bar, parity)) return true;
+    const long long t0 = clock64();
+    while (!mbar_try_wait(bar, parity))
+        if (clock64() - t0 > WAIT_CYCLES) return false;
+    return true;
+}
+__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar)
+{
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::
+            "r"(su32(dst)),
+        "l"(map), "r"(x), "r"(y), "r"(z), "r"(su32(bar))
+        : "memory");
+}
+__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
+
+struct View {  // one staged plane
+    const float *T, *E, *ax, *ay, *az, *irc, *J;
+};
+
+__global__ void __launch_bounds__(FX *FY, 4)
+    fused_tma_kernel(const __grid_constant__ FusedArgs a, const __grid_constant__ Maps m, int zchunk)
+{
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char *sm = smem_raw + ((128 - (su32(smem_raw) & 127)) & 127);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + TS * STAGE_BYTES);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = blockIdx.x * FX + tx, y = blockIdx.y * FY + ty;
+    const bool in = x < a.nx && y < a.ny;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(a.nz, z0 + zchunk);
+    const int nplanes = z1 - z0;
+    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, ni = sz * a.nz;
+    float *To = (float *)a.T_out, *Q = (float *)a.Q;
+    float *Eo = a.Tc_out;
+    const float dt = a.fc[FC_DT], Pdt = a.fc[FC_PDT];
+    const bool src_on = Pdt != 0.f;
+    const bool xy_inner = x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1;
+    const bool leader = tx == 0 && ty == 0;
+    const int gx = blockIdx.x * FX - 4, gy = blockIdx.y * FY - 1;
+    unsigned errbits = 0;
+
+    auto view = [&](int idx) {
+        const unsigned char *b = sm + (idx % TS) * STAGE_BYTES;
+        View v;
+        v.T = (const float *)(b + 0 * ARR_BYTES);
+        v.E = (const float *)(b + 1 * ARR_BYTES);
+        v.ax = (const float *)(b + 2 * ARR_BYTES);
+        v.ay = (const float *)(b + 3 * ARR_BYTES);
+        v.az = (const float *)(b + 4 * ARR_BYTES);
+        v.irc = (const float *)(b + 4 * ARR_BYTES + OWN_BYTES);
+        v.J = (const float *)(b + 4 * ARR_BYTES + 2 * OWN_BYTES);
+        return v;
+    };
+    // plane z0 - 1 + idx into stage idx % TS
+    auto issue = [&](int idx) {
+        unsigned char *b = sm + (idx % TS) * STAGE_BYTES;
+        uint64_t *br = bar + (idx % TS);
+        const int zz = z0 - 1 + idx;
+        fence_proxy_async();
+        mbar_expect_tx(br, TX_BYTES);
+        tma_load_3d(b + 0 * ARR_BYTES, &m.T, gx, gy, zz, br);
+        tma_load_3d(b + 1 * ARR_BYTES, &m.E, gx, gy, zz, br);
+        tma_load_3d(b + 2 * ARR_BYTES, &m.ax, gx, gy, zz, br);
+        tma_load_3d(b + 3 * ARR_BYTES, &m.ay, gx, gy, zz, br);
+        tma_load_3d(b + 4 * ARR_BYTES, &m.az, gx + 4, gy + 1, zz, br);
+        tma_load_3d(b + 4 * ARR_BYTES + OWN_BYTES, &m.irc, gx + 4, gy + 1, zz, br);
+        tma_load_3d(b + 4 * ARR_BYTES + 2 * OWN_BYTES, &m.J, gx + 4, gy + 1, zz, br);
+    };
+    auto wait = [&](int idx) { return mbar_wait(bar + (idx % TS), (uint32_t)((idx / TS) & 1)); };
+
+    if (leader) {
+        for (int s = 0; s < TS; ++s) mbar_init(bar + s, 1);
+        fence_mbar_init();
+        fence_proxy_async();
+    }
+    __syncthreads();
+    if (leader) {
+        issue(0);
+        issue(1);
+        if (nplanes >= 1) issue(2);
+    }
+    // every wait decision is made block-uniform before anyone acts on it
+    bool ok = __syncthreads_and(wait(0) && wait(1)) != 0;
+    const int q = (ty + 1) * TPITCH + tx + 4;  // own voxel in the halo'd arrays
+    const int o = ty * FX + tx;                // own voxel in the own-only arrays
+    // z column in registers: temperature, Kahan term, and the +z face coefficient
+    float Tp = 0.f, ep = 0.f, azp = 0.f, Tc = 0.f, ec = 0.f, azc = 0.f;
+    if (in && ok) {
+        const View C0 = view(1);
+        Tc = C0.T[q];
+        ec = C0.E[q];
+        azc = C0.az[o];
+        if (z0 > 0) {
+            const View Pm = view(0);
+            Tp = Pm.T[q];
+            ep = Pm.E[q];
+            azp = Pm.az[o];
+        }
+    }
+    int issued = nplanes >= 1 ? 3 : 2;  // planes idx < issued are (or were) in flight
+    for (int i = 0; i < nplanes && ok; ++i) {
+        const int z = z0 + i;
+        const int64_t v = (int64_t)x + sy * y + sz * z;
+        const bool has_n = z + 1 < a.nz;
+        if (leader && i + 3 <= nplanes + 1) issue(i + 3);
+        issued = i + 3 <= nplanes + 1 ? i + 4 : issued;
+        ok = __syncthreads_and(wait(i + 2)) != 0;  // plane z+1 has landed for the whole block
+        if (!ok) break;
+        const View P = view(i + 1), N = view(i + 2);
+        float Tn_ = 0.f, en_ = 0.f, azn = 0.f;
+        if (in && has_n) {
+            Tn_ = N.T[q];
+            en_ = N.E[q];
+            azn = N.az[o];
+        }
+        if (in) {
+            const float Jv = src_on ? P.J[o] : 0.f;
+            const float tzm = (Tp - Tc) - (ep - ec), tzp = (Tn_ - Tc) - (en_ - ec);
+            const float txm = (P.T[q - 1] - Tc) - (P.E[q - 1] - ec), txp = (P.T[q + 1] - Tc) - (P.E[q + 1] - ec);
+            const float tym = (P.T[q - TPITCH] - Tc) - (P.E[q - TPITCH] - ec),
+                        typ = (P.T[q + TPITCH] - Tc) - (P.E[q + TPITCH] - ec);
+            float lap;
+            if (xy_inner && z > 0 && has_n) {
+                lap = azp * tzm + azc * tzp + P.ay[q - TPITCH] * tym + P.ay[q] * typ + P.ax[q - 1] * txm +
+                      P.ax[q] * txp;
+            } else {
+                // a face of this voxel lies on the grid boundary: ghost faces
+                // use the voxel's own properties
+                const float kk = ((const float *)a.k)[v], rr = ((const float *)a.rho)[v],
+                            hh = ((const float *)a.c)[v];
+                lap = z > 0 ? azp * tzm : ghost_term<float>(a, 4, Tc, ec, kk, rr, hh);
+                lap += has_n ? azc * tzp : ghost_term<float>(a, 5, Tc, ec, kk, rr, hh);
+                lap += y > 0 ? P.ay[q - TPITCH] * tym : ghost_term<float>(a, 2, Tc, ec, kk, rr, hh);
+                lap += y < a.ny - 1 ? P.ay[q] * typ : ghost_term<float>(a, 3, Tc, ec, kk, rr, hh);
+                lap += x > 0 ? P.ax[q - 1] * txm : ghost_term<float>(a, 0, Tc, ec, kk, rr, hh);
+                lap += x < a.nx - 1 ? P.ax[q] * txp : ghost_term<float>(a, 1, Tc, ec, kk, rr, hh);
+            }
+            const float dT = dt * lap;
+            const float sPJ = Pdt * Jv;
+            const float src = sPJ * P.irc[o];
+            float Tnew, Enew = 0.f;
+            bool clamped = false;
+            if (a.boil && Tc >= a.fc[FC_TBOIL]) {
+                const float rr = ((const float *)a.rho)[v], rc = rr * ((const float *)a.c)[v];
+                const float qv = a.fc[FC_LW] * rr * a.fc[FC_VVOX];
+                const float Qv = Q[v];
+                if (Qv < qv) {
+                    const float Ein = (sPJ + rc * dT) * a.fc[FC_VVOX];
+                    if (Ein > 0.f) {
+                        const float qn = Qv + Ein;
+                        Q[v] = qn < qv ? qn : qv;
+                        Tnew = a.fc[FC_TBOIL];
+                        clamped = true;
+                    }
+                }
+            }
+            if (!clamped) {
+                const float inc = dT + src;
+                const float yk = inc - ec;
+                const float t = Tc + yk;
+                Enew = (t - Tc) - yk;
+                Tnew = t;
+            }
+            To[v] = Tnew;
+            Eo[v] = Enew;
+            const float Ts = Tnew - Enew;
+            if (!(Ts == Ts)) errbits |= DEVERR_NAN;
+            else if (Ts < 0.f) errbits |= DEVERR_NEG_T;
+            if (Ts >= a.fc[FC_SCREEN]) rare_update<float>(a, v, ni, (double)Tnew - (double)Enew);
+        }
+        __syncthreads();  // every thread is done with the stage the next issue overwrites
+        Tp = Tc;
+        ep = ec;
+        azp = azc;
+        Tc = Tn_;
+        ec = en_;
+        azc = azn;
+    }
+    if (!ok) {
+        // a stage never completed: record it and drain what is still in flight
+        errbits |= DEVERR_SYNC_TIMEOUT;
+        for (int idx = 0; idx < issued; ++idx) (void)wait(idx);
+    }
+    if (errbits) atomicOr(a.err, errbits);
+}
+
+CUresult (*p_encode)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *, const cuuint64_t *,
+                     const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                     CUtensorMapL2promotion, CUtensorMapFloatOOBfill) = nullptr;
+
+cudaError_t encoder()
+{
+    if (p_encode) return cudaSuccess;
+    void *fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
+    if (e != cudaSuccess) return e;
+    if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
+    p_encode = reinterpret_cast<decltype(p_encode)>(fn);
+    return cudaSuccess;
+}
+
+cudaError_t encode(CUtensorMap *m, const float *base, int nx, int ny, int nz, int bx, int by)
+{
+    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = p_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)base, dims, strides, box, estr,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// Forward face coefficients of the FP32 step: A_x(v) = opscale/dx^2 *
+// k_f/(rho_f c_f) on the face between v and v+x (arithmetic face means, as
+// in the stencil of src/3dFD.f90:119-164), likewise A_y, A_z; and 1/(rho c).
+__global__ void face_coeff_kernel(const float *k, const float *r, const float *c, float cx, float cy, float cz,
+                                  int nx, int ny, int nz, float *ax, float *ay, float *az, float *irc)
+{
+    const int64_t n = (int64_t)nx * ny * nz, sy = nx, sz = (int64_t)nx * ny;
+    for (int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / sz);
+        Pt<float> self;
+        self.k = k[v];
+        self.r = r[v];
+        self.h = c[v];
+        auto nb = [&](int64_t u) {
+            Pt<float> p;
+            p.k = k[u];
+            p.r = r[u];
+            p.h = c[u];
+            return p;
+        };
+        ax[v] = x + 1 < nx ? cx * falpha(self, nb(v + 1)) : 0.f;
+        ay[v] = y + 1 < ny ? cy * falpha(self, nb(v + sy)) : 0.f;
+        az[v] = z + 1 < nz ? cz * falpha(self, nb(v + sz)) : 0.f;
+        irc[v] = 1.f / (self.r * self.h);
+    }
+}
+
+}  // namespace
+
+cudaError_t launch_face_coeffs(const FusedArgs &a0, float *ax, float *ay, float *az, float *irc, cudaStream_t s)
+{
+    FusedArgs a = a0;
+    fill_fused_consts(a);
+    const int64_t n = (int64_t)a.nx * a.ny * a.nz;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    count_launch();
+    face_coeff_kernel<<<(unsigned)blocks, 256, 0, s>>>((const float *)a.k, (const float *)a.rho, (const float *)a.c,
+                                                       a.fc[FC_CX], a.fc[FC_CY], a.fc[FC_CZ], a.nx, a.ny, a.nz, ax,
+                                                       ay, az, irc);
+    return cudaGetLastError();
+}
+
+bool fused_tma_supported(int nx) { return nx >= 1 && (nx * 4) % 16 == 0; }
+
+cudaError_t fused_tma_create(FusedTma **out, int nx, int ny, int nz, float *const T[2], float *const Tc[2],
+                             const float *ax, const float *ay, const float *az, const float *irc, const float *J)
+{
+    *out = nullptr;
+    if (!fused_tma_supported(nx)) return cudaErrorNotSupported;
+    cudaError_t e = encoder();
+    if (e != cudaSuccess) return e;
+    FusedTma *m = new FusedTma();
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+        e = encode(&m->T[b], T[b], nx, ny, nz, TPITCH, TROWS);
+        if (e == cudaSuccess) e = encode(&m->E[b], Tc[b], nx, ny, nz, TPITCH, TROWS);
+    }
+    if (e == cudaSuccess) e = encode(&m->ax, ax, nx, ny, nz, TPITCH, TROWS);
+    if (e == cudaSuccess) e = encode(&m->ay, ay, nx, ny, nz, TPITCH, TROWS);
+    if (e == cudaSuccess) e = encode(&m->az, az, nx, ny, nz, FX, FY);
+    if (e == cudaSuccess) e = encode(&m->irc, irc, nx, ny, nz, FX, FY);
+    if (e == cudaSuccess) e = encode(&m->J, J, nx, ny, nz, FX, FY);
+    if (e != cudaSuccess) {
+        delete m;
+        return e;
+    }
+    *out = m;
+    return cudaSuccess;
+}
+
+void fused_tma_destroy(FusedTma *m) { delete m; }
+
+cudaError_t launch_fused_tma(const FusedArgs &a0, const FusedTma *tm, int which, cudaStream_t s)
+{
+    FusedArgs a = a0;
+    fill_fused_consts(a);
+    Maps m;
+    m.T = tm->T[which];
+    m.E = tm->E[which];
+    m.ax = tm->ax;
+    m.ay = tm->ay;
+    m.az = tm->az;
+    m.irc = tm->irc;
+    m.J = tm->J;
+    const int bx = (a.nx + FX - 1) / FX, by = (a.ny + FY - 1) / FY;
+    int zchunk = a.zchunk > 0 ? a.zchunk : 16;
+    if (zchunk > a.nz) zchunk = a.nz;
+    const int chunks = (a.nz + zchunk - 1) / zchunk;
+    static std::atomic<unsigned long long> attr_set{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(attr_set.load() & bit)) {
+        e = cudaFuncSetAttribute(fused_tma_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+        if (e != cudaSuccess) return e;
+        attr_set.fetch_or(bit);
+    }
+    count_launch();
+    fused_tma_kernel<<<dim3(bx, by, chunks), dim3(FX, FY), SMEM_BYTES, s>>>(a, m, zchunk);
+    return cudaGetLastError();
+}
+
+}  // namespace tam

@@ -89,6 +89,14 @@ struct tam_ctx {
     bool need_trace = true;
     long long nabl_at_trace = 0;
 
+    // tuning knobs
+    int scat_min = 16;
+    int zchunk = 0;
+    bool use_tma = true;
+    tam::FusedTma *tma = nullptr;  // tensor maps of the FP32 fused step
+    float *d_ax = nullptr, *d_ay = nullptr, *d_az = nullptr, *d_irc = nullptr;  // its face coefficients
+    bool coeff_dirty = true;
+
     // CUDA events around the transport kernel and the heat loop
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
     bool have_mc_time = false, have_heat_time = false;
@@ -352,6 +360,7 @@ int cfg_setup(tam_ctx *ctx)
     const uint8_t m0 = (uint8_t)(c.nmat > 1 ? 1 : 0);
     CK(tam::launch_fill_u8(ctx->d_mat, m0, ctx->ni, s));
     CK(tam::launch_props_from_mat(ctx->d_mat, c.nmat, ctx->lut, ctx->d_k, ctx->d_rho, ctx->d_c, ctx->fp64, ctx->ni, s));
+    ctx->coeff_dirty = true;
     for (int b = 0; b < 2; ++b) {
         CK(tam::launch_fill_real(ctx->d_Tf[b], ctx->fp64, c.T0, ctx->ni, s));
         if (!ctx->fp64) CK(cudaMemsetAsync(ctx->d_Tc[b], 0, ctx->ni * sizeof(float), s));
@@ -411,6 +420,7 @@ tam::FusedArgs fused_args(tam_ctx *ctx)
     a.mat = ctx->d_mat;
     a.n_ablated = ctx->d_nabl;
     a.err = ctx->d_err;
+    a.zchunk = ctx->zchunk;
     return a;
 }
 
@@ -458,6 +468,7 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream)
         a.max_steps = (int64_t)1 << 40;
         a.nudge = ctx->delta;  // src/mcpolar.f90:112
     }
+    a.scat_min = ctx->scat_min;
     a.seed = seed;
     a.stream = stream;
     a.p0 = 0;
@@ -578,6 +589,10 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
 {
     tam::FusedArgs a = fused_args(ctx);
     const int check = ctx->cfg.retrace_check > 0 ? ctx->cfg.retrace_check : 0;
+    if (ctx->tma && ctx->use_tma && ctx->coeff_dirty && nsteps > 0) {
+        CK(tam::launch_face_coeffs(a, ctx->d_ax, ctx->d_ay, ctx->d_az, ctx->d_irc, ctx->stream));
+        ctx->coeff_dirty = false;
+    }
     CK(cudaEventRecord(ctx->ev[2], ctx->stream));
     for (int32_t it = 0; it < nsteps; ++it) {
         a.T_in = ctx->d_Tf[ctx->fcur];
@@ -586,7 +601,8 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
         a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[1 - ctx->fcur];
         a.P = ctx->laserOn * get_pwr(ctx);
         a.t_new = ctx->time + ctx->cdt;
-        CK(tam::launch_fused_step(a, ctx->fp64, ctx->stream));
+        if (ctx->tma && ctx->use_tma) CK(tam::launch_fused_tma(a, ctx->tma, ctx->fcur, ctx->stream));
+        else CK(tam::launch_fused_step(a, ctx->fp64, ctx->stream));
         ctx->fcur = 1 - ctx->fcur;
         const bool on = pulse_update(ctx, ctx->cdt);
         const bool last = it + 1 == nsteps;
@@ -913,6 +929,18 @@ int tam_create(const tam_params *p, const tam_config *cfg, tam_ctx **out)
         return bail(fail(nullptr, TAM_E_CUDA, "initial memset failed"));
     if (!ctx->config && cudaMemsetAsync(ctx->d_jglob, 0, ctx->ni * 8, ctx->stream) != cudaSuccess)
         return bail(fail(nullptr, TAM_E_CUDA, "initial memset failed"));
+    if (ctx->config && !ctx->fp64 && tam::fused_tma_supported(ctx->nx)) {
+        float *T2[2] = {(float *)ctx->d_Tf[0], (float *)ctx->d_Tf[1]};
+        float *E2[2] = {ctx->d_Tc[0], ctx->d_Tc[1]};
+        if (dalloc_t(ctx, &ctx->d_ax, ctx->ni) != TAM_OK || dalloc_t(ctx, &ctx->d_ay, ctx->ni) != TAM_OK ||
+            dalloc_t(ctx, &ctx->d_az, ctx->ni) != TAM_OK || dalloc_t(ctx, &ctx->d_irc, ctx->ni) != TAM_OK)
+            return bail(TAM_E_NOMEM);
+        if (tam::fused_tma_create(&ctx->tma, ctx->nx, ctx->ny, ctx->nz, T2, E2, ctx->d_ax, ctx->d_ay, ctx->d_az,
+                                  ctx->d_irc, (const float *)ctx->d_J) != cudaSuccess) {
+            (void)cudaGetLastError();
+            ctx->tma = nullptr;  // the cp.async form runs instead
+        }
+    }
     r = ctx->config ? cfg_setup(ctx) : ref_setup(ctx);
     if (r == TAM_OK) r = finish(ctx, "tam_create");
     if (r != TAM_OK) {
@@ -931,6 +959,7 @@ int tam_destroy(tam_ctx *ctx)
     for (void *p : ctx->allocs) cudaFree(p);
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
+    if (ctx->tma) tam::fused_tma_destroy(ctx->tma);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return TAM_OK;
@@ -1079,6 +1108,7 @@ int tam_upload(tam_ctx *ctx, int field, const void *host, int64_t nbytes)
         CK(cudaMemcpyAsync(ctx->d_halo, host, b, cudaMemcpyHostToDevice, s));
         void *dst = field == TAM_F_KAPPA ? ctx->d_k : (field == TAM_F_DENSITY ? ctx->d_rho : ctx->d_c);
         CK(tam::launch_halo_to_interior(ctx->d_halo, dst, ctx->fp64, ctx->nx, ctx->ny, ctx->nz, s));
+        ctx->coeff_dirty = true;
         break;
     }
     case TAM_F_JMEAN: CK(h2d(ctx->d_jmean)); break;
@@ -1096,6 +1126,7 @@ int tam_upload(tam_ctx *ctx, int field, const void *host, int64_t nbytes)
         CK(h2d(ctx->d_mat));
         CK(tam::launch_props_from_mat(ctx->d_mat, ctx->cfg.nmat, ctx->lut, ctx->d_k, ctx->d_rho, ctx->d_c, ctx->fp64,
                                       ctx->ni, s));
+        ctx->coeff_dirty = true;
         ctx->need_trace = true;
         break;
     default: return fail(ctx, TAM_E_STATE, "field not uploadable in config mode");
@@ -1322,6 +1353,24 @@ int tam_get_timing(tam_ctx *ctx, double *transport_ms, double *heat_ms, int64_t 
 }
 
 int64_t tam_kernel_launches(void) { return tam::launch_count(); }
+
+int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
+{
+    if (!ctx || !key) return fail(ctx, TAM_E_INVALID, "null argument");
+    const std::string k(key);
+    if (k == "transport.scat_min") {
+        if (value < 1 || value > 32) return fail(ctx, TAM_E_INVALID, "transport.scat_min must be in 1..32");
+        ctx->scat_min = (int)value;
+    } else if (k == "heat.tma") {
+        ctx->use_tma = value != 0;
+    } else if (k == "heat.zchunk") {
+        if (value < 0 || value > ctx->nz) return fail(ctx, TAM_E_INVALID, "heat.zchunk must be in 0..nz");
+        ctx->zchunk = (int)value;
+    } else {
+        return fail(ctx, TAM_E_INVALID, "unknown tuning key " + k);
+    }
+    return TAM_OK;
+}
 
 namespace {
 // str() of src/utils.f90:109-207: integers optionally zero-padded to len;

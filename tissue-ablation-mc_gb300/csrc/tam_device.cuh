@@ -15,6 +15,7 @@ enum : unsigned {
     DEVERR_NAN = 1u << 1,         // a packet direction or a temperature became NaN
     DEVERR_NEG_T = 1u << 2,       // negative kelvin (src/3dFD.f90:179-182, thermalConst_mod.f90:20-23)
     DEVERR_EVENT_OVF = 1u << 3,   // event list overflow
+    DEVERR_SYNC_TIMEOUT = 1u << 4, // a bounded wait on an asynchronous copy gave up
 };
 
 // Truncated constants of src/constants.f90:13 (promoted to FP64).

@@ -46,6 +46,7 @@ struct TransportArgs {
     int64_t p0, n;
     int64_t max_steps;
     double nudge;                     // offset past a crossed face (reference delta), 0 in config mode
+    int32_t scat_min;                 // lanes that must wait before a warp scatters (0: default)
     double *jmean;                    // interior, packet units (sum of w*d*mua)
     double *tally;                    // N_TALLY doubles
     unsigned long long *work;         // dynamic packet counter (zeroed by the launcher)
@@ -106,6 +107,16 @@ cudaError_t launch_ref_finalize(int nx, int ny, int nz, const double *rhokap, do
 // --------------------------------------------------- fused config-mode step --
 enum Bc : int32_t { BC_DIRICHLET = 0, BC_ROBIN = 1 };
 
+// Slots of the pre-converted constant table of the fused step.
+enum FusedConst : int {
+    FC_CX = 0, FC_CY, FC_CZ,          // opscale / d^2 per axis
+    FC_DT, FC_PDT, FC_VVOX, FC_TBOIL, FC_LW, FC_TLO_S, FC_TABL_S, FC_SCREEN,
+    FC_BCT = 11,                      // 6 Dirichlet face temperatures
+    FC_BCHD = 17,                     // 6 Robin h * d (d: spacing normal to the face)
+    FC_BCTA = 23,                     // 6 Robin ambient temperatures
+    FC_N = 29
+};
+
 struct FusedArgs {
     int32_t nx, ny, nz;
     double dx, dy, dz;                // m
@@ -128,9 +139,28 @@ struct FusedArgs {
     uint8_t *mat;
     unsigned long long *n_ablated;    // running count
     unsigned *err;
+    int32_t zchunk;                   // z planes per thread column (0: automatic)
+    // the constants above in the kernel's storage precision (filled by
+    // launch_fused_step), so the kernel converts nothing per voxel
+    float fc[FC_N];
+    double dc[FC_N];
 };
 // fp64 == false: FP32 storage with Kahan compensation; true: plain FP64.
 cudaError_t launch_fused_step(const FusedArgs &a, bool fp64, cudaStream_t s);
+// Fill FusedArgs::fc / dc from the physical constants.
+void fill_fused_consts(FusedArgs &a);
+
+// TMA form of the FP32 fused step.  Needs nx * 4 bytes to be a multiple of
+// 16 (TMA row strides); tensor maps are built once per buffer set.
+struct FusedTma;  // opaque: tensor maps of T[2], Tc[2], Ax, Ay, Az, 1/(rho c), J
+bool fused_tma_supported(int nx);
+cudaError_t fused_tma_create(FusedTma **out, int nx, int ny, int nz, float *const T[2], float *const Tc[2],
+                             const float *ax, const float *ay, const float *az, const float *irc, const float *J);
+// Face coefficients (and 1/(rho c)) of the TMA form from k, rho, c.
+cudaError_t launch_face_coeffs(const FusedArgs &a, float *ax, float *ay, float *az, float *irc, cudaStream_t s);
+void fused_tma_destroy(FusedTma *m);
+// `which` selects the (T, Tc) buffer pair read by this step (0 or 1).
+cudaError_t launch_fused_tma(const FusedArgs &a, const FusedTma *m, int which, cudaStream_t s);
 
 // Halo (reference-layout) FP64 temperature from the interior state, with
 // ghosts filled from the boundary conditions.

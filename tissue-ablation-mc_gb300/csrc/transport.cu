@@ -31,7 +31,7 @@ template <typename Real> struct MatR {
 // the truncated constants of src/constants.f90:13).  Leaves the direction
 // unchanged when the sampled cosine is exactly +-1 (the `goto 100`).
 template <typename Real>
-__device__ __forceinline__ void stokes(Real hgg, Real g2, Real u0, Real u1, Real &cost, Real &sint, Real &phi,
+__device__ __forceinline__ bool stokes(Real hgg, Real g2, Real u0, Real u1, Real &cost, Real &sint, Real &phi,
                                        Real &cosp, Real &sinp)
 {
     const Real PI = (Real)PI_R, TWOPI = (Real)TWOPI_R;
@@ -42,7 +42,7 @@ __device__ __forceinline__ void stokes(Real hgg, Real g2, Real u0, Real u1, Real
         sint = s2 <= (Real)0 ? (Real)0 : M<Real>::sqrt(s2);
         phi = TWOPI * u1;
         M<Real>::sincos(phi, &sinp, &cosp);
-        return;
+        return true;
     }
     const Real costp = cost, sintp = sint, phip = phi;
     const Real t = M<Real>::div(one - g2, one - hgg + (Real)2 * hgg * u0);
@@ -52,7 +52,7 @@ __device__ __forceinline__ void stokes(Real hgg, Real g2, Real u0, Real u1, Real
         bmu = bmu > one ? one : -one;
         cosb2 = one;
     }
-    if (bmu == one || bmu == -one) return;
+    if (bmu == one || bmu == -one) return false;  // direction unchanged
     const Real sinbt = M<Real>::sqrt(one - cosb2);
     const Real ri1 = TWOPI * u1;
     const bool upper = ri1 > PI;
@@ -79,6 +79,7 @@ __device__ __forceinline__ void stokes(Real hgg, Real g2, Real u0, Real u1, Real
     if (phi > TWOPI) phi = phi - TWOPI;
     if (phi < (Real)0) phi = phi + TWOPI;
     M<Real>::sincos(phi, &sinp, &cosp);
+    return true;
 }
 
 // Unpolarised Fresnel reflectance n1 -> n2 at incidence cosine cosi.
@@ -108,44 +109,54 @@ template <typename Real> __device__ __forceinline__ double warp_sum(Real v)
     return d;
 }
 
+// Optical properties of the current cell: extinction and absorption for the
+// DDA, the material id for the albedo / HG / index lookups at events.
 template <typename Real, int MED>
-__device__ __forceinline__ void lookup(const TransportArgs &a, const MatR<Real> *lut, int ix, int iy, int iz,
-                                       MatR<Real> &m)
+__device__ __forceinline__ void fetch(const TransportArgs &a, const MatR<Real> *lut, int ix, int iy, int iz,
+                                      int cidx, Real &mut, Real &mua, int &mid)
 {
     if (MED == MED_RHOKAP) {
         const int64_t hx = a.nx + 2, hy = a.ny + 2;
         const Real v = (Real)__ldg(a.rhokap + ((ix + 1) + hx * ((iy + 1) + hy * (int64_t)(iz + 1))));
-        m.mut = v;
-        m.mua = v;
-        m.alb = (Real)0;
-        m.g = (Real)0;
-        m.g2 = (Real)0;
-        m.n = (Real)a.rhokap_n;
+        mut = v;
+        mua = v;
+        mid = 0;
     } else {
-        int id = __ldg(a.mat + (ix + (int64_t)a.nx * (iy + (int64_t)a.ny * iz)));
-        if (id >= a.nmat) id = 0;
-        m = lut[id];
+        int id = __ldg(a.mat + cidx);
+        id = id < a.nmat ? id : 0;
+        mid = id;
+        mut = lut[id].mut;
+        mua = lut[id].mua;
     }
 }
 
-template <typename Real, int MED> __global__ void __launch_bounds__(TPB) transport_kernel(const TransportArgs a)
+enum : int { M_DEAD = 0, M_FLY = 1, M_SCAT = 2 };
+
+// Event loop per lane: DEAD (needs a packet) -> FLY (one voxel step per
+// iteration: cross a face, reach an outer face, or reach the interaction
+// point) -> SCAT (waits at the interaction point) -> FLY ...  The scatter
+// (Philox block, HG rotation, roulette, new optical depth) is the expensive
+// part; it runs once at least scat_min lanes of the warp wait for it, or when
+// no lane is flying, so it executes with most lanes active.  Every packet
+// sees the same sequence of events and random numbers as a straight loop.
+template <typename Real, int MED>
+__global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 4 : 2) transport_kernel(const TransportArgs a, int scat_min)
 {
     __shared__ MatR<Real> lut[MAX_MAT];
-    if (MED == MED_MATERIAL) {
-        for (int t = threadIdx.x; t < MAX_MAT; t += blockDim.x) {
-            const OptMat &o = a.lut[t < a.nmat ? t : 0];
-            MatR<Real> m;
-            m.mut = (Real)(o.mua + o.mus);
-            m.mua = (Real)o.mua;
-            m.alb = (o.mua + o.mus) > 0.0 ? (Real)(o.mus / (o.mua + o.mus)) : (Real)0;
-            m.g = (Real)o.g;
-            m.g2 = (Real)(o.g * o.g);
-            m.n = (Real)o.n;
-            lut[t] = m;
-        }
+    for (int t = threadIdx.x; t < MAX_MAT; t += blockDim.x) {
+        const OptMat &o = a.lut[t < a.nmat ? t : 0];
+        MatR<Real> m;
+        m.mut = (Real)(o.mua + o.mus);
+        m.mua = (Real)o.mua;
+        m.alb = (o.mua + o.mus) > 0.0 ? (Real)(o.mus / (o.mua + o.mus)) : (Real)0;
+        m.g = (Real)o.g;
+        m.g2 = (Real)(o.g * o.g);
+        m.n = (Real)o.n;
+        lut[t] = m;
     }
     __syncthreads();
 
+    const unsigned FULL = 0xffffffffu;
     const Real hx = (Real)(2.0 * a.xmax / a.nx), hy = (Real)(2.0 * a.ymax / a.ny), hz = (Real)(2.0 * a.zmax / a.nz);
     const Real BIG = (Real)1.0e30;
     const Real TWOPI = (Real)TWOPI_R;
@@ -153,36 +164,34 @@ template <typename Real, int MED> __global__ void __launch_bounds__(TPB) transpo
     const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
     const unsigned lane = threadIdx.x & 31u;
     const Real wmin = (Real)a.roulette_w, rm = (Real)a.roulette_m, inv_rm = (Real)(1.0 / a.roulette_m);
+    const int NX = a.nx, NY = a.ny, NZ = a.nz, SY = a.nx, SZ = a.nx * a.ny;
+    const uint32_t max_steps = a.max_steps > 0xfffffff0ll ? 0xfffffff0u : (uint32_t)a.max_steps;
+    const Real namb = (Real)a.n_ambient;
 
-    // packet state
-    bool alive = false, exhausted = false;
-    int ix = 0, iy = 0, iz = 0;
-    Real fx = 0, fy = 0, fz = 0;
-    Real cost = 0, sint = 0, phi = 0, cosp = 0, sinp = 0;
-    Real nx = 0, ny = 0, nz = 0, inx = 0, iny = 0, inz = 0;
-    Real w = 0, tau = 0, dep = 0;
-    uint32_t ev = 0, plo = 0, phi32 = 0;
-    int64_t nsteps = 0;
-    MatR<Real> m;
-    m.mut = m.mua = m.alb = m.g = m.g2 = m.n = (Real)0;
-    // per-thread tallies
-    Real tSpec = 0, tRefl = 0, tTran = 0, tSide = 0, tRN = 0, tMiss = 0;
-    unsigned long long cSteps = 0, cScat = 0, cOvf = 0;
+    int mode = M_DEAD;
+    bool exhausted = false;
+    int ix = 0, iy = 0, iz = 0, cidx = 0, mid = 0;
+    Real fx = 0, fy = 0, fz = 0, nx = 0, ny = 0, nz = 0, inx = 0, iny = 0, inz = 0, sint = 0, phi = 0;
+    Real w = 0, tau = 0, dep = 0, mut = 0, mua = 0;
+    uint32_t ev = 0, plo = 0, phi32 = 0, nsteps = 0;
+    Real tSpec = 0, tRefl = 0, tTran = 0, tSide = 0, tRN = 0;
+    uint32_t cSteps = 0, cScat = 0;
     unsigned errbits = 0;
 
     for (;;) {
-        const unsigned need = __ballot_sync(0xffffffffu, !alive && !exhausted);
+        // ---------------------------------------------- refill dead lanes --
+        const unsigned need = __ballot_sync(FULL, mode == M_DEAD && !exhausted);
         if (need) {
             const int leader = __ffs(need) - 1;
             unsigned long long base = 0;
             if ((int)lane == leader) base = atomicAdd(a.work, (unsigned long long)__popc(need));
-            base = __shfl_sync(0xffffffffu, base, leader);
-            if (!alive && !exhausted) {
+            base = __shfl_sync(FULL, base, leader);
+            if (mode == M_DEAD && !exhausted) {
                 const unsigned long long my = base + __popc(need & ((1u << lane) - 1u));
                 if (my >= (unsigned long long)a.n) {
                     exhausted = true;
                 } else {
-                    // ---- launch (src/sourceph.f90:7-49 / Gaussian beam) ----
+                    // launch (src/sourceph.f90:7-49; Gaussian beam in config mode)
                     const uint64_t pid = (uint64_t)a.p0 + my;
                     plo = (uint32_t)pid;
                     phi32 = (uint32_t)(pid >> 32);
@@ -193,220 +202,216 @@ template <typename Real, int MED> __global__ void __launch_bounds__(TPB) transpo
                     const Real R = (Real)a.source_radius;
                     const Real rad = a.source == SRC_DISK ? M<Real>::sqrt(u0 * (R * R))
                                                           : R * M<Real>::sqrt((Real)-0.5 * M<Real>::log(u0));
-                    Real st, ct;
+                    Real st, ct, sp, cp;
                     M<Real>::sincos(u1 * TWOPI, &st, &ct);
                     const Real X = rad * ct + (Real)a.xmax, Y = rad * st + (Real)a.ymax;
                     phi = TWOPI * u2;
-                    M<Real>::sincos(phi, &sinp, &cosp);
-                    cost = (Real)-1;
+                    M<Real>::sincos(phi, &sp, &cp);
                     sint = (Real)0;
                     if (!(X >= (Real)0 && X < (Real)(2.0 * a.xmax) && Y >= (Real)0 && Y < (Real)(2.0 * a.ymax))) {
-                        tMiss += (Real)1;
+                        atomicAdd(a.tally + T_MISSED, 1.0);
                     } else {
-                        ix = (int)((Real)a.nx * X / (Real)(2.0 * a.xmax));
-                        iy = (int)((Real)a.ny * Y / (Real)(2.0 * a.ymax));
-                        ix = ix > a.nx - 1 ? a.nx - 1 : ix;
-                        iy = iy > a.ny - 1 ? a.ny - 1 : iy;
-                        iz = a.nz - 1;
+                        ix = (int)((Real)NX * X / (Real)(2.0 * a.xmax));
+                        iy = (int)((Real)NY * Y / (Real)(2.0 * a.ymax));
+                        ix = ix > NX - 1 ? NX - 1 : ix;
+                        iy = iy > NY - 1 ? NY - 1 : iy;
+                        iz = NZ - 1;
+                        cidx = ix + SY * iy + SZ * iz;
                         fx = X - (Real)ix * hx;
                         fy = Y - (Real)iy * hy;
                         fz = hz - (Real)1.e-8 * hz;
-                        lookup<Real, MED>(a, lut, ix, iy, iz, m);
+                        fetch<Real, MED>(a, lut, ix, iy, iz, cidx, mut, mua, mid);
                         w = (Real)1;
                         if (a.fresnel) {
-                            Real rsp = ((Real)a.n_ambient - m.n) / ((Real)a.n_ambient + m.n);
+                            const Real nt = MED == MED_RHOKAP ? (Real)a.rhokap_n : lut[mid].n;
+                            Real rsp = (namb - nt) / (namb + nt);
                             rsp = rsp * rsp;
                             tSpec += rsp;
                             w = (Real)1 - rsp;
                         }
                         tau = -M<Real>::log(u3);
-                        nx = sint * cosp;
-                        ny = sint * sinp;
-                        nz = cost;
+                        nx = sint * cp;  // direction (0, 0, -1): +-0 in x and y
+                        ny = sint * sp;
+                        nz = (Real)-1;
                         inx = (Real)1 / nx;
                         iny = (Real)1 / ny;
                         inz = (Real)1 / nz;
                         dep = (Real)0;
                         nsteps = 0;
-                        alive = true;
+                        mode = M_FLY;
                     }
                 }
             }
         }
-        if (__all_sync(0xffffffffu, exhausted && !alive)) break;
-        if (!alive) continue;
+        if (__ballot_sync(FULL, mode != M_DEAD) == 0) {
+            if (__all_sync(FULL, exhausted)) break;
+            continue;
+        }
 
-        // ---- flight: cross voxels until the interaction point (src/inttau2.f90:37-63) ----
-        bool interact = false;
-        for (;;) {
-            if (++nsteps > a.max_steps) {
-                cOvf += 1;
+        // -------------------------- one voxel step (src/inttau2.f90:37-63) --
+        if (mode == M_FLY) {
+            if (++nsteps > max_steps) {
+                if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
+                dep = (Real)0;
+                atomicAdd(a.tally + T_OVERFLOW, 1.0);
                 errbits |= DEVERR_STEP_CAP;
-                alive = false;
-                break;
-            }
-            Real ddx = nx > (Real)0 ? (hx - fx) * inx : (nx < (Real)0 ? -fx * inx : BIG);
-            Real ddy = ny > (Real)0 ? (hy - fy) * iny : (ny < (Real)0 ? -fy * iny : BIG);
-            Real ddz = nz > (Real)0 ? (hz - fz) * inz : (nz < (Real)0 ? -fz * inz : BIG);
-            ddx = ddx < (Real)0 ? (Real)0 : ddx;
-            ddy = ddy < (Real)0 ? (Real)0 : ddy;
-            ddz = ddz < (Real)0 ? (Real)0 : ddz;
-            // tie order of src/inttau2.f90:116-118 (z over y over x)
-            int ax = 2;
-            Real dw = ddz;
-            if (ddy < dw) { dw = ddy; ax = 1; }
-            if (ddx < dw) { dw = ddx; ax = 0; }
-            const Real taucell = dw * m.mut;
-            if (taucell < tau) {
-                dep += w * dw * m.mua;
-                tau -= taucell;
-                int nxt;
-                Real nc;
-                if (ax == 0) {
-                    fy = clamp0h(fy + ny * dw, hy);
-                    fz = clamp0h(fz + nz * dw, hz);
-                    nc = nx;
-                    nxt = nx > (Real)0 ? ix + 1 : ix - 1;
-                } else if (ax == 1) {
-                    fx = clamp0h(fx + nx * dw, hx);
-                    fz = clamp0h(fz + nz * dw, hz);
-                    nc = ny;
-                    nxt = ny > (Real)0 ? iy + 1 : iy - 1;
-                } else {
-                    fx = clamp0h(fx + nx * dw, hx);
-                    fy = clamp0h(fy + ny * dw, hy);
-                    nc = nz;
-                    nxt = nz > (Real)0 ? iz + 1 : iz - 1;
-                }
-                const int nax = ax == 0 ? a.nx : (ax == 1 ? a.ny : a.nz);
-                // flush the visit's deposit before leaving the cell
-                if (dep != (Real)0) {
-                    atomicAdd(a.jmean + (ix + (int64_t)a.nx * (iy + (int64_t)a.ny * iz)), (double)dep);
+                cSteps += nsteps;
+                mode = M_DEAD;
+            } else {
+                Real ddx = nx > (Real)0 ? (hx - fx) * inx : (nx < (Real)0 ? -fx * inx : BIG);
+                Real ddy = ny > (Real)0 ? (hy - fy) * iny : (ny < (Real)0 ? -fy * iny : BIG);
+                Real ddz = nz > (Real)0 ? (hz - fz) * inz : (nz < (Real)0 ? -fz * inz : BIG);
+                ddx = ddx < (Real)0 ? (Real)0 : ddx;
+                ddy = ddy < (Real)0 ? (Real)0 : ddy;
+                ddz = ddz < (Real)0 ? (Real)0 : ddz;
+                // tie order of src/inttau2.f90:116-118 (z over y over x)
+                int ax = 2;
+                Real dw = ddz;
+                if (ddy < dw) { dw = ddy; ax = 1; }
+                if (ddx < dw) { dw = ddx; ax = 0; }
+                const Real taucell = dw * mut;
+                if (taucell < tau) {
+                    dep += w * dw * mua;
+                    tau -= taucell;
+                    const bool cx = ax == 0, cy = ax == 1, cz = ax == 2;
+                    const int sx = nx > (Real)0 ? 1 : -1, sy = ny > (Real)0 ? 1 : -1, sz = nz > (Real)0 ? 1 : -1;
+                    // the two other coordinates advance; the crossed one steps a cell
+                    fx = cx ? fx : clamp0h(fx + nx * dw, hx);
+                    fy = cy ? fy : clamp0h(fy + ny * dw, hy);
+                    fz = cz ? fz : clamp0h(fz + nz * dw, hz);
+                    const int jx = ix + (cx ? sx : 0), jy = iy + (cy ? sy : 0), jz = iz + (cz ? sz : 0);
+                    const bool out = (unsigned)jx >= (unsigned)NX || (unsigned)jy >= (unsigned)NY ||
+                                     (unsigned)jz >= (unsigned)NZ;
+                    if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
                     dep = (Real)0;
-                }
-                if (nxt < 0 || nxt >= nax) {
-                    const Real hn = ax == 0 ? hx : (ax == 1 ? hy : hz);
-                    const Real face = nc > (Real)0 ? hn : (Real)0;
-                    if (ax == 0) fx = face;
-                    else if (ax == 1) fy = face;
-                    else fz = face;
-                    if (a.fresnel) {
-                        const U4 r = philox4x32_10(ev++, plo, phi32, a.stream, k0, k1);
-                        const Real R = fresnel<Real>(m.n, (Real)a.n_ambient, M<Real>::abs(nc));
-                        if (Uniform<Real>::from(r.x) < R) {
-                            if (ax == 2) {
-                                cost = -cost;
-                            } else if (ax == 0) {
-                                cosp = -cosp;
+                    if (!out) {
+                        ix = jx;
+                        iy = jy;
+                        iz = jz;
+                        cidx += cx ? sx : (cy ? sy * SY : sz * SZ);
+                        // the reference snaps a crossed coordinate to the face +- delta
+                        // (src/inttau2.f90:140-169); nudge carries that delta
+                        fx = cx ? (sx > 0 ? nudge : hx - nudge) : fx;
+                        fy = cy ? (sy > 0 ? nudge : hy - nudge) : fy;
+                        fz = cz ? (sz > 0 ? nudge : hz - nudge) : fz;
+                        fetch<Real, MED>(a, lut, ix, iy, iz, cidx, mut, mua, mid);
+                    } else {
+                        // outer face: stay in the cell on the face; Fresnel or escape
+                        fx = cx ? (sx > 0 ? hx : (Real)0) : fx;
+                        fy = cy ? (sy > 0 ? hy : (Real)0) : fy;
+                        fz = cz ? (sz > 0 ? hz : (Real)0) : fz;
+                        const Real nc = cx ? nx : (cy ? ny : nz);
+                        bool reflect = false;
+                        if (a.fresnel) {
+                            const U4 r = philox4x32_10(ev++, plo, phi32, a.stream, k0, k1);
+                            const Real nt = MED == MED_RHOKAP ? (Real)a.rhokap_n : lut[mid].n;
+                            reflect = Uniform<Real>::from(r.x) < fresnel<Real>(nt, namb, M<Real>::abs(nc));
+                        }
+                        if (reflect) {
+                            if (cz) {
+                                nz = -nz;
+                                inz = -inz;
+                            } else if (cx) {
+                                nx = -nx;
+                                inx = -inx;
                                 phi = (Real)PI_R - phi;
                                 if (phi < (Real)0) phi += TWOPI;
                             } else {
-                                sinp = -sinp;
+                                ny = -ny;
+                                iny = -iny;
                                 phi = TWOPI - phi;
                             }
-                            nx = sint * cosp;
-                            ny = sint * sinp;
+                        } else {
+                            if (cz) {
+                                if (sz > 0) tRefl += w;
+                                else tTran += w;
+                            } else {
+                                tSide += w;
+                            }
+                            cSteps += nsteps;
+                            mode = M_DEAD;
+                        }
+                    }
+                } else {
+                    const Real dd = M<Real>::div(tau, mut);
+                    dep += w * dd * mua;
+                    fx = clamp0h(fx + nx * dd, hx);
+                    fy = clamp0h(fy + ny * dd, hy);
+                    fz = clamp0h(fz + nz * dd, hz);
+                    mode = M_SCAT;
+                }
+            }
+        }
+
+        // ---------- interaction: implicit capture, HG scatter, roulette --
+        const unsigned sc = __ballot_sync(FULL, mode == M_SCAT);
+        if (sc) {
+            const unsigned fl = __ballot_sync(FULL, mode == M_FLY);
+            if (__popc(sc) >= scat_min || fl == 0) {
+                if (mode == M_SCAT) {
+                    const Real alb = MED == MED_RHOKAP ? (Real)0 : lut[mid].alb;
+                    w *= alb;
+                    bool die = !(w > (Real)0);
+                    if (!die) {
+                        cScat += 1;
+                        const U4 r = philox4x32_10(ev++, plo, phi32, a.stream, k0, k1);
+                        Real cost = nz, cp, sp;
+                        if (stokes<Real>(lut[mid].g, lut[mid].g2, Uniform<Real>::from(r.x), Uniform<Real>::from(r.y),
+                                         cost, sint, phi, cp, sp)) {
+                            nx = sint * cp;
+                            ny = sint * sp;
                             nz = cost;
                             inx = (Real)1 / nx;
                             iny = (Real)1 / ny;
                             inz = (Real)1 / nz;
-                            continue;
                         }
-                    }
-                    if (ax == 2) {
-                        if (nc > (Real)0) tRefl += w;
-                        else tTran += w;
-                    } else {
-                        tSide += w;
-                    }
-                    alive = false;
-                    break;
-                }
-                // the reference snaps a crossed coordinate to the face +- delta
-                // (src/inttau2.f90:140-169); nudge carries that delta
-                if (ax == 0) { ix = nxt; fx = nx > (Real)0 ? nudge : hx - nudge; }
-                else if (ax == 1) { iy = nxt; fy = ny > (Real)0 ? nudge : hy - nudge; }
-                else { iz = nxt; fz = nz > (Real)0 ? nudge : hz - nudge; }
-                lookup<Real, MED>(a, lut, ix, iy, iz, m);
-            } else {
-                const Real dd = M<Real>::div(tau, m.mut);
-                dep += w * dd * m.mua;
-                fx = clamp0h(fx + nx * dd, hx);
-                fy = clamp0h(fy + ny * dd, hy);
-                fz = clamp0h(fz + nz * dd, hz);
-                interact = true;
-                break;
-            }
-        }
-        if (!alive) {
-            if (dep != (Real)0) {
-                atomicAdd(a.jmean + (ix + (int64_t)a.nx * (iy + (int64_t)a.ny * iz)), (double)dep);
-                dep = (Real)0;
-            }
-            cSteps += (unsigned long long)nsteps;
-            continue;
-        }
-        if (interact) {
-            // ---- interaction: implicit capture, HG scatter, roulette ----
-            w *= m.alb;
-            bool die = !(w > (Real)0);
-            if (!die) {
-                cScat += 1;
-                const U4 r = philox4x32_10(ev++, plo, phi32, a.stream, k0, k1);
-                stokes<Real>(m.g, m.g2, Uniform<Real>::from(r.x), Uniform<Real>::from(r.y), cost, sint, phi, cosp,
-                             sinp);
-                nx = sint * cosp;
-                ny = sint * sinp;
-                nz = cost;
-                if (!(nz == nz) || !(nx == nx) || !(ny == ny)) {
-                    errbits |= DEVERR_NAN;
-                    die = true;
-                } else {
-                    inx = (Real)1 / nx;
-                    iny = (Real)1 / ny;
-                    inz = (Real)1 / nz;
-                    if (a.roulette && w < wmin) {
-                        if (Uniform<Real>::from(r.z) < inv_rm) {
-                            tRN += w * (rm - (Real)1);
-                            w *= rm;
-                        } else {
-                            tRN -= w;
+                        if (!(nz == nz) || !(nx == nx) || !(ny == ny)) {
+                            errbits |= DEVERR_NAN;
                             die = true;
+                        } else {
+                            if (a.roulette && w < wmin) {
+                                if (Uniform<Real>::from(r.z) < inv_rm) {
+                                    tRN += w * (rm - (Real)1);
+                                    w *= rm;
+                                } else {
+                                    tRN -= w;
+                                    die = true;
+                                }
+                            }
+                            tau = -M<Real>::log(Uniform<Real>::from(r.w));
                         }
                     }
-                    tau = -M<Real>::log(Uniform<Real>::from(r.w));
+                    if (die) {
+                        if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
+                        dep = (Real)0;
+                        cSteps += nsteps;
+                        mode = M_DEAD;
+                    } else {
+                        mode = M_FLY;
+                    }
                 }
-            }
-            if (die) {
-                if (dep != (Real)0) {
-                    atomicAdd(a.jmean + (ix + (int64_t)a.nx * (iy + (int64_t)a.ny * iz)), (double)dep);
-                    dep = (Real)0;
-                }
-                cSteps += (unsigned long long)nsteps;
-                alive = false;
             }
         }
     }
 
-    // ---- block reduction of the escape tallies ----
-    double v[7] = {warp_sum(tSpec), warp_sum(tRefl), warp_sum(tTran), warp_sum(tSide),
-                   warp_sum(tRN), warp_sum(tMiss), 0.0};
-    unsigned long long c3[3] = {cSteps, cScat, cOvf};
+    // ---- warp reduction of the per-lane tallies ----
+    const double v0 = warp_sum(tSpec), v1 = warp_sum(tRefl), v2 = warp_sum(tTran), v3 = warp_sum(tSide),
+                 v4 = warp_sum(tRN);
+    unsigned long long c0 = cSteps, c1 = cScat;
 #pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) c3[i] += __shfl_xor_sync(0xffffffffu, c3[i], o);
-    errbits = __reduce_or_sync(0xffffffffu, errbits);
+    for (int o = 16; o > 0; o >>= 1) {
+        c0 += __shfl_xor_sync(FULL, c0, o);
+        c1 += __shfl_xor_sync(FULL, c1, o);
+    }
+    errbits = __reduce_or_sync(FULL, errbits);
     if (lane == 0) {
-        atomicAdd(a.tally + T_SPECULAR, v[0]);
-        atomicAdd(a.tally + T_REFLECTED, v[1]);
-        atomicAdd(a.tally + T_TRANSMITTED, v[2]);
-        atomicAdd(a.tally + T_SIDE, v[3]);
-        atomicAdd(a.tally + T_ROULETTE_NET, v[4]);
-        atomicAdd(a.tally + T_MISSED, v[5]);
-        atomicAdd(a.tally + T_STEPS, (double)c3[0]);
-        atomicAdd(a.tally + T_SCATTERS, (double)c3[1]);
-        atomicAdd(a.tally + T_OVERFLOW, (double)c3[2]);
+        atomicAdd(a.tally + T_SPECULAR, v0);
+        atomicAdd(a.tally + T_REFLECTED, v1);
+        atomicAdd(a.tally + T_TRANSMITTED, v2);
+        atomicAdd(a.tally + T_SIDE, v3);
+        atomicAdd(a.tally + T_ROULETTE_NET, v4);
+        atomicAdd(a.tally + T_STEPS, (double)c0);
+        atomicAdd(a.tally + T_SCATTERS, (double)c1);
         if (errbits) atomicOr(a.err, errbits);
     }
 }
@@ -457,6 +462,7 @@ template <typename Real, int MED> cudaError_t launch_t(const TransportArgs &a, i
 {
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<Real, MED>, TPB, 0);
+    const int scat_min = a.scat_min > 0 ? a.scat_min : 16;
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     int64_t blocks = (int64_t)sm_count * per_sm;
@@ -464,7 +470,7 @@ template <typename Real, int MED> cudaError_t launch_t(const TransportArgs &a, i
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
     count_launch();
-    transport_kernel<Real, MED><<<(unsigned)blocks, TPB, 0, s>>>(a);
+    transport_kernel<Real, MED><<<(unsigned)blocks, TPB, 0, s>>>(a, scat_min);
     return cudaGetLastError();
 }
 

@@ -127,6 +127,7 @@ SIGNATURES = [
     ("tam_get_state", C.c_int, [_P, C.POINTER(State)]),
     ("tam_get_timing", C.c_int, [_P, _D, _D, C.POINTER(C.c_int64)]),
     ("tam_kernel_launches", C.c_int64, []),
+    ("tam_set_tuning", C.c_int, [_P, C.c_char_p, C.c_int64]),
     ("tam_write_output", C.c_int, [_P, C.c_char_p]),
     ("tam_selftest_philox", C.c_int, [_U32, _U32, _U32, C.c_int64]),
 ]

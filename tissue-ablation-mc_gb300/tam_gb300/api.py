@@ -173,6 +173,9 @@ class Context:
         self._ck(self._lib.tam_device_errors(self._h, C.byref(b)))
         return b.value
 
+    def set_tuning(self, key: str, value: int) -> None:
+        self._ck(self._lib.tam_set_tuning(self._h, key.encode(), int(value)))
+
     def timing(self):
         t = C.c_double(0)
         h = C.c_double(0)
