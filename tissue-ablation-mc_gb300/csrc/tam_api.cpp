@@ -96,6 +96,8 @@ struct tam_ctx {
     tam::FusedTma *tma = nullptr;  // tensor maps of the FP32 fused step
     float *d_ax = nullptr, *d_ay = nullptr, *d_az = nullptr, *d_irc = nullptr;  // its face coefficients
     bool coeff_dirty = true;
+    int uniform_id = -1;             // >= 0 while every voxel holds this material
+    long long nabl_at_uniform = 0;
 
     // CUDA events around the transport kernel and the heat loop
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -359,6 +361,8 @@ int cfg_setup(tam_ctx *ctx)
     ctx->total_time = p.total_time;
     const uint8_t m0 = (uint8_t)(c.nmat > 1 ? 1 : 0);
     CK(tam::launch_fill_u8(ctx->d_mat, m0, ctx->ni, s));
+    ctx->uniform_id = m0;
+    ctx->nabl_at_uniform = 0;
     CK(tam::launch_props_from_mat(ctx->d_mat, c.nmat, ctx->lut, ctx->d_k, ctx->d_rho, ctx->d_c, ctx->fp64, ctx->ni, s));
     ctx->coeff_dirty = true;
     for (int b = 0; b < 2; ++b) {
@@ -469,6 +473,15 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream)
         a.nudge = ctx->delta;  // src/mcpolar.f90:112
     }
     a.scat_min = ctx->scat_min;
+    a.uniform_id = -1;
+    if (ctx->config && ctx->uniform_id >= 0) {
+        // ablation turns voxels into material 0: the medium is no longer uniform
+        unsigned long long nab = 0;
+        CK(cudaMemcpyAsync(&nab, ctx->d_nabl, sizeof nab, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        if ((long long)nab != ctx->nabl_at_uniform) ctx->uniform_id = -1;
+        a.uniform_id = ctx->uniform_id;
+    }
     a.seed = seed;
     a.stream = stream;
     a.p0 = 0;
@@ -1122,13 +1135,23 @@ int tam_upload(tam_ctx *ctx, int field, const void *host, int64_t nbytes)
     }
     case TAM_F_TISSUE: CK(h2d(ctx->d_tissue)); break;
     case TAM_F_THRESTIME: CK(h2d(ctx->d_thres)); break;
-    case TAM_F_MATERIAL:
+    case TAM_F_MATERIAL: {
         CK(h2d(ctx->d_mat));
+        const uint8_t *hm = (const uint8_t *)host;
+        int u = hm[0] < ctx->cfg.nmat ? hm[0] : 0;
+        for (int64_t q = 1; q < ctx->ni && u >= 0; ++q)
+            if ((hm[q] < ctx->cfg.nmat ? hm[q] : 0) != u) u = -1;
+        ctx->uniform_id = u;
+        unsigned long long nab = 0;
+        CK(cudaMemcpyAsync(&nab, ctx->d_nabl, sizeof nab, cudaMemcpyDeviceToHost, s));
+        CK(cudaStreamSynchronize(s));
+        ctx->nabl_at_uniform = (long long)nab;
         CK(tam::launch_props_from_mat(ctx->d_mat, ctx->cfg.nmat, ctx->lut, ctx->d_k, ctx->d_rho, ctx->d_c, ctx->fp64,
                                       ctx->ni, s));
         ctx->coeff_dirty = true;
         ctx->need_trace = true;
         break;
+    }
     default: return fail(ctx, TAM_E_STATE, "field not uploadable in config mode");
     }
     return finish(ctx, "tam_upload");

@@ -76,7 +76,7 @@ template <> struct M<float> {
     __device__ __forceinline__ static float sqrt(float x) { return sqrtf(x); }
     __device__ __forceinline__ static float acos(float x) { return acosf(x); }
     __device__ __forceinline__ static float div(float a, float b) { return __fdividef(a, b); }
-    __device__ __forceinline__ static float rcp(float a) { return __frcp_rn(a); }
+    __device__ __forceinline__ static float rcp(float a) { return __frcp_rn(a); }  // correctly rounded 1/a
     __device__ __forceinline__ static float abs(float a) { return fabsf(a); }
 };
 template <> struct M<double> {

@@ -13,7 +13,7 @@ int64_t launch_count();
 
 constexpr int MAX_MAT = 16;
 
-enum Medium : int32_t { MED_RHOKAP = 0, MED_MATERIAL = 1 };
+enum Medium : int32_t { MED_RHOKAP = 0, MED_MATERIAL = 1, MED_UNIFORM = 2 };
 enum Source : int32_t { SRC_DISK = 0, SRC_GAUSSIAN = 1 };
 
 // Tally slots (double), same order as the oracle's ORC_T_*.
@@ -47,6 +47,7 @@ struct TransportArgs {
     int64_t max_steps;
     double nudge;                     // offset past a crossed face (reference delta), 0 in config mode
     int32_t scat_min;                 // lanes that must wait before a warp scatters (0: default)
+    int32_t uniform_id;               // >= 0: every voxel holds this material (no per-cell fetch)
     double *jmean;                    // interior, packet units (sum of w*d*mua)
     double *tally;                    // N_TALLY doubles
     unsigned long long *work;         // dynamic packet counter (zeroed by the launcher)

@@ -110,7 +110,8 @@ template <typename Real> __device__ __forceinline__ double warp_sum(Real v)
 }
 
 // Optical properties of the current cell: extinction and absorption for the
-// DDA, the material id for the albedo / HG / index lookups at events.
+// DDA, the material id for the albedo / HG / index lookups at events.  A
+// uniform medium (every voxel the same material) needs no per-cell fetch.
 template <typename Real, int MED>
 __device__ __forceinline__ void fetch(const TransportArgs &a, const MatR<Real> *lut, int ix, int iy, int iz,
                                       int cidx, Real &mut, Real &mua, int &mid)
@@ -121,16 +122,39 @@ __device__ __forceinline__ void fetch(const TransportArgs &a, const MatR<Real> *
         mut = v;
         mua = v;
         mid = 0;
-    } else {
+    } else if (MED == MED_MATERIAL) {
         int id = __ldg(a.mat + cidx);
         id = id < a.nmat ? id : 0;
         mid = id;
         mut = lut[id].mut;
         mua = lut[id].mua;
+    } else {
+        mid = a.uniform_id;
+        mut = lut[mid].mut;
+        mua = lut[mid].mua;
     }
 }
 
 enum : int { M_DEAD = 0, M_FLY = 1, M_SCAT = 2 };
+
+// Per-flight DDA set-up from the in-cell position f and direction n of one
+// axis: td = cell width along the ray, tm = distance to the next face.
+template <typename Real>
+__device__ __forceinline__ void axis_setup(Real n, Real f, Real h, Real BIG, Real &td, Real &tm, int &sg)
+{
+    const Real inv = M<Real>::rcp(n);
+    td = n != (Real)0 ? h * M<Real>::abs(inv) : BIG;
+    tm = n > (Real)0 ? (h - f) * inv : (n < (Real)0 ? -f * inv : BIG);
+    tm = tm < (Real)0 ? (Real)0 : tm;
+    sg = n > (Real)0 ? 1 : -1;
+}
+
+// In-cell position of one axis at distance t along the flight.
+template <typename Real> __device__ __forceinline__ Real axis_pos(Real n, Real f, Real h, Real tm, Real t)
+{
+    const Real r = n > (Real)0 ? h - (tm - t) * n : (n < (Real)0 ? -(tm - t) * n : f);
+    return clamp0h(r, h);
+}
 
 // Event loop per lane: DEAD (needs a packet) -> FLY (one voxel step per
 // iteration: cross a face, reach an outer face, or reach the interaction
@@ -139,8 +163,13 @@ enum : int { M_DEAD = 0, M_FLY = 1, M_SCAT = 2 };
 // part; it runs once at least scat_min lanes of the warp wait for it, or when
 // no lane is flying, so it executes with most lanes active.  Every packet
 // sees the same sequence of events and random numbers as a straight loop.
+//
+// The DDA is incremental (Amanatides & Woo): per flight, the distance tm to
+// the next face of each axis and the cell width td along the ray; a crossing
+// moves tm of the crossed axis by td.  In-cell positions are reconstructed
+// only at events (interaction, outer face).
 template <typename Real, int MED>
-__global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 4 : 2) transport_kernel(const TransportArgs a, int scat_min)
+__global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kernel(const TransportArgs a, int scat_min)
 {
     __shared__ MatR<Real> lut[MAX_MAT];
     for (int t = threadIdx.x; t < MAX_MAT; t += blockDim.x) {
@@ -160,7 +189,10 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 4 : 2) transport_kern
     const Real hx = (Real)(2.0 * a.xmax / a.nx), hy = (Real)(2.0 * a.ymax / a.ny), hz = (Real)(2.0 * a.zmax / a.nz);
     const Real BIG = (Real)1.0e30;
     const Real TWOPI = (Real)TWOPI_R;
-    const Real nudge = (Real)a.nudge;
+    // after a crossing the next face along the crossed axis is (h - nudge)
+    // away along the axis: tm advances by td * (1 - nudge / h)
+    const Real knx = (Real)(1.0 - a.nudge / (2.0 * a.xmax / a.nx)), kny = (Real)(1.0 - a.nudge / (2.0 * a.ymax / a.ny)),
+               knz = (Real)(1.0 - a.nudge / (2.0 * a.zmax / a.nz));
     const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
     const unsigned lane = threadIdx.x & 31u;
     const Real wmin = (Real)a.roulette_w, rm = (Real)a.roulette_m, inv_rm = (Real)(1.0 / a.roulette_m);
@@ -170,8 +202,9 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 4 : 2) transport_kern
 
     int mode = M_DEAD;
     bool exhausted = false;
-    int ix = 0, iy = 0, iz = 0, cidx = 0, mid = 0;
-    Real fx = 0, fy = 0, fz = 0, nx = 0, ny = 0, nz = 0, inx = 0, iny = 0, inz = 0, sint = 0, phi = 0;
+    int ix = 0, iy = 0, iz = 0, cidx = 0, mid = 0, sgx = 1, sgy = 1, sgz = 1;
+    Real fx = 0, fy = 0, fz = 0, nx = 0, ny = 0, nz = 0, sint = 0, phi = 0;
+    Real tdx = 0, tdy = 0, tdz = 0, tmx = 0, tmy = 0, tmz = 0, t = 0;
     Real w = 0, tau = 0, dep = 0, mut = 0, mua = 0;
     uint32_t ev = 0, plo = 0, phi32 = 0, nsteps = 0;
     Real tSpec = 0, tRefl = 0, tTran = 0, tSide = 0, tRN = 0;
@@ -233,9 +266,10 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 4 : 2) transport_kern
                         nx = sint * cp;  // direction (0, 0, -1): +-0 in x and y
                         ny = sint * sp;
                         nz = (Real)-1;
-                        inx = (Real)1 / nx;
-                        iny = (Real)1 / ny;
-                        inz = (Real)1 / nz;
+                        axis_setup(nx, fx, hx, BIG, tdx, tmx, sgx);
+                        axis_setup(ny, fy, hy, BIG, tdy, tmy, sgy);
+                        axis_setup(nz, fz, hz, BIG, tdz, tmz, sgz);
+                        t = (Real)0;
                         dep = (Real)0;
                         nsteps = 0;
                         mode = M_FLY;
@@ -258,48 +292,38 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 4 : 2) transport_kern
                 cSteps += nsteps;
                 mode = M_DEAD;
             } else {
-                Real ddx = nx > (Real)0 ? (hx - fx) * inx : (nx < (Real)0 ? -fx * inx : BIG);
-                Real ddy = ny > (Real)0 ? (hy - fy) * iny : (ny < (Real)0 ? -fy * iny : BIG);
-                Real ddz = nz > (Real)0 ? (hz - fz) * inz : (nz < (Real)0 ? -fz * inz : BIG);
-                ddx = ddx < (Real)0 ? (Real)0 : ddx;
-                ddy = ddy < (Real)0 ? (Real)0 : ddy;
-                ddz = ddz < (Real)0 ? (Real)0 : ddz;
-                // tie order of src/inttau2.f90:116-118 (z over y over x)
+                // nearest face; ties go z over y over x (src/inttau2.f90:116-118)
                 int ax = 2;
-                Real dw = ddz;
-                if (ddy < dw) { dw = ddy; ax = 1; }
-                if (ddx < dw) { dw = ddx; ax = 0; }
+                Real tmin = tmz;
+                if (tmy < tmin) { tmin = tmy; ax = 1; }
+                if (tmx < tmin) { tmin = tmx; ax = 0; }
+                Real dw = tmin - t;
+                dw = dw < (Real)0 ? (Real)0 : dw;
                 const Real taucell = dw * mut;
                 if (taucell < tau) {
                     dep += w * dw * mua;
                     tau -= taucell;
+                    t = tmin;
                     const bool cx = ax == 0, cy = ax == 1, cz = ax == 2;
-                    const int sx = nx > (Real)0 ? 1 : -1, sy = ny > (Real)0 ? 1 : -1, sz = nz > (Real)0 ? 1 : -1;
-                    // the two other coordinates advance; the crossed one steps a cell
-                    fx = cx ? fx : clamp0h(fx + nx * dw, hx);
-                    fy = cy ? fy : clamp0h(fy + ny * dw, hy);
-                    fz = cz ? fz : clamp0h(fz + nz * dw, hz);
-                    const int jx = ix + (cx ? sx : 0), jy = iy + (cy ? sy : 0), jz = iz + (cz ? sz : 0);
-                    const bool out = (unsigned)jx >= (unsigned)NX || (unsigned)jy >= (unsigned)NY ||
-                                     (unsigned)jz >= (unsigned)NZ;
-                    if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
+                    const int sg = cx ? sgx : (cy ? sgy : sgz);
+                    const int j = (cx ? ix : (cy ? iy : iz)) + sg;
+                    const int N = cx ? NX : (cy ? NY : NZ);
+                    atomicAdd(a.jmean + cidx, (double)dep);
                     dep = (Real)0;
-                    if (!out) {
-                        ix = jx;
-                        iy = jy;
-                        iz = jz;
-                        cidx += cx ? sx : (cy ? sy * SY : sz * SZ);
-                        // the reference snaps a crossed coordinate to the face +- delta
-                        // (src/inttau2.f90:140-169); nudge carries that delta
-                        fx = cx ? (sx > 0 ? nudge : hx - nudge) : fx;
-                        fy = cy ? (sy > 0 ? nudge : hy - nudge) : fy;
-                        fz = cz ? (sz > 0 ? nudge : hz - nudge) : fz;
+                    if ((unsigned)j < (unsigned)N) {
+                        // step into the next cell (branch-free over the axis); the
+                        // reference snaps the crossed coordinate to the face +- delta
+                        // (src/inttau2.f90:140-169), which knx/kny/knz carry
+                        ix = cx ? j : ix;
+                        iy = cy ? j : iy;
+                        iz = cz ? j : iz;
+                        cidx += cx ? sg : (cy ? sg * SY : sg * SZ);
+                        tmx = cx ? tmx + tdx * knx : tmx;
+                        tmy = cy ? tmy + tdy * kny : tmy;
+                        tmz = cz ? tmz + tdz * knz : tmz;
                         fetch<Real, MED>(a, lut, ix, iy, iz, cidx, mut, mua, mid);
                     } else {
-                        // outer face: stay in the cell on the face; Fresnel or escape
-                        fx = cx ? (sx > 0 ? hx : (Real)0) : fx;
-                        fy = cy ? (sy > 0 ? hy : (Real)0) : fy;
-                        fz = cz ? (sz > 0 ? hz : (Real)0) : fz;
+                        // outer face: the packet sits on it; Fresnel or escape
                         const Real nc = cx ? nx : (cy ? ny : nz);
                         bool reflect = false;
                         if (a.fresnel) {
@@ -308,22 +332,36 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 4 : 2) transport_kern
                             reflect = Uniform<Real>::from(r.x) < fresnel<Real>(nt, namb, M<Real>::abs(nc));
                         }
                         if (reflect) {
-                            if (cz) {
-                                nz = -nz;
-                                inz = -inz;
-                            } else if (cx) {
+                            // mirror the crossed direction component; the next
+                            // face along it is one cell width back
+                            if (cx) {
+                                fy = axis_pos(ny, fy, hy, tmy, t);
+                                fz = axis_pos(nz, fz, hz, tmz, t);
+                                fx = sgx > 0 ? hx : (Real)0;
                                 nx = -nx;
-                                inx = -inx;
+                                sgx = -sgx;
+                                tmx = t + tdx;
                                 phi = (Real)PI_R - phi;
                                 if (phi < (Real)0) phi += TWOPI;
-                            } else {
+                            } else if (cy) {
+                                fx = axis_pos(nx, fx, hx, tmx, t);
+                                fz = axis_pos(nz, fz, hz, tmz, t);
+                                fy = sgy > 0 ? hy : (Real)0;
                                 ny = -ny;
-                                iny = -iny;
+                                sgy = -sgy;
+                                tmy = t + tdy;
                                 phi = TWOPI - phi;
+                            } else {
+                                fx = axis_pos(nx, fx, hx, tmx, t);
+                                fy = axis_pos(ny, fy, hy, tmy, t);
+                                fz = sgz > 0 ? hz : (Real)0;
+                                nz = -nz;
+                                sgz = -sgz;
+                                tmz = t + tdz;
                             }
                         } else {
-                            if (cz) {
-                                if (sz > 0) tRefl += w;
+                            if (!cx && !cy) {
+                                if (sgz > 0) tRefl += w;
                                 else tTran += w;
                             } else {
                                 tSide += w;
@@ -335,9 +373,10 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 4 : 2) transport_kern
                 } else {
                     const Real dd = M<Real>::div(tau, mut);
                     dep += w * dd * mua;
-                    fx = clamp0h(fx + nx * dd, hx);
-                    fy = clamp0h(fy + ny * dd, hy);
-                    fz = clamp0h(fz + nz * dd, hz);
+                    t += dd;
+                    fx = axis_pos(nx, fx, hx, tmx, t);
+                    fy = axis_pos(ny, fy, hy, tmy, t);
+                    fz = axis_pos(nz, fz, hz, tmz, t);
                     mode = M_SCAT;
                 }
             }
@@ -361,14 +400,15 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 4 : 2) transport_kern
                             nx = sint * cp;
                             ny = sint * sp;
                             nz = cost;
-                            inx = (Real)1 / nx;
-                            iny = (Real)1 / ny;
-                            inz = (Real)1 / nz;
                         }
                         if (!(nz == nz) || !(nx == nx) || !(ny == ny)) {
                             errbits |= DEVERR_NAN;
                             die = true;
                         } else {
+                            axis_setup(nx, fx, hx, BIG, tdx, tmx, sgx);
+                            axis_setup(ny, fy, hy, BIG, tdy, tmy, sgy);
+                            axis_setup(nz, fz, hz, BIG, tdz, tmz, sgz);
+                            t = (Real)0;
                             if (a.roulette && w < wmin) {
                                 if (Uniform<Real>::from(r.z) < inv_rm) {
                                     tRN += w * (rm - (Real)1);
@@ -482,11 +522,13 @@ cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cu
     cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     if (fp64) {
-        return a.medium == MED_RHOKAP ? launch_t<double, MED_RHOKAP>(a, sm_count, s)
-                                      : launch_t<double, MED_MATERIAL>(a, sm_count, s);
+        if (a.medium == MED_RHOKAP) return launch_t<double, MED_RHOKAP>(a, sm_count, s);
+        if (a.uniform_id >= 0) return launch_t<double, MED_UNIFORM>(a, sm_count, s);
+        return launch_t<double, MED_MATERIAL>(a, sm_count, s);
     }
-    return a.medium == MED_RHOKAP ? launch_t<float, MED_RHOKAP>(a, sm_count, s)
-                                  : launch_t<float, MED_MATERIAL>(a, sm_count, s);
+    if (a.medium == MED_RHOKAP) return launch_t<float, MED_RHOKAP>(a, sm_count, s);
+    if (a.uniform_id >= 0) return launch_t<float, MED_UNIFORM>(a, sm_count, s);
+    return launch_t<float, MED_MATERIAL>(a, sm_count, s);
 }
 
 cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s)
