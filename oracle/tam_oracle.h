@@ -6,15 +6,15 @@
  * the CUDA library.  Only tests/, __graft_entry__.smoke() and the CPU legs of
  * bench.py may load it; the product library never links or calls it.
  *
- * Parity status: the reference cannot be compiled (no Fortran compiler or MPI
- * exists on either machine) and ships no tests, fixtures or golden vectors.
- * This oracle is therefore pinned by analytic known-answer tests derived from
+ * Parity status: parity unpinned.  The reference cannot be compiled (no
+ * Fortran compiler or MPI exists on either machine) and ships no tests,
+ * fixtures or golden vectors, so no reference output exists to pin against.
+ * The oracle is instead checked by analytic known-answer tests derived from
  * the reference's own equations (Beer-Lambert depth profile of the pure
  * absorber, the discrete eigen-decay of the reference's halved diffusion
- * operator, constant-temperature Arrhenius integrals, HG mean cosine, normal
- * incidence Fresnel, energy balance) and by golden vectors generated from it
- * and committed under tests/golden/.  No output of the reference program
- * itself is available: "parity pinned by analytic KATs, not by reference runs".
+ * operator, constant-temperature Arrhenius integrals and threshold chain, HG
+ * mean cosine, normal-incidence Fresnel, energy balance) and by regression
+ * vectors generated from it and committed under tests/golden/.
  *
  * Two semantic modes:
  *   (R) reference mode -- statement-by-statement restatement of the compiled
