@@ -256,6 +256,32 @@ int64_t tam_kernel_launches(void);
 /* writer (src/writer.f90:6-81): stream-unformatted FP64 files in `dir`. */
 int tam_write_output(struct tam_ctx *ctx, const char *dir);
 
+/*
+ * Allocation-free MC pass.  No counterpart in the reference: the reference
+ * allocates its module arrays itself and never runs on a GPU.  Some callers
+ * cannot let this library call cudaMalloc -- a Fortran host whose device
+ * arrays belong to another runtime (OpenACC, CUDA Fortran), a host working
+ * within a fixed device-memory budget, or code that must not allocate inside
+ * a stream capture or a real-time loop.  This entry point allocates nothing:
+ * the caller passes the reference-mode parameters, `rhokap` as a device
+ * pointer in the halo layout ((nx+2)(ny+2)(nz+2) doubles, input) and
+ * `jmean_global` as a device pointer (nx*ny*nz doubles, output), plus the
+ * laser power `power` (W) of the normalisation of src/mcpolar.f90:174.  It
+ * runs the same photon loop as tam_mc_pass in reference mode, on
+ * `cuda_stream` (NULL: the legacy default stream), and returns after that
+ * stream has finished the pass.
+ * The pass's scratch lives in one file-scope device array sized for grids of
+ * at most TAM_NOALLOC_MAX_VOXELS voxels (about 16 MiB, held by every GPU that
+ * loads the library until the process exits); larger grids are rejected with
+ * TAM_E_INVALID.  The first call on a device looks up the array's device
+ * address, so make that first call before any stream capture.  All calls
+ * share the array (it is cleared at the start of each call): calls that
+ * overlap on the GPU race.  Errors are reported by tam_last_error(NULL).
+ */
+#define TAM_NOALLOC_MAX_VOXELS 2097152
+int tam_mc_pass_noalloc(const tam_params *p, const double *rhokap, double *jmean_global, int64_t nphotons,
+                        uint64_t seed, uint32_t stream, double power, void *cuda_stream);
+
 /* Self-test: Philox4x32-10 of this library against cuRAND's device Philox on
  * n inputs of 6 words {c0,c1,c2,c3,k0,k1}; outputs 4 words each. */
 int tam_selftest_philox(const uint32_t *in, uint32_t *out_mine, uint32_t *out_curand, int64_t n);

@@ -113,6 +113,12 @@ struct tam_ctx {
 
 namespace {
 
+}  // namespace
+
+void tam::set_thread_error(const std::string &msg) { g_thread_err = msg; }
+
+namespace {
+
 int fail(tam_ctx *c, int code, const std::string &msg)
 {
     if (c) c->err = msg;

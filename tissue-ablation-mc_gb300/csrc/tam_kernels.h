@@ -3,6 +3,8 @@
 #pragma once
 
 #include <cstdint>
+#include <string>
+
 #include <cuda_runtime.h>
 
 namespace tam {
@@ -10,6 +12,8 @@ namespace tam {
 // Kernel launches issued by this library (process-wide).
 void count_launch(int n = 1);
 int64_t launch_count();
+// Message returned by tam_last_error(NULL) on this thread.
+void set_thread_error(const std::string &msg);
 
 constexpr int MAX_MAT = 16;
 

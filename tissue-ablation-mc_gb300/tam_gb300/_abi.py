@@ -24,6 +24,7 @@ TAM_DEVERR_STEP_CAP, TAM_DEVERR_NAN, TAM_DEVERR_NEG_T = 0x1, 0x2, 0x4
 (TAM_F_TEMP, TAM_F_RHOKAP, TAM_F_JMEAN, TAM_F_JMEAN_GLOBAL, TAM_F_TISSUE, TAM_F_THRESTIME, TAM_F_KAPPA,
  TAM_F_DENSITY, TAM_F_HEATCAP, TAM_F_COEFF, TAM_F_ALPHA, TAM_F_Q, TAM_F_WATER, TAM_F_MATERIAL) = range(14)
 TAM_MAX_MATERIALS = 16
+TAM_NOALLOC_MAX_VOXELS = 2097152
 TALLY_NAMES = ("absorbed", "specular", "reflected", "transmitted", "side", "roulette_net", "missed",
                "voxel_steps", "scatters", "overflow")
 
@@ -130,6 +131,7 @@ SIGNATURES = [
     ("tam_set_tuning", C.c_int, [_P, C.c_char_p, C.c_int64]),
     ("tam_write_output", C.c_int, [_P, C.c_char_p]),
     ("tam_selftest_philox", C.c_int, [_U32, _U32, _U32, C.c_int64]),
+    ("tam_mc_pass_noalloc", C.c_int, [C.POINTER(Params), _P, _P, C.c_int64, C.c_uint64, C.c_uint32, C.c_double, _P]),
 ]
 
 _lib = None
