@@ -360,7 +360,7 @@ def run_gpu(args):
 
 def profile_traffic(voxel_steps):
     """DRAM bytes of one full transport launch, scaled from the committed ncu summary."""
-    path = os.path.join(ROOT, "profiles", "transport_c2.txt")
+    path = os.path.join(ROOT, "profiles", "transport_kernel_200cube.txt")
     try:
         for ln in open(path):
             if ln.startswith("dram_bytes_per_voxel_step:"):

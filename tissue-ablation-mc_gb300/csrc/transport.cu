@@ -22,6 +22,10 @@ namespace tam {
 namespace {
 
 constexpr int TPB = 256;
+// Resident blocks per SM requested for the FP32 transport kernel (register cap).
+#ifndef TAM_TR_MINB
+#define TAM_TR_MINB 4
+#endif
 
 template <typename Real> struct MatR {
     Real mut, mua, alb, g, g2, n;
@@ -82,6 +86,78 @@ __device__ __forceinline__ bool stokes(Real hgg, Real g2, Real u0, Real u1, Real
     return true;
 }
 
+// PTX approximate forms (relative error ~2^-22) for the FP32 path, whose
+// results are checked statistically against the FP64 path.
+__device__ __forceinline__ float rcp_ax(float x)
+{
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float sqrt_ax(float x)
+{
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rsqrt_ax(float x)
+{
+    float r;
+    asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// FP32 form of the same HG deflection.  The azimuth is carried as the pair
+// (cos phi, sin phi) and rotated by the deflection angle dph, since
+// phi' = phi +- dph (src/stokes.f90:136-140) gives
+//   cos phi' = cos phi cos dph -+ sin phi sin dph,  sin dph = sqrt(1 - cos^2 dph),
+// which replaces acos(cosdph) and the sincos of phi by one square root; the
+// pair is renormalised so that rounding cannot drift over many scatters.
+// Every sampled quantity (t, bmu, ang, cost, cosdph) follows the reference's
+// formulas; only the evaluation of phi differs.
+__device__ __forceinline__ bool stokes_f32(float hgg, float g2, float u0, float u1, float &cost, float &sint, float &cp,
+                                           float &sp)
+{
+    const float PI = (float)PI_R, TWOPI = (float)TWOPI_R;
+    if (hgg == 0.f) {
+        cost = 2.f * u0 - 1.f;
+        const float s2 = 1.f - cost * cost;
+        sint = s2 <= 0.f ? 0.f : sqrt_ax(s2);
+        __sincosf(TWOPI * u1, &sp, &cp);
+        return true;
+    }
+    const float costp = cost, sintp = sint;
+    const float t = __fdividef(1.f - g2, 1.f - hgg + 2.f * hgg * u0);
+    const float bmu = __fdividef((1.f + g2) - t * t, 2.f * hgg);
+    if (fabsf(bmu) >= 1.f) return false;  // clamped to +-1: direction unchanged
+    const float sinbt = sqrt_ax(1.f - bmu * bmu);
+    const float ri1 = TWOPI * u1;
+    const bool upper = ri1 > PI;
+    float sa, ca;
+    __sincosf(upper ? TWOPI - ri1 : ri1, &sa, &ca);
+    cost = costp * bmu + sintp * sinbt * ca;
+    float sini2, cosi2;
+    if (fabsf(cost) < 1.f) {
+        sint = sqrt_ax(1.f - cost * cost);
+        const float rs = rcp_ax(sint);
+        sini2 = sa * sintp * rs;
+        cosi2 = (costp - cost * bmu) * rs * rcp_ax(sinbt);
+    } else {
+        sint = 0.f;
+        sini2 = 0.f;
+        cosi2 = cost >= 1.f ? -1.f : 1.f;
+    }
+    float cosdph = -cosi2 * ca + sini2 * sa * bmu;
+    cosdph = fminf(fmaxf(cosdph, -1.f), 1.f);
+    float sdph = sqrt_ax(1.f - cosdph * cosdph);
+    sdph = upper ? sdph : -sdph;
+    const float ncp = cp * cosdph - sp * sdph, nsp = sp * cosdph + cp * sdph;
+    const float rn = rsqrt_ax(ncp * ncp + nsp * nsp);
+    cp = ncp * rn;
+    sp = nsp * rn;
+    return true;
+}
+
 // Unpolarised Fresnel reflectance n1 -> n2 at incidence cosine cosi.
 template <typename Real> __device__ __forceinline__ Real fresnel(Real n1, Real n2, Real cosi)
 {
@@ -99,14 +175,6 @@ template <typename Real> __device__ __forceinline__ Real fresnel(Real n1, Real n
 template <typename Real> __device__ __forceinline__ Real clamp0h(Real f, Real h)
 {
     return f < (Real)0 ? (Real)0 : (f > h ? h : f);
-}
-
-template <typename Real> __device__ __forceinline__ double warp_sum(Real v)
-{
-    double d = (double)v;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-    return d;
 }
 
 // Optical properties of the current cell: extinction and absorption for the
@@ -148,6 +216,18 @@ __device__ __forceinline__ void axis_setup(Real n, Real f, Real h, Real BIG, Rea
     tm = tm < (Real)0 ? (Real)0 : tm;
     sg = n > (Real)0 ? 1 : -1;
 }
+// FP32: approximate reciprocal; |n| below 1e-30 counts as parallel to the
+// faces (its reciprocal would overflow and turn 0 * inf into NaN).
+template <>
+__device__ __forceinline__ void axis_setup<float>(float n, float f, float h, float BIG, float &td, float &tm, int &sg)
+{
+    const float inv = rcp_ax(n);
+    const bool par = fabsf(n) < 1e-30f;
+    td = par ? BIG : h * fabsf(inv);
+    tm = par ? BIG : (n > 0.f ? h - f : -f) * inv;
+    tm = tm < 0.f ? 0.f : tm;
+    sg = n > 0.f ? 1 : -1;
+}
 
 // In-cell position of one axis at distance t along the flight.
 template <typename Real> __device__ __forceinline__ Real axis_pos(Real n, Real f, Real h, Real tm, Real t)
@@ -169,7 +249,7 @@ template <typename Real> __device__ __forceinline__ Real axis_pos(Real n, Real f
 // moves tm of the crossed axis by td.  In-cell positions are reconstructed
 // only at events (interaction, outer face).
 template <typename Real, int MED>
-__global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kernel(const TransportArgs a, int scat_min)
+__global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) transport_kernel(const TransportArgs a, int scat_min)
 {
     __shared__ MatR<Real> lut[MAX_MAT];
     for (int t = threadIdx.x; t < MAX_MAT; t += blockDim.x) {
@@ -183,6 +263,13 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
         m.n = (Real)o.n;
         lut[t] = m;
     }
+    // per-packet (rare) tallies accumulate in shared memory, not registers
+    __shared__ double s_tal[5];  // specular, reflected, transmitted, side, roulette net
+    __shared__ unsigned long long s_cnt[2];  // voxel steps, scatters
+    __shared__ unsigned s_err;
+    if (threadIdx.x < 5) s_tal[threadIdx.x] = 0.0;
+    if (threadIdx.x < 2) s_cnt[threadIdx.x] = 0ull;
+    if (threadIdx.x == 0) s_err = 0u;
     __syncthreads();
 
     const unsigned FULL = 0xffffffffu;
@@ -204,26 +291,25 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
     bool exhausted = false;
     int ix = 0, iy = 0, iz = 0, cidx = 0, mid = 0, sgx = 1, sgy = 1, sgz = 1;
     Real fx = 0, fy = 0, fz = 0, nx = 0, ny = 0, nz = 0, sint = 0, phi = 0;
+    Real cpv = 1, spv = 0;  // FP32 path: (cos phi, sin phi) in place of phi
     Real tdx = 0, tdy = 0, tdz = 0, tmx = 0, tmy = 0, tmz = 0, t = 0;
     Real w = 0, tau = 0, dep = 0, mut = 0, mua = 0;
     uint32_t ev = 0, plo = 0, phi32 = 0, nsteps = 0;
-    Real tSpec = 0, tRefl = 0, tTran = 0, tSide = 0, tRN = 0;
-    uint32_t cSteps = 0, cScat = 0;
-    unsigned errbits = 0;
+    uint32_t cScat = 0;
 
     for (;;) {
         // ---------------------------------------------- refill dead lanes --
-        const unsigned need = __ballot_sync(FULL, mode == M_DEAD && !exhausted);
+        // (exhausted is warp-uniform: set once the counter has passed n)
+        const unsigned need = exhausted ? 0u : __ballot_sync(FULL, mode == M_DEAD);
         if (need) {
             const int leader = __ffs(need) - 1;
             unsigned long long base = 0;
             if ((int)lane == leader) base = atomicAdd(a.work, (unsigned long long)__popc(need));
             base = __shfl_sync(FULL, base, leader);
-            if (mode == M_DEAD && !exhausted) {
+            exhausted = base + (unsigned long long)__popc(need) >= (unsigned long long)a.n;
+            if (mode == M_DEAD) {
                 const unsigned long long my = base + __popc(need & ((1u << lane) - 1u));
-                if (my >= (unsigned long long)a.n) {
-                    exhausted = true;
-                } else {
+                if (my < (unsigned long long)a.n) {
                     // launch (src/sourceph.f90:7-49; Gaussian beam in config mode)
                     const uint64_t pid = (uint64_t)a.p0 + my;
                     plo = (uint32_t)pid;
@@ -240,6 +326,8 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
                     const Real X = rad * ct + (Real)a.xmax, Y = rad * st + (Real)a.ymax;
                     phi = TWOPI * u2;
                     M<Real>::sincos(phi, &sp, &cp);
+                    cpv = cp;
+                    spv = sp;
                     sint = (Real)0;
                     if (!(X >= (Real)0 && X < (Real)(2.0 * a.xmax) && Y >= (Real)0 && Y < (Real)(2.0 * a.ymax))) {
                         atomicAdd(a.tally + T_MISSED, 1.0);
@@ -259,7 +347,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
                             const Real nt = MED == MED_RHOKAP ? (Real)a.rhokap_n : lut[mid].n;
                             Real rsp = (namb - nt) / (namb + nt);
                             rsp = rsp * rsp;
-                            tSpec += rsp;
+                            atomicAdd(&s_tal[0], (double)rsp);
                             w = (Real)1 - rsp;
                         }
                         tau = -M<Real>::log(u3);
@@ -277,19 +365,19 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
                 }
             }
         }
-        if (__ballot_sync(FULL, mode != M_DEAD) == 0) {
-            if (__all_sync(FULL, exhausted)) break;
-            continue;
-        }
-
+        // ------------------------------------------------- flight phase --
+        // voxel steps of the flying lanes until enough lanes wait to scatter,
+        // no lane flies, or a lane needs a new packet
+        unsigned sc, fl;
+        for (;;) {
         // -------------------------- one voxel step (src/inttau2.f90:37-63) --
         if (mode == M_FLY) {
             if (++nsteps > max_steps) {
                 if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
                 dep = (Real)0;
                 atomicAdd(a.tally + T_OVERFLOW, 1.0);
-                errbits |= DEVERR_STEP_CAP;
-                cSteps += nsteps;
+                atomicOr(&s_err, (unsigned)DEVERR_STEP_CAP);
+                atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
                 mode = M_DEAD;
             } else {
                 // nearest face; ties go z over y over x (src/inttau2.f90:116-118)
@@ -341,8 +429,12 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
                                 nx = -nx;
                                 sgx = -sgx;
                                 tmx = t + tdx;
-                                phi = (Real)PI_R - phi;
-                                if (phi < (Real)0) phi += TWOPI;
+                                if constexpr (sizeof(Real) == 4) {
+                                    cpv = -cpv;  // phi -> PI - phi
+                                } else {
+                                    phi = (Real)PI_R - phi;
+                                    if (phi < (Real)0) phi += TWOPI;
+                                }
                             } else if (cy) {
                                 fx = axis_pos(nx, fx, hx, tmx, t);
                                 fz = axis_pos(nz, fz, hz, tmz, t);
@@ -350,7 +442,11 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
                                 ny = -ny;
                                 sgy = -sgy;
                                 tmy = t + tdy;
-                                phi = TWOPI - phi;
+                                if constexpr (sizeof(Real) == 4) {
+                                    spv = -spv;  // phi -> TWOPI - phi
+                                } else {
+                                    phi = TWOPI - phi;
+                                }
                             } else {
                                 fx = axis_pos(nx, fx, hx, tmx, t);
                                 fy = axis_pos(ny, fy, hy, tmy, t);
@@ -361,12 +457,11 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
                             }
                         } else {
                             if (!cx && !cy) {
-                                if (sgz > 0) tRefl += w;
-                                else tTran += w;
+                                atomicAdd(&s_tal[sgz > 0 ? 1 : 2], (double)w);
                             } else {
-                                tSide += w;
+                                atomicAdd(&s_tal[3], (double)w);
                             }
-                            cSteps += nsteps;
+                            atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
                             mode = M_DEAD;
                         }
                     }
@@ -382,11 +477,18 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
             }
         }
 
+            sc = __ballot_sync(FULL, mode == M_SCAT);
+            fl = __ballot_sync(FULL, mode == M_FLY);
+            if (fl == 0 || __popc(sc) >= scat_min || (!exhausted && (sc | fl) != FULL)) break;
+        }
+        if ((sc | fl) == 0) {
+            if (exhausted) break;
+            continue;
+        }
+
         // ---------- interaction: implicit capture, HG scatter, roulette --
-        const unsigned sc = __ballot_sync(FULL, mode == M_SCAT);
-        if (sc) {
-            const unsigned fl = __ballot_sync(FULL, mode == M_FLY);
-            if (__popc(sc) >= scat_min || fl == 0) {
+        if (sc && (__popc(sc) >= scat_min || fl == 0)) {
+            {
                 if (mode == M_SCAT) {
                     const Real alb = MED == MED_RHOKAP ? (Real)0 : lut[mid].alb;
                     w *= alb;
@@ -394,15 +496,25 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
                     if (!die) {
                         cScat += 1;
                         const U4 r = philox4x32_10(ev++, plo, phi32, a.stream, k0, k1);
-                        Real cost = nz, cp, sp;
-                        if (stokes<Real>(lut[mid].g, lut[mid].g2, Uniform<Real>::from(r.x), Uniform<Real>::from(r.y),
-                                         cost, sint, phi, cp, sp)) {
-                            nx = sint * cp;
-                            ny = sint * sp;
-                            nz = cost;
+                        Real cost = nz;
+                        if constexpr (sizeof(Real) == 4) {
+                            if (stokes_f32(lut[mid].g, lut[mid].g2, Uniform<Real>::from(r.x), Uniform<Real>::from(r.y),
+                                           cost, sint, cpv, spv)) {
+                                nx = sint * cpv;
+                                ny = sint * spv;
+                                nz = cost;
+                            }
+                        } else {
+                            Real cp, sp;
+                            if (stokes<Real>(lut[mid].g, lut[mid].g2, Uniform<Real>::from(r.x),
+                                             Uniform<Real>::from(r.y), cost, sint, phi, cp, sp)) {
+                                nx = sint * cp;
+                                ny = sint * sp;
+                                nz = cost;
+                            }
                         }
                         if (!(nz == nz) || !(nx == nx) || !(ny == ny)) {
-                            errbits |= DEVERR_NAN;
+                            atomicOr(&s_err, (unsigned)DEVERR_NAN);
                             die = true;
                         } else {
                             axis_setup(nx, fx, hx, BIG, tdx, tmx, sgx);
@@ -411,10 +523,10 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
                             t = (Real)0;
                             if (a.roulette && w < wmin) {
                                 if (Uniform<Real>::from(r.z) < inv_rm) {
-                                    tRN += w * (rm - (Real)1);
+                                    atomicAdd(&s_tal[4], (double)(w * (rm - (Real)1)));
                                     w *= rm;
                                 } else {
-                                    tRN -= w;
+                                    atomicAdd(&s_tal[4], -(double)w);
                                     die = true;
                                 }
                             }
@@ -424,7 +536,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
                     if (die) {
                         if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
                         dep = (Real)0;
-                        cSteps += nsteps;
+                        atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
                         mode = M_DEAD;
                     } else {
                         mode = M_FLY;
@@ -434,25 +546,19 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? 3 : 2) transport_kern
         }
     }
 
-    // ---- warp reduction of the per-lane tallies ----
-    const double v0 = warp_sum(tSpec), v1 = warp_sum(tRefl), v2 = warp_sum(tTran), v3 = warp_sum(tSide),
-                 v4 = warp_sum(tRN);
-    unsigned long long c0 = cSteps, c1 = cScat;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        c0 += __shfl_xor_sync(FULL, c0, o);
-        c1 += __shfl_xor_sync(FULL, c1, o);
-    }
-    errbits = __reduce_or_sync(FULL, errbits);
-    if (lane == 0) {
-        atomicAdd(a.tally + T_SPECULAR, v0);
-        atomicAdd(a.tally + T_REFLECTED, v1);
-        atomicAdd(a.tally + T_TRANSMITTED, v2);
-        atomicAdd(a.tally + T_SIDE, v3);
-        atomicAdd(a.tally + T_ROULETTE_NET, v4);
-        atomicAdd(a.tally + T_STEPS, (double)c0);
-        atomicAdd(a.tally + T_SCATTERS, (double)c1);
-        if (errbits) atomicOr(a.err, errbits);
+    // ---- block reduction of the tallies ----
+    const unsigned c1 = __reduce_add_sync(FULL, cScat);
+    if (lane == 0) atomicAdd(&s_cnt[1], (unsigned long long)c1);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        atomicAdd(a.tally + T_SPECULAR, s_tal[0]);
+        atomicAdd(a.tally + T_REFLECTED, s_tal[1]);
+        atomicAdd(a.tally + T_TRANSMITTED, s_tal[2]);
+        atomicAdd(a.tally + T_SIDE, s_tal[3]);
+        atomicAdd(a.tally + T_ROULETTE_NET, s_tal[4]);
+        atomicAdd(a.tally + T_STEPS, (double)s_cnt[0]);
+        atomicAdd(a.tally + T_SCATTERS, (double)s_cnt[1]);
+        if (s_err) atomicOr(a.err, s_err);
     }
 }
 
