@@ -248,8 +248,29 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * GB300).  Keys: "transport.scat_min" (lanes of a warp that wait at an
  * interaction before the warp scatters, 1..32), "heat.zchunk" (z planes per
  * thread column of the fused step, 0 = automatic), "heat.tma" (1: stage the
- * FP32 fused step's planes with TMA where the row pitch allows, 0: cp.async). */
+ * FP32 fused step's planes with TMA where the row pitch allows, 0: cp.async),
+ * "heat.cls" (1: while the thermal properties are those of the material
+ * classes, look the face coefficients up per class pair instead of reading
+ * per-voxel coefficient arrays; 0: always read the arrays),
+ * "heat.arrhenius_fp64" (FP32 form: 1 evaluates the Arrhenius exponent
+ * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits). */
 int tam_set_tuning(struct tam_ctx *ctx, const char *key, int64_t value);
+/*
+ * Batches of independent instances (no reference counterpart: the reference
+ * runs one tissue model per job).  The n contexts run concurrently, each
+ * driven by its own host thread on its own stream, so the device overlaps
+ * the instances' kernels.  Each context is used by one thread only; list a
+ * context once.  seeds[i] seeds instance i.  tam_batch_step_coupled runs
+ * `iters` outer iterations on every instance; tam_batch_run runs each
+ * instance's whole loop as tam_run does (iters, nullable, receives the
+ * per-instance iteration counts).  Both wait for every instance and check
+ * each one's device error word; on failure the first failing instance's status
+ * is returned and tam_last_error(NULL) names it (its own context holds the
+ * message too).
+ */
+int tam_batch_step_coupled(struct tam_ctx *const *ctxs, int32_t n, int32_t iters, const uint64_t *seeds);
+int tam_batch_run(struct tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, int64_t max_iters, int64_t *iters);
+
 /* Kernels this library has launched in this process (all contexts). */
 int64_t tam_kernel_launches(void);
 

@@ -1,0 +1,60 @@
+"""Batches of independent instances (tam_batch_step_coupled / tam_batch_run).
+
+Each instance of a batch must end in the state it reaches when run alone:
+FP64, same seeds, compared at 1e-9 relative (only the order of the FP64
+tally atomics differs between runs).
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def _instance(tam, edge, mua, mus, g, power, radius):
+    half = 0.005 * edge / 2  # 50 um voxels
+    p = tam.default_params(nxg=edge, nyg=edge, nzg=edge // 2, xmax=half, ymax=half, zmax=half / 2, mode=1,
+                           precision=0, nphotons=20000, pulse_type=1, power=power,
+                           energy_per_pixel=power * 0.05 * 1e3, total_time=0.05, loops=5)
+    c = tam.default_config(source_radius=radius, retrace_fraction=0.0)
+    tam.set_material(c, 1, mua, mus, g, 1.38, 0.56, 1070.0, 3400.0)
+    return tam.Context(p, c)
+
+
+CASES = [(32, 0.3, 100.0, 0.9, 1.0, 0.05), (48, 2.0, 50.0, 0.8, 3.0, 0.03), (40, 0.1, 200.0, 0.95, 2.0, 0.08)]
+SEEDS = [11, 22, 33]
+
+
+def _state(tam, ctx):
+    F = tam._abi
+    return ctx.download(F.TAM_F_TEMP), ctx.download(F.TAM_F_JMEAN_GLOBAL), ctx.download(F.TAM_F_TISSUE)
+
+
+def test_batch_step_coupled_matches_single_runs(tam):
+    alone = []
+    for case, seed in zip(CASES, SEEDS):
+        with _instance(tam, *case) as ctx:
+            ctx.step_coupled(3, seed=seed)
+            alone.append(_state(tam, ctx))
+    ctxs = [_instance(tam, *case) for case in CASES]
+    try:
+        tam.batch_step_coupled(ctxs, 3, SEEDS)
+        for ctx, want in zip(ctxs, alone):
+            got = _state(tam, ctx)
+            for a, b in zip(got, want):
+                np.testing.assert_allclose(a, b, rtol=1e-9, atol=1e-9 * max(np.abs(b).max(), 1e-300))
+            assert got[0].max() > 310.2  # heated
+    finally:
+        for c in ctxs:
+            c.close()
+
+
+def test_batch_run_counts_and_rejects_duplicates(tam):
+    ctxs = [_instance(tam, *case) for case in CASES[:2]]
+    try:
+        its = tam.batch_run(ctxs, SEEDS[:2], max_iters=4)
+        assert its == [4, 4]
+        with pytest.raises(tam.TamError):
+            tam.batch_run([ctxs[0], ctxs[0]], [1, 2], max_iters=1)
+    finally:
+        for c in ctxs:
+            c.close()

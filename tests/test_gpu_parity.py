@@ -387,3 +387,85 @@ def test_writer_files(tam, orc, tmp_path):
     assert (tmp_path / f"jmean-t{tail}").stat().st_size == 8 ** 3 * 8
     t = np.fromfile(tmp_path / f"temp-t{tail}").reshape((10, 10, 10), order="F")
     assert t[0, 5, 5] == 5.0 and t[5, 5, 0] == 25.0
+
+
+# ------------------------------------------- class-table fused heat step --
+def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats):
+    half = 0.0025 * nx  # cm: 50 um voxels
+    p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half * ny / nx, zmax=half * nz / nx, mode=1,
+                           precision=precision, pulse_type=1, power=1.0, energy_per_pixel=1e6, total_time=10.0)
+    c = tam.default_config(nmat=len(mats), dt=dt)
+    for i, (k, rho, cp) in enumerate(mats):
+        tam.set_material(c, i, 0.3, 10.0, 0.9, 1.4, k, rho, cp)
+    ctx = tam.Context(p, c)
+    ctx.set_tuning("heat.cls", cls)
+    ctx.upload(F.TAM_F_MATERIAL, grid)
+    ctx.upload(F.TAM_F_JMEAN_GLOBAL, J)
+    return ctx
+
+
+@pytest.mark.parametrize("nx", [44, 48])
+def test_fused_class_table_matches_coefficient_arrays(tam, nx):
+    # three thermal materials in slabs plus an inclusion; the class-table step
+    # (face coefficients looked up per class pair) against the per-voxel
+    # coefficient arrays (same FP32 + Kahan arithmetic up to the rounding of
+    # the coefficients) and against FP64
+    ny, nz = 40, 36
+    mats = [(0.026, 1.2, 1005.0), (0.56, 1070.0, 3400.0), (0.21, 911.0, 2348.0), (0.47, 1090.0, 3421.0)]
+    grid = np.ones((nx, ny, nz), dtype=np.uint8, order="F")
+    grid[:, :, 12:24] = 2
+    grid[:, :, :12] = 3
+    grid[10:20, 8:30, 20:30] = 3
+    rng = np.random.default_rng(11)
+    J = np.asfortranarray(rng.uniform(0, 1, (nx, ny, nz)) ** 2 * 5e8)
+    d = 5e-5  # voxel spacing, m
+    alpha = max(k / (r * c) for k, r, c in mats[1:])
+    dt = 0.9 / (2 * alpha * 3 / d ** 2)
+    out = {}
+    for name, prec, cls in (("cls", 1, 1), ("arr", 1, 0), ("f64", 0, 1)):
+        ctx = _layered_heat_ctx(tam, nx, ny, nz, prec, cls, dt, J, grid, mats)
+        T = ctx.heat_steps(300, want=True)
+        out[name] = (T, ctx.download(F.TAM_F_TISSUE), ctx.device_errors())
+        ctx.close()
+    rise = (out["f64"][0] - 310.15).max()
+    assert rise > 5.0, rise
+    assert out["cls"][2] == 0 and out["arr"][2] == 0
+    assert np.abs(out["cls"][0] - out["arr"][0]).max() <= 1e-4
+    assert np.abs(out["cls"][0] - out["f64"][0]).max() <= 1e-3
+
+
+def test_fused_class_table_off_after_per_voxel_properties(tam):
+    # uploading k per voxel switches the FP32 step to the coefficient arrays
+    nx, ny, nz = 32, 24, 20
+    mats = [(0.026, 1.2, 1005.0), (0.56, 1070.0, 3400.0)]
+    grid = np.ones((nx, ny, nz), dtype=np.uint8, order="F")
+    J = np.asfortranarray(np.full((nx, ny, nz), 2e8))
+    dt = 1e-3
+    res = []
+    for cls in (1, 0):
+        ctx = _layered_heat_ctx(tam, nx, ny, nz, 1, cls, dt, J, grid, mats)
+        kap = ctx.download(F.TAM_F_KAPPA)
+        kap[1:-1, 1:-1, 1:nz // 2] = 0.3
+        ctx.upload(F.TAM_F_KAPPA, kap)
+        res.append(ctx.heat_steps(100, want=True))
+        ctx.close()
+    np.testing.assert_array_equal(res[0], res[1])
+
+
+def test_fused_fp32_arrhenius_float_float_vs_fp64_exponent(tam, orc):
+    # the FP32 step's damage integral with the float-float exponent against the
+    # FP64 exponent on the same temperatures: relative 1e-6 of the largest Omega
+    nx = ny = nz = 32
+    half = 0.16
+    d = 2 * half * 1e-2 / nx
+    alpha = 0.56 / (1070 * 3400)
+    dt = 0.9 / (2 * alpha * 3 / d ** 2)
+    om = []
+    for fp64 in (0, 1):
+        ctx, _, _ = fused_setup(tam, orc, nx, ny, nz, half, 1, dt, np.random.default_rng(8), 5e7)
+        ctx.set_tuning("heat.arrhenius_fp64", fp64)
+        ctx.heat_steps(300)
+        om.append(ctx.download(F.TAM_F_TISSUE))
+        ctx.close()
+    assert om[1].max() > 1e-6, om[1].max()
+    assert np.abs(om[0] - om[1]).max() <= 1e-6 * om[1].max()

@@ -422,7 +422,10 @@ __global__ void __launch_bounds__(FX *FY, KAHAN ? 4 : 2) fused_kernel(const Fuse
             const Real Ts = Tn - En;
             if (!(Ts == Ts)) errbits |= DEVERR_NAN;
             else if (Ts < (Real)0) errbits |= DEVERR_NEG_T;
-            if (Ts >= cst<Real>(a, FC_SCREEN)) rare_update<Real>(a, v, ni, (double)Tn - (double)En);
+            if (Ts >= cst<Real>(a, FC_SCREEN)) {
+                if constexpr (sizeof(Real) == 4) rare_update_f32(a, v, ni, Tn, (float)En);
+                else rare_update<Real>(a, v, ni, (double)Tn - (double)En);
+            }
         }
         prv = cur;
         cur = nxt;
@@ -454,7 +457,16 @@ void fill_fused_consts(FusedArgs &a)
         d[FC_BCHD + f] = a.bc_h[f] * (f < 2 ? a.dx : (f < 4 ? a.dy : a.dz));
         d[FC_BCTA + f] = a.bc_Tamb[f];
     }
+    d[FC_LNA_HI] = a.lnA;
+    d[FC_LNA_LO] = 0.0;
+    d[FC_EAR_HI] = a.Ea / a.Rgas;
+    d[FC_EAR_LO] = 0.0;
+    d[FC_TLO] = a.T_lo;
+    d[FC_THI] = a.T_hi;
+    d[FC_TABL] = a.T_abl;
     for (int i = 0; i < FC_N; ++i) a.fc[i] = (float)d[i];
+    a.fc[FC_LNA_LO] = (float)(d[FC_LNA_HI] - (double)a.fc[FC_LNA_HI]);
+    a.fc[FC_EAR_LO] = (float)(d[FC_EAR_HI] - (double)a.fc[FC_EAR_HI]);
 }
 
 namespace {

@@ -78,6 +78,55 @@ template <typename Real> __device__ __noinline__ void rare_update(const FusedArg
     }
 }
 
+// FP32 form of rare_update from the Kahan pair (T, e), true temperature T - e.
+// The exponent ln A - (Ea/R)/(T - e) is a difference of two numbers near 200
+// whose FP32 rounding alone would put ~1e-5 relative error on the rate, so it
+// is evaluated in float-float arithmetic (about 44 significant bits): the
+// quotient's remainder comes exactly from one FMA, the difference from an
+// error-free TwoSum (Knuth), and exp(hi + lo) = expf(hi) (1 + lo).  Only the
+// damage sum itself is FP64 (one conversion and one add); threshold tests
+// compare the non-negative doubles by their bit patterns, which order the same
+// way.  Exponents beyond expf's range take the FP64 path, and so does every
+// voxel when arr_fp64 is set (FP64 exponent ln A - Ea/RT of T - e).
+__device__ __noinline__ void rare_update_f32(const FusedArgs &a, int64_t v, int64_t ni, float T, float e)
+{
+    if (a.arr_fp64) {
+        rare_update<float>(a, v, ni, (double)T - (double)e);
+        return;
+    }
+    const float Tt = T - e;
+    if (a.arrhenius && Tt >= a.fc[FC_TLO] && Tt < a.fc[FC_THI]) {
+        const float ear = a.fc[FC_EAR_HI], lna = a.fc[FC_LNA_HI];
+        const float yh = __fdiv_rn(ear, T);
+        // (Ea/R) - yh (T - e) = [ear - yh T] + ear_lo + yh e; the bracket is exact
+        const float r = (__fmaf_rn(-yh, T, ear) + a.fc[FC_EAR_LO]) + yh * e;
+        const float yl = __fdiv_rn(r, T);
+        const float s = lna - yh, bb = s - lna;
+        const float err = (lna - (s - bb)) + (-yh - bb);
+        const float xl = (err + a.fc[FC_LNA_LO]) - yl;
+        double inc;
+        if (s < 80.f) {
+            const float ex = expf(s);
+            inc = (double)(a.fc[FC_DT] * __fmaf_rn(ex, xl, ex));
+        } else {
+            inc = a.dt * exp(a.lnA - a.Ea / (a.Rgas * ((double)T - (double)e)));
+        }
+        const double o = a.omega[v];
+        const double on = o + inc;
+        a.omega[v] = on;
+        const long long ob = __double_as_longlong(o), nb = __double_as_longlong(on);
+#pragma unroll
+        for (int t = 0; t < 3; ++t) {
+            const long long tb = __double_as_longlong(a.thr[t]);
+            if (ob < tb && nb >= tb) a.thres[v + t * ni] = a.t_new;
+        }
+    }
+    if (Tt >= a.fc[FC_TABL] && a.mat[v] != 0) {
+        a.mat[v] = 0;  // optics -> air
+        ((float *)a.J)[v] = 0.f;
+        atomicAdd(a.n_ablated, 1ull);
+    }
+}
 
 }  // namespace
 }  // namespace tam

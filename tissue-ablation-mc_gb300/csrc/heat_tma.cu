@@ -23,6 +23,9 @@ namespace tam {
 struct FusedTma {
     CUtensorMap T[2], E[2], ax, ay, az, irc, J;
 };
+struct FusedCls {
+    CUtensorMap T[2], E[2], J, cls;
+};
 
 namespace {
 
@@ -237,7 +240,7 @@ __global__ void __launch_bounds__(FX *FY, 4)
             const float Ts = Tnew - Enew;
             if (!(Ts == Ts)) errbits |= DEVERR_NAN;
             else if (Ts < 0.f) errbits |= DEVERR_NEG_T;
-            if (Ts >= a.fc[FC_SCREEN]) rare_update<float>(a, v, ni, (double)Tnew - (double)Enew);
+            if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew);
         }
         __syncthreads();  // every thread is done with the stage the next issue overwrites
         Tp = Tc;
@@ -248,9 +251,208 @@ __global__ void __launch_bounds__(FX *FY, 4)
         azc = azn;
     }
     if (!ok) {
-        // a stage never completed: record it and drain what is still in flight
+        // a stage never completed: record it and drain what may still be in
+        // flight (the last phase of each stage)
         errbits |= DEVERR_SYNC_TIMEOUT;
-        for (int idx = 0; idx < issued; ++idx) (void)wait(idx);
+        for (int idx = issued > TS ? issued - TS : 0; idx < issued; ++idx) (void)wait(idx);
+    }
+    if (errbits) atomicOr(a.err, errbits);
+}
+
+// ------------------------------------------------------------------------
+// Class-table form.  When the thermal properties are those of a material
+// table indexed by a per-voxel class id (u8), the face coefficients need no
+// arrays: k_f/(rho_f c_f) for a pair of classes comes from a 16 x 16 table in
+// shared memory and 1/(rho c), k, rho, c from per-class tables.  Per plane the
+// ring then stages T and the Kahan term (with halo), J (own voxels) and the
+// class ids (with halo) -- 13 bytes read and 8 written per voxel instead of
+// 28 + 8.  A uniform grid (one class everywhere) stages no class ids at all.
+constexpr int CTS = 6;                          // stages of the class-table ring
+constexpr int CPITCH = 64;                      // class row: x from bx*32 - 16, 64 bytes
+constexpr int CLS_BYTES = TROWS * CPITCH;       // 640
+
+template <bool UNIFORM> struct ClsLayout {
+    static constexpr int T_OFF = 0, E_OFF = ARR_BYTES, J_OFF = 2 * ARR_BYTES, C_OFF = 2 * ARR_BYTES + OWN_BYTES;
+    static constexpr int STAGE = ((C_OFF + (UNIFORM ? 0 : CLS_BYTES) + 127) / 128) * 128;
+    static constexpr uint32_t TX = 2u * TROWS * TPITCH * 4 + FY * FX * 4 + (UNIFORM ? 0u : (uint32_t)CLS_BYTES);
+    static constexpr int SMEM = CTS * STAGE + CTS * 8 + 128;
+};
+
+struct ClsMaps {  // the maps of one launch
+    CUtensorMap T, E, J, cls;
+};
+
+template <bool UNIFORM>
+__global__ void __launch_bounds__(FX *FY, 4)
+    fused_cls_kernel(const __grid_constant__ FusedArgs a, const __grid_constant__ ClsMaps m,
+                     const __grid_constant__ ClassLut L, int zchunk)
+{
+    using Lay = ClsLayout<UNIFORM>;
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ float s_fa[MAX_MAT * MAX_MAT];
+    unsigned char *sm = smem_raw + ((128 - (su32(smem_raw) & 127)) & 127);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + CTS * Lay::STAGE);
+    const int tx = threadIdx.x, ty = threadIdx.y;
+    const int x = blockIdx.x * FX + tx, y = blockIdx.y * FY + ty;
+    const bool in = x < a.nx && y < a.ny;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(a.nz, z0 + zchunk);
+    const int nplanes = z1 - z0;
+    const int last = nplanes + 1;  // plane indices 0 .. last (z0 - 1 .. z1)
+    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, ni = sz * a.nz;
+    float *To = (float *)a.T_out, *Q = (float *)a.Q;
+    float *Eo = a.Tc_out;
+    const float dt = a.fc[FC_DT], Pdt = a.fc[FC_PDT];
+    const float cx = a.fc[FC_CX], cy = a.fc[FC_CY], cz = a.fc[FC_CZ];
+    const bool src_on = Pdt != 0.f;
+    const bool xy_inner = x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1;
+    const bool leader = tx == 0 && ty == 0;
+    const int gx = blockIdx.x * FX - 4, gy = blockIdx.y * FY - 1, gx8 = blockIdx.x * FX - 16;
+    const int uc = L.uniform >= 0 ? L.uniform : 0;
+    const float au = L.fa[uc * MAX_MAT + uc];
+    const float Cx = cx * au, Cy = cy * au, Cz = cz * au;
+    unsigned errbits = 0;
+    if (!UNIFORM)
+        for (int t = ty * FX + tx; t < MAX_MAT * MAX_MAT; t += FX * FY) s_fa[t] = L.fa[t];
+
+    auto stage = [&](int idx) { return sm + (idx % CTS) * Lay::STAGE; };
+    auto issue = [&](int idx) {
+        unsigned char *b = stage(idx);
+        uint64_t *br = bar + (idx % CTS);
+        const int zz = z0 - 1 + idx;
+        fence_proxy_async();
+        mbar_expect_tx(br, Lay::TX);
+        tma_load_3d(b + Lay::T_OFF, &m.T, gx, gy, zz, br);
+        tma_load_3d(b + Lay::E_OFF, &m.E, gx, gy, zz, br);
+        tma_load_3d(b + Lay::J_OFF, &m.J, gx + 4, gy + 1, zz, br);
+        if (!UNIFORM) tma_load_3d(b + Lay::C_OFF, &m.cls, gx8, gy, zz, br);
+    };
+    auto wait = [&](int idx) { return mbar_wait(bar + (idx % CTS), (uint32_t)((idx / CTS) & 1)); };
+
+    if (leader) {
+        for (int s = 0; s < CTS; ++s) mbar_init(bar + s, 1);
+        fence_mbar_init();
+        fence_proxy_async();
+    }
+    __syncthreads();
+    int issued = 0;  // planes 0 .. issued-1 have been issued
+    if (leader)
+        for (int idx = 0; idx <= CTS - 2 && idx <= last; ++idx) issue(idx);
+    issued = (CTS - 1 < last + 1) ? CTS - 1 : last + 1;
+    bool ok = __syncthreads_and(wait(0) && wait(1)) != 0;
+    const int q = (ty + 1) * TPITCH + tx + 4;   // own voxel in the T / E rows
+    const int o = ty * FX + tx;                 // own voxel in J
+    const int qc = (ty + 1) * CPITCH + tx + 16; // own voxel in the class rows
+    float Tp = 0.f, ep = 0.f, Tc = 0.f, ec = 0.f;
+    int kp = 0, kc = 0;  // classes of the planes below and at z
+    if (in && ok) {
+        const unsigned char *C0 = stage(1);
+        Tc = ((const float *)(C0 + Lay::T_OFF))[q];
+        ec = ((const float *)(C0 + Lay::E_OFF))[q];
+        if (!UNIFORM) kc = (C0 + Lay::C_OFF)[qc] & (MAX_MAT - 1);
+        if (z0 > 0) {
+            const unsigned char *Pm = stage(0);
+            Tp = ((const float *)(Pm + Lay::T_OFF))[q];
+            ep = ((const float *)(Pm + Lay::E_OFF))[q];
+            if (!UNIFORM) kp = (Pm + Lay::C_OFF)[qc] & (MAX_MAT - 1);
+        }
+    }
+    for (int i = 0; i < nplanes && ok; ++i) {
+        const int z = z0 + i;
+        const int64_t v = (int64_t)x + sy * y + sz * z;
+        const bool has_n = z + 1 < a.nz;
+        if (i + CTS - 1 <= last) {
+            if (leader) issue(i + CTS - 1);
+            issued = i + CTS;
+        }
+        ok = __syncthreads_and(wait(i + 2)) != 0;  // plane z+1 has landed for the whole block
+        if (!ok) break;
+        const unsigned char *P = stage(i + 1), *N = stage(i + 2);
+        const float *PT = (const float *)(P + Lay::T_OFF), *PE = (const float *)(P + Lay::E_OFF);
+        float Tn_ = 0.f, en_ = 0.f;
+        int kn = 0;
+        if (in && has_n) {
+            Tn_ = ((const float *)(N + Lay::T_OFF))[q];
+            en_ = ((const float *)(N + Lay::E_OFF))[q];
+            if (!UNIFORM) kn = (N + Lay::C_OFF)[qc] & (MAX_MAT - 1);
+        }
+        if (in) {
+            const int k = UNIFORM ? uc : kc;
+            const float Jv = src_on ? ((const float *)(P + Lay::J_OFF))[o] : 0.f;
+            const float tzm = (Tp - Tc) - (ep - ec), tzp = (Tn_ - Tc) - (en_ - ec);
+            const float txm = (PT[q - 1] - Tc) - (PE[q - 1] - ec), txp = (PT[q + 1] - Tc) - (PE[q + 1] - ec);
+            const float tym = (PT[q - TPITCH] - Tc) - (PE[q - TPITCH] - ec),
+                        typ = (PT[q + TPITCH] - Tc) - (PE[q + TPITCH] - ec);
+            // face coefficients of the six faces (uniform: one value per axis)
+            float axm = Cx, axp = Cx, aym = Cy, ayp = Cy, azm = Cz, azp = Cz;
+            if (!UNIFORM) {
+                const unsigned char *PC = P + Lay::C_OFF;
+                const float *row = s_fa + k * MAX_MAT;
+                axm = cx * row[PC[qc - 1] & (MAX_MAT - 1)];
+                axp = cx * row[PC[qc + 1] & (MAX_MAT - 1)];
+                aym = cy * row[PC[qc - CPITCH] & (MAX_MAT - 1)];
+                ayp = cy * row[PC[qc + CPITCH] & (MAX_MAT - 1)];
+                azm = cz * row[kp];
+                azp = cz * row[kn];
+            }
+            float lap;
+            if (xy_inner && z > 0 && has_n) {
+                lap = azm * tzm + azp * tzp + aym * tym + ayp * typ + axm * txm + axp * txp;
+            } else {
+                // a face of this voxel lies on the grid boundary: ghost faces
+                // use the voxel's own properties
+                const float kk = L.k[k], rr = L.rho[k], hh = L.c[k];
+                lap = z > 0 ? azm * tzm : ghost_term<float>(a, 4, Tc, ec, kk, rr, hh);
+                lap += has_n ? azp * tzp : ghost_term<float>(a, 5, Tc, ec, kk, rr, hh);
+                lap += y > 0 ? aym * tym : ghost_term<float>(a, 2, Tc, ec, kk, rr, hh);
+                lap += y < a.ny - 1 ? ayp * typ : ghost_term<float>(a, 3, Tc, ec, kk, rr, hh);
+                lap += x > 0 ? axm * txm : ghost_term<float>(a, 0, Tc, ec, kk, rr, hh);
+                lap += x < a.nx - 1 ? axp * txp : ghost_term<float>(a, 1, Tc, ec, kk, rr, hh);
+            }
+            const float dT = dt * lap;
+            const float sPJ = Pdt * Jv;
+            const float src = sPJ * L.irc[k];
+            float Tnew, Enew = 0.f;
+            bool clamped = false;
+            if (a.boil && Tc >= a.fc[FC_TBOIL]) {
+                const float rr = L.rho[k], rc = rr * L.c[k];
+                const float qv = a.fc[FC_LW] * rr * a.fc[FC_VVOX];
+                const float Qv = Q[v];
+                if (Qv < qv) {
+                    const float Ein = (sPJ + rc * dT) * a.fc[FC_VVOX];
+                    if (Ein > 0.f) {
+                        const float qn = Qv + Ein;
+                        Q[v] = qn < qv ? qn : qv;
+                        Tnew = a.fc[FC_TBOIL];
+                        clamped = true;
+                    }
+                }
+            }
+            if (!clamped) {
+                const float inc = dT + src;
+                const float yk = inc - ec;
+                const float t = Tc + yk;
+                Enew = (t - Tc) - yk;
+                Tnew = t;
+            }
+            To[v] = Tnew;
+            Eo[v] = Enew;
+            const float Ts = Tnew - Enew;
+            if (!(Ts == Ts)) errbits |= DEVERR_NAN;
+            else if (Ts < 0.f) errbits |= DEVERR_NEG_T;
+            if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew);
+        }
+        __syncthreads();  // every thread is done with the stage the next issue overwrites
+        Tp = Tc;
+        ep = ec;
+        Tc = Tn_;
+        ec = en_;
+        kp = kc;
+        kc = kn;
+    }
+    if (!ok) {
+        errbits |= DEVERR_SYNC_TIMEOUT;
+        for (int idx = issued > CTS ? issued - CTS : 0; idx < issued; ++idx) (void)wait(idx);
     }
     if (errbits) atomicOr(a.err, errbits);
 }
@@ -281,6 +483,36 @@ cudaError_t encode(CUtensorMap *m, const float *base, int nx, int ny, int nz, in
                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// Tensor map of the u8 class grid, rows of `pitch` bytes (a multiple of 16).
+cudaError_t encode_u8(CUtensorMap *m, const uint8_t *base, int pitch, int ny, int nz, int bx, int by)
+{
+    const cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)ny, (cuuint64_t)nz};
+    const cuuint64_t strides[2] = {(cuuint64_t)pitch, (cuuint64_t)pitch * ny};
+    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    const CUresult r = p_encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, (void *)base, dims, strides, box, estr,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
+}
+
+// Class grid (row pitch `pitch`) from the material ids; ids beyond the table
+// map to 0 as in the property fill.
+__global__ void cls_from_mat_kernel(const uint8_t *mat, int nmat, uint8_t *cls, int nx, int ny, int nz, int pitch)
+{
+    const int64_t n = (int64_t)pitch * ny * nz;
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int x = (int)(u % pitch);
+        const int64_t row = u / pitch;
+        uint8_t c = 0;
+        if (x < nx) {
+            const int m = mat[row * nx + x];
+            c = (uint8_t)(m < nmat ? m : 0);
+        }
+        cls[u] = c;
+    }
 }
 
 // Forward face coefficients of the FP32 step: A_x(v) = opscale/dx^2 *
@@ -354,6 +586,81 @@ cudaError_t fused_tma_create(FusedTma **out, int nx, int ny, int nz, float *cons
 }
 
 void fused_tma_destroy(FusedTma *m) { delete m; }
+
+int cls_pitch_for(int nx) { return (nx + 15) / 16 * 16; }
+
+cudaError_t launch_cls_from_mat(const uint8_t *mat, int nmat, uint8_t *cls, int nx, int ny, int nz, int pitch,
+                                cudaStream_t s)
+{
+    const int64_t n = (int64_t)pitch * ny * nz;
+    int64_t blocks = (n + 255) / 256;
+    if (blocks > 152 * 16) blocks = 152 * 16;
+    if (blocks < 1) return cudaSuccess;
+    count_launch();
+    cls_from_mat_kernel<<<(unsigned)blocks, 256, 0, s>>>(mat, nmat, cls, nx, ny, nz, pitch);
+    return cudaGetLastError();
+}
+
+cudaError_t fused_cls_create(FusedCls **out, int nx, int ny, int nz, float *const T[2], float *const Tc[2],
+                             const float *J, const uint8_t *cls, int pitch)
+{
+    *out = nullptr;
+    if (!fused_tma_supported(nx) || pitch % 16 != 0 || pitch < nx) return cudaErrorNotSupported;
+    cudaError_t e = encoder();
+    if (e != cudaSuccess) return e;
+    FusedCls *m = new FusedCls();
+    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+        e = encode(&m->T[b], T[b], nx, ny, nz, TPITCH, TROWS);
+        if (e == cudaSuccess) e = encode(&m->E[b], Tc[b], nx, ny, nz, TPITCH, TROWS);
+    }
+    if (e == cudaSuccess) e = encode(&m->J, J, nx, ny, nz, FX, FY);
+    if (e == cudaSuccess) e = encode_u8(&m->cls, cls, pitch, ny, nz, CPITCH, TROWS);
+    if (e != cudaSuccess) {
+        delete m;
+        return e;
+    }
+    *out = m;
+    return cudaSuccess;
+}
+
+void fused_cls_destroy(FusedCls *m) { delete m; }
+
+namespace {
+template <bool UNIFORM>
+cudaError_t launch_cls_t(const FusedArgs &a, const ClsMaps &m, const ClassLut &L, cudaStream_t s)
+{
+    const int bx = (a.nx + FX - 1) / FX, by = (a.ny + FY - 1) / FY;
+    int zchunk = a.zchunk > 0 ? a.zchunk : 16;
+    if (zchunk > a.nz) zchunk = a.nz;
+    const int chunks = (a.nz + zchunk - 1) / zchunk;
+    static std::atomic<unsigned long long> attr_set{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(attr_set.load() & bit)) {
+        e = cudaFuncSetAttribute(fused_cls_kernel<UNIFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 ClsLayout<UNIFORM>::SMEM);
+        if (e != cudaSuccess) return e;
+        attr_set.fetch_or(bit);
+    }
+    count_launch();
+    fused_cls_kernel<UNIFORM><<<dim3(bx, by, chunks), dim3(FX, FY), ClsLayout<UNIFORM>::SMEM, s>>>(a, m, L, zchunk);
+    return cudaGetLastError();
+}
+}  // namespace
+
+cudaError_t launch_fused_cls(const FusedArgs &a0, const FusedCls *cm, int which, const ClassLut &L, cudaStream_t s)
+{
+    FusedArgs a = a0;
+    fill_fused_consts(a);
+    ClsMaps m;
+    m.T = cm->T[which];
+    m.E = cm->E[which];
+    m.J = cm->J;
+    m.cls = cm->cls;
+    return L.uniform >= 0 ? launch_cls_t<true>(a, m, L, s) : launch_cls_t<false>(a, m, L, s);
+}
 
 cudaError_t launch_fused_tma(const FusedArgs &a0, const FusedTma *tm, int which, cudaStream_t s)
 {

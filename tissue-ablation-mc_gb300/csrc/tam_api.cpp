@@ -13,6 +13,7 @@
 #include <fstream>
 #include <sstream>
 #include <string>
+#include <thread>
 #include <type_traits>
 #include <vector>
 
@@ -96,6 +97,16 @@ struct tam_ctx {
     tam::FusedTma *tma = nullptr;  // tensor maps of the FP32 fused step
     float *d_ax = nullptr, *d_ay = nullptr, *d_az = nullptr, *d_irc = nullptr;  // its face coefficients
     bool coeff_dirty = true;
+    // class-table form of the FP32 fused step: thermal properties by material
+    // class (valid until k, rho or c are uploaded per voxel)
+    bool use_cls = true;
+    bool arr_fp64 = false;           // FP32 form: FP64 Arrhenius exponent instead of float-float
+    tam::FusedCls *fcls = nullptr;
+    uint8_t *d_cls = nullptr;
+    int cls_pitch = 0;
+    bool thermal_by_class = false;
+    int cls_uniform = -1;            // >= 0 while every voxel has this thermal class
+    tam::ClassLut clut{};
     int uniform_id = -1;             // >= 0 while every voxel holds this material
     long long nabl_at_uniform = 0;
 
@@ -326,6 +337,35 @@ int ref_setup(tam_ctx *ctx)
 }
 
 // -------------------------------------------------------- config set-up --
+// Thermal properties by material class: the class grid (a pitched copy of the
+// material ids) and the per-class tables of the class-table heat step.  `u` is
+// the material every voxel holds, or -1.
+int set_thermal_classes(tam_ctx *ctx, int u)
+{
+    tam::ClassLut &L = ctx->clut;
+    const int nm = ctx->cfg.nmat;
+    for (int i = 0; i < tam::MAX_MAT; ++i) {
+        const int a = i < nm ? i : 0;
+        const double ki = ctx->lut.k[a], ri = ctx->lut.rho[a], ci = ctx->lut.c[a];
+        L.k[i] = (float)ki;
+        L.rho[i] = (float)ri;
+        L.c[i] = (float)ci;
+        L.irc[i] = (float)(1.0 / (ri * ci));
+        for (int j = 0; j < tam::MAX_MAT; ++j) {
+            const int b = j < nm ? j : 0;
+            const double kf = 0.5 * (ki + ctx->lut.k[b]), rf = 0.5 * (ri + ctx->lut.rho[b]),
+                         cf = 0.5 * (ci + ctx->lut.c[b]);
+            L.fa[i * tam::MAX_MAT + j] = (float)(kf / (rf * cf));
+        }
+    }
+    ctx->cls_uniform = u;
+    L.uniform = u;
+    ctx->thermal_by_class = true;
+    if (ctx->d_cls)
+        CK(tam::launch_cls_from_mat(ctx->d_mat, nm, ctx->d_cls, ctx->nx, ctx->ny, ctx->nz, ctx->cls_pitch, ctx->stream));
+    return TAM_OK;
+}
+
 int cfg_setup(tam_ctx *ctx)
 {
     reset_scalars(ctx);
@@ -371,6 +411,7 @@ int cfg_setup(tam_ctx *ctx)
     ctx->nabl_at_uniform = 0;
     CK(tam::launch_props_from_mat(ctx->d_mat, c.nmat, ctx->lut, ctx->d_k, ctx->d_rho, ctx->d_c, ctx->fp64, ctx->ni, s));
     ctx->coeff_dirty = true;
+    RC(set_thermal_classes(ctx, m0));
     for (int b = 0; b < 2; ++b) {
         CK(tam::launch_fill_real(ctx->d_Tf[b], ctx->fp64, c.T0, ctx->ni, s));
         if (!ctx->fp64) CK(cudaMemsetAsync(ctx->d_Tc[b], 0, ctx->ni * sizeof(float), s));
@@ -398,6 +439,7 @@ tam::FusedArgs fused_args(tam_ctx *ctx)
     a.dz = ctx->dz;
     a.opscale = c.opscale;
     a.dt = ctx->cdt;
+    a.arr_fp64 = ctx->arr_fp64 ? 1 : 0;
     a.vvox = ctx->volumeVoxel;
     a.boil = c.boil;
     a.T_boil = c.T_boil;
@@ -608,7 +650,8 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
 {
     tam::FusedArgs a = fused_args(ctx);
     const int check = ctx->cfg.retrace_check > 0 ? ctx->cfg.retrace_check : 0;
-    if (ctx->tma && ctx->use_tma && ctx->coeff_dirty && nsteps > 0) {
+    const bool cls = ctx->fcls && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class;
+    if (!cls && ctx->tma && ctx->use_tma && ctx->coeff_dirty && nsteps > 0) {
         CK(tam::launch_face_coeffs(a, ctx->d_ax, ctx->d_ay, ctx->d_az, ctx->d_irc, ctx->stream));
         ctx->coeff_dirty = false;
     }
@@ -620,7 +663,8 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
         a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[1 - ctx->fcur];
         a.P = ctx->laserOn * get_pwr(ctx);
         a.t_new = ctx->time + ctx->cdt;
-        if (ctx->tma && ctx->use_tma) CK(tam::launch_fused_tma(a, ctx->tma, ctx->fcur, ctx->stream));
+        if (cls) CK(tam::launch_fused_cls(a, ctx->fcls, ctx->fcur, ctx->clut, ctx->stream));
+        else if (ctx->tma && ctx->use_tma) CK(tam::launch_fused_tma(a, ctx->tma, ctx->fcur, ctx->stream));
         else CK(tam::launch_fused_step(a, ctx->fp64, ctx->stream));
         ctx->fcur = 1 - ctx->fcur;
         const bool on = pulse_update(ctx, ctx->cdt);
@@ -959,6 +1003,13 @@ int tam_create(const tam_params *p, const tam_config *cfg, tam_ctx **out)
             (void)cudaGetLastError();
             ctx->tma = nullptr;  // the cp.async form runs instead
         }
+        ctx->cls_pitch = tam::cls_pitch_for(ctx->nx);
+        if (dalloc_t(ctx, &ctx->d_cls, (int64_t)ctx->cls_pitch * ctx->ny * ctx->nz) != TAM_OK) return bail(TAM_E_NOMEM);
+        if (tam::fused_cls_create(&ctx->fcls, ctx->nx, ctx->ny, ctx->nz, T2, E2, (const float *)ctx->d_J, ctx->d_cls,
+                                  ctx->cls_pitch) != cudaSuccess) {
+            (void)cudaGetLastError();
+            ctx->fcls = nullptr;
+        }
     }
     r = ctx->config ? cfg_setup(ctx) : ref_setup(ctx);
     if (r == TAM_OK) r = finish(ctx, "tam_create");
@@ -979,6 +1030,7 @@ int tam_destroy(tam_ctx *ctx)
     for (cudaEvent_t e : ctx->ev)
         if (e) cudaEventDestroy(e);
     if (ctx->tma) tam::fused_tma_destroy(ctx->tma);
+    if (ctx->fcls) tam::fused_cls_destroy(ctx->fcls);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return TAM_OK;
@@ -1128,6 +1180,7 @@ int tam_upload(tam_ctx *ctx, int field, const void *host, int64_t nbytes)
         void *dst = field == TAM_F_KAPPA ? ctx->d_k : (field == TAM_F_DENSITY ? ctx->d_rho : ctx->d_c);
         CK(tam::launch_halo_to_interior(ctx->d_halo, dst, ctx->fp64, ctx->nx, ctx->ny, ctx->nz, s));
         ctx->coeff_dirty = true;
+        ctx->thermal_by_class = false;  // per-voxel properties: coefficient arrays from now on
         break;
     }
     case TAM_F_JMEAN: CK(h2d(ctx->d_jmean)); break;
@@ -1155,6 +1208,7 @@ int tam_upload(tam_ctx *ctx, int field, const void *host, int64_t nbytes)
         CK(tam::launch_props_from_mat(ctx->d_mat, ctx->cfg.nmat, ctx->lut, ctx->d_k, ctx->d_rho, ctx->d_c, ctx->fp64,
                                       ctx->ni, s));
         ctx->coeff_dirty = true;
+        RC(set_thermal_classes(ctx, u));
         ctx->need_trace = true;
         break;
     }
@@ -1298,6 +1352,70 @@ int tam_run(tam_ctx *ctx, uint64_t seed, int64_t max_iters, int64_t *iters)
     return TAM_OK;
 }
 
+// ------------------------------------------------------------ batches --
+// Independent instances (the multi-instance workload): one host thread per
+// context drives that context's loop on its own stream, so the device runs
+// the instances' kernels side by side; a small instance's short heat kernels
+// fill the gaps of the others.  Contexts are distinct objects, so the
+// single-thread rule of a context holds.
+}  // extern "C"
+namespace {
+template <typename F> int run_batch(tam_ctx *const *ctxs, int32_t n, F &&body)
+{
+    if (n < 0 || (n > 0 && !ctxs)) return fail(nullptr, TAM_E_INVALID, "bad batch");
+    for (int32_t i = 0; i < n; ++i) {
+        if (!ctxs[i]) return fail(nullptr, TAM_E_INVALID, "null context in batch");
+        for (int32_t j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) return fail(nullptr, TAM_E_INVALID, "context listed twice in batch");
+    }
+    std::vector<int> rc(n, TAM_OK);
+    std::vector<std::thread> th;
+    th.reserve(n);
+    for (int32_t i = 0; i < n; ++i)
+        th.emplace_back([&, i] {
+            tam_ctx *c = ctxs[i];
+            if (cudaSetDevice(c->device) != cudaSuccess) {
+                rc[i] = fail(c, TAM_E_CUDA, "cudaSetDevice failed");
+                return;
+            }
+            rc[i] = body(c, i);
+            if (rc[i] == TAM_OK) rc[i] = finish(c, "tam_batch");
+        });
+    for (auto &t : th) t.join();
+    for (int32_t i = 0; i < n; ++i)
+        if (rc[i] != TAM_OK) {
+            g_thread_err = "batch instance " + std::to_string(i) + ": " + ctxs[i]->err;
+            return rc[i];
+        }
+    return TAM_OK;
+}
+}  // namespace
+extern "C" {
+
+int tam_batch_step_coupled(tam_ctx *const *ctxs, int32_t n, int32_t iters, const uint64_t *seeds)
+{
+    if (iters < 0 || (n > 0 && !seeds)) return fail(nullptr, TAM_E_INVALID, "bad batch arguments");
+    return run_batch(ctxs, n, [&](tam_ctx *c, int32_t i) {
+        for (int32_t k = 0; k < iters; ++k) RC(outer_iteration(c, seeds[i]));
+        return (int)TAM_OK;
+    });
+}
+
+int tam_batch_run(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, int64_t max_iters, int64_t *iters)
+{
+    if (n > 0 && !seeds) return fail(nullptr, TAM_E_INVALID, "bad batch arguments");
+    return run_batch(ctxs, n, [&](tam_ctx *c, int32_t i) {
+        int64_t it = 0;
+        while (c->time <= c->total_time) {
+            if (max_iters > 0 && it >= max_iters) break;
+            RC(outer_iteration(c, seeds[i]));
+            ++it;
+        }
+        if (iters) iters[i] = it;
+        return (int)TAM_OK;
+    });
+}
+
 int tam_finalize(tam_ctx *ctx)
 {
     if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
@@ -1392,6 +1510,10 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
         ctx->scat_min = (int)value;
     } else if (k == "heat.tma") {
         ctx->use_tma = value != 0;
+    } else if (k == "heat.cls") {
+        ctx->use_cls = value != 0;
+    } else if (k == "heat.arrhenius_fp64") {
+        ctx->arr_fp64 = value != 0;
     } else if (k == "heat.zchunk") {
         if (value < 0 || value > ctx->nz) return fail(ctx, TAM_E_INVALID, "heat.zchunk must be in 0..nz");
         ctx->zchunk = (int)value;

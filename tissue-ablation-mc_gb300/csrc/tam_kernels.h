@@ -119,7 +119,10 @@ enum FusedConst : int {
     FC_BCT = 11,                      // 6 Dirichlet face temperatures
     FC_BCHD = 17,                     // 6 Robin h * d (d: spacing normal to the face)
     FC_BCTA = 23,                     // 6 Robin ambient temperatures
-    FC_N = 29
+    // Arrhenius constants for the FP32 form: ln A and Ea/R as float-float
+    // pairs (high part, low part), exact window and ablation temperatures
+    FC_LNA_HI = 29, FC_LNA_LO, FC_EAR_HI, FC_EAR_LO, FC_TLO, FC_THI, FC_TABL,
+    FC_N = 36
 };
 
 struct FusedArgs {
@@ -145,6 +148,7 @@ struct FusedArgs {
     unsigned long long *n_ablated;    // running count
     unsigned *err;
     int32_t zchunk;                   // z planes per thread column (0: automatic)
+    int32_t arr_fp64;                 // FP32 form: 1 = Arrhenius exponent in FP64, 0 = float-float
     // the constants above in the kernel's storage precision (filled by
     // launch_fused_step), so the kernel converts nothing per voxel
     float fc[FC_N];
@@ -166,6 +170,24 @@ cudaError_t launch_face_coeffs(const FusedArgs &a, float *ax, float *ay, float *
 void fused_tma_destroy(FusedTma *m);
 // `which` selects the (T, Tc) buffer pair read by this step (0 or 1).
 cudaError_t launch_fused_tma(const FusedArgs &a, const FusedTma *m, int which, cudaStream_t s);
+
+// Class-table form of the FP32 TMA step: thermal properties given per class
+// (material) and a u8 class id per voxel, stored with a row pitch that is a
+// multiple of 16 bytes (cls_pitch_for).  No coefficient arrays are read.
+struct ClassLut {
+    float fa[MAX_MAT * MAX_MAT];  // k_f / (rho_f c_f) of the face between classes i and j (arithmetic means)
+    float irc[MAX_MAT];           // 1 / (rho c)
+    float k[MAX_MAT], rho[MAX_MAT], c[MAX_MAT];
+    int32_t uniform;              // >= 0: every voxel has this class
+};
+struct FusedCls;  // opaque: tensor maps of T[2], Tc[2], J and the class grid
+int cls_pitch_for(int nx);
+cudaError_t launch_cls_from_mat(const uint8_t *mat, int nmat, uint8_t *cls, int nx, int ny, int nz, int pitch,
+                                cudaStream_t s);
+cudaError_t fused_cls_create(FusedCls **out, int nx, int ny, int nz, float *const T[2], float *const Tc[2],
+                             const float *J, const uint8_t *cls, int pitch);
+void fused_cls_destroy(FusedCls *m);
+cudaError_t launch_fused_cls(const FusedArgs &a, const FusedCls *m, int which, const ClassLut &L, cudaStream_t s);
 
 // Halo (reference-layout) FP64 temperature from the interior state, with
 // ghosts filled from the boundary conditions.

@@ -127,6 +127,9 @@ SIGNATURES = [
     ("tam_get_tallies_ex", C.c_int, [_P, _D, C.c_int32]),
     ("tam_get_state", C.c_int, [_P, C.POINTER(State)]),
     ("tam_get_timing", C.c_int, [_P, _D, _D, C.POINTER(C.c_int64)]),
+    ("tam_batch_step_coupled", C.c_int, [C.POINTER(_P), C.c_int32, C.c_int32, C.POINTER(C.c_uint64)]),
+    ("tam_batch_run", C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(C.c_uint64), C.c_int64,
+                                C.POINTER(C.c_int64)]),
     ("tam_kernel_launches", C.c_int64, []),
     ("tam_set_tuning", C.c_int, [_P, C.c_char_p, C.c_int64]),
     ("tam_write_output", C.c_int, [_P, C.c_char_p]),

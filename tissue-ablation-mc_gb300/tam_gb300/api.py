@@ -187,6 +187,29 @@ class Context:
         self._ck(self._lib.tam_write_output(self._h, directory.encode()))
 
 
+def _batch_args(contexts, seeds):
+    n = len(contexts)
+    if len(seeds) != n:
+        raise ValueError("one seed per context")
+    hs = (_abi._P * n)(*[c._h for c in contexts])
+    sd = (C.c_uint64 * n)(*[int(x) for x in seeds])
+    return n, hs, sd
+
+
+def batch_step_coupled(contexts, iters: int, seeds) -> None:
+    """`iters` outer iterations on every context, the instances running concurrently."""
+    n, hs, sd = _batch_args(contexts, seeds)
+    check(lib().tam_batch_step_coupled(hs, n, int(iters), sd))
+
+
+def batch_run(contexts, seeds, max_iters: int = 0):
+    """Each context's whole coupled loop (as Context.run), concurrently; returns iteration counts."""
+    n, hs, sd = _batch_args(contexts, seeds)
+    it = (C.c_int64 * n)()
+    check(lib().tam_batch_run(hs, n, sd, int(max_iters), it))
+    return list(it)
+
+
 def kernel_launches() -> int:
     return int(lib().tam_kernel_launches())
 

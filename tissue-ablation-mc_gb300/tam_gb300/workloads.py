@@ -1,0 +1,174 @@
+"""Synthetic workloads of the five benchmark configurations, built from seeds.
+
+Each builder returns a ``Workload``: run parameters, the config-mode extension,
+an optional per-voxel material grid (u8, Fortran order) and a description.
+Sizes default to the full configurations; ``edge``/``scale`` arguments build
+smaller copies of the same geometry for tests.
+
+  C1  100^3 homogeneous cube 1x1x1 cm, 1e6 packets, 1 W for 1 s
+  C2  200^3 homogeneous cube, 1e8 packets, 2 W for 2 s (FP32 + Kahan)
+  C3  256x256x128 three-layer skin slab over 1x1x0.5 cm, 1e8 packets per pass,
+      2e4 heat steps at 5 W, MC re-run when 0.1 % of the grid has ablated
+  C4  64 instances with edges uniform in [64,192] per axis and per-instance
+      optics and laser drawn from a seeded generator; 1e7 packets, 5e3 steps
+  C5  512^3 over 2x2x2 cm: dermis with 20 seeded vessel cylinders and 5
+      spherical inclusions; 1e9 packets, 10 pulses of 50 ms at 10 W, 1 Hz
+
+Thermal constants that the configurations leave open (the C3 layers, the C5
+blood and inclusions) are literature-typical skin values, fixed here:
+
+  epidermis  k 0.21 W/m/K, rho 1200 kg/m^3, c 3590 J/kg/K
+  dermis     k 0.37,       rho 1200,        c 3300
+  subcutis   k 0.16,       rho 1000,        c 2674
+  blood      k 0.52,       rho 1060,        c 3770
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import api
+
+AIR = (0.0, 0.0, 0.0, 1.0, 0.56, 1070.0, 3400.0)  # material 0: optics of air (ablated voxels)
+TISSUE = (0.3, 100.0, 0.9, 1.38, 0.56, 1070.0, 3400.0)
+EPIDERMIS = (1.0, 200.0, 0.8, 1.4, 0.21, 1200.0, 3590.0)
+DERMIS = (0.3, 120.0, 0.9, 1.4, 0.37, 1200.0, 3300.0)
+SUBCUTIS = (0.1, 80.0, 0.9, 1.4, 0.16, 1000.0, 2674.0)
+BLOOD = (20.0, 300.0, 0.98, 1.4, 0.52, 1060.0, 3770.0)
+INCLUSION = (2.0, 120.0, 0.9, 1.4, 0.37, 1200.0, 3300.0)
+
+
+@dataclass
+class Workload:
+    name: str
+    params: object
+    config: object
+    grid: np.ndarray | None = None          # u8 material ids, (nx, ny, nz) Fortran order
+    packets: int = 0
+    heat_steps: int = 0
+    info: dict = field(default_factory=dict)
+
+    def context(self):
+        """A library context holding this workload (material grid uploaded)."""
+        ctx = api.Context(self.params, self.config)
+        if self.grid is not None:
+            ctx.upload(api._abi.TAM_F_MATERIAL, self.grid)
+        return ctx
+
+
+def _config(mats, **kw):
+    c = api.default_config(nmat=len(mats), **kw)
+    for i, m in enumerate(mats):
+        api.set_material(c, i, *m)
+    return c
+
+
+def _steps(mats_used, d, total_time, factor=0.9):
+    amax = max(m[4] / (m[5] * m[6]) for m in mats_used)
+    dt = factor / (2.0 * amax * 3.0 / (d * d))
+    return int(math.ceil(total_time / dt))
+
+
+def homogeneous(edge, packets, power, seconds, precision=1):
+    """C1 (edge 100, 1e6 packets, 1 W, 1 s) and C2 (edge 200, 1e8, 2 W, 2 s)."""
+    p = api.default_params(nxg=edge, nyg=edge, nzg=edge, xmax=0.5, ymax=0.5, zmax=0.5, mode=1, precision=precision,
+                           nphotons=packets, pulse_type=1, power=power, energy_per_pixel=power * seconds * 1e3,
+                           total_time=seconds, loops=1)
+    c = _config([AIR, TISSUE])
+    return Workload(f"homogeneous {edge}^3", p, c, None, packets, _steps([TISSUE], 1e-2 / edge, seconds))
+
+
+def c1():
+    return homogeneous(100, 1_000_000, 1.0, 1.0, precision=0)
+
+
+def c2():
+    return homogeneous(200, 100_000_000, 2.0, 2.0, precision=1)
+
+
+def c3(scale=1.0, packets=100_000_000, steps=20_000):
+    """Three-layer skin slab; `scale` shrinks the grid (same physical size)."""
+    nx = ny = max(8, int(round(256 * scale)))
+    nz = max(8, int(round(128 * scale)))
+    dz = 0.5 / nz  # cm
+    grid = np.full((nx, ny, nz), 3, dtype=np.uint8, order="F")  # subcutis
+    ztop = lambda depth: nz - int(round(depth / dz))  # first z index below `depth` from the top face
+    grid[:, :, ztop(0.21):] = 2   # dermis 0.01 .. 0.21 cm
+    grid[:, :, ztop(0.01):] = 1   # epidermis, top 0.01 cm (at least one plane)
+    grid[:, :, nz - 1] = 1
+    mats = [AIR, EPIDERMIS, DERMIS, SUBCUTIS]
+    dt_steps = steps
+    p = api.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=0.5, ymax=0.5, zmax=0.25, mode=1, precision=1,
+                           nphotons=packets, pulse_type=1, power=5.0, energy_per_pixel=5.0 * 1e3, total_time=1.0,
+                           loops=1)
+    c = _config(mats, retrace_fraction=1e-3, retrace_check=50)
+    return Workload("C3 three-layer skin slab", p, c, grid, packets, dt_steps,
+                    {"grid": (nx, ny, nz), "layers_cm": (0.01, 0.2, 0.29)})
+
+
+def c4_instances(n=64, seed=4, packets=10_000_000, steps=5_000, edge_range=(64, 192)):
+    """Per-instance parameters of the batched form, from a seeded Philox stream."""
+    rng = np.random.Generator(np.random.Philox(seed))
+    out = []
+    for i in range(n):
+        nx, ny, nz = (int(v) for v in rng.integers(edge_range[0], edge_range[1] + 1, size=3))
+        mua = float(math.exp(rng.uniform(math.log(0.05), math.log(5.0))))
+        mus = float(math.exp(rng.uniform(math.log(20.0), math.log(300.0))))
+        g = float(rng.uniform(0.7, 0.95))
+        power = float(rng.uniform(0.5, 5.0))
+        radius = float(rng.uniform(0.05, 0.3))
+        out.append(dict(edges=(nx, ny, nz), mua=mua, mus=mus, g=g, power=power, radius=radius, packets=packets,
+                        steps=steps))
+    return out
+
+
+def c4(n=64, seed=4, packets=10_000_000, steps=5_000, edge_range=(64, 192), precision=1):
+    """Workloads of the batched form (50 um voxels, so the cube edge follows the grid)."""
+    ws = []
+    for k, q in enumerate(c4_instances(n, seed, packets, steps, edge_range)):
+        nx, ny, nz = q["edges"]
+        h = 0.005  # cm
+        mat = (q["mua"], q["mus"], q["g"], 1.38, 0.56, 1070.0, 3400.0)
+        p = api.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=nx * h / 2, ymax=ny * h / 2, zmax=nz * h / 2, mode=1,
+                               precision=precision, nphotons=packets, pulse_type=1, power=q["power"],
+                               energy_per_pixel=q["power"] * 1e3, total_time=1.0, loops=1)
+        c = _config([AIR, mat], source_radius=q["radius"], retrace_fraction=0.0)
+        ws.append(Workload(f"C4 instance {k}", p, c, None, packets, steps, q))
+    return ws
+
+
+def c5(scale=1.0, seed=5, packets=1_000_000_000, steps=100_000):
+    """Large heterogeneous instance: dermis, 20 vessels, 5 inclusions; `scale` shrinks the grid."""
+    n = max(16, int(round(512 * scale)))
+    L = 2.0  # cm
+    h = L / n
+    rng = np.random.Generator(np.random.Philox(seed))
+    cyl = []
+    for _ in range(20):
+        v = rng.normal(size=3)
+        v /= np.linalg.norm(v)
+        cyl.append((rng.uniform(0.0, L, size=3), v, float(rng.uniform(0.01, 0.05))))
+    sph = [(rng.uniform(0.1, L - 0.1, size=3), 0.1) for _ in range(5)]
+    grid = np.ones((n, n, n), dtype=np.uint8, order="F")  # dermis
+    c = (np.arange(n) + 0.5) * h
+    X, Y = np.meshgrid(c, c, indexing="ij")
+    for k in range(n):
+        z = c[k]
+        sl = grid[:, :, k]
+        for p0, v, r in cyl:
+            dx, dy, dz = X - p0[0], Y - p0[1], z - p0[2]
+            t = dx * v[0] + dy * v[1] + dz * v[2]
+            d2 = dx * dx + dy * dy + dz * dz - t * t
+            sl[d2 <= r * r] = 2
+        for p0, r in sph:
+            d2 = (X - p0[0]) ** 2 + (Y - p0[1]) ** 2 + (z - p0[2]) ** 2
+            sl[d2 <= r * r] = 3
+    mats = [AIR, DERMIS, BLOOD, INCLUSION]
+    p = api.default_params(nxg=n, nyg=n, nzg=n, xmax=L / 2, ymax=L / 2, zmax=L / 2, mode=1, precision=1,
+                           nphotons=packets, pulse_type=1, power=10.0, energy_per_pixel=10.0 * 50.0,
+                           repetition_rate_1=1.0, pulses_to_do=10, total_time=10.0, loops=1)
+    cfg = _config(mats, retrace_fraction=1e-9, retrace_check=0)
+    return Workload("C5 vessels and inclusions", p, cfg, grid, packets, steps,
+                    {"grid": (n, n, n), "cylinders": len(cyl), "spheres": len(sph)})
