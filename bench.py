@@ -169,7 +169,7 @@ def run_gpu(args):
     ev0 = torch.cuda.Event(enable_timing=True)
     ev1 = torch.cuda.Event(enable_timing=True)
     l0 = tam.kernel_launches()
-    t_tr, t_heat, vsteps = [], [], []
+    t_tr, t_heat, vsteps, scats = [], [], [], []
     with Clocks(local) as clk:
         torch.cuda.synchronize()
         ev0.record(stream)
@@ -178,7 +178,9 @@ def run_gpu(args):
             tr, hm, _ = ctx.timing()
             t_tr.append(tr)
             t_heat.append(hm)
-            vsteps.append(ctx.tallies()["voxel_steps"])
+            tl = ctx.tallies()
+            vsteps.append(tl["voxel_steps"])
+            scats.append(tl["scatters"])
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = tam.kernel_launches() - l0
@@ -191,7 +193,9 @@ def run_gpu(args):
     tr_ms = statistics.mean(t_tr)
     heat_ms = statistics.mean(t_heat)
     vs = statistics.mean(vsteps)
+    nsc = statistics.mean(scats)
     hbm, peak_kind = peaks()
+    red_peak = red_f64_peak(torch, local)
 
     # ---- end to end through the C ABI with pinned host buffers ----
     mat_h = torch.ones((nvox,), dtype=torch.uint8).pin_memory().numpy()
@@ -321,6 +325,15 @@ def run_gpu(args):
             "voxel_steps_per_packet": vs / packets,
             "voxel_steps_per_s": world * vs / (tr_ms * 1e-3),
             "kernel_ms": tr_ms,
+            # one red.global.add.f64 per voxel step that ends on a face (the
+            # steps that end at an interaction carry their deposit onward)
+            "l2_atomics": {
+                "achieved_per_s": world * (vs - nsc) / (tr_ms * 1e-3),
+                "peak_per_s": red_peak,
+                "frac": (vs - nsc) / (tr_ms * 1e-3) / red_peak if red_peak else None,
+                "peak_kind": "measured: torch index_add_ of FP64 at random cells of a 64 MB array (L2-resident), "
+                             "the same access pattern as the tally",
+            },
         },
         "heat": {"ms_per_step_segment": heat_ms, "ms_per_heat_step": heat_ms / nsteps},
         "roofline": {
@@ -363,6 +376,25 @@ def run_gpu(args):
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def red_f64_peak(torch, device, cells=GRID ** 3, ops=1 << 26):
+    """FP64 atomic adds per second at random cells of an L2-resident array."""
+    g = torch.Generator(device=f"cuda:{device}")
+    g.manual_seed(7)
+    idx = torch.randint(0, cells, (ops,), device=f"cuda:{device}", generator=g)
+    val = torch.rand((ops,), device=f"cuda:{device}", dtype=torch.float64, generator=g)
+    acc = torch.zeros((cells,), device=f"cuda:{device}", dtype=torch.float64)
+    best = None
+    for _ in range(4):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        acc.index_add_(0, idx, val)
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        best = ms if best is None else min(best, ms)
+    return ops / (best * 1e-3)
 
 
 def profile_traffic(voxel_steps):

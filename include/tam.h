@@ -252,6 +252,7 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * "heat.cls" (1: while the thermal properties are those of the material
  * classes, look the face coefficients up per class pair instead of reading
  * per-voxel coefficient arrays; 0: always read the arrays),
+ * "heat.cls_rows" (voxel rows per thread of the class-table step, 1 or 2),
  * "heat.arrhenius_fp64" (FP32 form: 1 evaluates the Arrhenius exponent
  * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits). */
 int tam_set_tuning(struct tam_ctx *ctx, const char *key, int64_t value);
@@ -269,7 +270,24 @@ int tam_set_tuning(struct tam_ctx *ctx, const char *key, int64_t value);
  * message too).
  */
 int tam_batch_step_coupled(struct tam_ctx *const *ctxs, int32_t n, int32_t iters, const uint64_t *seeds);
+/* nsteps heat steps of every instance in persistent launches that each
+ * advance all instances by a chunk of steps (FP32 config-mode contexts on one
+ * device whose thermal properties are those of their material classes;
+ * TAM_E_STATE otherwise).  tam_batch_step_coupled and tam_batch_run use the
+ * same batched heat step whenever every context qualifies; MC passes and
+ * re-trace decisions then happen at chunk boundaries. */
+int tam_batch_heat_steps(struct tam_ctx *const *ctxs, int32_t n, int32_t nsteps);
 int tam_batch_run(struct tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, int64_t max_iters, int64_t *iters);
+
+/*
+ * Autotuner (no reference counterpart).  Config mode: times the context's own
+ * workload under candidate settings of "transport.scat_min" (an MC pass of
+ * `packets`) and of "heat.zchunk" / "heat.cls_rows" (`steps` heat steps),
+ * keeps the fastest and puts the context's state back as it was (fields,
+ * clock, pulse state, tallies).  0 packets or 0 steps skips that part.
+ * chosen (nullable) receives up to nchosen values: scat_min, zchunk, cls_rows.
+ */
+int tam_autotune(struct tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, int32_t nchosen);
 
 /* Kernels this library has launched in this process (all contexts). */
 int64_t tam_kernel_launches(void);

@@ -58,3 +58,70 @@ def test_batch_run_counts_and_rejects_duplicates(tam):
     finally:
         for c in ctxs:
             c.close()
+
+
+# ------------------------------------------- device-batched FP32 heat steps --
+def _fp32_instance(tam, nx, ny, nz, layered, power):
+    half = 0.0025 * nx  # cm: 50 um voxels
+    p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half * ny / nx, zmax=half * nz / nx, mode=1,
+                           precision=1, nphotons=20000, pulse_type=1, power=power, energy_per_pixel=power * 1e3,
+                           total_time=1.0, loops=1)
+    mats = [(0.0, 0.0, 0.0, 1.0, 0.026, 1.2, 1005.0), (0.3, 100.0, 0.9, 1.38, 0.56, 1070.0, 3400.0),
+            (1.0, 200.0, 0.8, 1.4, 0.21, 1200.0, 3590.0)]
+    c = tam.default_config(nmat=3, retrace_fraction=0.0, source_radius=0.05)
+    for i, m in enumerate(mats):
+        tam.set_material(c, i, *m)
+    ctx = tam.Context(p, c)
+    if layered:
+        g = np.ones((nx, ny, nz), dtype=np.uint8, order="F")
+        g[:, :, nz - 3:] = 2
+        g[nx // 3: nx // 2, :, : nz // 2] = 2
+        ctx.upload(tam._abi.TAM_F_MATERIAL, g)
+    rng = np.random.default_rng(nx * 1000 + ny)
+    ctx.upload(tam._abi.TAM_F_JMEAN_GLOBAL, np.asfortranarray(rng.uniform(0, 1, (nx, ny, nz)) ** 2 * 4e8))
+    return ctx
+
+
+SHAPES = [(37, 29, 23, True, 1.0), (48, 40, 36, False, 2.0), (64, 20, 18, True, 3.0)]
+
+
+def test_batch_heat_steps_matches_single_contexts(tam):
+    F = tam._abi
+    want = []
+    for shp in SHAPES:
+        with _fp32_instance(tam, *shp) as ctx:
+            ctx.heat_steps(150)
+            want.append((ctx.download(F.TAM_F_TEMP), ctx.download(F.TAM_F_TISSUE), ctx.state().time))
+    ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
+    try:
+        tam.batch_heat_steps(ctxs, 150)
+        for ctx, (T, om, t) in zip(ctxs, want):
+            assert ctx.device_errors() == 0
+            got_T = ctx.download(F.TAM_F_TEMP)
+            assert (T - 310.15).max() > 1.0
+            assert np.abs(got_T - T).max() <= 1e-4
+            assert np.abs(ctx.download(F.TAM_F_TISSUE) - om).max() <= 1e-4 * max(om.max(), 1e-30)
+            assert ctx.state().time == pytest.approx(t, rel=1e-12)
+    finally:
+        for c in ctxs:
+            c.close()
+
+
+def test_batch_coupled_fp32_matches_single_runs(tam):
+    F = tam._abi
+    seeds = [5, 6, 7]
+    want = []
+    for shp, sd in zip(SHAPES, seeds):
+        with _fp32_instance(tam, *shp) as ctx:
+            ctx.step_coupled(40, seed=sd)
+            want.append(ctx.download(F.TAM_F_TEMP))
+    ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
+    try:
+        tam.batch_step_coupled(ctxs, 40, seeds)
+        for ctx, T in zip(ctxs, want):
+            assert np.abs(ctx.download(F.TAM_F_TEMP) - T).max() <= 1e-4
+        its = tam.batch_run(ctxs, seeds, max_iters=45)
+        assert its == [45, 45, 45]
+    finally:
+        for c in ctxs:
+            c.close()

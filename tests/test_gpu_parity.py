@@ -390,7 +390,7 @@ def test_writer_files(tam, orc, tmp_path):
 
 
 # ------------------------------------------- class-table fused heat step --
-def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats):
+def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats, rows=2):
     half = 0.0025 * nx  # cm: 50 um voxels
     p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half * ny / nx, zmax=half * nz / nx, mode=1,
                            precision=precision, pulse_type=1, power=1.0, energy_per_pixel=1e6, total_time=10.0)
@@ -399,6 +399,7 @@ def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats):
         tam.set_material(c, i, 0.3, 10.0, 0.9, 1.4, k, rho, cp)
     ctx = tam.Context(p, c)
     ctx.set_tuning("heat.cls", cls)
+    ctx.set_tuning("heat.cls_rows", rows)
     ctx.upload(F.TAM_F_MATERIAL, grid)
     ctx.upload(F.TAM_F_JMEAN_GLOBAL, J)
     return ctx
@@ -422,8 +423,8 @@ def test_fused_class_table_matches_coefficient_arrays(tam, nx):
     alpha = max(k / (r * c) for k, r, c in mats[1:])
     dt = 0.9 / (2 * alpha * 3 / d ** 2)
     out = {}
-    for name, prec, cls in (("cls", 1, 1), ("arr", 1, 0), ("f64", 0, 1)):
-        ctx = _layered_heat_ctx(tam, nx, ny, nz, prec, cls, dt, J, grid, mats)
+    for name, prec, cls, rows in (("cls", 1, 1, 2), ("cls1", 1, 1, 1), ("arr", 1, 0, 1), ("f64", 0, 1, 1)):
+        ctx = _layered_heat_ctx(tam, nx, ny, nz, prec, cls, dt, J, grid, mats, rows)
         T = ctx.heat_steps(300, want=True)
         out[name] = (T, ctx.download(F.TAM_F_TISSUE), ctx.device_errors())
         ctx.close()
@@ -431,6 +432,7 @@ def test_fused_class_table_matches_coefficient_arrays(tam, nx):
     assert rise > 5.0, rise
     assert out["cls"][2] == 0 and out["arr"][2] == 0
     assert np.abs(out["cls"][0] - out["arr"][0]).max() <= 1e-4
+    assert np.abs(out["cls1"][0] - out["cls"][0]).max() <= 1e-5
     assert np.abs(out["cls"][0] - out["f64"][0]).max() <= 1e-3
 
 

@@ -423,8 +423,8 @@ __global__ void __launch_bounds__(FX *FY, KAHAN ? 4 : 2) fused_kernel(const Fuse
             if (!(Ts == Ts)) errbits |= DEVERR_NAN;
             else if (Ts < (Real)0) errbits |= DEVERR_NEG_T;
             if (Ts >= cst<Real>(a, FC_SCREEN)) {
-                if constexpr (sizeof(Real) == 4) rare_update_f32(a, v, ni, Tn, (float)En);
-                else rare_update<Real>(a, v, ni, (double)Tn - (double)En);
+                if constexpr (sizeof(Real) == 4) rare_update_f32(a, v, ni, Tn, (float)En, a.t_new);
+                else rare_update<Real>(a, v, ni, (double)Tn - (double)En, a.t_new);
             }
         }
         prv = cur;
@@ -467,6 +467,9 @@ void fill_fused_consts(FusedArgs &a)
     for (int i = 0; i < FC_N; ++i) a.fc[i] = (float)d[i];
     a.fc[FC_LNA_LO] = (float)(d[FC_LNA_HI] - (double)a.fc[FC_LNA_HI]);
     a.fc[FC_EAR_LO] = (float)(d[FC_EAR_HI] - (double)a.fc[FC_EAR_HI]);
+    a.fc[FC_TLO_LO] = (float)(d[FC_TLO] - (double)a.fc[FC_TLO]);
+    a.fc[FC_THI_LO] = (float)(d[FC_THI] - (double)a.fc[FC_THI]);
+    a.fc[FC_TABL_LO] = (float)(d[FC_TABL] - (double)a.fc[FC_TABL]);
 }
 
 namespace {

@@ -8,7 +8,7 @@
 namespace tam {
 namespace {
 
-constexpr int FX = 32, FY = 8;
+constexpr int FX = FX_TILE, FY = FY_TILE;
 
 template <typename Real> struct Pt {
     Real T, e, k, r, h;  // temperature, Kahan compensation (true T = T - e), k, rho, c
@@ -61,7 +61,8 @@ __device__ __noinline__ Real ghost_term(const FusedArgs &a, int f, Real T, Real 
 // every crossed threshold stamped) and ablation of the optics for one voxel
 // whose new true temperature is Tt.  Kept out of line so that no FP64 work is
 // scheduled for the voxels that never reach it.
-template <typename Real> __device__ __noinline__ void rare_update(const FusedArgs &a, int64_t v, int64_t ni, double Tt)
+template <typename Real>
+__device__ __noinline__ void rare_update(const FusedArgs &a, int64_t v, int64_t ni, double Tt, double t_new)
 {
     if (a.arrhenius && Tt >= a.T_lo && Tt < a.T_hi) {
         const double o = a.omega[v];
@@ -69,7 +70,7 @@ template <typename Real> __device__ __noinline__ void rare_update(const FusedArg
         a.omega[v] = on;
 #pragma unroll
         for (int t = 0; t < 3; ++t)
-            if (o < a.thr[t] && on >= a.thr[t]) a.thres[v + t * ni] = a.t_new;
+            if (o < a.thr[t] && on >= a.thr[t]) a.thres[v + t * ni] = t_new;
     }
     if (Tt >= a.T_abl && a.mat[v] != 0) {
         a.mat[v] = 0;  // optics -> air
@@ -77,6 +78,11 @@ template <typename Real> __device__ __noinline__ void rare_update(const FusedArg
         atomicAdd(a.n_ablated, 1ull);
     }
 }
+
+// (T - e) >= hi + lo for a double threshold split into floats (hi, lo),
+// decided as the FP64 comparison of the exact T - e decides it: near the
+// threshold T - hi is exact (Sterbenz), so only an error of ~1e-12 K remains.
+__device__ __forceinline__ bool ge_ff(float T, float e, float hi, float lo) { return (T - hi) - (e + lo) >= 0.f; }
 
 // FP32 form of rare_update from the Kahan pair (T, e), true temperature T - e.
 // The exponent ln A - (Ea/R)/(T - e) is a difference of two numbers near 200
@@ -88,14 +94,14 @@ template <typename Real> __device__ __noinline__ void rare_update(const FusedArg
 // compare the non-negative doubles by their bit patterns, which order the same
 // way.  Exponents beyond expf's range take the FP64 path, and so does every
 // voxel when arr_fp64 is set (FP64 exponent ln A - Ea/RT of T - e).
-__device__ __noinline__ void rare_update_f32(const FusedArgs &a, int64_t v, int64_t ni, float T, float e)
+__device__ __noinline__ void rare_update_f32(const FusedArgs &a, int64_t v, int64_t ni, float T, float e,
+                                            double t_new)
 {
     if (a.arr_fp64) {
-        rare_update<float>(a, v, ni, (double)T - (double)e);
+        rare_update<float>(a, v, ni, (double)T - (double)e, t_new);
         return;
     }
-    const float Tt = T - e;
-    if (a.arrhenius && Tt >= a.fc[FC_TLO] && Tt < a.fc[FC_THI]) {
+    if (a.arrhenius && ge_ff(T, e, a.fc[FC_TLO], a.fc[FC_TLO_LO]) && !ge_ff(T, e, a.fc[FC_THI], a.fc[FC_THI_LO])) {
         const float ear = a.fc[FC_EAR_HI], lna = a.fc[FC_LNA_HI];
         const float yh = __fdiv_rn(ear, T);
         // (Ea/R) - yh (T - e) = [ear - yh T] + ear_lo + yh e; the bracket is exact
@@ -118,10 +124,10 @@ __device__ __noinline__ void rare_update_f32(const FusedArgs &a, int64_t v, int6
 #pragma unroll
         for (int t = 0; t < 3; ++t) {
             const long long tb = __double_as_longlong(a.thr[t]);
-            if (ob < tb && nb >= tb) a.thres[v + t * ni] = a.t_new;
+            if (ob < tb && nb >= tb) a.thres[v + t * ni] = t_new;
         }
     }
-    if (Tt >= a.fc[FC_TABL] && a.mat[v] != 0) {
+    if (ge_ff(T, e, a.fc[FC_TABL], a.fc[FC_TABL_LO]) && a.mat[v] != 0) {
         a.mat[v] = 0;  // optics -> air
         ((float *)a.J)[v] = 0.f;
         atomicAdd(a.n_ablated, 1ull);

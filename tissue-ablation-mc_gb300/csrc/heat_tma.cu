@@ -23,8 +23,8 @@ namespace tam {
 struct FusedTma {
     CUtensorMap T[2], E[2], ax, ay, az, irc, J;
 };
-struct FusedCls {
-    CUtensorMap T[2], E[2], J, cls;
+struct FusedCls {  // tensor maps for 1 and 2 rows of voxels per thread
+    CUtensorMap T[2][2], E[2][2], J[2], cls[2];
 };
 
 namespace {
@@ -240,7 +240,7 @@ __global__ void __launch_bounds__(FX *FY, 4)
             const float Ts = Tnew - Enew;
             if (!(Ts == Ts)) errbits |= DEVERR_NAN;
             else if (Ts < 0.f) errbits |= DEVERR_NEG_T;
-            if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew);
+            if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew, a.t_new);
         }
         __syncthreads();  // every thread is done with the stage the next issue overwrites
         Tp = Tc;
@@ -269,12 +269,18 @@ __global__ void __launch_bounds__(FX *FY, 4)
 // 28 + 8.  A uniform grid (one class everywhere) stages no class ids at all.
 constexpr int CTS = 6;                          // stages of the class-table ring
 constexpr int CPITCH = 64;                      // class row: x from bx*32 - 16, 64 bytes
-constexpr int CLS_BYTES = TROWS * CPITCH;       // 640
 
-template <bool UNIFORM> struct ClsLayout {
-    static constexpr int T_OFF = 0, E_OFF = ARR_BYTES, J_OFF = 2 * ARR_BYTES, C_OFF = 2 * ARR_BYTES + OWN_BYTES;
-    static constexpr int STAGE = ((C_OFF + (UNIFORM ? 0 : CLS_BYTES) + 127) / 128) * 128;
-    static constexpr uint32_t TX = 2u * TROWS * TPITCH * 4 + FY * FX * 4 + (UNIFORM ? 0u : (uint32_t)CLS_BYTES);
+// Stage layout of the class-table ring for RY rows of voxels per thread (the
+// block covers 32 x 8*RY voxels per plane).
+template <bool UNIFORM, int RY> struct ClsLayout {
+    static constexpr int ROWS = FY * RY + 2;                                  // staged rows with halo
+    static constexpr int TE_BYTES = ((ROWS * TPITCH * 4 + 127) / 128) * 128;  // T or Kahan term
+    static constexpr int J_BYTES = FY * RY * FX * 4;                          // own voxels only
+    static constexpr int C_BYTES = ((ROWS * CPITCH + 127) / 128) * 128;       // class ids with halo
+    static constexpr int T_OFF = 0, E_OFF = TE_BYTES, J_OFF = 2 * TE_BYTES, C_OFF = 2 * TE_BYTES + J_BYTES;
+    static constexpr int STAGE = ((C_OFF + (UNIFORM ? 0 : C_BYTES) + 127) / 128) * 128;
+    static constexpr uint32_t TX =
+        2u * ROWS * TPITCH * 4 + (uint32_t)J_BYTES + (UNIFORM ? 0u : (uint32_t)(ROWS * CPITCH));
     static constexpr int SMEM = CTS * STAGE + CTS * 8 + 128;
 };
 
@@ -282,19 +288,18 @@ struct ClsMaps {  // the maps of one launch
     CUtensorMap T, E, J, cls;
 };
 
-template <bool UNIFORM>
-__global__ void __launch_bounds__(FX *FY, 4)
+template <bool UNIFORM, int RY>
+__global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
     fused_cls_kernel(const __grid_constant__ FusedArgs a, const __grid_constant__ ClsMaps m,
                      const __grid_constant__ ClassLut L, int zchunk)
 {
-    using Lay = ClsLayout<UNIFORM>;
+    using Lay = ClsLayout<UNIFORM, RY>;
     extern __shared__ unsigned char smem_raw[];
     __shared__ float s_fa[MAX_MAT * MAX_MAT];
     unsigned char *sm = smem_raw + ((128 - (su32(smem_raw) & 127)) & 127);
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + CTS * Lay::STAGE);
     const int tx = threadIdx.x, ty = threadIdx.y;
-    const int x = blockIdx.x * FX + tx, y = blockIdx.y * FY + ty;
-    const bool in = x < a.nx && y < a.ny;
+    const int x = blockIdx.x * FX + tx, ybase = blockIdx.y * FY * RY + ty;
     const int z0 = blockIdx.z * zchunk;
     const int z1 = min(a.nz, z0 + zchunk);
     const int nplanes = z1 - z0;
@@ -305,9 +310,8 @@ __global__ void __launch_bounds__(FX *FY, 4)
     const float dt = a.fc[FC_DT], Pdt = a.fc[FC_PDT];
     const float cx = a.fc[FC_CX], cy = a.fc[FC_CY], cz = a.fc[FC_CZ];
     const bool src_on = Pdt != 0.f;
-    const bool xy_inner = x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1;
     const bool leader = tx == 0 && ty == 0;
-    const int gx = blockIdx.x * FX - 4, gy = blockIdx.y * FY - 1, gx8 = blockIdx.x * FX - 16;
+    const int gx = blockIdx.x * FX - 4, gy = blockIdx.y * FY * RY - 1, gx8 = blockIdx.x * FX - 16;
     const int uc = L.uniform >= 0 ? L.uniform : 0;
     const float au = L.fa[uc * MAX_MAT + uc];
     const float Cx = cx * au, Cy = cy * au, Cz = cz * au;
@@ -340,26 +344,30 @@ __global__ void __launch_bounds__(FX *FY, 4)
         for (int idx = 0; idx <= CTS - 2 && idx <= last; ++idx) issue(idx);
     issued = (CTS - 1 < last + 1) ? CTS - 1 : last + 1;
     bool ok = __syncthreads_and(wait(0) && wait(1)) != 0;
-    const int q = (ty + 1) * TPITCH + tx + 4;   // own voxel in the T / E rows
-    const int o = ty * FX + tx;                 // own voxel in J
-    const int qc = (ty + 1) * CPITCH + tx + 16; // own voxel in the class rows
-    float Tp = 0.f, ep = 0.f, Tc = 0.f, ec = 0.f;
-    int kp = 0, kc = 0;  // classes of the planes below and at z
-    if (in && ok) {
-        const unsigned char *C0 = stage(1);
-        Tc = ((const float *)(C0 + Lay::T_OFF))[q];
-        ec = ((const float *)(C0 + Lay::E_OFF))[q];
-        if (!UNIFORM) kc = (C0 + Lay::C_OFF)[qc] & (MAX_MAT - 1);
-        if (z0 > 0) {
-            const unsigned char *Pm = stage(0);
-            Tp = ((const float *)(Pm + Lay::T_OFF))[q];
-            ep = ((const float *)(Pm + Lay::E_OFF))[q];
-            if (!UNIFORM) kp = (Pm + Lay::C_OFF)[qc] & (MAX_MAT - 1);
+    // z columns of this thread's RY voxels in registers
+    float Tp[RY], ep[RY], Tc[RY], ec[RY];
+    int kp[RY], kc[RY];
+#pragma unroll
+    for (int r = 0; r < RY; ++r) {
+        const int row = ty + r * FY + 1;
+        const int q = row * TPITCH + tx + 4, qc = row * CPITCH + tx + 16;
+        Tp[r] = ep[r] = Tc[r] = ec[r] = 0.f;
+        kp[r] = kc[r] = 0;
+        if (ok) {
+            const unsigned char *C0 = stage(1);
+            Tc[r] = ((const float *)(C0 + Lay::T_OFF))[q];
+            ec[r] = ((const float *)(C0 + Lay::E_OFF))[q];
+            if (!UNIFORM) kc[r] = (C0 + Lay::C_OFF)[qc] & (MAX_MAT - 1);
+            if (z0 > 0) {
+                const unsigned char *Pm = stage(0);
+                Tp[r] = ((const float *)(Pm + Lay::T_OFF))[q];
+                ep[r] = ((const float *)(Pm + Lay::E_OFF))[q];
+                if (!UNIFORM) kp[r] = (Pm + Lay::C_OFF)[qc] & (MAX_MAT - 1);
+            }
         }
     }
     for (int i = 0; i < nplanes && ok; ++i) {
         const int z = z0 + i;
-        const int64_t v = (int64_t)x + sy * y + sz * z;
         const bool has_n = z + 1 < a.nz;
         if (i + CTS - 1 <= last) {
             if (leader) issue(i + CTS - 1);
@@ -369,86 +377,94 @@ __global__ void __launch_bounds__(FX *FY, 4)
         if (!ok) break;
         const unsigned char *P = stage(i + 1), *N = stage(i + 2);
         const float *PT = (const float *)(P + Lay::T_OFF), *PE = (const float *)(P + Lay::E_OFF);
-        float Tn_ = 0.f, en_ = 0.f;
-        int kn = 0;
-        if (in && has_n) {
-            Tn_ = ((const float *)(N + Lay::T_OFF))[q];
-            en_ = ((const float *)(N + Lay::E_OFF))[q];
-            if (!UNIFORM) kn = (N + Lay::C_OFF)[qc] & (MAX_MAT - 1);
-        }
-        if (in) {
-            const int k = UNIFORM ? uc : kc;
-            const float Jv = src_on ? ((const float *)(P + Lay::J_OFF))[o] : 0.f;
-            const float tzm = (Tp - Tc) - (ep - ec), tzp = (Tn_ - Tc) - (en_ - ec);
-            const float txm = (PT[q - 1] - Tc) - (PE[q - 1] - ec), txp = (PT[q + 1] - Tc) - (PE[q + 1] - ec);
-            const float tym = (PT[q - TPITCH] - Tc) - (PE[q - TPITCH] - ec),
-                        typ = (PT[q + TPITCH] - Tc) - (PE[q + TPITCH] - ec);
-            // face coefficients of the six faces (uniform: one value per axis)
-            float axm = Cx, axp = Cx, aym = Cy, ayp = Cy, azm = Cz, azp = Cz;
-            if (!UNIFORM) {
-                const unsigned char *PC = P + Lay::C_OFF;
-                const float *row = s_fa + k * MAX_MAT;
-                axm = cx * row[PC[qc - 1] & (MAX_MAT - 1)];
-                axp = cx * row[PC[qc + 1] & (MAX_MAT - 1)];
-                aym = cy * row[PC[qc - CPITCH] & (MAX_MAT - 1)];
-                ayp = cy * row[PC[qc + CPITCH] & (MAX_MAT - 1)];
-                azm = cz * row[kp];
-                azp = cz * row[kn];
+#pragma unroll
+        for (int r = 0; r < RY; ++r) {
+            const int y = ybase + r * FY;
+            const int row = ty + r * FY + 1;
+            const int q = row * TPITCH + tx + 4, qc = row * CPITCH + tx + 16, o = (ty + r * FY) * FX + tx;
+            float Tn_ = 0.f, en_ = 0.f;
+            int kn = 0;
+            if (has_n) {
+                Tn_ = ((const float *)(N + Lay::T_OFF))[q];
+                en_ = ((const float *)(N + Lay::E_OFF))[q];
+                if (!UNIFORM) kn = (N + Lay::C_OFF)[qc] & (MAX_MAT - 1);
             }
-            float lap;
-            if (xy_inner && z > 0 && has_n) {
-                lap = azm * tzm + azp * tzp + aym * tym + ayp * typ + axm * txm + axp * txp;
-            } else {
-                // a face of this voxel lies on the grid boundary: ghost faces
-                // use the voxel's own properties
-                const float kk = L.k[k], rr = L.rho[k], hh = L.c[k];
-                lap = z > 0 ? azm * tzm : ghost_term<float>(a, 4, Tc, ec, kk, rr, hh);
-                lap += has_n ? azp * tzp : ghost_term<float>(a, 5, Tc, ec, kk, rr, hh);
-                lap += y > 0 ? aym * tym : ghost_term<float>(a, 2, Tc, ec, kk, rr, hh);
-                lap += y < a.ny - 1 ? ayp * typ : ghost_term<float>(a, 3, Tc, ec, kk, rr, hh);
-                lap += x > 0 ? axm * txm : ghost_term<float>(a, 0, Tc, ec, kk, rr, hh);
-                lap += x < a.nx - 1 ? axp * txp : ghost_term<float>(a, 1, Tc, ec, kk, rr, hh);
-            }
-            const float dT = dt * lap;
-            const float sPJ = Pdt * Jv;
-            const float src = sPJ * L.irc[k];
-            float Tnew, Enew = 0.f;
-            bool clamped = false;
-            if (a.boil && Tc >= a.fc[FC_TBOIL]) {
-                const float rr = L.rho[k], rc = rr * L.c[k];
-                const float qv = a.fc[FC_LW] * rr * a.fc[FC_VVOX];
-                const float Qv = Q[v];
-                if (Qv < qv) {
-                    const float Ein = (sPJ + rc * dT) * a.fc[FC_VVOX];
-                    if (Ein > 0.f) {
-                        const float qn = Qv + Ein;
-                        Q[v] = qn < qv ? qn : qv;
-                        Tnew = a.fc[FC_TBOIL];
-                        clamped = true;
+            if (x < a.nx && y < a.ny) {
+                const float tc = Tc[r], e0 = ec[r];
+                const int k = UNIFORM ? uc : kc[r];
+                const int64_t v = (int64_t)x + sy * y + sz * z;
+                const float Jv = src_on ? ((const float *)(P + Lay::J_OFF))[o] : 0.f;
+                const float tzm = (Tp[r] - tc) - (ep[r] - e0), tzp = (Tn_ - tc) - (en_ - e0);
+                const float txm = (PT[q - 1] - tc) - (PE[q - 1] - e0), txp = (PT[q + 1] - tc) - (PE[q + 1] - e0);
+                const float tym = (PT[q - TPITCH] - tc) - (PE[q - TPITCH] - e0),
+                            typ = (PT[q + TPITCH] - tc) - (PE[q + TPITCH] - e0);
+                // face coefficients of the six faces (uniform: one value per axis)
+                float axm = Cx, axp = Cx, aym = Cy, ayp = Cy, azm = Cz, azp = Cz;
+                if (!UNIFORM) {
+                    const unsigned char *PC = P + Lay::C_OFF;
+                    const float *frow = s_fa + k * MAX_MAT;
+                    axm = cx * frow[PC[qc - 1] & (MAX_MAT - 1)];
+                    axp = cx * frow[PC[qc + 1] & (MAX_MAT - 1)];
+                    aym = cy * frow[PC[qc - CPITCH] & (MAX_MAT - 1)];
+                    ayp = cy * frow[PC[qc + CPITCH] & (MAX_MAT - 1)];
+                    azm = cz * frow[kp[r]];
+                    azp = cz * frow[kn];
+                }
+                float lap;
+                if (x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1 && z > 0 && has_n) {
+                    lap = azm * tzm + azp * tzp + aym * tym + ayp * typ + axm * txm + axp * txp;
+                } else {
+                    // a face of this voxel lies on the grid boundary: ghost faces
+                    // use the voxel's own properties
+                    const float kk = L.k[k], rr = L.rho[k], hh = L.c[k];
+                    lap = z > 0 ? azm * tzm : ghost_term<float>(a, 4, tc, e0, kk, rr, hh);
+                    lap += has_n ? azp * tzp : ghost_term<float>(a, 5, tc, e0, kk, rr, hh);
+                    lap += y > 0 ? aym * tym : ghost_term<float>(a, 2, tc, e0, kk, rr, hh);
+                    lap += y < a.ny - 1 ? ayp * typ : ghost_term<float>(a, 3, tc, e0, kk, rr, hh);
+                    lap += x > 0 ? axm * txm : ghost_term<float>(a, 0, tc, e0, kk, rr, hh);
+                    lap += x < a.nx - 1 ? axp * txp : ghost_term<float>(a, 1, tc, e0, kk, rr, hh);
+                }
+                const float dT = dt * lap;
+                const float sPJ = Pdt * Jv;
+                const float src = sPJ * L.irc[k];
+                float Tnew, Enew = 0.f;
+                bool clamped = false;
+                if (a.boil && tc >= a.fc[FC_TBOIL]) {
+                    const float rr = L.rho[k], rc = rr * L.c[k];
+                    const float qv = a.fc[FC_LW] * rr * a.fc[FC_VVOX];
+                    const float Qv = Q[v];
+                    if (Qv < qv) {
+                        const float Ein = (sPJ + rc * dT) * a.fc[FC_VVOX];
+                        if (Ein > 0.f) {
+                            const float qn = Qv + Ein;
+                            Q[v] = qn < qv ? qn : qv;
+                            Tnew = a.fc[FC_TBOIL];
+                            clamped = true;
+                        }
                     }
                 }
+                if (!clamped) {
+                    const float inc = dT + src;
+                    const float yk = inc - e0;
+                    const float t = tc + yk;
+                    Enew = (t - tc) - yk;
+                    Tnew = t;
+                }
+                To[v] = Tnew;
+                Eo[v] = Enew;
+                const float Ts = Tnew - Enew;
+                if (!(Ts == Ts)) errbits |= DEVERR_NAN;
+                else if (Ts < 0.f) errbits |= DEVERR_NEG_T;
+                if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew, a.t_new);
             }
-            if (!clamped) {
-                const float inc = dT + src;
-                const float yk = inc - ec;
-                const float t = Tc + yk;
-                Enew = (t - Tc) - yk;
-                Tnew = t;
-            }
-            To[v] = Tnew;
-            Eo[v] = Enew;
-            const float Ts = Tnew - Enew;
-            if (!(Ts == Ts)) errbits |= DEVERR_NAN;
-            else if (Ts < 0.f) errbits |= DEVERR_NEG_T;
-            if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew);
+            Tp[r] = Tc[r];
+            ep[r] = ec[r];
+            Tc[r] = Tn_;
+            ec[r] = en_;
+            kp[r] = kc[r];
+            kc[r] = kn;
         }
         __syncthreads();  // every thread is done with the stage the next issue overwrites
-        Tp = Tc;
-        ep = ec;
-        Tc = Tn_;
-        ec = en_;
-        kp = kc;
-        kc = kn;
     }
     if (!ok) {
         errbits |= DEVERR_SYNC_TIMEOUT;
@@ -609,12 +625,15 @@ cudaError_t fused_cls_create(FusedCls **out, int nx, int ny, int nz, float *cons
     cudaError_t e = encoder();
     if (e != cudaSuccess) return e;
     FusedCls *m = new FusedCls();
-    for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
-        e = encode(&m->T[b], T[b], nx, ny, nz, TPITCH, TROWS);
-        if (e == cudaSuccess) e = encode(&m->E[b], Tc[b], nx, ny, nz, TPITCH, TROWS);
+    for (int ry = 1; ry <= 2 && e == cudaSuccess; ++ry) {
+        const int rows = FY * ry + 2;
+        for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
+            e = encode(&m->T[ry - 1][b], T[b], nx, ny, nz, TPITCH, rows);
+            if (e == cudaSuccess) e = encode(&m->E[ry - 1][b], Tc[b], nx, ny, nz, TPITCH, rows);
+        }
+        if (e == cudaSuccess) e = encode(&m->J[ry - 1], J, nx, ny, nz, FX, FY * ry);
+        if (e == cudaSuccess) e = encode_u8(&m->cls[ry - 1], cls, pitch, ny, nz, CPITCH, rows);
     }
-    if (e == cudaSuccess) e = encode(&m->J, J, nx, ny, nz, FX, FY);
-    if (e == cudaSuccess) e = encode_u8(&m->cls, cls, pitch, ny, nz, CPITCH, TROWS);
     if (e != cudaSuccess) {
         delete m;
         return e;
@@ -626,10 +645,10 @@ cudaError_t fused_cls_create(FusedCls **out, int nx, int ny, int nz, float *cons
 void fused_cls_destroy(FusedCls *m) { delete m; }
 
 namespace {
-template <bool UNIFORM>
+template <bool UNIFORM, int RY>
 cudaError_t launch_cls_t(const FusedArgs &a, const ClsMaps &m, const ClassLut &L, cudaStream_t s)
 {
-    const int bx = (a.nx + FX - 1) / FX, by = (a.ny + FY - 1) / FY;
+    const int bx = (a.nx + FX - 1) / FX, by = (a.ny + FY * RY - 1) / (FY * RY);
     int zchunk = a.zchunk > 0 ? a.zchunk : 16;
     if (zchunk > a.nz) zchunk = a.nz;
     const int chunks = (a.nz + zchunk - 1) / zchunk;
@@ -639,27 +658,31 @@ cudaError_t launch_cls_t(const FusedArgs &a, const ClsMaps &m, const ClassLut &L
     if (e != cudaSuccess) return e;
     const unsigned long long bit = 1ull << (dev & 63);
     if (!(attr_set.load() & bit)) {
-        e = cudaFuncSetAttribute(fused_cls_kernel<UNIFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 ClsLayout<UNIFORM>::SMEM);
+        e = cudaFuncSetAttribute(fused_cls_kernel<UNIFORM, RY>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 ClsLayout<UNIFORM, RY>::SMEM);
         if (e != cudaSuccess) return e;
         attr_set.fetch_or(bit);
     }
     count_launch();
-    fused_cls_kernel<UNIFORM><<<dim3(bx, by, chunks), dim3(FX, FY), ClsLayout<UNIFORM>::SMEM, s>>>(a, m, L, zchunk);
+    fused_cls_kernel<UNIFORM, RY><<<dim3(bx, by, chunks), dim3(FX, FY), ClsLayout<UNIFORM, RY>::SMEM, s>>>(a, m, L,
+                                                                                                     zchunk);
     return cudaGetLastError();
 }
 }  // namespace
 
-cudaError_t launch_fused_cls(const FusedArgs &a0, const FusedCls *cm, int which, const ClassLut &L, cudaStream_t s)
+cudaError_t launch_fused_cls(const FusedArgs &a0, const FusedCls *cm, int which, const ClassLut &L, int rows,
+                             cudaStream_t s)
 {
     FusedArgs a = a0;
     fill_fused_consts(a);
+    const int ry = rows == 1 ? 1 : 2;
     ClsMaps m;
-    m.T = cm->T[which];
-    m.E = cm->E[which];
-    m.J = cm->J;
-    m.cls = cm->cls;
-    return L.uniform >= 0 ? launch_cls_t<true>(a, m, L, s) : launch_cls_t<false>(a, m, L, s);
+    m.T = cm->T[ry - 1][which];
+    m.E = cm->E[ry - 1][which];
+    m.J = cm->J[ry - 1];
+    m.cls = cm->cls[ry - 1];
+    if (ry == 1) return L.uniform >= 0 ? launch_cls_t<true, 1>(a, m, L, s) : launch_cls_t<false, 1>(a, m, L, s);
+    return L.uniform >= 0 ? launch_cls_t<true, 2>(a, m, L, s) : launch_cls_t<false, 2>(a, m, L, s);
 }
 
 cudaError_t launch_fused_tma(const FusedArgs &a0, const FusedTma *tm, int which, cudaStream_t s)

@@ -91,7 +91,7 @@ struct tam_ctx {
     long long nabl_at_trace = 0;
 
     // tuning knobs
-    int scat_min = 16;
+    int scat_min = 20;
     int zchunk = 0;
     bool use_tma = true;
     tam::FusedTma *tma = nullptr;  // tensor maps of the FP32 fused step
@@ -100,6 +100,7 @@ struct tam_ctx {
     // class-table form of the FP32 fused step: thermal properties by material
     // class (valid until k, rho or c are uploaded per voxel)
     bool use_cls = true;
+    int cls_rows = 1;                // voxel rows per thread of the class-table step (1 measured fastest)
     bool arr_fp64 = false;           // FP32 form: FP64 Arrhenius exponent instead of float-float
     tam::FusedCls *fcls = nullptr;
     uint8_t *d_cls = nullptr;
@@ -663,7 +664,7 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
         a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[1 - ctx->fcur];
         a.P = ctx->laserOn * get_pwr(ctx);
         a.t_new = ctx->time + ctx->cdt;
-        if (cls) CK(tam::launch_fused_cls(a, ctx->fcls, ctx->fcur, ctx->clut, ctx->stream));
+        if (cls) CK(tam::launch_fused_cls(a, ctx->fcls, ctx->fcur, ctx->clut, ctx->cls_rows, ctx->stream));
         else if (ctx->tma && ctx->use_tma) CK(tam::launch_fused_tma(a, ctx->tma, ctx->fcur, ctx->stream));
         else CK(tam::launch_fused_step(a, ctx->fp64, ctx->stream));
         ctx->fcur = 1 - ctx->fcur;
@@ -1003,9 +1004,15 @@ int tam_create(const tam_params *p, const tam_config *cfg, tam_ctx **out)
             (void)cudaGetLastError();
             ctx->tma = nullptr;  // the cp.async form runs instead
         }
+    }
+    if (ctx->config && !ctx->fp64) {
+        // class grid of the class-table step (TMA form) and of the batched step
         ctx->cls_pitch = tam::cls_pitch_for(ctx->nx);
         if (dalloc_t(ctx, &ctx->d_cls, (int64_t)ctx->cls_pitch * ctx->ny * ctx->nz) != TAM_OK) return bail(TAM_E_NOMEM);
-        if (tam::fused_cls_create(&ctx->fcls, ctx->nx, ctx->ny, ctx->nz, T2, E2, (const float *)ctx->d_J, ctx->d_cls,
+        float *T2[2] = {(float *)ctx->d_Tf[0], (float *)ctx->d_Tf[1]};
+        float *E2[2] = {ctx->d_Tc[0], ctx->d_Tc[1]};
+        if (tam::fused_tma_supported(ctx->nx) &&
+            tam::fused_cls_create(&ctx->fcls, ctx->nx, ctx->ny, ctx->nz, T2, E2, (const float *)ctx->d_J, ctx->d_cls,
                                   ctx->cls_pitch) != cudaSuccess) {
             (void)cudaGetLastError();
             ctx->fcls = nullptr;
@@ -1392,9 +1399,265 @@ template <typename F> int run_batch(tam_ctx *const *ctxs, int32_t n, F &&body)
 }  // namespace
 extern "C" {
 
+}  // extern "C"
+// ---------------------------------------------- device-batched heat steps --
+namespace {
+// Every instance FP32 config mode on one device with thermal properties by
+// class: the heat steps of all of them can run in one persistent launch.
+bool batchable(tam_ctx *const *ctxs, int32_t n)
+{
+    if (n < 1) return false;
+    for (int32_t i = 0; i < n; ++i) {
+        const tam_ctx *c = ctxs[i];
+        if (!c->config || c->fp64 || !c->d_cls || !c->thermal_by_class || !c->use_cls) return false;
+        if (c->device != ctxs[0]->device || c->ni >= ((int64_t)1 << 31)) return false;
+    }
+    return true;
+}
+
+struct DevBatch {
+    tam::BatchInst *d_inst = nullptr;
+    int *d_prefix = nullptr;
+    tam::BatchStep *d_steps = nullptr;
+    tam::BatchSync *d_sync = nullptr;
+    unsigned *d_err = nullptr;
+    std::vector<tam::BatchInst> inst;
+    std::vector<int> prefix;
+    std::vector<tam::BatchStep> steps;
+    int blocks = 0, kmax = 0;
+    ~DevBatch()
+    {
+        cudaFree(d_inst);
+        cudaFree(d_prefix);
+        cudaFree(d_steps);
+        cudaFree(d_sync);
+        cudaFree(d_err);
+    }
+};
+
+constexpr int BATCH_ZCHUNK = 16;
+
+int batch_setup(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int kmax)
+{
+    tam_ctx *const ctx = ctxs[0];  // CUDA errors are reported on the first instance
+    B.inst.resize(n);
+    B.prefix.assign(n + 1, 0);
+    for (int32_t i = 0; i < n; ++i) {
+        tam_ctx *c = ctxs[i];
+        tam::BatchInst &I = B.inst[i];
+        I.a = fused_args(c);
+        tam::fill_fused_consts(I.a);
+        I.L = c->clut;
+        I.cls = c->d_cls;
+        I.cls_pitch = c->cls_pitch;
+        for (int q = 0; q < 2; ++q) {
+            I.T[q] = (float *)c->d_Tf[q];
+            I.E[q] = c->d_Tc[q];
+        }
+        I.tiles_x = (c->nx + tam::FX_TILE - 1) / tam::FX_TILE;
+        I.tiles_y = (c->ny + tam::FY_TILE - 1) / tam::FY_TILE;
+        I.zchunk = c->zchunk > 0 ? c->zchunk : BATCH_ZCHUNK;
+        const int chunks = (c->nz + I.zchunk - 1) / I.zchunk;
+        B.prefix[i + 1] = B.prefix[i] + I.tiles_x * I.tiles_y * chunks;
+    }
+    B.kmax = kmax;
+    B.steps.resize((size_t)kmax * n);
+    CK(tam::batch_heat_blocks(&B.blocks));
+    CK(cudaMalloc(&B.d_inst, sizeof(tam::BatchInst) * n));
+    CK(cudaMalloc(&B.d_prefix, sizeof(int) * (n + 1)));
+    CK(cudaMalloc(&B.d_steps, sizeof(tam::BatchStep) * B.steps.size()));
+    CK(cudaMalloc(&B.d_sync, sizeof(tam::BatchSync)));
+    CK(cudaMalloc(&B.d_err, sizeof(unsigned)));
+    CK(cudaMemset(B.d_err, 0, sizeof(unsigned)));
+    CK(cudaMemcpy(B.d_prefix, B.prefix.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+    return TAM_OK;
+}
+
+// K steps of every instance with active[i] set (each advancing its own pulse
+// state and clock as cfg_heat does); re-trace checks at the end of the chunk.
+int batch_heat_chunk(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int K, const std::vector<int> &active)
+{
+    tam_ctx *const ctx = ctxs[0];
+    cudaStream_t s = ctxs[0]->stream;
+    std::vector<int> turned_on(n, 0);
+    for (int32_t i = 0; i < n; ++i) {
+        tam_ctx *c = ctxs[i];
+        B.inst[i].fcur = c->fcur;
+        for (int k = 0; k < K; ++k) {
+            tam::BatchStep &st = B.steps[(size_t)k * n + i];
+            st.active = active[i];
+            st.pdt = 0.f;
+            st.t_new = 0.0;
+            if (!active[i]) continue;
+            const double P = c->laserOn * get_pwr(c);
+            st.pdt = (float)(P * c->cdt);
+            st.t_new = c->time + c->cdt;
+            if (pulse_update(c, c->cdt)) turned_on[i] = 1;
+        }
+        if (active[i] && (K & 1)) c->fcur = 1 - c->fcur;
+    }
+    // the instances' own streams must have finished what reads or writes their fields
+    for (int32_t i = 0; i < n; ++i)
+        if (ctxs[i]->stream != s) CK(cudaStreamSynchronize(ctxs[i]->stream));
+    CK(cudaMemcpyAsync(B.d_inst, B.inst.data(), sizeof(tam::BatchInst) * n, cudaMemcpyHostToDevice, s));
+    CK(cudaMemcpyAsync(B.d_steps, B.steps.data(), sizeof(tam::BatchStep) * (size_t)K * n, cudaMemcpyHostToDevice, s));
+    CK(tam::launch_batch_heat(B.d_inst, n, B.d_prefix, B.d_steps, K, B.d_sync, B.d_err, B.blocks, s));
+    CK(cudaStreamSynchronize(s));
+    unsigned bits = 0;
+    CK(cudaMemcpy(&bits, B.d_err, sizeof bits, cudaMemcpyDeviceToHost));
+    if (bits) return fail(ctxs[0], TAM_E_DEVICE, "batched heat step: device error word " + std::to_string(bits));
+    for (int32_t i = 0; i < n; ++i) {
+        tam_ctx *c = ctxs[i];
+        if (!active[i] || !(c->cfg.retrace_fraction > 0)) continue;
+        unsigned long long nab = 0;
+        CK(cudaMemcpy(&nab, c->d_nabl, sizeof nab, cudaMemcpyDeviceToHost));
+        const long long fresh = (long long)nab - c->nabl_at_trace;
+        if ((double)fresh > c->cfg.retrace_fraction * (double)c->ni || (turned_on[i] && fresh > 0)) c->need_trace = true;
+    }
+    return TAM_OK;
+}
+
+// Chunk length of the batched loop: the re-trace check interval, else 64.
+int batch_chunk(tam_ctx *const *ctxs, int32_t n)
+{
+    int K = 64;
+    for (int32_t i = 0; i < n; ++i)
+        if (ctxs[i]->cfg.retrace_fraction > 0 && ctxs[i]->cfg.retrace_check > 0)
+            K = std::min(K, (int)ctxs[i]->cfg.retrace_check);
+    return std::max(K, 1);
+}
+
+// MC passes of the instances that need one, back to back on their streams.
+int batch_traces(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, const std::vector<int> &active)
+{
+    for (int32_t i = 0; i < n; ++i) {
+        tam_ctx *c = ctxs[i];
+        if (!active[i] || !c->need_trace) continue;
+        RC(mc_pass(c, c->p.nphotons * (int64_t)c->p.numproc, seeds[i], (uint32_t)c->mc_passes));
+        tam_ctx *const ctx = c;
+        unsigned long long nab = 0;
+        CK(cudaMemcpyAsync(&nab, c->d_nabl, sizeof nab, cudaMemcpyDeviceToHost, c->stream));
+        CK(cudaStreamSynchronize(c->stream));
+        c->nabl_at_trace = (long long)nab;
+        c->need_trace = false;
+    }
+    return TAM_OK;
+}
+}  // namespace
+extern "C" {
+
+int tam_batch_heat_steps(tam_ctx *const *ctxs, int32_t n, int32_t nsteps)
+{
+    if (n < 1 || !ctxs || nsteps < 0) return fail(nullptr, TAM_E_INVALID, "bad batch arguments");
+    for (int32_t i = 0; i < n; ++i)
+        for (int32_t j = 0; j < i; ++j)
+            if (!ctxs[i] || ctxs[j] == ctxs[i]) return fail(nullptr, TAM_E_INVALID, "null or repeated context in batch");
+    if (!batchable(ctxs, n))
+        return fail(nullptr, TAM_E_STATE, "batched heat steps need FP32 config-mode contexts on one device with "
+                                           "thermal properties by material class");
+    tam_ctx *const ctx = ctxs[0];
+    CK(cudaSetDevice(ctx->device));
+    DevBatch B;
+    const int kmax = std::min(batch_chunk(ctxs, n), std::max(nsteps, 1));
+    RC(batch_setup(B, ctxs, n, kmax));
+    std::vector<int> active(n, 1);
+    for (int32_t done = 0; done < nsteps;) {
+        const int K = std::min(kmax, nsteps - done);
+        RC(batch_heat_chunk(B, ctxs, n, K, active));
+        done += K;
+    }
+    for (int32_t i = 0; i < n; ++i) RC(finish(ctxs[i], "tam_batch_heat_steps"));
+    return TAM_OK;
+}
+
+}  // extern "C"
+namespace {
+// Outer loops of all instances with the heat steps batched on the device:
+// per instance, iteration `it` runs while `more(c, it)` holds and is `loops`
+// heat steps preceded by an MC pass when one is due.  Passes and re-trace
+// decisions happen at chunk boundaries (chunks of batch_chunk steps).
+template <typename More>
+int batch_loop_device(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, More &&more, std::vector<int64_t> &its)
+{
+    tam_ctx *const ctx = ctxs[0];
+    CK(cudaSetDevice(ctx->device));
+    DevBatch B;
+    const int K = batch_chunk(ctxs, n);
+    RC(batch_setup(B, ctxs, n, K));
+    std::vector<int> left(n, 0), live(n, 1);
+    its.assign(n, 0);
+    for (;;) {
+        // which instances still run, and which steps of the next chunk they take
+        std::vector<int> act(n, 0);
+        bool any = false;
+        for (int32_t i = 0; i < n; ++i) {
+            if (!live[i]) continue;
+            if (left[i] == 0) {
+                if (!more(ctxs[i], its[i])) {
+                    live[i] = 0;
+                    continue;
+                }
+                ++its[i];
+                left[i] = ctxs[i]->p.loops;
+            }
+            act[i] = 1;
+            any = true;
+        }
+        if (!any) break;
+        RC(batch_traces(ctxs, n, seeds, act));
+        // steps of this chunk: the instance's current iteration, then further
+        // iterations while its loop condition holds (checked step by step)
+        int k = 0;
+        for (; k < K; ++k) {
+            bool stepping = false;
+            for (int32_t i = 0; i < n; ++i) {
+                if (!act[i]) continue;
+                if (left[i] == 0) {
+                    if (ctxs[i]->need_trace || !more(ctxs[i], its[i])) {
+                        act[i] = 0;  // resumes (with its pass, if due) in the next chunk
+                        continue;
+                    }
+                    ++its[i];
+                    left[i] = ctxs[i]->p.loops;
+                }
+                stepping = true;
+            }
+            if (!stepping) break;
+            std::vector<int> one(n, 0);
+            for (int32_t i = 0; i < n; ++i)
+                if (act[i] && left[i] > 0) {
+                    one[i] = 1;
+                    --left[i];
+                }
+            RC(batch_heat_chunk(B, ctxs, n, 1, one));
+        }
+    }
+    for (int32_t i = 0; i < n; ++i) RC(finish(ctxs[i], "tam_batch"));
+    return TAM_OK;
+}
+
+int check_batch(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds)
+{
+    if (n < 0 || (n > 0 && (!ctxs || !seeds))) return fail(nullptr, TAM_E_INVALID, "bad batch arguments");
+    for (int32_t i = 0; i < n; ++i) {
+        if (!ctxs[i]) return fail(nullptr, TAM_E_INVALID, "null context in batch");
+        for (int32_t j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) return fail(nullptr, TAM_E_INVALID, "context listed twice in batch");
+    }
+    return TAM_OK;
+}
+}  // namespace
+extern "C" {
+
 int tam_batch_step_coupled(tam_ctx *const *ctxs, int32_t n, int32_t iters, const uint64_t *seeds)
 {
-    if (iters < 0 || (n > 0 && !seeds)) return fail(nullptr, TAM_E_INVALID, "bad batch arguments");
+    RC(check_batch(ctxs, n, seeds));
+    if (iters < 0) return fail(nullptr, TAM_E_INVALID, "iters must be >= 0");
+    if (batchable(ctxs, n)) {
+        std::vector<int64_t> its;
+        return batch_loop_device(
+            ctxs, n, seeds, [&](tam_ctx *, int64_t it) { return it < iters; }, its);
+    }
     return run_batch(ctxs, n, [&](tam_ctx *c, int32_t i) {
         for (int32_t k = 0; k < iters; ++k) RC(outer_iteration(c, seeds[i]));
         return (int)TAM_OK;
@@ -1403,7 +1666,17 @@ int tam_batch_step_coupled(tam_ctx *const *ctxs, int32_t n, int32_t iters, const
 
 int tam_batch_run(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, int64_t max_iters, int64_t *iters)
 {
-    if (n > 0 && !seeds) return fail(nullptr, TAM_E_INVALID, "bad batch arguments");
+    RC(check_batch(ctxs, n, seeds));
+    if (batchable(ctxs, n)) {
+        std::vector<int64_t> its;
+        RC(batch_loop_device(
+            ctxs, n, seeds,
+            [&](tam_ctx *c, int64_t it) { return c->time <= c->total_time && (max_iters <= 0 || it < max_iters); },
+            its));
+        if (iters)
+            for (int32_t i = 0; i < n; ++i) iters[i] = its[i];
+        return TAM_OK;
+    }
     return run_batch(ctxs, n, [&](tam_ctx *c, int32_t i) {
         int64_t it = 0;
         while (c->time <= c->total_time) {
@@ -1512,6 +1785,9 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
         ctx->use_tma = value != 0;
     } else if (k == "heat.cls") {
         ctx->use_cls = value != 0;
+    } else if (k == "heat.cls_rows") {
+        if (value != 1 && value != 2) return fail(ctx, TAM_E_INVALID, "heat.cls_rows must be 1 or 2");
+        ctx->cls_rows = (int)value;
     } else if (k == "heat.arrhenius_fp64") {
         ctx->arr_fp64 = value != 0;
     } else if (k == "heat.zchunk") {
@@ -1521,6 +1797,146 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
         return fail(ctx, TAM_E_INVALID, "unknown tuning key " + k);
     }
     return TAM_OK;
+}
+
+// ------------------------------------------------------------ autotune --
+namespace {
+// Device copies of the config-mode state a trial run changes.
+struct Snapshot {
+    std::vector<std::pair<void *, void *>> bufs;  // (saved copy, live buffer)
+    std::vector<size_t> bytes;
+    double time = 0, pulseCount = 0, repetitionCount = 0, laserOn = 0;
+    int laser_flag = 0, pulseFlag = 0, pulsesDone = 0, counter = 0, fcur = 0;
+    int64_t mc_passes = 0;
+    bool need_trace = false;
+    int uniform_id = -1;
+    double tally[tam::N_TALLY] = {0};
+    int64_t last_n = 0;
+    ~Snapshot()
+    {
+        for (auto &b : bufs) cudaFree(b.first);
+    }
+};
+
+int snap_take(tam_ctx *ctx, Snapshot &S)
+{
+    const int64_t ni = ctx->ni;
+    const size_t r = ctx->fp64 ? 8 : 4;
+    auto add = [&](void *live, size_t bytes) -> int {
+        if (!live || !bytes) return TAM_OK;
+        void *cp = nullptr;
+        if (cudaMalloc(&cp, bytes) != cudaSuccess) return fail(ctx, TAM_E_NOMEM, "autotune: no room for the state copy");
+        S.bufs.push_back({cp, live});
+        S.bytes.push_back(bytes);
+        CK(cudaMemcpyAsync(cp, live, bytes, cudaMemcpyDeviceToDevice, ctx->stream));
+        return TAM_OK;
+    };
+    for (int q = 0; q < 2; ++q) {
+        RC(add(ctx->d_Tf[q], ni * r));
+        if (!ctx->fp64) RC(add(ctx->d_Tc[q], ni * 4));
+    }
+    RC(add(ctx->d_J, ni * r));
+    RC(add(ctx->d_Qf, ni * r));
+    RC(add(ctx->d_jmean, ni * 8));
+    RC(add(ctx->d_tissue, ni * 8));
+    RC(add(ctx->d_thres, 3 * ni * 8));
+    RC(add(ctx->d_mat, ni));
+    RC(add(ctx->d_nabl, sizeof(unsigned long long)));
+    RC(add(ctx->d_tally, tam::N_TALLY * 8));
+    S.time = ctx->time;
+    S.pulseCount = ctx->pulseCount;
+    S.repetitionCount = ctx->repetitionCount;
+    S.laserOn = ctx->laserOn;
+    S.laser_flag = ctx->laser_flag;
+    S.pulseFlag = ctx->pulseFlag;
+    S.pulsesDone = ctx->pulsesDone;
+    S.counter = ctx->counter;
+    S.fcur = ctx->fcur;
+    S.mc_passes = ctx->mc_passes;
+    S.need_trace = ctx->need_trace;
+    S.uniform_id = ctx->uniform_id;
+    std::memcpy(S.tally, ctx->tally, sizeof S.tally);
+    S.last_n = ctx->last_n;
+    return TAM_OK;
+}
+
+int snap_restore(tam_ctx *ctx, const Snapshot &S)
+{
+    for (size_t i = 0; i < S.bufs.size(); ++i)
+        CK(cudaMemcpyAsync(S.bufs[i].second, S.bufs[i].first, S.bytes[i], cudaMemcpyDeviceToDevice, ctx->stream));
+    ctx->time = S.time;
+    ctx->pulseCount = S.pulseCount;
+    ctx->repetitionCount = S.repetitionCount;
+    ctx->laserOn = S.laserOn;
+    ctx->laser_flag = S.laser_flag;
+    ctx->pulseFlag = S.pulseFlag;
+    ctx->pulsesDone = S.pulsesDone;
+    ctx->counter = S.counter;
+    ctx->fcur = S.fcur;
+    ctx->mc_passes = S.mc_passes;
+    ctx->need_trace = S.need_trace;
+    ctx->uniform_id = S.uniform_id;
+    std::memcpy(ctx->tally, S.tally, sizeof S.tally);
+    ctx->last_n = S.last_n;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return TAM_OK;
+}
+}  // namespace
+
+int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, int32_t nchosen)
+{
+    if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    if (!ctx->config) return fail(ctx, TAM_E_STATE, "autotune applies to config mode");
+    if (packets < 0 || steps < 0) return fail(ctx, TAM_E_INVALID, "packets and steps must be >= 0");
+    CK(cudaSetDevice(ctx->device));
+    Snapshot S;
+    RC(snap_take(ctx, S));
+    float ms = 0.f;
+    // transport: lanes that must wait at an interaction before the warp's event batch
+    if (packets > 0) {
+        int best = ctx->scat_min;
+        float best_ms = 1e30f;
+        for (int cand : {12, 16, 20, 24, 28}) {
+            ctx->scat_min = cand;
+            RC(mc_pass(ctx, packets, 0x5eedull, 0xA070u));
+            CK(cudaEventSynchronize(ctx->ev[1]));
+            CK(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = cand;
+            }
+        }
+        ctx->scat_min = best;
+        RC(snap_restore(ctx, S));
+    }
+    // heat: z planes per thread column (and voxel rows per thread of the class-table step)
+    if (steps > 0) {
+        int best_z = ctx->zchunk, best_r = ctx->cls_rows;
+        float best_ms = 1e30f;
+        const bool cls = ctx->fcls && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class;
+        for (int rows : {1, 2}) {
+            if (rows == 2 && !cls) continue;
+            for (int zc : {4, 8, 12, 16, 24}) {
+                if (zc > ctx->nz) continue;
+                ctx->zchunk = zc;
+                ctx->cls_rows = rows;
+                RC(cfg_heat(ctx, steps));
+                CK(cudaEventSynchronize(ctx->ev[3]));
+                CK(cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
+                RC(snap_restore(ctx, S));
+                if (ms < best_ms) {
+                    best_ms = ms;
+                    best_z = zc;
+                    best_r = rows;
+                }
+            }
+        }
+        ctx->zchunk = best_z;
+        ctx->cls_rows = best_r;
+    }
+    const int64_t v[3] = {ctx->scat_min, ctx->zchunk, ctx->cls_rows};
+    for (int32_t i = 0; i < nchosen && i < 3 && chosen; ++i) chosen[i] = v[i];
+    return finish(ctx, "tam_autotune");
 }
 
 namespace {

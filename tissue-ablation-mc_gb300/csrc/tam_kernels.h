@@ -16,6 +16,7 @@ int64_t launch_count();
 void set_thread_error(const std::string &msg);
 
 constexpr int MAX_MAT = 16;
+constexpr int FX_TILE = 32, FY_TILE = 8;  // x / y tile (thread block) of the fused heat kernels
 
 enum Medium : int32_t { MED_RHOKAP = 0, MED_MATERIAL = 1, MED_UNIFORM = 2 };
 enum Source : int32_t { SRC_DISK = 0, SRC_GAUSSIAN = 1 };
@@ -122,7 +123,8 @@ enum FusedConst : int {
     // Arrhenius constants for the FP32 form: ln A and Ea/R as float-float
     // pairs (high part, low part), exact window and ablation temperatures
     FC_LNA_HI = 29, FC_LNA_LO, FC_EAR_HI, FC_EAR_LO, FC_TLO, FC_THI, FC_TABL,
-    FC_N = 36
+    FC_TLO_LO, FC_THI_LO, FC_TABL_LO, // low parts of the three temperatures
+    FC_N = 39
 };
 
 struct FusedArgs {
@@ -187,7 +189,35 @@ cudaError_t launch_cls_from_mat(const uint8_t *mat, int nmat, uint8_t *cls, int 
 cudaError_t fused_cls_create(FusedCls **out, int nx, int ny, int nz, float *const T[2], float *const Tc[2],
                              const float *J, const uint8_t *cls, int pitch);
 void fused_cls_destroy(FusedCls *m);
-cudaError_t launch_fused_cls(const FusedArgs &a, const FusedCls *m, int which, const ClassLut &L, cudaStream_t s);
+// rows: voxel rows per thread (1 or 2).
+cudaError_t launch_fused_cls(const FusedArgs &a, const FusedCls *m, int which, const ClassLut &L, int rows,
+                             cudaStream_t s);
+
+// Batched FP32 heat step of many instances in one persistent cooperative
+// launch (batch.cu).  BatchInst lives in device memory, one per instance.
+struct BatchInst {
+    FusedArgs a;                  // constants filled by fill_fused_consts; the instance's buffers
+    ClassLut L;
+    const uint8_t *cls;           // class grid, rows of cls_pitch bytes
+    int32_t cls_pitch;
+    float *T[2], *E[2];           // temperature and Kahan-term buffer pairs
+    int32_t fcur;                 // pair read by the first step of the launch
+    int32_t tiles_x, tiles_y, zchunk;
+};
+struct BatchStep {                // per step and instance
+    double t_new;                 // time stamp at the end of the step
+    float pdt;                    // laser power * dt of the step (0: source off)
+    int32_t active;               // 0: the instance does not step
+};
+struct BatchSync {
+    unsigned count, gen, abort;
+};
+// Resident blocks of the batched kernel on the current device (its grid size).
+cudaError_t batch_heat_blocks(int *blocks);
+// K steps of every instance; prefix[i] = first work item of instance i,
+// prefix[n] = total work items; steps is K x n (step-major).
+cudaError_t launch_batch_heat(const BatchInst *insts, int n, const int *prefix, const BatchStep *steps, int K,
+                              BatchSync *sync, unsigned *err, int blocks, cudaStream_t s);
 
 // Halo (reference-layout) FP64 temperature from the interior state, with
 // ghosts filled from the boundary conditions.

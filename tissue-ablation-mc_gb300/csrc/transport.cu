@@ -203,7 +203,7 @@ __device__ __forceinline__ void fetch(const TransportArgs &a, const MatR<Real> *
     }
 }
 
-enum : int { M_DEAD = 0, M_FLY = 1, M_SCAT = 2 };
+enum : int { M_DEAD = 0, M_FLY = 1, M_SCAT = 2, M_FACE = 3 };  // M_SCAT, M_FACE: waiting for the event batch
 
 // Per-flight DDA set-up from the in-cell position f and direction n of one
 // axis: td = cell width along the ray, tm = distance to the next face.
@@ -286,10 +286,14 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
     const int NX = a.nx, NY = a.ny, NZ = a.nz, SY = a.nx, SZ = a.nx * a.ny;
     const uint32_t max_steps = a.max_steps > 0xfffffff0ll ? 0xfffffff0u : (uint32_t)a.max_steps;
     const Real namb = (Real)a.n_ambient;
+    // FP32 in a uniform medium: the flight is tracked by distance (tau / mut
+    // once per flight) instead of optical depth per voxel step
+    constexpr bool DIST = sizeof(Real) == 4 && MED == MED_UNIFORM;
+    const Real inv_mut = DIST ? (Real)1 / lut[a.uniform_id >= 0 ? a.uniform_id : 0].mut : (Real)0;
 
     int mode = M_DEAD;
     bool exhausted = false;
-    int ix = 0, iy = 0, iz = 0, cidx = 0, mid = 0, sgx = 1, sgy = 1, sgz = 1;
+    int ix = 0, iy = 0, iz = 0, cidx = 0, mid = 0, sgx = 1, sgy = 1, sgz = 1, fax = 0;
     Real fx = 0, fy = 0, fz = 0, nx = 0, ny = 0, nz = 0, sint = 0, phi = 0;
     Real cpv = 1, spv = 0;  // FP32 path: (cos phi, sin phi) in place of phi
     Real tdx = 0, tdy = 0, tdz = 0, tmx = 0, tmy = 0, tmz = 0, t = 0;
@@ -351,6 +355,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                             w = (Real)1 - rsp;
                         }
                         tau = -M<Real>::log(u3);
+                        if constexpr (DIST) tau *= inv_mut;
                         nx = sint * cp;  // direction (0, 0, -1): +-0 in x and y
                         ny = sint * sp;
                         nz = (Real)-1;
@@ -385,13 +390,28 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                 Real tmin = tmz;
                 if (tmy < tmin) { tmin = tmy; ax = 1; }
                 if (tmx < tmin) { tmin = tmx; ax = 0; }
-                Real dw = tmin - t;
-                dw = dw < (Real)0 ? (Real)0 : dw;
-                const Real taucell = dw * mut;
-                if (taucell < tau) {
+                Real dw;
+                bool cross;
+                if constexpr (DIST) {
+                    // tau holds the flight distance of the interaction point
+                    cross = tmin < tau;
+                    const Real tend = cross ? tmin : tau;
+                    dw = tend - t;
+                    dw = dw < (Real)0 ? (Real)0 : dw;
                     dep += w * dw * mua;
-                    tau -= taucell;
-                    t = tmin;
+                    t = tend;
+                } else {
+                    dw = tmin - t;
+                    dw = dw < (Real)0 ? (Real)0 : dw;
+                    const Real taucell = dw * mut;
+                    cross = taucell < tau;
+                    if (cross) {
+                        dep += w * dw * mua;
+                        tau -= taucell;
+                        t = tmin;
+                    }
+                }
+                if (cross) {
                     const bool cx = ax == 0, cy = ax == 1, cz = ax == 2;
                     const int sg = cx ? sgx : (cy ? sgy : sgz);
                     const int j = (cx ? ix : (cy ? iy : iz)) + sg;
@@ -410,74 +430,31 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                         tmy = cy ? tmy + tdy * kny : tmy;
                         tmz = cz ? tmz + tdz * knz : tmz;
                         fetch<Real, MED>(a, lut, ix, iy, iz, cidx, mut, mua, mid);
+                    } else if (a.fresnel) {
+                        // outer face: the packet sits on it; the Fresnel draw
+                        // waits for the event batch
+                        fax = ax;
+                        mode = M_FACE;
                     } else {
-                        // outer face: the packet sits on it; Fresnel or escape
-                        const Real nc = cx ? nx : (cy ? ny : nz);
-                        bool reflect = false;
-                        if (a.fresnel) {
-                            const U4 r = philox4x32_10(ev++, plo, phi32, a.stream, k0, k1);
-                            const Real nt = MED == MED_RHOKAP ? (Real)a.rhokap_n : lut[mid].n;
-                            reflect = Uniform<Real>::from(r.x) < fresnel<Real>(nt, namb, M<Real>::abs(nc));
-                        }
-                        if (reflect) {
-                            // mirror the crossed direction component; the next
-                            // face along it is one cell width back
-                            if (cx) {
-                                fy = axis_pos(ny, fy, hy, tmy, t);
-                                fz = axis_pos(nz, fz, hz, tmz, t);
-                                fx = sgx > 0 ? hx : (Real)0;
-                                nx = -nx;
-                                sgx = -sgx;
-                                tmx = t + tdx;
-                                if constexpr (sizeof(Real) == 4) {
-                                    cpv = -cpv;  // phi -> PI - phi
-                                } else {
-                                    phi = (Real)PI_R - phi;
-                                    if (phi < (Real)0) phi += TWOPI;
-                                }
-                            } else if (cy) {
-                                fx = axis_pos(nx, fx, hx, tmx, t);
-                                fz = axis_pos(nz, fz, hz, tmz, t);
-                                fy = sgy > 0 ? hy : (Real)0;
-                                ny = -ny;
-                                sgy = -sgy;
-                                tmy = t + tdy;
-                                if constexpr (sizeof(Real) == 4) {
-                                    spv = -spv;  // phi -> TWOPI - phi
-                                } else {
-                                    phi = TWOPI - phi;
-                                }
-                            } else {
-                                fx = axis_pos(nx, fx, hx, tmx, t);
-                                fy = axis_pos(ny, fy, hy, tmy, t);
-                                fz = sgz > 0 ? hz : (Real)0;
-                                nz = -nz;
-                                sgz = -sgz;
-                                tmz = t + tdz;
-                            }
-                        } else {
-                            if (!cx && !cy) {
-                                atomicAdd(&s_tal[sgz > 0 ? 1 : 2], (double)w);
-                            } else {
-                                atomicAdd(&s_tal[3], (double)w);
-                            }
-                            atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
-                            mode = M_DEAD;
-                        }
+                        // outer face without Fresnel: escape
+                        atomicAdd(&s_tal[cz ? (sgz > 0 ? 1 : 2) : 3], (double)w);
+                        atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
+                        mode = M_DEAD;
                     }
                 } else {
-                    const Real dd = M<Real>::div(tau, mut);
-                    dep += w * dd * mua;
-                    t += dd;
-                    fx = axis_pos(nx, fx, hx, tmx, t);
-                    fy = axis_pos(ny, fy, hy, tmy, t);
-                    fz = axis_pos(nz, fz, hz, tmz, t);
+                    // interaction point inside this cell; the in-cell position
+                    // is reconstructed in the event batch
+                    if constexpr (!DIST) {
+                        const Real dd = M<Real>::div(tau, mut);
+                        dep += w * dd * mua;
+                        t += dd;
+                    }
                     mode = M_SCAT;
                 }
             }
         }
 
-            sc = __ballot_sync(FULL, mode == M_SCAT);
+            sc = __ballot_sync(FULL, mode >= M_SCAT);
             fl = __ballot_sync(FULL, mode == M_FLY);
             if (fl == 0 || __popc(sc) >= scat_min || (!exhausted && (sc | fl) != FULL)) break;
         }
@@ -486,61 +463,112 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
             continue;
         }
 
-        // ---------- interaction: implicit capture, HG scatter, roulette --
+        // ------------------------------------------------- event batch --
+        // interactions (implicit capture, HG scatter, roulette) and Fresnel
+        // faces, handled together once enough lanes wait; both kinds draw
+        // their uniforms from one Philox block per lane
         if (sc && (__popc(sc) >= scat_min || fl == 0)) {
-            {
-                if (mode == M_SCAT) {
-                    const Real alb = MED == MED_RHOKAP ? (Real)0 : lut[mid].alb;
-                    w *= alb;
-                    bool die = !(w > (Real)0);
-                    if (!die) {
-                        cScat += 1;
-                        const U4 r = philox4x32_10(ev++, plo, phi32, a.stream, k0, k1);
-                        Real cost = nz;
-                        if constexpr (sizeof(Real) == 4) {
-                            if (stokes_f32(lut[mid].g, lut[mid].g2, Uniform<Real>::from(r.x), Uniform<Real>::from(r.y),
-                                           cost, sint, cpv, spv)) {
-                                nx = sint * cpv;
-                                ny = sint * spv;
-                                nz = cost;
+            if (mode >= M_SCAT) {
+                const bool face = mode == M_FACE;
+                if (!face) w *= MED == MED_RHOKAP ? (Real)0 : lut[mid].alb;
+                bool die = !face && !(w > (Real)0);
+                U4 r{0u, 0u, 0u, 0u};
+                if (!die) r = philox4x32_10(ev++, plo, phi32, a.stream, k0, k1);
+                if (face) {
+                    const bool cx = fax == 0, cy = fax == 1;
+                    const Real nc = cx ? nx : (cy ? ny : nz);
+                    const Real nt = MED == MED_RHOKAP ? (Real)a.rhokap_n : lut[mid].n;
+                    if (Uniform<Real>::from(r.x) < fresnel<Real>(nt, namb, M<Real>::abs(nc))) {
+                        // reflect: mirror the crossed direction component; the
+                        // next face along it is one cell width back
+                        if (cx) {
+                            fy = axis_pos(ny, fy, hy, tmy, t);
+                            fz = axis_pos(nz, fz, hz, tmz, t);
+                            fx = sgx > 0 ? hx : (Real)0;
+                            nx = -nx;
+                            sgx = -sgx;
+                            tmx = t + tdx;
+                            if constexpr (sizeof(Real) == 4) {
+                                cpv = -cpv;  // phi -> PI - phi
+                            } else {
+                                phi = (Real)PI_R - phi;
+                                if (phi < (Real)0) phi += TWOPI;
+                            }
+                        } else if (cy) {
+                            fx = axis_pos(nx, fx, hx, tmx, t);
+                            fz = axis_pos(nz, fz, hz, tmz, t);
+                            fy = sgy > 0 ? hy : (Real)0;
+                            ny = -ny;
+                            sgy = -sgy;
+                            tmy = t + tdy;
+                            if constexpr (sizeof(Real) == 4) {
+                                spv = -spv;  // phi -> TWOPI - phi
+                            } else {
+                                phi = TWOPI - phi;
                             }
                         } else {
-                            Real cp, sp;
-                            if (stokes<Real>(lut[mid].g, lut[mid].g2, Uniform<Real>::from(r.x),
-                                             Uniform<Real>::from(r.y), cost, sint, phi, cp, sp)) {
-                                nx = sint * cp;
-                                ny = sint * sp;
-                                nz = cost;
-                            }
+                            fx = axis_pos(nx, fx, hx, tmx, t);
+                            fy = axis_pos(ny, fy, hy, tmy, t);
+                            fz = sgz > 0 ? hz : (Real)0;
+                            nz = -nz;
+                            sgz = -sgz;
+                            tmz = t + tdz;
                         }
-                        if (!(nz == nz) || !(nx == nx) || !(ny == ny)) {
-                            atomicOr(&s_err, (unsigned)DEVERR_NAN);
-                            die = true;
-                        } else {
-                            axis_setup(nx, fx, hx, BIG, tdx, tmx, sgx);
-                            axis_setup(ny, fy, hy, BIG, tdy, tmy, sgy);
-                            axis_setup(nz, fz, hz, BIG, tdz, tmz, sgz);
-                            t = (Real)0;
-                            if (a.roulette && w < wmin) {
-                                if (Uniform<Real>::from(r.z) < inv_rm) {
-                                    atomicAdd(&s_tal[4], (double)(w * (rm - (Real)1)));
-                                    w *= rm;
-                                } else {
-                                    atomicAdd(&s_tal[4], -(double)w);
-                                    die = true;
-                                }
-                            }
-                            tau = -M<Real>::log(Uniform<Real>::from(r.w));
-                        }
-                    }
-                    if (die) {
-                        if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
-                        dep = (Real)0;
+                        mode = M_FLY;
+                    } else {
+                        atomicAdd(&s_tal[(!cx && !cy) ? (sgz > 0 ? 1 : 2) : 3], (double)w);
                         atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
                         mode = M_DEAD;
-                    } else {
-                        mode = M_FLY;
                     }
+                } else if (!die) {
+                    cScat += 1;
+                    fx = axis_pos(nx, fx, hx, tmx, t);
+                    fy = axis_pos(ny, fy, hy, tmy, t);
+                    fz = axis_pos(nz, fz, hz, tmz, t);
+                    Real cost = nz;
+                    if constexpr (sizeof(Real) == 4) {
+                        if (stokes_f32(lut[mid].g, lut[mid].g2, Uniform<Real>::from(r.x), Uniform<Real>::from(r.y), cost,
+                                       sint, cpv, spv)) {
+                            nx = sint * cpv;
+                            ny = sint * spv;
+                            nz = cost;
+                        }
+                    } else {
+                        Real cp, sp;
+                        if (stokes<Real>(lut[mid].g, lut[mid].g2, Uniform<Real>::from(r.x), Uniform<Real>::from(r.y),
+                                         cost, sint, phi, cp, sp)) {
+                            nx = sint * cp;
+                            ny = sint * sp;
+                            nz = cost;
+                        }
+                    }
+                    if (!(nz == nz) || !(nx == nx) || !(ny == ny)) {
+                        atomicOr(&s_err, (unsigned)DEVERR_NAN);
+                        die = true;
+                    } else {
+                        axis_setup(nx, fx, hx, BIG, tdx, tmx, sgx);
+                        axis_setup(ny, fy, hy, BIG, tdy, tmy, sgy);
+                        axis_setup(nz, fz, hz, BIG, tdz, tmz, sgz);
+                        t = (Real)0;
+                        if (a.roulette && w < wmin) {
+                            if (Uniform<Real>::from(r.z) < inv_rm) {
+                                atomicAdd(&s_tal[4], (double)(w * (rm - (Real)1)));
+                                w *= rm;
+                            } else {
+                                atomicAdd(&s_tal[4], -(double)w);
+                                die = true;
+                            }
+                        }
+                        tau = -M<Real>::log(Uniform<Real>::from(r.w));
+                        if constexpr (DIST) tau *= inv_mut;
+                    }
+                    if (!die) mode = M_FLY;
+                }
+                if (die) {
+                    if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
+                    dep = (Real)0;
+                    atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
+                    mode = M_DEAD;
                 }
             }
         }
@@ -608,7 +636,7 @@ template <typename Real, int MED> cudaError_t launch_t(const TransportArgs &a, i
 {
     int per_sm = 0;
     cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<Real, MED>, TPB, 0);
-    const int scat_min = a.scat_min > 0 ? a.scat_min : 16;
+    const int scat_min = a.scat_min > 0 ? a.scat_min : 20;
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
     int64_t blocks = (int64_t)sm_count * per_sm;

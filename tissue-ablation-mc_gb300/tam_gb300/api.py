@@ -183,6 +183,12 @@ class Context:
         self._ck(self._lib.tam_get_timing(self._h, C.byref(t), C.byref(h), C.byref(n)))
         return t.value, h.value, n.value
 
+    def autotune(self, packets: int = 1_000_000, steps: int = 20) -> dict:
+        """Pick the fastest kernel settings on this context's workload; state is restored."""
+        out = (C.c_int64 * 3)()
+        self._ck(self._lib.tam_autotune(self._h, int(packets), int(steps), out, 3))
+        return {"transport.scat_min": out[0], "heat.zchunk": out[1], "heat.cls_rows": out[2]}
+
     def write_output(self, directory: str) -> None:
         self._ck(self._lib.tam_write_output(self._h, directory.encode()))
 
@@ -208,6 +214,13 @@ def batch_run(contexts, seeds, max_iters: int = 0):
     it = (C.c_int64 * n)()
     check(lib().tam_batch_run(hs, n, sd, int(max_iters), it))
     return list(it)
+
+
+def batch_heat_steps(contexts, nsteps: int) -> None:
+    """`nsteps` FP32 heat steps of every context in persistent batched launches."""
+    n = len(contexts)
+    hs = (_abi._P * n)(*[c._h for c in contexts])
+    check(lib().tam_batch_heat_steps(hs, n, int(nsteps)))
 
 
 def kernel_launches() -> int:
