@@ -471,3 +471,26 @@ def test_fused_fp32_arrhenius_float_float_vs_fp64_exponent(tam, orc):
         ctx.close()
     assert om[1].max() > 1e-6, om[1].max()
     assert np.abs(om[0] - om[1]).max() <= 1e-6 * om[1].max()
+
+
+def test_autotune_restores_state(tam):
+    # the autotuner times trial passes and steps, keeps the fastest settings and
+    # leaves fields, clock and pulse state as they were
+    nx = 40
+    half = 0.0025 * nx
+    p = tam.default_params(nxg=nx, nyg=nx, nzg=nx, xmax=half, ymax=half, zmax=half, mode=1, precision=1,
+                           nphotons=20000, pulse_type=1, power=2.0, energy_per_pixel=2e3, total_time=1.0)
+    with tam.Context(p, tam.default_config(source_radius=0.03)) as ctx:
+        ctx.step_coupled(5, seed=2)
+        before = {f: ctx.download(f) for f in (F.TAM_F_TEMP, F.TAM_F_JMEAN_GLOBAL, F.TAM_F_TISSUE, F.TAM_F_MATERIAL)}
+        st0 = ctx.state()
+        t0, passes0 = st0.time, st0.mc_passes
+        chosen = ctx.autotune(packets=50000, steps=10)
+        assert chosen["transport.scat_min"] in (12, 16, 20, 24, 28)
+        assert chosen["heat.zchunk"] in (4, 8, 12, 16, 24) and chosen["heat.cls_rows"] in (1, 2)
+        for f, arr in before.items():
+            np.testing.assert_array_equal(ctx.download(f), arr)
+        st = ctx.state()
+        assert st.time == t0 and st.mc_passes == passes0
+        ctx.step_coupled(2, seed=2)  # the tuned context keeps running
+        assert ctx.device_errors() == 0
