@@ -649,7 +649,7 @@ template <bool UNIFORM, int RY>
 cudaError_t launch_cls_t(const FusedArgs &a, const ClsMaps &m, const ClassLut &L, cudaStream_t s)
 {
     const int bx = (a.nx + FX - 1) / FX, by = (a.ny + FY * RY - 1) / (FY * RY);
-    int zchunk = a.zchunk > 0 ? a.zchunk : 16;
+    int zchunk = a.zchunk > 0 ? a.zchunk : 8;  // 8 planes per block measured fastest at 200^3
     if (zchunk > a.nz) zchunk = a.nz;
     const int chunks = (a.nz + zchunk - 1) / zchunk;
     static std::atomic<unsigned long long> attr_set{0};
