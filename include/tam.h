@@ -280,6 +280,16 @@ int tam_batch_heat_steps(struct tam_ctx *const *ctxs, int32_t n, int32_t nsteps)
 int tam_batch_run(struct tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, int64_t max_iters, int64_t *iters);
 
 /*
+ * Checkpoint / resume (no reference counterpart: the reference restarts from
+ * input.params).  tam_save_state writes every device field of the context in
+ * its storage precision together with the clock, pulse state and counters,
+ * so a context created with the same parameters and configuration continues
+ * bit for bit after tam_load_state (TAM_E_STATE if they differ).
+ */
+int tam_save_state(struct tam_ctx *ctx, const char *path);
+int tam_load_state(struct tam_ctx *ctx, const char *path);
+
+/*
  * Autotuner (no reference counterpart).  Config mode: times the context's own
  * workload under candidate settings of "transport.scat_min" (an MC pass of
  * `packets`) and of "heat.zchunk" / "heat.cls_rows" (`steps` heat steps),

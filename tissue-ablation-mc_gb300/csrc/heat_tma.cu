@@ -309,12 +309,12 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
     float *Eo = a.Tc_out;
     const float dt = a.fc[FC_DT], Pdt = a.fc[FC_PDT];
     const float cx = a.fc[FC_CX], cy = a.fc[FC_CY], cz = a.fc[FC_CZ];
-    const bool src_on = Pdt != 0.f;
     const bool leader = tx == 0 && ty == 0;
     const int gx = blockIdx.x * FX - 4, gy = blockIdx.y * FY * RY - 1, gx8 = blockIdx.x * FX - 16;
     const int uc = L.uniform >= 0 ? L.uniform : 0;
     const float au = L.fa[uc * MAX_MAT + uc];
     const float Cx = cx * au, Cy = cy * au, Cz = cz * au;
+    const float irc_u = L.irc[uc];
     unsigned errbits = 0;
     if (!UNIFORM)
         for (int t = ty * FX + tx; t < MAX_MAT * MAX_MAT; t += FX * FY) s_fa[t] = L.fa[t];
@@ -393,7 +393,7 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
                 const float tc = Tc[r], e0 = ec[r];
                 const int k = UNIFORM ? uc : kc[r];
                 const int64_t v = (int64_t)x + sy * y + sz * z;
-                const float Jv = src_on ? ((const float *)(P + Lay::J_OFF))[o] : 0.f;
+                const float Jv = ((const float *)(P + Lay::J_OFF))[o];  // Pdt is 0 while the source is off
                 const float tzm = (Tp[r] - tc) - (ep[r] - e0), tzp = (Tn_ - tc) - (en_ - e0);
                 const float txm = (PT[q - 1] - tc) - (PE[q - 1] - e0), txp = (PT[q + 1] - tc) - (PE[q + 1] - e0);
                 const float tym = (PT[q - TPITCH] - tc) - (PE[q - TPITCH] - e0),
@@ -426,7 +426,7 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
                 }
                 const float dT = dt * lap;
                 const float sPJ = Pdt * Jv;
-                const float src = sPJ * L.irc[k];
+                const float src = sPJ * (UNIFORM ? irc_u : L.irc[k]);
                 float Tnew, Enew = 0.f;
                 bool clamped = false;
                 if (a.boil && tc >= a.fc[FC_TBOIL]) {
@@ -453,8 +453,7 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
                 To[v] = Tnew;
                 Eo[v] = Enew;
                 const float Ts = Tnew - Enew;
-                if (!(Ts == Ts)) errbits |= DEVERR_NAN;
-                else if (Ts < 0.f) errbits |= DEVERR_NEG_T;
+                errbits |= (Ts == Ts) ? (Ts < 0.f ? (unsigned)DEVERR_NEG_T : 0u) : (unsigned)DEVERR_NAN;
                 if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew, a.t_new);
             }
             Tp[r] = Tc[r];

@@ -1799,6 +1799,189 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
     return TAM_OK;
 }
 
+// ---------------------------------------------------------- checkpoint --
+namespace {
+// Device buffers that hold the state of a context (the raw storage, so a
+// resumed run continues bit for bit), by mode.
+std::vector<std::pair<void *, size_t>> state_buffers(tam_ctx *ctx)
+{
+    const int64_t ni = ctx->ni, nh = ctx->nh;
+    std::vector<std::pair<void *, size_t>> b;
+    auto add = [&](void *p, size_t n) {
+        if (p && n) b.push_back({p, n});
+    };
+    add(ctx->d_jmean, ni * 8);
+    add(ctx->d_tissue, ni * 8);
+    add(ctx->d_thres, 3 * ni * 8);
+    add(ctx->d_nabl, sizeof(unsigned long long));
+    add(ctx->d_tally, tam::N_TALLY * 8);
+    if (ctx->config) {
+        const size_t r = ctx->fp64 ? 8 : 4;
+        for (int q = 0; q < 2; ++q) {
+            add(ctx->d_Tf[q], ni * r);
+            if (!ctx->fp64) add(ctx->d_Tc[q], ni * 4);
+        }
+        add(ctx->d_k, ni * r);
+        add(ctx->d_rho, ni * r);
+        add(ctx->d_c, ni * r);
+        add(ctx->d_J, ni * r);
+        add(ctx->d_Qf, ni * r);
+        add(ctx->d_mat, ni);
+        if (ctx->d_cls) add(ctx->d_cls, (size_t)ctx->cls_pitch * ctx->ny * ctx->nz);
+    } else {
+        for (int q = 0; q < 2; ++q) {
+            add(ctx->d_T[q], nh * 8);
+            add(ctx->d_rk[q], nh * 8);
+        }
+        add(ctx->d_kappa, nh * 8);
+        add(ctx->d_density, nh * 8);
+        add(ctx->d_heatcap, nh * 8);
+        add(ctx->d_coeff, nh * 8);
+        add(ctx->d_alpha, nh * 8);
+        add(ctx->d_jglob, ni * 8);
+        add(ctx->d_Q, ni * 8);
+        add(ctx->d_water, ni * 8);
+    }
+    return b;
+}
+
+// Mutable host scalars of a context, in file order.
+struct Scalars {
+    double time, pulseCount, repetitionCount, laserOn, delt, total_time, cdt;
+    int32_t laser_flag, pulseFlag, pulsesDone, counter, tcur, rcur, fcur, need_trace, uniform_id, cls_uniform,
+        thermal_by_class, pad;
+    int64_t mc_passes, nabl_at_trace, nabl_at_uniform, last_n;
+    uint32_t errbits_seen, pad2;
+};
+
+void get_scalars(const tam_ctx *c, Scalars &S)
+{
+    std::memset(&S, 0, sizeof S);
+    S.time = c->time;
+    S.pulseCount = c->pulseCount;
+    S.repetitionCount = c->repetitionCount;
+    S.laserOn = c->laserOn;
+    S.delt = c->delt;
+    S.total_time = c->total_time;
+    S.cdt = c->cdt;
+    S.laser_flag = c->laser_flag;
+    S.pulseFlag = c->pulseFlag;
+    S.pulsesDone = c->pulsesDone;
+    S.counter = c->counter;
+    S.tcur = c->tcur;
+    S.rcur = c->rcur;
+    S.fcur = c->fcur;
+    S.need_trace = c->need_trace;
+    S.uniform_id = c->uniform_id;
+    S.cls_uniform = c->cls_uniform;
+    S.thermal_by_class = c->thermal_by_class;
+    S.mc_passes = c->mc_passes;
+    S.nabl_at_trace = c->nabl_at_trace;
+    S.nabl_at_uniform = c->nabl_at_uniform;
+    S.last_n = c->last_n;
+    S.errbits_seen = c->errbits_seen;
+}
+
+void set_scalars(tam_ctx *c, const Scalars &S)
+{
+    c->time = S.time;
+    c->pulseCount = S.pulseCount;
+    c->repetitionCount = S.repetitionCount;
+    c->laserOn = S.laserOn;
+    c->delt = S.delt;
+    c->total_time = S.total_time;
+    c->cdt = S.cdt;
+    c->laser_flag = S.laser_flag;
+    c->pulseFlag = S.pulseFlag;
+    c->pulsesDone = S.pulsesDone;
+    c->counter = S.counter;
+    c->tcur = S.tcur;
+    c->rcur = S.rcur;
+    c->fcur = S.fcur;
+    c->need_trace = S.need_trace != 0;
+    c->uniform_id = S.uniform_id;
+    c->cls_uniform = S.cls_uniform;
+    c->thermal_by_class = S.thermal_by_class != 0;
+    c->clut.uniform = S.cls_uniform;
+    c->mc_passes = S.mc_passes;
+    c->nabl_at_trace = S.nabl_at_trace;
+    c->nabl_at_uniform = S.nabl_at_uniform;
+    c->last_n = S.last_n;
+    c->errbits_seen = S.errbits_seen;
+    c->coeff_dirty = true;
+}
+
+const char CKPT_MAGIC[8] = {'T', 'A', 'M', 'C', 'K', 'P', 'T', '1'};
+}  // namespace
+
+int tam_save_state(tam_ctx *ctx, const char *path)
+{
+    if (!ctx || !path) return fail(ctx, TAM_E_INVALID, "null argument");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    std::ofstream f(path, std::ios::binary);
+    if (!f) return fail(ctx, TAM_E_IO, std::string("cannot open ") + path);
+    Scalars S;
+    get_scalars(ctx, S);
+    const auto bufs = state_buffers(ctx);
+    const uint32_t nb = (uint32_t)bufs.size();
+    f.write(CKPT_MAGIC, 8);
+    f.write((const char *)&ctx->p, sizeof ctx->p);
+    f.write((const char *)&ctx->cfg, sizeof ctx->cfg);
+    f.write((const char *)&S, sizeof S);
+    f.write((const char *)ctx->tally, sizeof ctx->tally);
+    f.write((const char *)&nb, sizeof nb);
+    std::vector<char> host;
+    for (const auto &b : bufs) {
+        const uint64_t n = b.second;
+        host.resize(n);
+        CK(cudaMemcpy(host.data(), b.first, n, cudaMemcpyDeviceToHost));
+        f.write((const char *)&n, sizeof n);
+        f.write(host.data(), (std::streamsize)n);
+    }
+    if (!f) return fail(ctx, TAM_E_IO, std::string("write failed: ") + path);
+    return TAM_OK;
+}
+
+int tam_load_state(tam_ctx *ctx, const char *path)
+{
+    if (!ctx || !path) return fail(ctx, TAM_E_INVALID, "null argument");
+    CK(cudaSetDevice(ctx->device));
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return fail(ctx, TAM_E_IO, std::string("cannot open ") + path);
+    char magic[8];
+    tam_params p;
+    tam_config c;
+    Scalars S;
+    double tally[tam::N_TALLY];
+    uint32_t nb = 0;
+    f.read(magic, 8);
+    f.read((char *)&p, sizeof p);
+    f.read((char *)&c, sizeof c);
+    f.read((char *)&S, sizeof S);
+    f.read((char *)tally, sizeof tally);
+    f.read((char *)&nb, sizeof nb);
+    if (!f || std::memcmp(magic, CKPT_MAGIC, 8) != 0) return fail(ctx, TAM_E_PARSE, "not a state file");
+    if (std::memcmp(&p, &ctx->p, sizeof p) != 0 || (ctx->config && std::memcmp(&c, &ctx->cfg, sizeof c) != 0))
+        return fail(ctx, TAM_E_STATE, "state file was written by a context with other parameters");
+    const auto bufs = state_buffers(ctx);
+    if (nb != bufs.size()) return fail(ctx, TAM_E_STATE, "state file holds another set of fields");
+    std::vector<char> host;
+    CK(cudaStreamSynchronize(ctx->stream));
+    for (const auto &b : bufs) {
+        uint64_t n = 0;
+        f.read((char *)&n, sizeof n);
+        if (!f || n != b.second) return fail(ctx, TAM_E_STATE, "state file field size mismatch");
+        host.resize(n);
+        f.read(host.data(), (std::streamsize)n);
+        if (!f) return fail(ctx, TAM_E_PARSE, "state file truncated");
+        CK(cudaMemcpy(b.first, host.data(), n, cudaMemcpyHostToDevice));
+    }
+    set_scalars(ctx, S);
+    std::memcpy(ctx->tally, tally, sizeof tally);
+    return finish(ctx, "tam_load_state");
+}
+
 // ------------------------------------------------------------ autotune --
 namespace {
 // Device copies of the config-mode state a trial run changes.

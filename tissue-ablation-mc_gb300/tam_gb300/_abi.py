@@ -132,6 +132,8 @@ SIGNATURES = [
                                 C.POINTER(C.c_int64)]),
     ("tam_batch_heat_steps", C.c_int, [C.POINTER(_P), C.c_int32, C.c_int32]),
     ("tam_autotune", C.c_int, [_P, C.c_int64, C.c_int32, C.POINTER(C.c_int64), C.c_int32]),
+    ("tam_save_state", C.c_int, [_P, C.c_char_p]),
+    ("tam_load_state", C.c_int, [_P, C.c_char_p]),
     ("tam_kernel_launches", C.c_int64, []),
     ("tam_set_tuning", C.c_int, [_P, C.c_char_p, C.c_int64]),
     ("tam_write_output", C.c_int, [_P, C.c_char_p]),

@@ -183,6 +183,12 @@ class Context:
         self._ck(self._lib.tam_get_timing(self._h, C.byref(t), C.byref(h), C.byref(n)))
         return t.value, h.value, n.value
 
+    def save_state(self, path: str) -> None:
+        self._ck(self._lib.tam_save_state(self._h, str(path).encode()))
+
+    def load_state(self, path: str) -> None:
+        self._ck(self._lib.tam_load_state(self._h, str(path).encode()))
+
     def autotune(self, packets: int = 1_000_000, steps: int = 20) -> dict:
         """Pick the fastest kernel settings on this context's workload; state is restored."""
         out = (C.c_int64 * 3)()
