@@ -412,7 +412,8 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
                 }
                 float lap;
                 if (x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1 && z > 0 && has_n) {
-                    lap = azm * tzm + azp * tzp + aym * tym + ayp * typ + axm * txm + axp * txp;
+                    // three independent two-term chains (short dependency depth)
+                    lap = ((azm * tzm + azp * tzp) + (aym * tym + ayp * typ)) + (axm * txm + axp * txp);
                 } else {
                     // a face of this voxel lies on the grid boundary: ghost faces
                     // use the voxel's own properties
