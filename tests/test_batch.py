@@ -125,3 +125,37 @@ def test_batch_coupled_fp32_matches_single_runs(tam):
     finally:
         for c in ctxs:
             c.close()
+
+
+def test_batch_device_path_with_mc_passes(tam):
+    # FP32 instances that start without a source: the batched loop runs each
+    # instance's MC pass (overlapped on the instances' streams), then the
+    # batched heat steps; every instance ends where it ends when run alone
+    F = tam._abi
+
+    def make(shp):
+        nx, ny, nz, layered, power = shp
+        half = 0.0025 * nx
+        p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half * ny / nx, zmax=half * nz / nx, mode=1,
+                               precision=1, nphotons=20000, pulse_type=1, power=power, energy_per_pixel=power * 1e3,
+                               total_time=1.0, loops=1)
+        c = tam.default_config(retrace_fraction=0.0, source_radius=0.05)
+        return tam.Context(p, c)
+
+    seeds = [3, 4, 5]
+    want = []
+    for shp, sd in zip(SHAPES, seeds):
+        with make(shp) as ctx:
+            ctx.step_coupled(20, seed=sd)
+            want.append((ctx.download(F.TAM_F_TEMP), ctx.download(F.TAM_F_JMEAN_GLOBAL), ctx.state().mc_passes))
+    ctxs = [make(shp) for shp in SHAPES]
+    try:
+        tam.batch_step_coupled(ctxs, 20, seeds)
+        for ctx, (T, J, passes) in zip(ctxs, want):
+            assert ctx.state().mc_passes == passes == 1
+            np.testing.assert_allclose(ctx.download(F.TAM_F_JMEAN_GLOBAL), J, rtol=1e-6, atol=1e-9 * J.max())
+            assert np.abs(ctx.download(F.TAM_F_TEMP) - T).max() <= 1e-4
+            assert (T - 310.15).max() > 0.01
+    finally:
+        for c in ctxs:
+            c.close()

@@ -94,8 +94,10 @@ __device__ __forceinline__ bool ge_ff(float T, float e, float hi, float lo) { re
 // compare the non-negative doubles by their bit patterns, which order the same
 // way.  Exponents beyond expf's range take the FP64 path, and so does every
 // voxel when arr_fp64 is set (FP64 exponent ln A - Ea/RT of T - e).
+// `o_pre` is the voxel's damage integral when the caller loaded it early
+// (have_o), so that its latency overlapped the step's arithmetic.
 __device__ __noinline__ void rare_update_f32(const FusedArgs &a, int64_t v, int64_t ni, float T, float e,
-                                            double t_new)
+                                            double t_new, bool have_o = false, double o_pre = 0.0)
 {
     if (a.arr_fp64) {
         rare_update<float>(a, v, ni, (double)T - (double)e, t_new);
@@ -117,7 +119,7 @@ __device__ __noinline__ void rare_update_f32(const FusedArgs &a, int64_t v, int6
         } else {
             inc = a.dt * exp(a.lnA - a.Ea / (a.Rgas * ((double)T - (double)e)));
         }
-        const double o = a.omega[v];
+        const double o = have_o ? o_pre : a.omega[v];
         const double on = o + inc;
         a.omega[v] = on;
         const long long ob = __double_as_longlong(o), nb = __double_as_longlong(on);

@@ -394,6 +394,11 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
                 const int k = UNIFORM ? uc : kc[r];
                 const int64_t v = (int64_t)x + sy * y + sz * z;
                 const float Jv = ((const float *)(P + Lay::J_OFF))[o];  // Pdt is 0 while the source is off
+                // a voxel near the damage window: load its damage integral now so
+                // the load overlaps the update below
+                const bool near = tc >= a.fc[FC_SCREEN];
+                double o_pre = 0.0;
+                if (near) o_pre = a.omega[v];
                 const float tzm = (Tp[r] - tc) - (ep[r] - e0), tzp = (Tn_ - tc) - (en_ - e0);
                 const float txm = (PT[q - 1] - tc) - (PE[q - 1] - e0), txp = (PT[q + 1] - tc) - (PE[q + 1] - e0);
                 const float tym = (PT[q - TPITCH] - tc) - (PE[q - TPITCH] - e0),
@@ -455,7 +460,7 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
                 Eo[v] = Enew;
                 const float Ts = Tnew - Enew;
                 errbits |= (Ts == Ts) ? (Ts < 0.f ? (unsigned)DEVERR_NEG_T : 0u) : (unsigned)DEVERR_NAN;
-                if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew, a.t_new);
+                if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew, a.t_new, near, o_pre);
             }
             Tp[r] = Tc[r];
             ep[r] = ec[r];

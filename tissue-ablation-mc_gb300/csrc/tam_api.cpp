@@ -1527,19 +1527,25 @@ int batch_chunk(tam_ctx *const *ctxs, int32_t n)
     return std::max(K, 1);
 }
 
-// MC passes of the instances that need one, back to back on their streams.
+// MC passes of the instances that need one, each on its own stream so that
+// the passes (and their tails of long-lived packets) overlap.
 int batch_traces(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, const std::vector<int> &active)
 {
+    std::vector<unsigned long long> nab(n, 0);
+    std::vector<int> traced(n, 0);
     for (int32_t i = 0; i < n; ++i) {
         tam_ctx *c = ctxs[i];
         if (!active[i] || !c->need_trace) continue;
         RC(mc_pass(c, c->p.nphotons * (int64_t)c->p.numproc, seeds[i], (uint32_t)c->mc_passes));
-        tam_ctx *const ctx = c;
-        unsigned long long nab = 0;
-        CK(cudaMemcpyAsync(&nab, c->d_nabl, sizeof nab, cudaMemcpyDeviceToHost, c->stream));
-        CK(cudaStreamSynchronize(c->stream));
-        c->nabl_at_trace = (long long)nab;
-        c->need_trace = false;
+        traced[i] = 1;
+    }
+    for (int32_t i = 0; i < n; ++i) {
+        if (!traced[i]) continue;
+        tam_ctx *const ctx = ctxs[i];
+        CK(cudaStreamSynchronize(ctx->stream));
+        CK(cudaMemcpy(&nab[i], ctx->d_nabl, sizeof(unsigned long long), cudaMemcpyDeviceToHost));
+        ctx->nabl_at_trace = (long long)nab[i];
+        ctx->need_trace = false;
     }
     return TAM_OK;
 }
