@@ -57,9 +57,11 @@ template <typename Real> struct Uniform;
 template <> struct Uniform<double> {
     __device__ __forceinline__ static double from(uint32_t x) { return ((double)x + 0.5) * 0x1p-32; }
 };
-// FP32: u = ((x >> 8) + 0.5) 2^-24, exact in (0,1).
+// FP32: u = ((x >> 9) + 0.5) 2^-23: k + 0.5 is exact in FP32 for k < 2^23, so
+// u lies on a 2^-23 grid strictly inside (0,1), the largest value 1 - 2^-24.
+// (24 bits would round k + 0.5 to even above 2^23 and could give u = 1.)
 template <> struct Uniform<float> {
-    __device__ __forceinline__ static float from(uint32_t x) { return ((float)(x >> 8) + 0.5f) * 0x1p-24f; }
+    __device__ __forceinline__ static float from(uint32_t x) { return ((float)(x >> 9) + 0.5f) * 0x1p-23f; }
 };
 
 // ------------------------------------------- exact FP64 helpers (no FMA) --
@@ -72,6 +74,9 @@ __device__ __forceinline__ double DIV(double a, double b) { return __ddiv_rn(a, 
 template <typename Real> struct M;
 template <> struct M<float> {
     __device__ __forceinline__ static float log(float x) { return __logf(x); }
+    // -log(u) for u in (0,1), never below 1 - u (> 0): the fast logarithm's
+    // absolute error near 1 could otherwise give 0 or a negative value
+    __device__ __forceinline__ static float neglog(float u) { return fmaxf(-__logf(u), 1.f - u); }
     __device__ __forceinline__ static void sincos(float x, float *s, float *c) { __sincosf(x, s, c); }
     __device__ __forceinline__ static float sqrt(float x) { return sqrtf(x); }
     __device__ __forceinline__ static float acos(float x) { return acosf(x); }
@@ -81,6 +86,7 @@ template <> struct M<float> {
 };
 template <> struct M<double> {
     __device__ __forceinline__ static double log(double x) { return ::log(x); }
+    __device__ __forceinline__ static double neglog(double u) { return -::log(u); }
     __device__ __forceinline__ static void sincos(double x, double *s, double *c) { ::sincos(x, s, c); }
     __device__ __forceinline__ static double sqrt(double x) { return ::sqrt(x); }
     __device__ __forceinline__ static double acos(double x) { return ::acos(x); }

@@ -324,7 +324,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     const Real u2 = Uniform<Real>::from(r.z), u3 = Uniform<Real>::from(r.w);
                     const Real R = (Real)a.source_radius;
                     const Real rad = a.source == SRC_DISK ? M<Real>::sqrt(u0 * (R * R))
-                                                          : R * M<Real>::sqrt((Real)-0.5 * M<Real>::log(u0));
+                                                          : R * M<Real>::sqrt((Real)0.5 * M<Real>::neglog(u0));
                     Real st, ct, sp, cp;
                     M<Real>::sincos(u1 * TWOPI, &st, &ct);
                     const Real X = rad * ct + (Real)a.xmax, Y = rad * st + (Real)a.ymax;
@@ -354,7 +354,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                             atomicAdd(&s_tal[0], (double)rsp);
                             w = (Real)1 - rsp;
                         }
-                        tau = -M<Real>::log(u3);
+                        tau = M<Real>::neglog(u3);
                         if constexpr (DIST) tau *= inv_mut;
                         nx = sint * cp;  // direction (0, 0, -1): +-0 in x and y
                         ny = sint * sp;
@@ -559,7 +559,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                                 die = true;
                             }
                         }
-                        tau = -M<Real>::log(Uniform<Real>::from(r.w));
+                        tau = M<Real>::neglog(Uniform<Real>::from(r.w));
                         if constexpr (DIST) tau *= inv_mut;
                     }
                     if (!die) mode = M_FLY;
