@@ -6,10 +6,12 @@
 //    / ablation update of src/3dFD.f90:312-361, each evaluated with explicit
 //    round-to-nearest operations in the reference's order of evaluation so
 //    the result matches the Fortran arithmetic (no FMA contraction);
-//  * fused config-mode step: stencil + latent-heat clamp + Arrhenius (FP64
-//    exponent ln A - Ea/RT) + ablation in one pass, with FP32 storage and a
-//    Kahan-compensated temperature, or plain FP64.  Each thread marches a
-//    (x, y) column through a z-chunk keeping the z-neighbours in registers.
+//  * fused config-mode step: stencil + latent-heat clamp + Arrhenius (exponent
+//    ln A - Ea/RT in FP64, or float-float in the FP32 form) + ablation in one
+//    pass, with FP32 storage and a Kahan-compensated temperature, or plain
+//    FP64.  Each thread marches a (x, y) column through a z-chunk keeping the
+//    z-neighbours in registers; this cp.async form serves the FP64 step and
+//    FP32 grids whose rows are not 16-byte aligned for TMA (heat_tma.cu).
 #include <algorithm>
 #include <atomic>
 #include <cstdio>

@@ -1,17 +1,20 @@
 // heat_tma.cu -- the FP32 + Kahan fused heat step with TMA plane staging.
 //
-// The physics of fused_kernel<float, true> (heat.cu) with two changes made
-// for GB300: the face diffusivities k_f/(rho_f c_f) and 1/(rho c), which only
-// change when the properties do, are precomputed per voxel (face_coeff_kernel),
-// and the planes are staged by TMA.  One elected thread streams each z-plane
-// of the block's tile -- T, the Kahan term and the x / y face coefficients
-// with a one-cell x/y halo; the z face coefficient, 1/(rho c) and J --
-// into a ring of shared-memory stages with cp.async.bulk.tensor, three planes
-// ahead of the plane being updated; completion is tracked by one mbarrier per
-// stage (transaction bytes), and every wait is bounded.  The x origin of a
-// tile is rounded down to a 16-byte boundary (bx*32 - 4), so the x halo sits
-// in columns 3 and 36 of a 40-wide row; out-of-range rows, columns and planes
-// read as zeros and are never used (those faces take the boundary path).
+// The physics of fused_kernel<float, true> (heat.cu) in two TMA forms:
+//  * fused_tma_kernel: the face diffusivities k_f/(rho_f c_f) and 1/(rho c)
+//    are precomputed per voxel (face_coeff_kernel) and staged with the planes;
+//    used once k, rho or c have been uploaded per voxel;
+//  * fused_cls_kernel: thermal properties by material class, face
+//    coefficients from a class-pair table in shared memory; only T, the Kahan
+//    term, J and (for heterogeneous grids) the class ids are staged.
+// One elected thread streams each z-plane of the block's tile into a ring of
+// shared-memory stages with cp.async.bulk.tensor, several planes ahead of the
+// plane being updated; completion is tracked by one mbarrier per stage
+// (transaction bytes), and every wait is bounded.  The x origin of a tile is
+// rounded down to a 16-byte boundary (bx*32 - 4 for FP32, bx*32 - 16 for u8),
+// so the FP32 x halo sits in columns 3 and 36 of a 40-wide row; out-of-range
+// rows, columns and planes read as zeros and are never used (those faces take
+// the boundary path).
 #include <cuda.h>
 
 #include <atomic>

@@ -238,11 +238,13 @@ template <typename Real> __device__ __forceinline__ Real axis_pos(Real n, Real f
 
 // Event loop per lane: DEAD (needs a packet) -> FLY (one voxel step per
 // iteration: cross a face, reach an outer face, or reach the interaction
-// point) -> SCAT (waits at the interaction point) -> FLY ...  The scatter
-// (Philox block, HG rotation, roulette, new optical depth) is the expensive
-// part; it runs once at least scat_min lanes of the warp wait for it, or when
-// no lane is flying, so it executes with most lanes active.  Every packet
-// sees the same sequence of events and random numbers as a straight loop.
+// point) -> SCAT (waits at the interaction point) or FACE (waits on an outer
+// face for its Fresnel draw) -> FLY ...  The events (Philox block, HG
+// rotation, roulette, new optical depth; Fresnel reflect-or-escape) are the
+// expensive part; the event batch runs once at least scat_min lanes of the
+// warp wait, or when no lane is flying, so it executes with most lanes
+// active.  Every packet sees the same sequence of events and random numbers
+// as a straight loop.
 //
 // The DDA is incremental (Amanatides & Woo): per flight, the distance tm to
 // the next face of each axis and the cell width td along the ray; a crossing
