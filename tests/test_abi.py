@@ -133,3 +133,24 @@ def test_no_cpu_fallback_without_gpu(tam):
 
         a, b = tam.selftest_philox(np.zeros((4, 6), dtype=np.uint32))
     assert e.value.code == tam._abi.TAM_E_NODEV
+
+
+def test_fortran_module_matches_header(tam):
+    # include/tam.f90 (not compiled here: no Fortran compiler) binds names the
+    # library exports, with the header's enum values and struct field order
+    import re
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    src = open(os.path.join(root, "include", "tam.f90")).read()
+    lib = tam._abi.load()
+    names = re.findall(r"function (tam_\w+)\(", src)
+    assert len(names) >= 20
+    for n in names:
+        assert hasattr(lib, n), n
+    params = dict((k, int(v)) for k, v in re.findall(r"(TAM_\w+) = (\d+)", src))
+    for k, v in params.items():
+        if hasattr(tam._abi, k):
+            assert getattr(tam._abi, k) == v, k
+    # bind(C) tam_params: the ctypes mirror's field order
+    block = src[src.index("type, bind(C) :: tam_params"): src.index("end type")].split("\n", 1)[1]
+    fields = [f.strip() for line in re.findall(r"::\s*(.*)", block) for f in line.split(",")]
+    assert fields == [f[0] for f in tam._abi.Params._fields_]
