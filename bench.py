@@ -350,7 +350,7 @@ def run_gpu(args):
         },
         "roofline_stencil": {
             "bound": "hbm",
-            "kernel": "fused_cls_kernel<uniform> (FP32 + Kahan, class-table coefficients)",
+            "kernel": "fused_cls2_kernel<uniform> (FP32 + Kahan, class-table coefficients, voxel pairs)",
             "achieved": B_STENCIL32 * nvox * nsteps / (heat_ms * 1e-3) / 1e9,
             "peak": hbm,
             "unit": "GB/s",

@@ -252,7 +252,8 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * "heat.cls" (1: while the thermal properties are those of the material
  * classes, look the face coefficients up per class pair instead of reading
  * per-voxel coefficient arrays; 0: always read the arrays),
- * "heat.cls_rows" (voxel rows per thread of the class-table step, 1 or 2),
+ * "heat.cls_rows" (class-table step: 0 = two x-adjacent voxels per thread,
+ * the default; 1 or 2 = that many voxel rows per thread),
  * "heat.arrhenius_fp64" (FP32 form: 1 evaluates the Arrhenius exponent
  * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits). */
 int tam_set_tuning(struct tam_ctx *ctx, const char *key, int64_t value);

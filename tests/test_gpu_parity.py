@@ -423,7 +423,8 @@ def test_fused_class_table_matches_coefficient_arrays(tam, nx):
     alpha = max(k / (r * c) for k, r, c in mats[1:])
     dt = 0.9 / (2 * alpha * 3 / d ** 2)
     out = {}
-    for name, prec, cls, rows in (("cls", 1, 1, 2), ("cls1", 1, 1, 1), ("arr", 1, 0, 1), ("f64", 0, 1, 1)):
+    for name, prec, cls, rows in (("cls", 1, 1, 2), ("cls1", 1, 1, 1), ("cls0", 1, 1, 0), ("arr", 1, 0, 1),
+                                  ("f64", 0, 1, 1)):
         ctx = _layered_heat_ctx(tam, nx, ny, nz, prec, cls, dt, J, grid, mats, rows)
         T = ctx.heat_steps(300, want=True)
         out[name] = (T, ctx.download(F.TAM_F_TISSUE), ctx.device_errors())
@@ -433,6 +434,7 @@ def test_fused_class_table_matches_coefficient_arrays(tam, nx):
     assert out["cls"][2] == 0 and out["arr"][2] == 0
     assert np.abs(out["cls"][0] - out["arr"][0]).max() <= 1e-4
     assert np.abs(out["cls1"][0] - out["cls"][0]).max() <= 1e-5
+    assert np.abs(out["cls0"][0] - out["cls1"][0]).max() <= 1e-5 and out["cls0"][2] == 0
     assert np.abs(out["cls"][0] - out["f64"][0]).max() <= 1e-3
 
 
@@ -487,7 +489,7 @@ def test_autotune_restores_state(tam):
         t0, passes0 = st0.time, st0.mc_passes
         chosen = ctx.autotune(packets=50000, steps=10)
         assert chosen["transport.scat_min"] in (12, 16, 20, 24, 28)
-        assert chosen["heat.zchunk"] in (4, 8, 12, 16, 24) and chosen["heat.cls_rows"] in (1, 2)
+        assert chosen["heat.zchunk"] in (2, 3, 4, 8, 16) and chosen["heat.cls_rows"] in (0, 1)
         for f, arr in before.items():
             np.testing.assert_array_equal(ctx.download(f), arr)
         st = ctx.state()

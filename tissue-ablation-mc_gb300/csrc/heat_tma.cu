@@ -481,6 +481,227 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
     if (errbits) atomicOr(a.err, errbits);
 }
 
+// Paired form of the class-table step: the same ring and stage layout, 128
+// threads per 32 x 8 tile, each updating two x-adjacent voxels with 64-bit
+// shared-memory loads and global stores (the staged rows start 16 bytes
+// before the tile, so a pair sits at an even offset).  Per voxel it issues
+// half the shared-memory loads, stores and per-plane work of the one-voxel
+// form.  Needs nx even (the pair never straddles a row end).
+// 6 resident blocks of 128 threads per SM (80 registers) measured fastest
+#ifndef TAM_CLS2_MINB
+#define TAM_CLS2_MINB 6
+#endif
+template <bool UNIFORM>
+__global__ void __launch_bounds__(FX / 2 * FY, TAM_CLS2_MINB)
+    fused_cls2_kernel(const __grid_constant__ FusedArgs a, const __grid_constant__ ClsMaps m,
+                      const __grid_constant__ ClassLut L, int zchunk)
+{
+    using Lay = ClsLayout<UNIFORM, 1>;
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ float s_fa[MAX_MAT * MAX_MAT];
+    unsigned char *sm = smem_raw + ((128 - (su32(smem_raw) & 127)) & 127);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + CTS * Lay::STAGE);
+    const int tp = threadIdx.x, ty = threadIdx.y;  // pair index 0..15, row 0..7
+    const int tx = 2 * tp;                          // first voxel of the pair within the tile
+    const int x = blockIdx.x * FX + tx, y = blockIdx.y * FY + ty;
+    const int z0 = blockIdx.z * zchunk;
+    const int z1 = min(a.nz, z0 + zchunk);
+    const int nplanes = z1 - z0;
+    const int last = nplanes + 1;
+    const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, ni = sz * a.nz;
+    float *To = (float *)a.T_out, *Q = (float *)a.Q;
+    float *Eo = a.Tc_out;
+    const float dt = a.fc[FC_DT], Pdt = a.fc[FC_PDT];
+    const float cx = a.fc[FC_CX], cy = a.fc[FC_CY], cz = a.fc[FC_CZ];
+    const bool leader = tp == 0 && ty == 0;
+    const int gx = blockIdx.x * FX - 4, gy = blockIdx.y * FY - 1, gx8 = blockIdx.x * FX - 16;
+    const int uc = L.uniform >= 0 ? L.uniform : 0;
+    const float au = L.fa[uc * MAX_MAT + uc];
+    const float Cx = cx * au, Cy = cy * au, Cz = cz * au;
+    const float irc_u = L.irc[uc];
+    unsigned errbits = 0;
+    if (!UNIFORM)
+        for (int t = ty * (FX / 2) + tp; t < MAX_MAT * MAX_MAT; t += FX / 2 * FY) s_fa[t] = L.fa[t];
+
+    auto stage = [&](int idx) { return sm + (idx % CTS) * Lay::STAGE; };
+    auto issue = [&](int idx) {
+        unsigned char *b = stage(idx);
+        uint64_t *br = bar + (idx % CTS);
+        const int zz = z0 - 1 + idx;
+        fence_proxy_async();
+        mbar_expect_tx(br, Lay::TX);
+        tma_load_3d(b + Lay::T_OFF, &m.T, gx, gy, zz, br);
+        tma_load_3d(b + Lay::E_OFF, &m.E, gx, gy, zz, br);
+        tma_load_3d(b + Lay::J_OFF, &m.J, gx + 4, gy + 1, zz, br);
+        if (!UNIFORM) tma_load_3d(b + Lay::C_OFF, &m.cls, gx8, gy, zz, br);
+    };
+    auto wait = [&](int idx) { return mbar_wait(bar + (idx % CTS), (uint32_t)((idx / CTS) & 1)); };
+
+    if (leader) {
+        for (int s = 0; s < CTS; ++s) mbar_init(bar + s, 1);
+        fence_mbar_init();
+        fence_proxy_async();
+    }
+    __syncthreads();
+    int issued = 0;
+    if (leader)
+        for (int idx = 0; idx <= CTS - 2 && idx <= last; ++idx) issue(idx);
+    issued = (CTS - 1 < last + 1) ? CTS - 1 : last + 1;
+    bool ok = __syncthreads_and(wait(0) && wait(1)) != 0;
+    const int q = (ty + 1) * TPITCH + tx + 4;     // first voxel of the pair in the T / E rows (even)
+    const int qc = (ty + 1) * CPITCH + tx + 16;   // ... in the class rows (even)
+    const int o = ty * FX + tx;                   // ... in J (even)
+    const bool in0 = x < a.nx && y < a.ny, in1 = x + 1 < a.nx && y < a.ny;
+    float2 Tp = {0.f, 0.f}, ep = {0.f, 0.f}, Tc = {0.f, 0.f}, ec = {0.f, 0.f};
+    int kp0 = 0, kp1 = 0, kc0 = 0, kc1 = 0;
+    auto cls2 = [&](const unsigned char *b, int i, int &k0, int &k1) {
+        const unsigned short w = *reinterpret_cast<const unsigned short *>(b + Lay::C_OFF + i);
+        k0 = w & (MAX_MAT - 1);
+        k1 = (w >> 8) & (MAX_MAT - 1);
+    };
+    if (ok) {
+        const unsigned char *C0 = stage(1);
+        Tc = *reinterpret_cast<const float2 *>((const float *)(C0 + Lay::T_OFF) + q);
+        ec = *reinterpret_cast<const float2 *>((const float *)(C0 + Lay::E_OFF) + q);
+        if (!UNIFORM) cls2(C0, qc, kc0, kc1);
+        if (z0 > 0) {
+            const unsigned char *Pm = stage(0);
+            Tp = *reinterpret_cast<const float2 *>((const float *)(Pm + Lay::T_OFF) + q);
+            ep = *reinterpret_cast<const float2 *>((const float *)(Pm + Lay::E_OFF) + q);
+            if (!UNIFORM) cls2(Pm, qc, kp0, kp1);
+        }
+    }
+    for (int i = 0; i < nplanes && ok; ++i) {
+        const int z = z0 + i;
+        const bool has_n = z + 1 < a.nz;
+        if (i + CTS - 1 <= last) {
+            if (leader) issue(i + CTS - 1);
+            issued = i + CTS;
+        }
+        ok = __syncthreads_and(wait(i + 2)) != 0;
+        if (!ok) break;
+        const unsigned char *P = stage(i + 1), *N = stage(i + 2);
+        const float *PT = (const float *)(P + Lay::T_OFF), *PE = (const float *)(P + Lay::E_OFF);
+        float2 Tn = {0.f, 0.f}, en = {0.f, 0.f};
+        int kn0 = 0, kn1 = 0;
+        if (has_n) {
+            Tn = *reinterpret_cast<const float2 *>((const float *)(N + Lay::T_OFF) + q);
+            en = *reinterpret_cast<const float2 *>((const float *)(N + Lay::E_OFF) + q);
+            if (!UNIFORM) cls2(N, qc, kn0, kn1);
+        }
+        if (in0) {
+            const float2 Ty0 = *reinterpret_cast<const float2 *>(PT + q - TPITCH),
+                         Ty1 = *reinterpret_cast<const float2 *>(PT + q + TPITCH);
+            const float2 Ey0 = *reinterpret_cast<const float2 *>(PE + q - TPITCH),
+                         Ey1 = *reinterpret_cast<const float2 *>(PE + q + TPITCH);
+            const float Txl = PT[q - 1], Txr = PT[q + 2], Exl = PE[q - 1], Exr = PE[q + 2];
+            const float2 Jv = *reinterpret_cast<const float2 *>((const float *)(P + Lay::J_OFF) + o);
+            const int64_t v = (int64_t)x + sy * y + sz * z;
+            float Tnew[2], Enew[2];
+            // voxels near the damage window: load their damage integrals now so
+            // the loads overlap the update below
+            const bool near0 = Tc.x >= a.fc[FC_SCREEN], near1 = Tc.y >= a.fc[FC_SCREEN];
+            double o_pre[2] = {0.0, 0.0};
+            if (near0) o_pre[0] = a.omega[v];
+            if (near1) o_pre[1] = a.omega[v + 1];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const bool inh = h == 0 || in1;
+                const int xx = x + h;
+                const float tc = h ? Tc.y : Tc.x, e0 = h ? ec.y : ec.x;
+                const float tpz = h ? Tp.y : Tp.x, epz = h ? ep.y : ep.x;
+                const float tnz = h ? Tn.y : Tn.x, enz = h ? en.y : en.x;
+                const float txmT = h ? Tc.x : Txl, txmE = h ? ec.x : Exl;  // x- neighbour
+                const float txpT = h ? Txr : Tc.y, txpE = h ? Exr : ec.y;  // x+ neighbour
+                const float tymT = h ? Ty0.y : Ty0.x, tymE = h ? Ey0.y : Ey0.x;
+                const float typT = h ? Ty1.y : Ty1.x, typE = h ? Ey1.y : Ey1.x;
+                const int k = UNIFORM ? uc : (h ? kc1 : kc0);
+                const float tzm = (tpz - tc) - (epz - e0), tzp = (tnz - tc) - (enz - e0);
+                const float txm = (txmT - tc) - (txmE - e0), txp = (txpT - tc) - (txpE - e0);
+                const float tym = (tymT - tc) - (tymE - e0), typ = (typT - tc) - (typE - e0);
+                float axm = Cx, axp = Cx, aym = Cy, ayp = Cy, azm = Cz, azp = Cz;
+                if (!UNIFORM) {
+                    const unsigned char *PC = P + Lay::C_OFF;
+                    const float *frow = s_fa + k * MAX_MAT;
+                    const int cxm = h ? kc0 : (PC[qc - 1] & (MAX_MAT - 1));
+                    const int cxp = h ? (PC[qc + 2] & (MAX_MAT - 1)) : kc1;
+                    axm = cx * frow[cxm];
+                    axp = cx * frow[cxp];
+                    aym = cy * frow[PC[qc + h - CPITCH] & (MAX_MAT - 1)];
+                    ayp = cy * frow[PC[qc + h + CPITCH] & (MAX_MAT - 1)];
+                    azm = cz * frow[h ? kp1 : kp0];
+                    azp = cz * frow[h ? kn1 : kn0];
+                }
+                float lap;
+                if (xx > 0 && xx < a.nx - 1 && y > 0 && y < a.ny - 1 && z > 0 && has_n) {
+                    lap = ((azm * tzm + azp * tzp) + (aym * tym + ayp * typ)) + (axm * txm + axp * txp);
+                } else {
+                    const float kk = L.k[k], rr = L.rho[k], hh = L.c[k];
+                    lap = z > 0 ? azm * tzm : ghost_term<float>(a, 4, tc, e0, kk, rr, hh);
+                    lap += has_n ? azp * tzp : ghost_term<float>(a, 5, tc, e0, kk, rr, hh);
+                    lap += y > 0 ? aym * tym : ghost_term<float>(a, 2, tc, e0, kk, rr, hh);
+                    lap += y < a.ny - 1 ? ayp * typ : ghost_term<float>(a, 3, tc, e0, kk, rr, hh);
+                    lap += xx > 0 ? axm * txm : ghost_term<float>(a, 0, tc, e0, kk, rr, hh);
+                    lap += xx < a.nx - 1 ? axp * txp : ghost_term<float>(a, 1, tc, e0, kk, rr, hh);
+                }
+                const float dT = dt * lap;
+                const float sPJ = Pdt * (h ? Jv.y : Jv.x);
+                const float src = sPJ * (UNIFORM ? irc_u : L.irc[k]);
+                float tn = a.fc[FC_TBOIL], en_ = 0.f;
+                bool clamped = false;
+                if (inh && a.boil && tc >= a.fc[FC_TBOIL]) {
+                    const float rr = L.rho[k], rc = rr * L.c[k];
+                    const float qv = a.fc[FC_LW] * rr * a.fc[FC_VVOX];
+                    const float Qv = Q[v + h];
+                    if (Qv < qv) {
+                        const float Ein = (sPJ + rc * dT) * a.fc[FC_VVOX];
+                        if (Ein > 0.f) {
+                            const float qn = Qv + Ein;
+                            Q[v + h] = qn < qv ? qn : qv;
+                            clamped = true;
+                        }
+                    }
+                }
+                if (!clamped) {
+                    const float inc = dT + src;
+                    const float yk = inc - e0;
+                    const float t = tc + yk;
+                    en_ = (t - tc) - yk;
+                    tn = t;
+                }
+                Tnew[h] = tn;
+                Enew[h] = en_;
+                const float Ts = tn - en_;
+                if (inh) {
+                    errbits |= (Ts == Ts) ? (Ts < 0.f ? (unsigned)DEVERR_NEG_T : 0u) : (unsigned)DEVERR_NAN;
+                    if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v + h, ni, tn, en_, a.t_new, h ? near1 : near0, o_pre[h]);
+                }
+            }
+            if (in1) {
+                *reinterpret_cast<float2 *>(To + v) = make_float2(Tnew[0], Tnew[1]);
+                *reinterpret_cast<float2 *>(Eo + v) = make_float2(Enew[0], Enew[1]);
+            } else {
+                To[v] = Tnew[0];
+                Eo[v] = Enew[0];
+            }
+        }
+        __syncthreads();
+        Tp = Tc;
+        ep = ec;
+        Tc = Tn;
+        ec = en;
+        kp0 = kc0;
+        kp1 = kc1;
+        kc0 = kn0;
+        kc1 = kn1;
+    }
+    if (!ok) {
+        errbits |= DEVERR_SYNC_TIMEOUT;
+        for (int idx = issued > CTS ? issued - CTS : 0; idx < issued; ++idx) (void)wait(idx);
+    }
+    if (errbits) atomicOr(a.err, errbits);
+}
+
 CUresult (*p_encode)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *, const cuuint64_t *,
                      const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
                      CUtensorMapL2promotion, CUtensorMapFloatOOBfill) = nullptr;
@@ -678,12 +899,45 @@ cudaError_t launch_cls_t(const FusedArgs &a, const ClsMaps &m, const ClassLut &L
 }
 }  // namespace
 
+namespace {
+template <bool UNIFORM>
+cudaError_t launch_cls2_t(const FusedArgs &a, const ClsMaps &m, const ClassLut &L, cudaStream_t s)
+{
+    const int bx = (a.nx + FX - 1) / FX, by = (a.ny + FY - 1) / FY;
+    int zchunk = a.zchunk > 0 ? a.zchunk : 3;  // short columns, many blocks: measured fastest at 200^3
+    if (zchunk > a.nz) zchunk = a.nz;
+    const int chunks = (a.nz + zchunk - 1) / zchunk;
+    const int smem = ClsLayout<UNIFORM, 1>::SMEM;
+    static std::atomic<unsigned long long> attr_set{0};
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    const unsigned long long bit = 1ull << (dev & 63);
+    if (!(attr_set.load() & bit)) {
+        e = cudaFuncSetAttribute(fused_cls2_kernel<UNIFORM>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+        if (e != cudaSuccess) return e;
+        attr_set.fetch_or(bit);
+    }
+    count_launch();
+    fused_cls2_kernel<UNIFORM><<<dim3(bx, by, chunks), dim3(FX / 2, FY), smem, s>>>(a, m, L, zchunk);
+    return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t launch_fused_cls(const FusedArgs &a0, const FusedCls *cm, int which, const ClassLut &L, int rows,
                              cudaStream_t s)
 {
     FusedArgs a = a0;
     fill_fused_consts(a);
-    const int ry = rows == 1 ? 1 : 2;
+    if (rows == 0 && a.nx % 2 == 0) {  // paired form
+        ClsMaps m;
+        m.T = cm->T[0][which];
+        m.E = cm->E[0][which];
+        m.J = cm->J[0];
+        m.cls = cm->cls[0];
+        return L.uniform >= 0 ? launch_cls2_t<true>(a, m, L, s) : launch_cls2_t<false>(a, m, L, s);
+    }
+    const int ry = rows == 2 ? 2 : 1;
     ClsMaps m;
     m.T = cm->T[ry - 1][which];
     m.E = cm->E[ry - 1][which];

@@ -100,7 +100,7 @@ struct tam_ctx {
     // class-table form of the FP32 fused step: thermal properties by material
     // class (valid until k, rho or c are uploaded per voxel)
     bool use_cls = true;
-    int cls_rows = 1;                // voxel rows per thread of the class-table step (1 measured fastest)
+    int cls_rows = 0;                // class-table step: 0 = voxel pairs (measured fastest), 1 or 2 rows
     bool arr_fp64 = false;           // FP32 form: FP64 Arrhenius exponent instead of float-float
     tam::FusedCls *fcls = nullptr;
     uint8_t *d_cls = nullptr;
@@ -1792,7 +1792,7 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
     } else if (k == "heat.cls") {
         ctx->use_cls = value != 0;
     } else if (k == "heat.cls_rows") {
-        if (value != 1 && value != 2) return fail(ctx, TAM_E_INVALID, "heat.cls_rows must be 1 or 2");
+        if (value < 0 || value > 2) return fail(ctx, TAM_E_INVALID, "heat.cls_rows must be 0 (voxel pairs), 1 or 2");
         ctx->cls_rows = (int)value;
     } else if (k == "heat.arrhenius_fp64") {
         ctx->arr_fp64 = value != 0;
@@ -2103,9 +2103,9 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
         int best_z = ctx->zchunk, best_r = ctx->cls_rows;
         float best_ms = 1e30f;
         const bool cls = ctx->fcls && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class;
-        for (int rows : {1, 2}) {
-            if (rows == 2 && !cls) continue;
-            for (int zc : {4, 8, 12, 16, 24}) {
+        for (int rows : {0, 1}) {
+            if (rows == 0 && !cls) continue;
+            for (int zc : {2, 3, 4, 8, 16}) {
                 if (zc > ctx->nz) continue;
                 ctx->zchunk = zc;
                 ctx->cls_rows = rows;
