@@ -255,7 +255,10 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * "heat.cls_rows" (class-table step: 0 = two x-adjacent voxels per thread,
  * the default; 1 or 2 = that many voxel rows per thread),
  * "heat.arrhenius_fp64" (FP32 form: 1 evaluates the Arrhenius exponent
- * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits). */
+ * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits),
+ * "batch.staged" (batched heat steps, read from the first context of the
+ * batch: 1 (default) stages each tile's planes in shared memory with
+ * cp.async, 0 reads neighbours with cached global loads). */
 int tam_set_tuning(struct tam_ctx *ctx, const char *key, int64_t value);
 /*
  * Batches of independent instances (no reference counterpart: the reference

@@ -159,3 +159,29 @@ def test_batch_device_path_with_mc_passes(tam):
     finally:
         for c in ctxs:
             c.close()
+
+
+@pytest.mark.parametrize("zchunk", [0, 1, 7])
+def test_batch_staged_matches_cached_loads(tam, zchunk):
+    # the two forms of the batched step (planes staged in shared memory by
+    # cp.async; neighbours by cached global loads) on odd, layered and uniform
+    # instances, with z-chunks of one plane (items of three slots), a ragged
+    # last chunk and the default
+    F = tam._abi
+    res = []
+    for staged in (0, 1):
+        ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
+        try:
+            for c in ctxs:
+                c.set_tuning("batch.staged", staged)
+                c.set_tuning("heat.zchunk", zchunk)
+            tam.batch_heat_steps(ctxs, 60)
+            res.append([(c.download(F.TAM_F_TEMP), c.download(F.TAM_F_TISSUE), c.device_errors()) for c in ctxs])
+        finally:
+            for c in ctxs:
+                c.close()
+    for (Ta, Oa, ea), (Tb, Ob, eb) in zip(*res):
+        assert ea == eb == 0
+        assert (Tb - 310.15).max() > 0.5
+        assert np.abs(Ta - Tb).max() <= 1e-4
+        assert np.abs(Oa - Ob).max() <= 1e-4 * max(Ob.max(), 1e-30)

@@ -105,6 +105,323 @@ __device__ __noinline__ bool boil_clamp(const FusedArgs &a, const ClassLut &L, i
     return false;
 }
 
+// ------------------------------------------------ staged class-table step --
+// The same per-voxel update with the tile's planes staged in shared memory by
+// cp.async (LDGSTS, 4-byte copies: instance rows need not be 16-byte aligned)
+// through a ring of AS stages, AD planes ahead of the plane being updated.
+// The block's work items are tile columns of a z-chunk, across instances.
+// Per voxel: T, the Kahan term, J and the class id read once
+// from HBM (tile halos from L2), T and the Kahan term written once.
+__device__ __forceinline__ void async4(void *s, const void *g)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"((unsigned)__cvta_generic_to_shared(s)), "l"(g)
+                 : "memory");
+}
+__device__ __forceinline__ void async16(void *s, const void *g)
+{
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"((unsigned)__cvta_generic_to_shared(s)),
+                 "l"(g)
+                 : "memory");
+}
+__device__ __forceinline__ void async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N> __device__ __forceinline__ void async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+constexpr int AS = 6;                  // ring stages
+constexpr int AD = AS - 1;             // planes in flight: plane i + AD is issued at the update of plane i
+constexpr int AP = 40;                 // floats per staged T / E row: x0 - 4 .. x0 + 35
+constexpr int AR = FY + 2;             // staged rows y0 - 1 .. y0 + 8
+constexpr int ACP = 64;                // class bytes per staged row: x0 - 16 .. x0 + 47
+constexpr int A_T = 0, A_E = AR * AP * 4, A_J = 2 * AR * AP * 4, A_C = A_J + FX * FY * 4;
+constexpr int A_STAGE = ((A_C + AR * ACP + 127) / 128) * 128;  // 4864 bytes
+constexpr int A_SMEM = AS * A_STAGE + 128;                     // + alignment slack
+
+// Tile column of one instance: voxels x0..x0+31, y0..y0+7, z0..z1-1.
+struct Item {
+    int inst, x0, y0, z0, z1;
+};
+
+__device__ __forceinline__ Item item_at(const BatchInst *insts, int n, const int *prefix, int item)
+{
+    int lo = 0, hi = n - 1;  // last i with prefix[i] <= item
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(prefix + mid) <= item) lo = mid;
+        else hi = mid - 1;
+    }
+    const BatchInst &I = insts[lo];
+    const int local = item - __ldg(prefix + lo), tx = I.tiles_x, ty = I.tiles_y;
+    Item it;
+    it.inst = lo;
+    it.x0 = (local % tx) * FX;
+    it.y0 = ((local / tx) % ty) * FY;
+    it.z0 = (local / (tx * ty)) * I.zchunk;
+    it.z1 = min(I.a.nz, it.z0 + I.zchunk);
+    return it;
+}
+
+// Per-thread copies of every plane of an item (offsets within a plane; -1:
+// no copy): own voxel, one halo element (rows y0-1 / y0+8 by the first two
+// warps, columns x0-1 / x0+32 by lanes 1-8 of the next two) and one 16-byte
+// chunk of class ids (warps 4-5, four chunks per staged row).
+struct Offs {
+    int own, ext, c;
+    int sx;  // shared offsets: halo element (floats) in the low 16 bits, class chunk (bytes) in the high
+};
+
+__device__ __forceinline__ Offs offsets_for(int nx, int ny, int cp, bool uni, const Item &it, int tx, int ty)
+{
+    Offs o;
+    const int x = it.x0 + tx, y = it.y0 + ty;
+    int s_ext = 0, s_c = 0;
+    o.own = (x < nx && y < ny) ? x + nx * y : -1;
+    o.ext = -1;
+    if (ty == 0) {
+        if (it.y0 > 0 && x < nx) o.ext = x + nx * (it.y0 - 1), s_ext = tx + 4;
+    } else if (ty == 1) {
+        if (it.y0 + FY < ny && x < nx) o.ext = x + nx * (it.y0 + FY), s_ext = (FY + 1) * AP + tx + 4;
+    } else if ((ty == 2 || ty == 3) && tx >= 1 && tx <= FY) {
+        const int yy = it.y0 - 1 + tx;
+        if (ty == 2 && it.x0 > 0 && yy < ny) o.ext = it.x0 - 1 + nx * yy, s_ext = tx * AP + 3;
+        if (ty == 3 && it.x0 + FX < nx && yy < ny) o.ext = it.x0 + FX + nx * yy, s_ext = tx * AP + FX + 4;
+    }
+    o.c = -1;
+    const int q = (ty - 4) * FX + tx;
+    if (!uni && q >= 0 && q < AR * 4) {
+        const int r = q >> 2, ch = q & 3;
+        const int yy = it.y0 - 1 + r, xb = it.x0 - 16 + 16 * ch;
+        if (yy >= 0 && yy < ny && xb >= 0 && xb + 16 <= cp) o.c = xb + cp * yy, s_c = r * ACP + 16 * ch;
+    }
+    o.sx = s_ext | s_c << 16;
+    return o;
+}
+
+// Block-uniform description of the item being updated, in shared memory
+// (written by one thread, read after a barrier) so that it holds no
+// registers: where its planes come from and go to, and the step's source.
+struct __align__(16) Src {
+    const float *T, *E;
+    const float *J;
+    const uint8_t *C;
+    float *To, *Eo;
+    double t_new;
+    int sz, csz, nz, z0;
+    int np, jon, nx, ny;
+    float pdt;
+};
+
+// Issue the copies of plane p (z = z0 - 1 + p, nothing past z1 or outside
+// the grid) into stage b; every call commits one group.
+__device__ __forceinline__ void issue_plane(const Src &d, const Offs &o, int p, unsigned char *b, int tx, int ty)
+{
+    const int zz = d.z0 - 1 + p;
+    if (p <= d.np + 1 && zz >= 0 && zz < d.nz) {
+        const int po = d.sz * zz;
+        float *bT = (float *)(b + A_T), *bE = (float *)(b + A_E);
+        if (o.own >= 0) {
+            const int so = (ty + 1) * AP + tx + 4;
+            async4(bT + so, d.T + po + o.own);
+            async4(bE + so, d.E + po + o.own);
+            if (d.jon && p >= 1 && p <= d.np) async4((float *)(b + A_J) + ty * FX + tx, d.J + po + o.own);
+        }
+        if (o.ext >= 0) {
+            const int se = o.sx & 0xffff;
+            async4(bT + se, d.T + po + o.ext);
+            async4(bE + se, d.E + po + o.ext);
+        }
+        if (o.c >= 0) async16(b + A_C + (o.sx >> 16), d.C + d.csz * zz + o.c);
+    }
+    async_commit();
+}
+
+// Sum of the ghost terms of the boundary faces in mask gm (bit f = face f).
+__device__ __noinline__ float ghost_sum(const FusedArgs &a, const ClassLut &L, unsigned gm, int kc, float Tc,
+                                        float ec)
+{
+    const float kk = L.k[kc], rr = L.rho[kc], hh = L.c[kc];
+    float g = 0.f;
+    for (int f = 0; f < 6; ++f)
+        if (gm >> f & 1u) g += ghost_term<float>(a, f, Tc, ec, kk, rr, hh);
+    return g;
+}
+
+constexpr int ARGS_WORDS = (int)(sizeof(FusedArgs) / 4), LUT_WORDS = (int)(sizeof(ClassLut) / 4);
+static_assert(sizeof(FusedArgs) % 4 == 0 && sizeof(ClassLut) % 4 == 0, "word copies");
+
+// K steps of every instance (GRID: persistent cooperative launch, items
+// strided over the grid, a bounded grid barrier between steps) or one step
+// with one item per block (!GRID, K == 1).  Each item streams its planes
+// z0-1 .. z1 through the ring, AD - 2 planes ahead of the next one needed;
+// the instance's constants and class table sit in shared memory.
+#ifndef TAM_STAGED_MINB
+#define TAM_STAGED_MINB 3
+#endif
+template <bool GRID>
+__global__ void __launch_bounds__(FX *FY, TAM_STAGED_MINB)
+    batch_staged_kernel(const BatchInst *__restrict__ insts, int n, const int *__restrict__ prefix,
+                        const BatchStep *__restrict__ steps, int K, BatchSync *sync, unsigned *err)
+{
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(16) unsigned char s_args_raw[sizeof(FusedArgs)];
+    __shared__ __align__(16) unsigned char s_lut_raw[sizeof(ClassLut)];
+    __shared__ Src d;
+    const FusedArgs &A = *reinterpret_cast<const FusedArgs *>(s_args_raw);
+    const ClassLut &L = *reinterpret_cast<const ClassLut *>(s_lut_raw);
+    unsigned char *sm = smem_raw + ((128 - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127)) & 127);
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * FX + tx;
+    const int total = __ldg(prefix + n);
+    const int stride = GRID ? (int)gridDim.x : total;
+    int loaded = -1;
+    for (int k = 0; k < K; ++k) {
+        for (int item = blockIdx.x; item < total; item += stride) {
+            const Item it = item_at(insts, n, prefix, item);
+            const BatchStep st = steps[(int64_t)k * n + it.inst];
+            if (!st.active) continue;  // block-uniform
+            const BatchInst &I = insts[it.inst];
+            // every thread finished the previous item (its last barrier)
+            if (it.inst != loaded) {
+                for (int w = tid; w < ARGS_WORDS; w += FX * FY)
+                    ((uint32_t *)s_args_raw)[w] = ((const uint32_t *)&I.a)[w];
+                for (int w = tid; w < LUT_WORDS; w += FX * FY)
+                    ((uint32_t *)s_lut_raw)[w] = ((const uint32_t *)&I.L)[w];
+                loaded = it.inst;
+            }
+            if (tid == 0) {
+                const int fc = (I.fcur + k) & 1;
+                d.T = I.T[fc];
+                d.E = I.E[fc];
+                d.To = I.T[fc ^ 1];
+                d.Eo = I.E[fc ^ 1];
+                d.J = (const float *)I.a.J;
+                d.C = I.cls;
+                d.nx = I.a.nx;
+                d.ny = I.a.ny;
+                d.sz = I.a.nx * I.a.ny;
+                d.csz = I.cls_pitch * I.a.ny;
+                d.nz = I.a.nz;
+                d.z0 = it.z0;
+                d.np = it.z1 - it.z0;
+                d.jon = st.pdt != 0.f;
+                d.pdt = st.pdt;
+                d.t_new = st.t_new;
+            }
+            const int uc = I.L.uniform;
+            const Offs o = offsets_for(I.a.nx, I.a.ny, I.cls_pitch, uc >= 0, it, tx, ty);
+            __syncthreads();  // the item's description is visible
+            // planes 0 .. AD-1 (z0-1 .. z0+AD-2) in flight
+#pragma unroll
+            for (int p = 0; p < AD; ++p) issue_plane(d, o, p, sm + p * A_STAGE, tx, ty);
+            async_wait<AD - 2>();
+            __syncthreads();  // planes 0 and 1 (and the instance's tables) are visible to the block
+            const int x = it.x0 + tx, y = it.y0 + ty;
+            const bool own = o.own >= 0;
+            const bool xy_inner = x > 0 && x < d.nx - 1 && y > 0 && y < d.ny - 1;
+            const int so = (ty + 1) * AP + tx + 4, co = (ty + 1) * ACP + tx + 16;
+            float Tp = 0.f, ep = 0.f, Tc = 0.f, ec = 0.f;
+            int kp = uc, kc = uc;
+            if (own) {
+                if (it.z0 > 0) {
+                    Tp = ((const float *)(sm + A_T))[so];
+                    ep = ((const float *)(sm + A_E))[so];
+                    if (uc < 0) kp = (sm + A_C)[co] & (MAX_MAT - 1);
+                }
+                Tc = ((const float *)(sm + A_STAGE + A_T))[so];
+                ec = ((const float *)(sm + A_STAGE + A_E))[so];
+                if (uc < 0) kc = (sm + A_STAGE + A_C)[co] & (MAX_MAT - 1);
+            }
+            int v = x + d.nx * y + d.sz * it.z0;
+            unsigned errbits = 0;
+            int si = AD % AS, sc = 1, sn = 2;  // stages: next issue, plane z, plane z+1
+            for (int i = 0; i < d.np; ++i, v += d.sz) {
+                issue_plane(d, o, i + AD, sm + si * A_STAGE, tx, ty);
+                async_wait<AD - 2>();
+                __syncthreads();  // plane z+1 has landed for the whole block
+                const unsigned char *P = sm + sc * A_STAGE, *N = sm + sn * A_STAGE;
+                const int z = it.z0 + i;
+                const bool has_n = z + 1 < d.nz;
+                float Tn_ = 0.f, en_ = 0.f;
+                int kn = uc;
+                if (own && has_n) {
+                    Tn_ = ((const float *)(N + A_T))[so];
+                    en_ = ((const float *)(N + A_E))[so];
+                    if (uc < 0) kn = (N + A_C)[co] & (MAX_MAT - 1);
+                }
+                if (own) {
+                    const float *PT = (const float *)(P + A_T), *PE = (const float *)(P + A_E);
+                    const float *row = L.fa + kc * MAX_MAT;
+                    const float Jv = d.jon ? ((const float *)(P + A_J))[ty * FX + tx] : 0.f;
+                    const bool near = Tc >= A.fc[FC_SCREEN];
+                    double o_pre = 0.0;
+                    if (near) o_pre = A.omega[v];
+                    const float tzm = (Tp - Tc) - (ep - ec), tzp = (Tn_ - Tc) - (en_ - ec);
+                    const float txm = (PT[so - 1] - Tc) - (PE[so - 1] - ec), txp = (PT[so + 1] - Tc) - (PE[so + 1] - ec);
+                    const float tym = (PT[so - AP] - Tc) - (PE[so - AP] - ec),
+                                typ = (PT[so + AP] - Tc) - (PE[so + AP] - ec);
+                    float axm, axp, aym, ayp;
+                    if (uc >= 0) {
+                        axm = axp = aym = ayp = row[uc];
+                    } else {
+                        const unsigned char *PC = P + A_C;
+                        axm = row[PC[co - 1] & (MAX_MAT - 1)];
+                        axp = row[PC[co + 1] & (MAX_MAT - 1)];
+                        aym = row[PC[co - ACP] & (MAX_MAT - 1)];
+                        ayp = row[PC[co + ACP] & (MAX_MAT - 1)];
+                    }
+                    const float azm = row[kp], azp = row[kn];
+                    const float cx = A.fc[FC_CX], cy = A.fc[FC_CY], cz = A.fc[FC_CZ];
+                    float lap;
+                    if (xy_inner && z > 0 && has_n) {
+                        lap = (cz * (azm * tzm + azp * tzp) + cy * (aym * tym + ayp * typ)) + cx * (axm * txm + axp * txp);
+                    } else {
+                        // faces on the grid boundary (bit f: x-, x+, y-, y+, z-, z+)
+                        // take the ghost term instead of the neighbour's
+                        const unsigned gm = (unsigned)(x == 0) | (unsigned)(x == d.nx - 1) << 1 | (unsigned)(y == 0) << 2 |
+                                            (unsigned)(y == d.ny - 1) << 3 | (unsigned)(z == 0) << 4 |
+                                            (unsigned)(!has_n) << 5;
+                        lap = (cz * ((gm & 16 ? 0.f : azm * tzm) + (gm & 32 ? 0.f : azp * tzp)) +
+                               cy * ((gm & 4 ? 0.f : aym * tym) + (gm & 8 ? 0.f : ayp * typ))) +
+                              cx * ((gm & 1 ? 0.f : axm * txm) + (gm & 2 ? 0.f : axp * txp));
+                        lap += ghost_sum(A, L, gm, kc, Tc, ec);
+                    }
+                    const float dT = A.fc[FC_DT] * lap;
+                    const float sPJ = d.pdt * Jv;
+                    const float srcT = sPJ * L.irc[kc];
+                    float Tnew = A.fc[FC_TBOIL], Enew = 0.f;
+                    const bool clamped = A.boil && Tc >= Tnew && boil_clamp(A, L, kc, v, sPJ, dT);
+                    if (!clamped) {
+                        const float inc = dT + srcT;
+                        const float yk = inc - ec;
+                        const float t = Tc + yk;
+                        Enew = (t - Tc) - yk;
+                        Tnew = t;
+                    }
+                    d.To[v] = Tnew;
+                    d.Eo[v] = Enew;
+                    const float Ts = Tnew - Enew;
+                    errbits |= (Ts == Ts) ? (Ts < 0.f ? (unsigned)DEVERR_NEG_T : 0u) : (unsigned)DEVERR_NAN;
+                    if (Ts >= A.fc[FC_SCREEN])
+                        rare_update_f32(A, v, (int64_t)d.sz * d.nz, Tnew, Enew, d.t_new, near, o_pre);
+                }
+                Tp = Tc;
+                ep = ec;
+                kp = kc;
+                Tc = Tn_;
+                ec = en_;
+                kc = kn;
+                si = si + 1 == AS ? 0 : si + 1;
+                sc = sn;
+                sn = sn + 1 == AS ? 0 : sn + 1;
+                // no barrier here: the issue of the next iteration overwrites the
+                // stage of plane z-1, last read one iteration ago, before the
+                // barrier every thread has passed
+            }
+            async_wait<0>();
+            __syncthreads();  // the next item rewrites the stages and the instance's tables
+            if (errbits) atomicOr(I.a.err, errbits);  // (the shared copy may already hold the next instance)
+        }
+        if (GRID && k + 1 < K && !grid_barrier(sync, gridDim.x, err)) return;
+    }
+}
+
 __global__ void __launch_bounds__(FX *FY, 4)
     batch_heat_kernel(const BatchInst *__restrict__ insts, int n, const int *__restrict__ prefix,
                       const BatchStep *__restrict__ steps, int K, BatchSync *sync, unsigned *err)
@@ -236,19 +553,21 @@ __global__ void __launch_bounds__(FX *FY, 4)
 
 }  // namespace
 
-cudaError_t batch_heat_blocks(int *blocks)
+cudaError_t batch_heat_blocks(int *blocks, int staged)
 {
     int dev = 0, sms = 0, per = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_heat_kernel, FX * FY, 0);
+    if (e == cudaSuccess)
+        e = staged ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_staged_kernel<true>, FX * FY, A_SMEM)
+                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_heat_kernel, FX * FY, 0);
     if (e != cudaSuccess) return e;
     *blocks = sms * (per > 0 ? per : 1);
     return cudaSuccess;
 }
 
 cudaError_t launch_batch_heat(const BatchInst *insts, int n, const int *prefix, const BatchStep *steps, int K,
-                              BatchSync *sync, unsigned *err, int blocks, cudaStream_t s)
+                              BatchSync *sync, unsigned *err, int blocks, int staged, cudaStream_t s)
 {
     if (n <= 0 || K <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(BatchSync), s);
@@ -256,7 +575,19 @@ cudaError_t launch_batch_heat(const BatchInst *insts, int n, const int *prefix, 
     void *args[] = {(void *)&insts, (void *)&n, (void *)&prefix, (void *)&steps, (void *)&K, (void *)&sync,
                     (void *)&err};
     count_launch();
+    if (staged)
+        return cudaLaunchCooperativeKernel((const void *)batch_staged_kernel<true>, dim3(blocks), dim3(FX, FY), args,
+                                           A_SMEM, s);
     return cudaLaunchCooperativeKernel((const void *)batch_heat_kernel, dim3(blocks), dim3(FX, FY), args, 0, s);
+}
+
+cudaError_t launch_staged_step(const BatchInst *inst, const int *prefix, const BatchStep *step, int items,
+                               cudaStream_t s)
+{
+    if (items <= 0) return cudaSuccess;
+    count_launch();
+    batch_staged_kernel<false><<<items, dim3(FX, FY), A_SMEM, s>>>(inst, 1, prefix, step, 1, nullptr, nullptr);
+    return cudaGetLastError();
 }
 
 }  // namespace tam

@@ -102,6 +102,7 @@ struct tam_ctx {
     bool use_cls = true;
     int cls_rows = 0;                // class-table step: 0 = voxel pairs (measured fastest), 1 or 2 rows
     bool arr_fp64 = false;           // FP32 form: FP64 Arrhenius exponent instead of float-float
+    int batch_staged = 1;            // batched steps: planes staged by cp.async (1) or cached global loads (0)
     tam::FusedCls *fcls = nullptr;
     uint8_t *d_cls = nullptr;
     int cls_pitch = 0;
@@ -1424,7 +1425,7 @@ struct DevBatch {
     std::vector<tam::BatchInst> inst;
     std::vector<int> prefix;
     std::vector<tam::BatchStep> steps;
-    int blocks = 0, kmax = 0;
+    int blocks = 0, kmax = 0, staged = 1;
     ~DevBatch()
     {
         cudaFree(d_inst);
@@ -1462,7 +1463,8 @@ int batch_setup(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int kmax)
     }
     B.kmax = kmax;
     B.steps.resize((size_t)kmax * n);
-    CK(tam::batch_heat_blocks(&B.blocks));
+    B.staged = ctx->batch_staged;
+    CK(tam::batch_heat_blocks(&B.blocks, B.staged));
     CK(cudaMalloc(&B.d_inst, sizeof(tam::BatchInst) * n));
     CK(cudaMalloc(&B.d_prefix, sizeof(int) * (n + 1)));
     CK(cudaMalloc(&B.d_steps, sizeof(tam::BatchStep) * B.steps.size()));
@@ -1501,7 +1503,7 @@ int batch_heat_chunk(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int K, const 
         if (ctxs[i]->stream != s) CK(cudaStreamSynchronize(ctxs[i]->stream));
     CK(cudaMemcpyAsync(B.d_inst, B.inst.data(), sizeof(tam::BatchInst) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(B.d_steps, B.steps.data(), sizeof(tam::BatchStep) * (size_t)K * n, cudaMemcpyHostToDevice, s));
-    CK(tam::launch_batch_heat(B.d_inst, n, B.d_prefix, B.d_steps, K, B.d_sync, B.d_err, B.blocks, s));
+    CK(tam::launch_batch_heat(B.d_inst, n, B.d_prefix, B.d_steps, K, B.d_sync, B.d_err, B.blocks, B.staged, s));
     CK(cudaStreamSynchronize(s));
     unsigned bits = 0;
     CK(cudaMemcpy(&bits, B.d_err, sizeof bits, cudaMemcpyDeviceToHost));
@@ -1796,6 +1798,8 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
         ctx->cls_rows = (int)value;
     } else if (k == "heat.arrhenius_fp64") {
         ctx->arr_fp64 = value != 0;
+    } else if (k == "batch.staged") {
+        ctx->batch_staged = value != 0;
     } else if (k == "heat.zchunk") {
         if (value < 0 || value > ctx->nz) return fail(ctx, TAM_E_INVALID, "heat.zchunk must be in 0..nz");
         ctx->zchunk = (int)value;
