@@ -251,14 +251,17 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * FP32 fused step's planes with TMA where the row pitch allows, 0: cp.async),
  * "heat.cls" (1: while the thermal properties are those of the material
  * classes, look the face coefficients up per class pair instead of reading
- * per-voxel coefficient arrays; 0: always read the arrays),
+ * per-voxel coefficient arrays; 0: always read the arrays; with TMA off or
+ * rows whose pitch TMA cannot take (nx not a multiple of 4) the class-table
+ * step stages its planes with cp.async, two voxels per thread),
  * "heat.cls_rows" (class-table step: 0 = two x-adjacent voxels per thread,
  * the default; 1 or 2 = that many voxel rows per thread),
  * "heat.arrhenius_fp64" (FP32 form: 1 evaluates the Arrhenius exponent
  * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits),
  * "batch.staged" (batched heat steps, read from the first context of the
- * batch: 1 (default) stages each tile's planes in shared memory with
- * cp.async, 0 reads neighbours with cached global loads). */
+ * batch: 2 (default) stages each tile's planes in shared memory with
+ * cp.async and updates two x-adjacent voxels per thread, 1 the same with one
+ * voxel per thread, 0 reads neighbours with cached global loads). */
 int tam_set_tuning(struct tam_ctx *ctx, const char *key, int64_t value);
 /*
  * Batches of independent instances (no reference counterpart: the reference

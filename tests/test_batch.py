@@ -163,13 +163,13 @@ def test_batch_device_path_with_mc_passes(tam):
 
 @pytest.mark.parametrize("zchunk", [0, 1, 7])
 def test_batch_staged_matches_cached_loads(tam, zchunk):
-    # the two forms of the batched step (planes staged in shared memory by
-    # cp.async; neighbours by cached global loads) on odd, layered and uniform
-    # instances, with z-chunks of one plane (items of three slots), a ragged
-    # last chunk and the default
+    # the three forms of the batched step (neighbours by cached global loads;
+    # planes staged in shared memory by cp.async, one voxel or a pair of
+    # voxels per thread) on odd, layered and uniform instances, with z-chunks
+    # of one plane, a ragged last chunk and the default
     F = tam._abi
     res = []
-    for staged in (0, 1):
+    for staged in (0, 1, 2):
         ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
         try:
             for c in ctxs:
@@ -180,8 +180,9 @@ def test_batch_staged_matches_cached_loads(tam, zchunk):
         finally:
             for c in ctxs:
                 c.close()
-    for (Ta, Oa, ea), (Tb, Ob, eb) in zip(*res):
-        assert ea == eb == 0
-        assert (Tb - 310.15).max() > 0.5
-        assert np.abs(Ta - Tb).max() <= 1e-4
-        assert np.abs(Oa - Ob).max() <= 1e-4 * max(Ob.max(), 1e-30)
+    for form in res[1:]:
+        for (Ta, Oa, ea), (Tb, Ob, eb) in zip(res[0], form):
+            assert ea == eb == 0
+            assert (Tb - 310.15).max() > 0.5
+            assert np.abs(Ta - Tb).max() <= 1e-4
+            assert np.abs(Oa - Ob).max() <= 1e-4 * max(Ob.max(), 1e-30)

@@ -390,7 +390,7 @@ def test_writer_files(tam, orc, tmp_path):
 
 
 # ------------------------------------------- class-table fused heat step --
-def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats, rows=2):
+def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats, rows=2, tma=1):
     half = 0.0025 * nx  # cm: 50 um voxels
     p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half * ny / nx, zmax=half * nz / nx, mode=1,
                            precision=precision, pulse_type=1, power=1.0, energy_per_pixel=1e6, total_time=10.0)
@@ -400,17 +400,20 @@ def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats, rows=2
     ctx = tam.Context(p, c)
     ctx.set_tuning("heat.cls", cls)
     ctx.set_tuning("heat.cls_rows", rows)
+    ctx.set_tuning("heat.tma", tma)
     ctx.upload(F.TAM_F_MATERIAL, grid)
     ctx.upload(F.TAM_F_JMEAN_GLOBAL, J)
     return ctx
 
 
-@pytest.mark.parametrize("nx", [44, 48])
+@pytest.mark.parametrize("nx", [44, 45, 48])
 def test_fused_class_table_matches_coefficient_arrays(tam, nx):
     # three thermal materials in slabs plus an inclusion; the class-table step
     # (face coefficients looked up per class pair) against the per-voxel
     # coefficient arrays (same FP32 + Kahan arithmetic up to the rounding of
-    # the coefficients) and against FP64
+    # the coefficients) and against FP64.  Rows of 45 voxels are not 16-byte
+    # aligned, so every class-table case there runs the cp.async-staged step;
+    # "stg" runs that step on every size (TMA off).
     ny, nz = 40, 36
     mats = [(0.026, 1.2, 1005.0), (0.56, 1070.0, 3400.0), (0.21, 911.0, 2348.0), (0.47, 1090.0, 3421.0)]
     grid = np.ones((nx, ny, nz), dtype=np.uint8, order="F")
@@ -423,9 +426,9 @@ def test_fused_class_table_matches_coefficient_arrays(tam, nx):
     alpha = max(k / (r * c) for k, r, c in mats[1:])
     dt = 0.9 / (2 * alpha * 3 / d ** 2)
     out = {}
-    for name, prec, cls, rows in (("cls", 1, 1, 2), ("cls1", 1, 1, 1), ("cls0", 1, 1, 0), ("arr", 1, 0, 1),
-                                  ("f64", 0, 1, 1)):
-        ctx = _layered_heat_ctx(tam, nx, ny, nz, prec, cls, dt, J, grid, mats, rows)
+    for name, prec, cls, rows, tma in (("cls", 1, 1, 2, 1), ("cls1", 1, 1, 1, 1), ("cls0", 1, 1, 0, 1),
+                                       ("arr", 1, 0, 1, 1), ("f64", 0, 1, 1, 1), ("stg", 1, 1, 0, 0)):
+        ctx = _layered_heat_ctx(tam, nx, ny, nz, prec, cls, dt, J, grid, mats, rows, tma)
         T = ctx.heat_steps(300, want=True)
         out[name] = (T, ctx.download(F.TAM_F_TISSUE), ctx.device_errors())
         ctx.close()
@@ -436,6 +439,8 @@ def test_fused_class_table_matches_coefficient_arrays(tam, nx):
     assert np.abs(out["cls1"][0] - out["cls"][0]).max() <= 1e-5
     assert np.abs(out["cls0"][0] - out["cls1"][0]).max() <= 1e-5 and out["cls0"][2] == 0
     assert np.abs(out["cls"][0] - out["f64"][0]).max() <= 1e-3
+    assert np.abs(out["stg"][0] - out["cls"][0]).max() <= 1e-4 and out["stg"][2] == 0
+    assert np.abs(out["stg"][1] - out["cls"][1]).max() <= 1e-4 * max(out["cls"][1].max(), 1e-30)
 
 
 def test_fused_class_table_off_after_per_voxel_properties(tam):

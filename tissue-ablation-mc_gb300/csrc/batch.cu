@@ -422,6 +422,302 @@ __global__ void __launch_bounds__(FX *FY, TAM_STAGED_MINB)
     }
 }
 
+// ------------------------------------------- staged step, voxel pairs --
+// The staged step with 128 threads per 32 x 8 tile, each updating two
+// x-adjacent voxels: 64-bit shared-memory loads of a pair's own, y- and
+// z-neighbour values and J, its inner x-neighbours from registers.  The
+// stage layout and the ring are those of the one-voxel form.
+struct Offs2 {
+    int own, ext, c;
+    int sx;  // halo (floats) in bits 0-15, class chunk (bytes) in bits 16-30
+    int next, n1;  // halo elements (0, 1 or 2); second own voxel present
+};
+
+__device__ __forceinline__ Offs2 offsets2_for(int nx, int ny, int cp, bool uni, const Item &it, int tp, int ty)
+{
+    Offs2 o;
+    const int tx = 2 * tp, x = it.x0 + tx, y = it.y0 + ty;
+    int s_ext = 0, s_c = 0;
+    o.own = (x < nx && y < ny) ? x + nx * y : -1;
+    o.n1 = x + 1 < nx;
+    o.ext = -1;
+    o.next = 0;
+    if (ty == 0 || ty == 1) {
+        const int yy = ty == 0 ? it.y0 - 1 : it.y0 + FY;
+        if (yy >= 0 && yy < ny && x < nx) {
+            o.ext = x + nx * yy;
+            o.next = x + 1 < nx ? 2 : 1;
+            s_ext = (ty == 0 ? 0 : (FY + 1) * AP) + tx + 4;
+        }
+    } else if ((ty == 2 || ty == 3) && tp >= 1 && tp <= FY) {
+        const int yy = it.y0 - 1 + tp;
+        if (ty == 2 && it.x0 > 0 && yy < ny) o.ext = it.x0 - 1 + nx * yy, o.next = 1, s_ext = tp * AP + 3;
+        if (ty == 3 && it.x0 + FX < nx && yy < ny) o.ext = it.x0 + FX + nx * yy, o.next = 1, s_ext = tp * AP + FX + 4;
+    }
+    o.c = -1;
+    const int q = (ty - 4) * (FX / 2) + tp;
+    if (!uni && q >= 0 && q < AR * 4) {
+        const int r = q >> 2, ch = q & 3;
+        const int yy = it.y0 - 1 + r, xb = it.x0 - 16 + 16 * ch;
+        if (yy >= 0 && yy < ny && xb >= 0 && xb + 16 <= cp) o.c = xb + cp * yy, s_c = r * ACP + 16 * ch;
+    }
+    o.sx = s_ext | s_c << 16;
+    return o;
+}
+
+__device__ __forceinline__ void issue_plane2(const Src &d, const Offs2 &o, int p, unsigned char *b, int tp, int ty)
+{
+    const int zz = d.z0 - 1 + p;
+    if (p <= d.np + 1 && zz >= 0 && zz < d.nz) {
+        const int po = d.sz * zz;
+        float *bT = (float *)(b + A_T), *bE = (float *)(b + A_E);
+        if (o.own >= 0) {
+            const int so = (ty + 1) * AP + 2 * tp + 4;
+            const float *gT = d.T + po + o.own, *gE = d.E + po + o.own;
+            async4(bT + so, gT);
+            async4(bE + so, gE);
+            if (o.n1) {
+                async4(bT + so + 1, gT + 1);
+                async4(bE + so + 1, gE + 1);
+            }
+            if (d.jon && p >= 1 && p <= d.np) {
+                float *bJ = (float *)(b + A_J) + ty * FX + 2 * tp;
+                const float *gJ = d.J + po + o.own;
+                async4(bJ, gJ);
+                if (o.n1) async4(bJ + 1, gJ + 1);
+            }
+        }
+        if (o.next) {
+            const int se = o.sx & 0xffff;
+            const float *gT = d.T + po + o.ext, *gE = d.E + po + o.ext;
+            async4(bT + se, gT);
+            async4(bE + se, gE);
+            if (o.next == 2) {
+                async4(bT + se + 1, gT + 1);
+                async4(bE + se + 1, gE + 1);
+            }
+        }
+        if (o.c >= 0) async16(b + A_C + (o.sx >> 16), d.C + d.csz * zz + o.c);
+    }
+    async_commit();
+}
+
+#ifndef TAM_PAIRS_MINB
+#define TAM_PAIRS_MINB 4  // 125 registers: more resident blocks spill, and spills cost more than warps
+#endif
+// GRID: K steps of every instance (persistent cooperative launch).  !GRID:
+// one step of one instance, one block per item; the step (`one`) and the
+// buffer pair it reads (`one_fcur`) come as parameters.
+template <bool GRID>
+__global__ void __launch_bounds__(FX / 2 * FY, TAM_PAIRS_MINB)
+    batch_pairs_kernel(const BatchInst *__restrict__ insts, int n, const int *__restrict__ prefix,
+                       const BatchStep *__restrict__ steps, int K, BatchSync *sync, unsigned *err, BatchStep one,
+                       int one_fcur)
+{
+    extern __shared__ unsigned char smem_raw[];
+    __shared__ __align__(16) unsigned char s_args_raw[sizeof(FusedArgs)];
+    __shared__ __align__(16) unsigned char s_lut_raw[sizeof(ClassLut)];
+    __shared__ Src d;
+    const FusedArgs &A = *reinterpret_cast<const FusedArgs *>(s_args_raw);
+    const ClassLut &L = *reinterpret_cast<const ClassLut *>(s_lut_raw);
+    unsigned char *sm = smem_raw + ((128 - ((unsigned)__cvta_generic_to_shared(smem_raw) & 127)) & 127);
+    const int tp = threadIdx.x, ty = threadIdx.y, tid = ty * (FX / 2) + tp;
+    const int total = __ldg(prefix + n);
+    const int stride = GRID ? (int)gridDim.x : total;
+    int loaded = -1;
+    for (int k = 0; k < K; ++k) {
+        for (int item = blockIdx.x; item < total; item += stride) {
+            const Item it = item_at(insts, n, prefix, item);
+            const BatchStep st = GRID ? steps[(int64_t)k * n + it.inst] : one;
+            if (!st.active) continue;  // block-uniform
+            const BatchInst &I = insts[it.inst];
+            // every thread finished the previous item (its last barrier)
+            if (it.inst != loaded) {
+                for (int w = tid; w < ARGS_WORDS; w += FX / 2 * FY)
+                    ((uint32_t *)s_args_raw)[w] = ((const uint32_t *)&I.a)[w];
+                for (int w = tid; w < LUT_WORDS; w += FX / 2 * FY)
+                    ((uint32_t *)s_lut_raw)[w] = ((const uint32_t *)&I.L)[w];
+                loaded = it.inst;
+            }
+            if (tid == 0) {
+                const int fc = ((GRID ? I.fcur : one_fcur) + k) & 1;
+                d.T = I.T[fc];
+                d.E = I.E[fc];
+                d.To = I.T[fc ^ 1];
+                d.Eo = I.E[fc ^ 1];
+                d.J = (const float *)I.a.J;
+                d.C = I.cls;
+                d.nx = I.a.nx;
+                d.ny = I.a.ny;
+                d.sz = I.a.nx * I.a.ny;
+                d.csz = I.cls_pitch * I.a.ny;
+                d.nz = I.a.nz;
+                d.z0 = it.z0;
+                d.np = it.z1 - it.z0;
+                d.jon = st.pdt != 0.f;
+                d.pdt = st.pdt;
+                d.t_new = st.t_new;
+            }
+            const int uc = I.L.uniform;
+            const Offs2 o = offsets2_for(I.a.nx, I.a.ny, I.cls_pitch, uc >= 0, it, tp, ty);
+            __syncthreads();  // the item's description is visible
+#pragma unroll 1
+            for (int p = 0; p < AD; ++p) issue_plane2(d, o, p, sm + p * A_STAGE, tp, ty);
+            async_wait<AD - 2>();
+            __syncthreads();  // planes 0 and 1 (and the instance's tables) are visible to the block
+            const int tx = 2 * tp, x = it.x0 + tx, y = it.y0 + ty;
+            const bool in0 = o.own >= 0, in1 = in0 && o.n1;
+            const int q = (ty + 1) * AP + tx + 4, qc = (ty + 1) * ACP + tx + 16, oj = ty * FX + tx;
+            auto cls2 = [&](const unsigned char *b, int &k0, int &k1) {
+                const unsigned short w = *reinterpret_cast<const unsigned short *>(b + A_C + qc);
+                k0 = w & (MAX_MAT - 1);
+                k1 = (w >> 8) & (MAX_MAT - 1);
+            };
+            float2 Tp = {0.f, 0.f}, ep = {0.f, 0.f}, Tc = {0.f, 0.f}, ec = {0.f, 0.f};
+            int kp0 = uc, kp1 = uc, kc0 = uc, kc1 = uc;
+            if (in0) {
+                if (it.z0 > 0) {
+                    Tp = *reinterpret_cast<const float2 *>((const float *)(sm + A_T) + q);
+                    ep = *reinterpret_cast<const float2 *>((const float *)(sm + A_E) + q);
+                    if (uc < 0) cls2(sm, kp0, kp1);
+                }
+                Tc = *reinterpret_cast<const float2 *>((const float *)(sm + A_STAGE + A_T) + q);
+                ec = *reinterpret_cast<const float2 *>((const float *)(sm + A_STAGE + A_E) + q);
+                if (uc < 0) cls2(sm + A_STAGE, kc0, kc1);
+            }
+            int v = x + d.nx * y + d.sz * it.z0;
+            unsigned errbits = 0;
+            int si = AD % AS, sc = 1, sn = 2;  // stages: next issue, plane z, plane z+1
+            for (int i = 0; i < d.np; ++i, v += d.sz) {
+                issue_plane2(d, o, i + AD, sm + si * A_STAGE, tp, ty);
+                async_wait<AD - 2>();
+                __syncthreads();  // plane z+1 has landed for the whole block
+                const unsigned char *P = sm + sc * A_STAGE, *N = sm + sn * A_STAGE;
+                const int z = it.z0 + i;
+                const bool has_n = z + 1 < d.nz;
+                float2 Tn = {0.f, 0.f}, en = {0.f, 0.f};
+                int kn0 = uc, kn1 = uc;
+                if (in0 && has_n) {
+                    Tn = *reinterpret_cast<const float2 *>((const float *)(N + A_T) + q);
+                    en = *reinterpret_cast<const float2 *>((const float *)(N + A_E) + q);
+                    if (uc < 0) cls2(N, kn0, kn1);
+                }
+                if (in0) {
+                    const float *PT = (const float *)(P + A_T), *PE = (const float *)(P + A_E);
+                    const float2 Ty0 = *reinterpret_cast<const float2 *>(PT + q - AP),
+                                 Ty1 = *reinterpret_cast<const float2 *>(PT + q + AP);
+                    const float2 Ey0 = *reinterpret_cast<const float2 *>(PE + q - AP),
+                                 Ey1 = *reinterpret_cast<const float2 *>(PE + q + AP);
+                    const float Txl = PT[q - 1], Txr = PT[q + 2], Exl = PE[q - 1], Exr = PE[q + 2];
+                    const float2 Jv = d.jon ? *reinterpret_cast<const float2 *>((const float *)(P + A_J) + oj)
+                                            : make_float2(0.f, 0.f);
+                    const float screen = A.fc[FC_SCREEN];
+                    const bool near0 = Tc.x >= screen, near1 = in1 && Tc.y >= screen;
+                    double o_pre[2] = {0.0, 0.0};
+                    if (near0) o_pre[0] = A.omega[v];
+                    if (near1) o_pre[1] = A.omega[v + 1];
+                    const float cx = A.fc[FC_CX], cy = A.fc[FC_CY], cz = A.fc[FC_CZ];
+                    const bool yz_inner = y > 0 && y < d.ny - 1 && z > 0 && has_n;
+                    float Tnew[2], Enew[2];
+                    unsigned hot = 0;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const bool inh = h == 0 || in1;
+                        const int xx = x + h;
+                        const float tc = h ? Tc.y : Tc.x, e0 = h ? ec.y : ec.x;
+                        const float tzm = ((h ? Tp.y : Tp.x) - tc) - ((h ? ep.y : ep.x) - e0);
+                        const float tzp = ((h ? Tn.y : Tn.x) - tc) - ((h ? en.y : en.x) - e0);
+                        const float txm = ((h ? Tc.x : Txl) - tc) - ((h ? ec.x : Exl) - e0);
+                        const float txp = ((h ? Txr : Tc.y) - tc) - ((h ? Exr : ec.y) - e0);
+                        const float tym = ((h ? Ty0.y : Ty0.x) - tc) - ((h ? Ey0.y : Ey0.x) - e0);
+                        const float typ = ((h ? Ty1.y : Ty1.x) - tc) - ((h ? Ey1.y : Ey1.x) - e0);
+                        const int kk = h ? kc1 : kc0;
+                        const float *row = L.fa + kk * MAX_MAT;
+                        float axm, axp, aym, ayp;
+                        if (uc >= 0) {
+                            axm = axp = aym = ayp = row[uc];
+                        } else {
+                            const unsigned char *PC = P + A_C;
+                            axm = row[h ? kc0 : (PC[qc - 1] & (MAX_MAT - 1))];
+                            axp = row[h ? (PC[qc + 2] & (MAX_MAT - 1)) : kc1];
+                            aym = row[PC[qc + h - ACP] & (MAX_MAT - 1)];
+                            ayp = row[PC[qc + h + ACP] & (MAX_MAT - 1)];
+                        }
+                        const float azm = row[h ? kp1 : kp0], azp = row[h ? kn1 : kn0];
+                        float lap;
+                        if (yz_inner && xx > 0 && xx < d.nx - 1) {
+                            lap = (cz * (azm * tzm + azp * tzp) + cy * (aym * tym + ayp * typ)) +
+                                  cx * (axm * txm + axp * txp);
+                        } else {
+                            const unsigned gm = (unsigned)(xx == 0) | (unsigned)(xx >= d.nx - 1) << 1 |
+                                                (unsigned)(y == 0) << 2 | (unsigned)(y == d.ny - 1) << 3 |
+                                                (unsigned)(z == 0) << 4 | (unsigned)(!has_n) << 5;
+                            lap = (cz * ((gm & 16 ? 0.f : azm * tzm) + (gm & 32 ? 0.f : azp * tzp)) +
+                                   cy * ((gm & 4 ? 0.f : aym * tym) + (gm & 8 ? 0.f : ayp * typ))) +
+                                  cx * ((gm & 1 ? 0.f : axm * txm) + (gm & 2 ? 0.f : axp * txp));
+                            if (inh) lap += ghost_sum(A, L, gm, kk, tc, e0);
+                        }
+                        const float dT = A.fc[FC_DT] * lap;
+                        const float sPJ = d.pdt * (h ? Jv.y : Jv.x);
+                        const float srcT = sPJ * L.irc[kk];
+                        float tn = A.fc[FC_TBOIL], en_ = 0.f;
+                        const bool clamped = inh && A.boil && tc >= tn && boil_clamp(A, L, kk, v + h, sPJ, dT);
+                        if (!clamped) {
+                            const float inc = dT + srcT;
+                            const float yk = inc - e0;
+                            const float t = tc + yk;
+                            en_ = (t - tc) - yk;
+                            tn = t;
+                        }
+                        Tnew[h] = tn;
+                        Enew[h] = en_;
+                        const float Ts = tn - en_;
+                        if (inh) {
+                            errbits |= (Ts == Ts) ? (Ts < 0.f ? (unsigned)DEVERR_NEG_T : 0u) : (unsigned)DEVERR_NAN;
+                            if (Ts >= screen) hot |= 1u << h;
+                        }
+                    }
+                    // damage and ablation of the pair's voxels in the window, from one call site
+#pragma unroll 1
+                    for (unsigned m = hot; m; m &= m - 1) {
+                        const int h = __ffs(m) - 1;
+                        rare_update_f32(A, v + h, (int64_t)d.sz * d.nz, h ? Tnew[1] : Tnew[0], h ? Enew[1] : Enew[0],
+                                        d.t_new, h ? near1 : near0, h ? o_pre[1] : o_pre[0]);
+                    }
+                    float *To = d.To, *Eo = d.Eo;
+                    if (in1 && !(v & 1)) {  // 8-byte aligned pair
+                        *reinterpret_cast<float2 *>(To + v) = make_float2(Tnew[0], Tnew[1]);
+                        *reinterpret_cast<float2 *>(Eo + v) = make_float2(Enew[0], Enew[1]);
+                    } else {
+                        To[v] = Tnew[0];
+                        Eo[v] = Enew[0];
+                        if (in1) {
+                            To[v + 1] = Tnew[1];
+                            Eo[v + 1] = Enew[1];
+                        }
+                    }
+                }
+                Tp = Tc;
+                ep = ec;
+                Tc = Tn;
+                ec = en;
+                kp0 = kc0;
+                kp1 = kc1;
+                kc0 = kn0;
+                kc1 = kn1;
+                si = si + 1 == AS ? 0 : si + 1;
+                sc = sn;
+                sn = sn + 1 == AS ? 0 : sn + 1;
+                // no barrier here (as in the one-voxel form)
+            }
+            async_wait<0>();
+            __syncthreads();  // the next item rewrites the stages and the instance's tables
+            if (errbits) atomicOr(I.a.err, errbits);
+        }
+        if (GRID && k + 1 < K && !grid_barrier(sync, gridDim.x, err)) return;
+    }
+}
+
 __global__ void __launch_bounds__(FX *FY, 4)
     batch_heat_kernel(const BatchInst *__restrict__ insts, int n, const int *__restrict__ prefix,
                       const BatchStep *__restrict__ steps, int K, BatchSync *sync, unsigned *err)
@@ -559,8 +855,11 @@ cudaError_t batch_heat_blocks(int *blocks, int staged)
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e == cudaSuccess)
-        e = staged ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_staged_kernel<true>, FX * FY, A_SMEM)
-                   : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_heat_kernel, FX * FY, 0);
+        e = staged == 2   ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_pairs_kernel<true>, FX / 2 * FY,
+                                                                          A_SMEM)
+            : staged == 1 ? cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_staged_kernel<true>, FX * FY,
+                                                                          A_SMEM)
+                          : cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, batch_heat_kernel, FX * FY, 0);
     if (e != cudaSuccess) return e;
     *blocks = sms * (per > 0 ? per : 1);
     return cudaSuccess;
@@ -572,21 +871,29 @@ cudaError_t launch_batch_heat(const BatchInst *insts, int n, const int *prefix, 
     if (n <= 0 || K <= 0) return cudaSuccess;
     cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(BatchSync), s);
     if (e != cudaSuccess) return e;
+    BatchStep one{};
+    int one_fcur = 0;
     void *args[] = {(void *)&insts, (void *)&n, (void *)&prefix, (void *)&steps, (void *)&K, (void *)&sync,
                     (void *)&err};
+    void *args2[] = {(void *)&insts, (void *)&n,    (void *)&prefix, (void *)&steps,   (void *)&K,
+                     (void *)&sync,  (void *)&err,  (void *)&one,    (void *)&one_fcur};
     count_launch();
-    if (staged)
+    if (staged == 2)
+        return cudaLaunchCooperativeKernel((const void *)batch_pairs_kernel<true>, dim3(blocks), dim3(FX / 2, FY),
+                                           args2, A_SMEM, s);
+    if (staged == 1)
         return cudaLaunchCooperativeKernel((const void *)batch_staged_kernel<true>, dim3(blocks), dim3(FX, FY), args,
                                            A_SMEM, s);
     return cudaLaunchCooperativeKernel((const void *)batch_heat_kernel, dim3(blocks), dim3(FX, FY), args, 0, s);
 }
 
-cudaError_t launch_staged_step(const BatchInst *inst, const int *prefix, const BatchStep *step, int items,
+cudaError_t launch_staged_step(const BatchInst *inst, const int *prefix, int items, const BatchStep &step, int fcur,
                                cudaStream_t s)
 {
     if (items <= 0) return cudaSuccess;
     count_launch();
-    batch_staged_kernel<false><<<items, dim3(FX, FY), A_SMEM, s>>>(inst, 1, prefix, step, 1, nullptr, nullptr);
+    batch_pairs_kernel<false><<<items, dim3(FX / 2, FY), A_SMEM, s>>>(inst, 1, prefix, nullptr, 1, nullptr, nullptr,
+                                                                       step, fcur);
     return cudaGetLastError();
 }
 

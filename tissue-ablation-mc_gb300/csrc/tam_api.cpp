@@ -102,7 +102,12 @@ struct tam_ctx {
     bool use_cls = true;
     int cls_rows = 0;                // class-table step: 0 = voxel pairs (measured fastest), 1 or 2 rows
     bool arr_fp64 = false;           // FP32 form: FP64 Arrhenius exponent instead of float-float
-    int batch_staged = 1;            // batched steps: planes staged by cp.async (1) or cached global loads (0)
+    int batch_staged = 2;            // batched steps: staged voxel pairs (2), staged voxels (1), cached loads (0)
+    // staged class-table step of this context alone (rows not aligned for TMA)
+    tam::BatchInst *d_sinst = nullptr;
+    int *d_sprefix = nullptr;
+    tam::BatchInst h_sinst{};
+    int s_items = 0;
     tam::FusedCls *fcls = nullptr;
     uint8_t *d_cls = nullptr;
     int cls_pitch = 0;
@@ -648,12 +653,64 @@ int ref_props(tam_ctx *ctx, double ablate_temp)
 }
 
 // --------------------------------------------------------- heat (config) --
+// Default z planes per work item of the staged step: long columns for the
+// batched launch (fewer halo planes; the batch's items fill the device) and
+// shorter ones for one context alone (enough items for every SM).
+constexpr int BATCH_ZCHUNK = 32, SINGLE_ZCHUNK = 8;
+
+// The batched-step description of one context; returns its work items.
+int batch_inst(tam_ctx *c, tam::BatchInst &I, int zdefault)
+{
+    I.a = fused_args(c);
+    tam::fill_fused_consts(I.a);
+    I.L = c->clut;
+    I.cls = c->d_cls;
+    I.cls_pitch = c->cls_pitch;
+    for (int q = 0; q < 2; ++q) {
+        I.T[q] = (float *)c->d_Tf[q];
+        I.E[q] = c->d_Tc[q];
+    }
+    I.fcur = c->fcur;
+    I.tiles_x = (c->nx + tam::FX_TILE - 1) / tam::FX_TILE;
+    I.tiles_y = (c->ny + tam::FY_TILE - 1) / tam::FY_TILE;
+    I.zchunk = c->zchunk > 0 ? c->zchunk : zdefault;
+    return I.tiles_x * I.tiles_y * ((c->nz + I.zchunk - 1) / I.zchunk);
+}
+
+// Device description of this context for the staged class-table step (its
+// rows are not 16-byte aligned for TMA, or TMA is off), rebuilt before each
+// run of steps and copied only when it changed (classes, constants, tuning).
+// The per-step source, time and buffer pair travel as kernel parameters.
+int staged_setup(tam_ctx *ctx)
+{
+    if (!ctx->d_sinst) {
+        RC(dalloc_t(ctx, &ctx->d_sinst, 1));
+        RC(dalloc_t(ctx, &ctx->d_sprefix, 2));
+    }
+    tam::BatchInst I{};
+    const int items = batch_inst(ctx, I, SINGLE_ZCHUNK);
+    I.a.P = 0.0;
+    I.a.t_new = 0.0;
+    I.fcur = 0;
+    if (items != ctx->s_items || std::memcmp(&I, &ctx->h_sinst, sizeof I) != 0) {
+        // pageable sources: the copies take the bytes before they return
+        ctx->h_sinst = I;
+        ctx->s_items = items;
+        const int pre[2] = {0, items};
+        CK(cudaMemcpyAsync(ctx->d_sinst, &ctx->h_sinst, sizeof I, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->d_sprefix, pre, sizeof pre, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    return TAM_OK;
+}
+
 int cfg_heat(tam_ctx *ctx, int32_t nsteps)
 {
     tam::FusedArgs a = fused_args(ctx);
     const int check = ctx->cfg.retrace_check > 0 ? ctx->cfg.retrace_check : 0;
     const bool cls = ctx->fcls && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class;
-    if (!cls && ctx->tma && ctx->use_tma && ctx->coeff_dirty && nsteps > 0) {
+    const bool staged = !cls && !ctx->fp64 && ctx->use_cls && ctx->thermal_by_class && ctx->d_cls;
+    if (staged && nsteps > 0) RC(staged_setup(ctx));
+    if (!cls && !staged && ctx->tma && ctx->use_tma && ctx->coeff_dirty && nsteps > 0) {
         CK(tam::launch_face_coeffs(a, ctx->d_ax, ctx->d_ay, ctx->d_az, ctx->d_irc, ctx->stream));
         ctx->coeff_dirty = false;
     }
@@ -665,8 +722,15 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
         a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[1 - ctx->fcur];
         a.P = ctx->laserOn * get_pwr(ctx);
         a.t_new = ctx->time + ctx->cdt;
-        if (cls) CK(tam::launch_fused_cls(a, ctx->fcls, ctx->fcur, ctx->clut, ctx->cls_rows, ctx->stream));
-        else if (ctx->tma && ctx->use_tma) CK(tam::launch_fused_tma(a, ctx->tma, ctx->fcur, ctx->stream));
+        if (cls) {
+            CK(tam::launch_fused_cls(a, ctx->fcls, ctx->fcur, ctx->clut, ctx->cls_rows, ctx->stream));
+        } else if (staged) {
+            tam::BatchStep st{};
+            st.t_new = a.t_new;
+            st.pdt = (float)(a.P * ctx->cdt);
+            st.active = 1;
+            CK(tam::launch_staged_step(ctx->d_sinst, ctx->d_sprefix, ctx->s_items, st, ctx->fcur, ctx->stream));
+        } else if (ctx->tma && ctx->use_tma) CK(tam::launch_fused_tma(a, ctx->tma, ctx->fcur, ctx->stream));
         else CK(tam::launch_fused_step(a, ctx->fp64, ctx->stream));
         ctx->fcur = 1 - ctx->fcur;
         const bool on = pulse_update(ctx, ctx->cdt);
@@ -1436,31 +1500,13 @@ struct DevBatch {
     }
 };
 
-constexpr int BATCH_ZCHUNK = 16;
 
 int batch_setup(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int kmax)
 {
     tam_ctx *const ctx = ctxs[0];  // CUDA errors are reported on the first instance
     B.inst.resize(n);
     B.prefix.assign(n + 1, 0);
-    for (int32_t i = 0; i < n; ++i) {
-        tam_ctx *c = ctxs[i];
-        tam::BatchInst &I = B.inst[i];
-        I.a = fused_args(c);
-        tam::fill_fused_consts(I.a);
-        I.L = c->clut;
-        I.cls = c->d_cls;
-        I.cls_pitch = c->cls_pitch;
-        for (int q = 0; q < 2; ++q) {
-            I.T[q] = (float *)c->d_Tf[q];
-            I.E[q] = c->d_Tc[q];
-        }
-        I.tiles_x = (c->nx + tam::FX_TILE - 1) / tam::FX_TILE;
-        I.tiles_y = (c->ny + tam::FY_TILE - 1) / tam::FY_TILE;
-        I.zchunk = c->zchunk > 0 ? c->zchunk : BATCH_ZCHUNK;
-        const int chunks = (c->nz + I.zchunk - 1) / I.zchunk;
-        B.prefix[i + 1] = B.prefix[i] + I.tiles_x * I.tiles_y * chunks;
-    }
+    for (int32_t i = 0; i < n; ++i) B.prefix[i + 1] = B.prefix[i] + batch_inst(ctxs[i], B.inst[i], BATCH_ZCHUNK);
     B.kmax = kmax;
     B.steps.resize((size_t)kmax * n);
     B.staged = ctx->batch_staged;
@@ -1799,7 +1845,8 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
     } else if (k == "heat.arrhenius_fp64") {
         ctx->arr_fp64 = value != 0;
     } else if (k == "batch.staged") {
-        ctx->batch_staged = value != 0;
+        if (value < 0 || value > 2) return fail(ctx, TAM_E_INVALID, "batch.staged must be 0, 1 or 2");
+        ctx->batch_staged = (int)value;
     } else if (k == "heat.zchunk") {
         if (value < 0 || value > ctx->nz) return fail(ctx, TAM_E_INVALID, "heat.zchunk must be in 0..nz");
         ctx->zchunk = (int)value;
@@ -2107,9 +2154,11 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
         int best_z = ctx->zchunk, best_r = ctx->cls_rows;
         float best_ms = 1e30f;
         const bool cls = ctx->fcls && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class;
+        const bool staged = !cls && !ctx->fp64 && ctx->use_cls && ctx->thermal_by_class && ctx->d_cls;
+        const std::vector<int> zcs = staged ? std::vector<int>{4, 8, 16, 32} : std::vector<int>{2, 3, 4, 8, 16};
         for (int rows : {0, 1}) {
             if (rows == 0 && !cls) continue;
-            for (int zc : {2, 3, 4, 8, 16}) {
+            for (int zc : zcs) {
                 if (zc > ctx->nz) continue;
                 ctx->zchunk = zc;
                 ctx->cls_rows = rows;

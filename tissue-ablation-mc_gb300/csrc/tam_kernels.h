@@ -213,16 +213,18 @@ struct BatchSync {
     unsigned count, gen, abort;
 };
 // Resident blocks of the batched kernel on the current device (its grid size);
-// staged: the cp.async form that stages planes in shared memory, else the
-// form that reads neighbours with cached global loads.
+// staged: 2 = planes staged in shared memory by cp.async, a pair of voxels
+// per thread; 1 = the same with one voxel per thread; 0 = neighbours read
+// with cached global loads.
 cudaError_t batch_heat_blocks(int *blocks, int staged);
 // K steps of every instance; prefix[i] = first work item of instance i,
 // prefix[n] = total work items; steps is K x n (step-major).
 cudaError_t launch_batch_heat(const BatchInst *insts, int n, const int *prefix, const BatchStep *steps, int K,
                               BatchSync *sync, unsigned *err, int blocks, int staged, cudaStream_t s);
-// One step of one instance by the staged kernel, one block per work item
-// (prefix = {0, items}); any row pitch.
-cudaError_t launch_staged_step(const BatchInst *inst, const int *prefix, const BatchStep *step, int items,
+// One step of one instance (inst: device copy of its BatchInst) by the staged
+// voxel-pair kernel, one block per work item (prefix = {0, items}); any row
+// pitch.  fcur selects the buffer pair read by the step.
+cudaError_t launch_staged_step(const BatchInst *inst, const int *prefix, int items, const BatchStep &step, int fcur,
                                cudaStream_t s);
 
 // Halo (reference-layout) FP64 temperature from the interior state, with
