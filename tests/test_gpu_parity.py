@@ -501,3 +501,26 @@ def test_autotune_restores_state(tam):
         assert st.time == t0 and st.mc_passes == passes0
         ctx.step_coupled(2, seed=2)  # the tuned context keeps running
         assert ctx.device_errors() == 0
+
+
+def test_fp32_tally_flushed_matches_fp64_tally(tam):
+    # FP32 transport with deposits into the FP32 tally, flushed into the FP64
+    # jmean every 30000 packets (four flushes), against FP64 deposits on the
+    # same Philox streams: only the rounding of the accumulation differs
+    nx = 40
+    half = 0.0025 * nx
+    p = tam.default_params(nxg=nx, nyg=nx, nzg=nx, xmax=half, ymax=half, zmax=half, mode=1, precision=1,
+                           nphotons=100000)
+    out = []
+    for t32 in (0, 1):
+        with tam.Context(p, tam.default_config(source_radius=0.03)) as ctx:
+            ctx.set_tuning("transport.tally32", t32)
+            ctx.set_tuning("transport.tally32_chunk", 30000)
+            J = ctx.mc_pass(100000, seed=4, stream=1, want=True)
+            out.append((J, ctx.tallies(), ctx.device_errors()))
+    (Ja, ta, ea), (Jb, tb, eb) = out
+    assert ea == eb == 0
+    assert ta["voxel_steps"] == tb["voxel_steps"] and ta["scatters"] == tb["scatters"]
+    assert np.abs(Ja - Jb).sum() / np.abs(Ja).sum() < 1e-6
+    sig = Ja > 1e-3 * Ja.max()
+    assert (np.abs(Ja - Jb)[sig] / Ja[sig]).max() < 1e-4

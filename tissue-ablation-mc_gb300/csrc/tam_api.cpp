@@ -7,6 +7,7 @@
 // res/input.params reader (src/mcpolar.f90:79-94) and the writer
 // (src/writer.f90:6-81).  All grid work runs in the sm_103a kernels; there
 // is no CPU fallback.
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -92,6 +93,9 @@ struct tam_ctx {
 
     // tuning knobs
     int scat_min = 20;
+    int tally32 = -1;                // FP32 transport: -1 auto (FP32 tally when the FP64 one exceeds 256 MB), 0 off, 1 on
+    int64_t tally32_chunk = (int64_t)1 << 24;  // packets per flush of the FP32 tally (each launch ends in a tail)
+    float *d_j32 = nullptr;
     int zchunk = 0;
     bool use_tma = true;
     tam::FusedTma *tma = nullptr;  // tensor maps of the FP32 fused step
@@ -545,10 +549,29 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream)
     a.tally = ctx->d_tally;
     a.work = ctx->d_work;
     a.err = ctx->d_err;
+    // FP32 tally for grids whose FP64 tally is far larger than L2: deposits in
+    // FP32, flushed into the FP64 jmean after every chunk of packets, so each
+    // voxel's FP32 partial sum stays short
+    const bool t32 = !ctx->fp64 && (ctx->tally32 > 0 || (ctx->tally32 < 0 && ctx->ni * 8 > ((int64_t)256 << 20)));
+    if (t32 && !ctx->d_j32) {
+        RC(dalloc_t(ctx, &ctx->d_j32, ctx->ni));
+        CK(cudaMemsetAsync(ctx->d_j32, 0, ctx->ni * sizeof(float), s));
+    }
+    a.jmean32 = t32 ? ctx->d_j32 : nullptr;
     CK(cudaMemsetAsync(ctx->d_jmean, 0, ctx->ni * sizeof(double), s));
     CK(cudaMemsetAsync(ctx->d_tally, 0, tam::N_TALLY * sizeof(double), s));
     CK(cudaEventRecord(ctx->ev[0], s));
-    CK(tam::launch_transport(a, ctx->fp64, ctx->sm_count, s));
+    if (t32) {
+        // chunks of packets with their global ids: the same Philox streams as one launch
+        for (int64_t p0 = 0; p0 < n; p0 += ctx->tally32_chunk) {
+            a.p0 = p0;
+            a.n = std::min(ctx->tally32_chunk, n - p0);
+            CK(tam::launch_transport(a, ctx->fp64, ctx->sm_count, s));
+            CK(tam::launch_flush_f32(ctx->d_jmean, ctx->d_j32, ctx->ni, s));
+        }
+    } else {
+        CK(tam::launch_transport(a, ctx->fp64, ctx->sm_count, s));
+    }
     CK(cudaEventRecord(ctx->ev[1], s));
     ctx->have_mc_time = true;
     CK(tam::launch_sum_f64(ctx->d_jmean, ctx->ni, ctx->d_tally + tam::T_ABSORBED, s));
@@ -1835,6 +1858,12 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
     if (k == "transport.scat_min") {
         if (value < 1 || value > 32) return fail(ctx, TAM_E_INVALID, "transport.scat_min must be in 1..32");
         ctx->scat_min = (int)value;
+    } else if (k == "transport.tally32") {
+        if (value < -1 || value > 1) return fail(ctx, TAM_E_INVALID, "transport.tally32 must be -1 (auto), 0 or 1");
+        ctx->tally32 = (int)value;
+    } else if (k == "transport.tally32_chunk") {
+        if (value < 1) return fail(ctx, TAM_E_INVALID, "transport.tally32_chunk must be positive");
+        ctx->tally32_chunk = value;
     } else if (k == "heat.tma") {
         ctx->use_tma = value != 0;
     } else if (k == "heat.cls") {

@@ -54,6 +54,7 @@ struct TransportArgs {
     int32_t scat_min;                 // lanes that must wait before a warp scatters (0: default)
     int32_t uniform_id;               // >= 0: every voxel holds this material (no per-cell fetch)
     double *jmean;                    // interior, packet units (sum of w*d*mua)
+    float *jmean32;                   // non-null: deposits go here in FP32 (the host flushes them into jmean)
     double *tally;                    // N_TALLY doubles
     unsigned long long *work;         // dynamic packet counter (zeroed by the launcher)
     unsigned *err;                    // device error word
@@ -61,6 +62,9 @@ struct TransportArgs {
 
 // Launch the transport kernel in FP32 (fp64 == false) or FP64.
 cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cudaStream_t s);
+
+// acc[q] += (double)part[q], part[q] = 0 for q < n (flush of an FP32 tally).
+cudaError_t launch_flush_f32(double *acc, float *part, int64_t n, cudaStream_t s);
 
 // out[q] = in[q] * f for q < n; in is then zeroed when zero_in is set.
 cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s);

@@ -172,6 +172,16 @@ template <typename Real> __device__ __forceinline__ Real fresnel(Real n1, Real n
     return (Real)0.5 * (rs * rs + rp * rp);
 }
 
+// Tally update of one voxel visit: an FP64 reduction into jmean (L2-resident
+// for grids up to ~16 M voxels), or an FP32 reduction into the half-size
+// scratch tally that the host flushes into jmean every few million packets
+// (grids whose FP64 tally is far larger than L2).
+template <typename Real> __device__ __forceinline__ void deposit(const TransportArgs &a, int cidx, Real dep)
+{
+    if (a.jmean32) atomicAdd(a.jmean32 + cidx, (float)dep);
+    else atomicAdd(a.jmean + cidx, (double)dep);
+}
+
 template <typename Real> __device__ __forceinline__ Real clamp0h(Real f, Real h)
 {
     return f < (Real)0 ? (Real)0 : (f > h ? h : f);
@@ -380,7 +390,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
         // -------------------------- one voxel step (src/inttau2.f90:37-63) --
         if (mode == M_FLY) {
             if (++nsteps > max_steps) {
-                if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
+                if (dep != (Real)0) deposit(a, cidx, dep);
                 dep = (Real)0;
                 atomicAdd(a.tally + T_OVERFLOW, 1.0);
                 atomicOr(&s_err, (unsigned)DEVERR_STEP_CAP);
@@ -418,7 +428,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     const int sg = cx ? sgx : (cy ? sgy : sgz);
                     const int j = (cx ? ix : (cy ? iy : iz)) + sg;
                     const int N = cx ? NX : (cy ? NY : NZ);
-                    atomicAdd(a.jmean + cidx, (double)dep);
+                    deposit(a, cidx, dep);
                     dep = (Real)0;
                     if ((unsigned)j < (unsigned)N) {
                         // step into the next cell (branch-free over the axis); the
@@ -567,7 +577,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     if (!die) mode = M_FLY;
                 }
                 if (die) {
-                    if (dep != (Real)0) atomicAdd(a.jmean + cidx, (double)dep);
+                    if (dep != (Real)0) deposit(a, cidx, dep);
                     dep = (Real)0;
                     atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
                     mode = M_DEAD;
@@ -605,6 +615,17 @@ __global__ void scale_f32_kernel(float *out, double *in, double f, int64_t n, in
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
         out[q] = (float)(in[q] * f);
         if (zero_in) in[q] = 0.0;
+    }
+}
+
+__global__ void flush_f32_kernel(double *acc, float *part, int64_t n)
+{
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const float v = part[q];
+        if (v != 0.f) {
+            acc[q] += (double)v;
+            part[q] = 0.f;
+        }
     }
 }
 
@@ -672,6 +693,14 @@ cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool 
     if (n <= 0) return cudaSuccess;
     count_launch();
     scale_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_flush_f32(double *acc, float *part, int64_t n, cudaStream_t s)
+{
+    if (n <= 0) return cudaSuccess;
+    count_launch();
+    flush_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(acc, part, n);
     return cudaGetLastError();
 }
 
