@@ -261,6 +261,9 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * the default; 1 or 2 = that many voxel rows per thread),
  * "heat.arrhenius_fp64" (FP32 form: 1 evaluates the Arrhenius exponent
  * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits),
+ * "batch.zchunk" (batched heat steps, read from the first context of the
+ * batch: z planes per work item; 0 (default) uses each instance's
+ * "heat.zchunk" if set, else 32),
  * "batch.staged" (batched heat steps, read from the first context of the
  * batch: 2 (default) stages each tile's planes in shared memory with
  * cp.async and updates two x-adjacent voxels per thread, 1 the same with one
@@ -308,6 +311,12 @@ int tam_load_state(struct tam_ctx *ctx, const char *path);
  * chosen (nullable) receives up to nchosen values: scat_min, zchunk, cls_rows.
  */
 int tam_autotune(struct tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, int32_t nchosen);
+/* Autotuner of the batched heat step: times `steps` batched steps of the n
+ * contexts (as tam_batch_heat_steps requires them) for each candidate form
+ * and z-chunk length ("batch.staged" 2 or 1, "batch.zchunk" 8..64), keeps the
+ * fastest on ctxs[0] (whose settings the batch reads) and puts every
+ * instance's state back.  chosen (nullable): staged form, z-chunk. */
+int tam_batch_autotune(struct tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *chosen, int32_t nchosen);
 
 /* Kernels this library has launched in this process (all contexts). */
 int64_t tam_kernel_launches(void);

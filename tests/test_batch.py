@@ -186,3 +186,24 @@ def test_batch_staged_matches_cached_loads(tam, zchunk):
             assert (Tb - 310.15).max() > 0.5
             assert np.abs(Ta - Tb).max() <= 1e-4
             assert np.abs(Oa - Ob).max() <= 1e-4 * max(Ob.max(), 1e-30)
+
+
+def test_batch_autotune_restores_state(tam):
+    # the batch autotuner times forms and z-chunks on the instances, keeps the
+    # fastest and leaves every instance's fields and clock as they were
+    F = tam._abi
+    ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
+    try:
+        tam.batch_heat_steps(ctxs, 5)
+        before = [(c.download(F.TAM_F_TEMP), c.download(F.TAM_F_TISSUE), c.state().time) for c in ctxs]
+        chosen = tam.batch_autotune(ctxs, steps=8)
+        assert chosen["batch.staged"] in (1, 2) and chosen["batch.zchunk"] in (8, 16, 32, 64)
+        for c, (T, om, t) in zip(ctxs, before):
+            np.testing.assert_array_equal(c.download(F.TAM_F_TEMP), T)
+            np.testing.assert_array_equal(c.download(F.TAM_F_TISSUE), om)
+            assert c.state().time == t
+        tam.batch_heat_steps(ctxs, 5)  # the tuned batch keeps running
+        assert all(c.device_errors() == 0 for c in ctxs)
+    finally:
+        for c in ctxs:
+            c.close()

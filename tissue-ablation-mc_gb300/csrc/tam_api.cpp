@@ -8,10 +8,12 @@
 // (src/writer.f90:6-81).  All grid work runs in the sm_103a kernels; there
 // is no CPU fallback.
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <memory>
 #include <sstream>
 #include <string>
 #include <thread>
@@ -107,6 +109,7 @@ struct tam_ctx {
     int cls_rows = 0;                // class-table step: 0 = voxel pairs (measured fastest), 1 or 2 rows
     bool arr_fp64 = false;           // FP32 form: FP64 Arrhenius exponent instead of float-float
     int batch_staged = 2;            // batched steps: staged voxel pairs (2), staged voxels (1), cached loads (0)
+    int batch_zchunk = 0;            // batched steps: z planes per work item (0: heat.zchunk, else the default)
     // staged class-table step of this context alone (rows not aligned for TMA)
     tam::BatchInst *d_sinst = nullptr;
     int *d_sprefix = nullptr;
@@ -682,7 +685,9 @@ int ref_props(tam_ctx *ctx, double ablate_temp)
 constexpr int BATCH_ZCHUNK = 32, SINGLE_ZCHUNK = 8;
 
 // The batched-step description of one context; returns its work items.
-int batch_inst(tam_ctx *c, tam::BatchInst &I, int zdefault)
+// z planes per item: zforce if positive, else the context's heat.zchunk if
+// set, else zdefault.
+int batch_inst(tam_ctx *c, tam::BatchInst &I, int zdefault, int zforce = 0)
 {
     I.a = fused_args(c);
     tam::fill_fused_consts(I.a);
@@ -696,7 +701,8 @@ int batch_inst(tam_ctx *c, tam::BatchInst &I, int zdefault)
     I.fcur = c->fcur;
     I.tiles_x = (c->nx + tam::FX_TILE - 1) / tam::FX_TILE;
     I.tiles_y = (c->ny + tam::FY_TILE - 1) / tam::FY_TILE;
-    I.zchunk = c->zchunk > 0 ? c->zchunk : zdefault;
+    I.zchunk = zforce > 0 ? zforce : (c->zchunk > 0 ? c->zchunk : zdefault);
+    if (I.zchunk > c->nz) I.zchunk = c->nz;
     return I.tiles_x * I.tiles_y * ((c->nz + I.zchunk - 1) / I.zchunk);
 }
 
@@ -1529,7 +1535,7 @@ int batch_setup(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int kmax)
     tam_ctx *const ctx = ctxs[0];  // CUDA errors are reported on the first instance
     B.inst.resize(n);
     B.prefix.assign(n + 1, 0);
-    for (int32_t i = 0; i < n; ++i) B.prefix[i + 1] = B.prefix[i] + batch_inst(ctxs[i], B.inst[i], BATCH_ZCHUNK);
+    for (int32_t i = 0; i < n; ++i) B.prefix[i + 1] = B.prefix[i] + batch_inst(ctxs[i], B.inst[i], BATCH_ZCHUNK, ctx->batch_zchunk);
     B.kmax = kmax;
     B.steps.resize((size_t)kmax * n);
     B.staged = ctx->batch_staged;
@@ -1873,6 +1879,9 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
         ctx->cls_rows = (int)value;
     } else if (k == "heat.arrhenius_fp64") {
         ctx->arr_fp64 = value != 0;
+    } else if (k == "batch.zchunk") {
+        if (value < 0 || value > 1 << 20) return fail(ctx, TAM_E_INVALID, "batch.zchunk must be >= 0");
+        ctx->batch_zchunk = (int)value;
     } else if (k == "batch.staged") {
         if (value < 0 || value > 2) return fail(ctx, TAM_E_INVALID, "batch.staged must be 0, 1 or 2");
         ctx->batch_staged = (int)value;
@@ -2208,6 +2217,57 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
     const int64_t v[3] = {ctx->scat_min, ctx->zchunk, ctx->cls_rows};
     for (int32_t i = 0; i < nchosen && i < 3 && chosen; ++i) chosen[i] = v[i];
     return finish(ctx, "tam_autotune");
+}
+
+int tam_batch_autotune(tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *chosen, int32_t nchosen)
+{
+    if (n < 1 || !ctxs || steps < 1) return fail(nullptr, TAM_E_INVALID, "bad batch autotune arguments");
+    for (int32_t i = 0; i < n; ++i)
+        for (int32_t j = 0; j < i; ++j)
+            if (!ctxs[i] || ctxs[j] == ctxs[i]) return fail(nullptr, TAM_E_INVALID, "null or repeated context in batch");
+    if (!batchable(ctxs, n))
+        return fail(nullptr, TAM_E_STATE, "batch autotune needs FP32 config-mode contexts on one device with "
+                                           "thermal properties by material class");
+    tam_ctx *const ctx = ctxs[0];
+    CK(cudaSetDevice(ctx->device));
+    std::vector<std::unique_ptr<Snapshot>> S(n);
+    for (int32_t i = 0; i < n; ++i) {
+        S[i].reset(new Snapshot);
+        RC(snap_take(ctxs[i], *S[i]));
+        CK(cudaStreamSynchronize(ctxs[i]->stream));
+    }
+    const int form0 = ctx->batch_staged, z0 = ctx->batch_zchunk;
+    int best_form = form0, best_z = z0;
+    double best = 1e300;
+    const std::vector<int> active(n, 1);
+    struct Cand {
+        int form, z;
+    };
+    const Cand cands[] = {{2, 8}, {2, 16}, {2, 32}, {2, 64}, {1, 16}, {1, 32}};
+    for (const Cand &c : cands) {
+        ctx->batch_staged = c.form;
+        ctx->batch_zchunk = c.z;
+        DevBatch B;
+        const int K = std::min(batch_chunk(ctxs, n), (int)steps);
+        RC(batch_setup(B, ctxs, n, K));
+        RC(batch_heat_chunk(B, ctxs, n, K, active));  // warm-up (instruction cache, L2)
+        for (int32_t i = 0; i < n; ++i) RC(snap_restore(ctxs[i], *S[i]));
+        const auto t0 = std::chrono::steady_clock::now();
+        for (int32_t done = 0; done < steps; done += K) RC(batch_heat_chunk(B, ctxs, n, std::min(K, steps - done), active));
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        for (int32_t i = 0; i < n; ++i) RC(snap_restore(ctxs[i], *S[i]));
+        if (dt < best) {
+            best = dt;
+            best_form = c.form;
+            best_z = c.z;
+        }
+    }
+    ctx->batch_staged = best_form;
+    ctx->batch_zchunk = best_z;
+    const int64_t v[2] = {best_form, best_z};
+    for (int32_t i = 0; i < nchosen && i < 2 && chosen; ++i) chosen[i] = v[i];
+    for (int32_t i = 0; i < n; ++i) RC(finish(ctxs[i], "tam_batch_autotune"));
+    return TAM_OK;
 }
 
 namespace {

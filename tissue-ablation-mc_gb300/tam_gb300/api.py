@@ -229,6 +229,15 @@ def batch_heat_steps(contexts, nsteps: int) -> None:
     check(lib().tam_batch_heat_steps(hs, n, int(nsteps)))
 
 
+def batch_autotune(contexts, steps: int = 20) -> dict:
+    """Pick the fastest batched-step form and z-chunk on these contexts; their state is restored."""
+    n = len(contexts)
+    hs = (_abi._P * n)(*[c._h for c in contexts])
+    out = (C.c_int64 * 2)()
+    check(lib().tam_batch_autotune(hs, n, int(steps), out, 2))
+    return {"batch.staged": out[0], "batch.zchunk": out[1]}
+
+
 def kernel_launches() -> int:
     return int(lib().tam_kernel_launches())
 
