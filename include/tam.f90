@@ -12,6 +12,8 @@
 !   tam_run                 replaces the whole loop src/mcpolar.f90:148-186
 !   tam_finalize            replaces src/mcpolar.f90:196-205
 !   tam_write_output        replaces src/writer.f90:6-81
+! and, with no reference counterpart: device error word, timing, tuning and
+! the autotuner, and the batches of instances (tam_batch_*).
 ! Arrays are passed as c_loc of the reference's own arrays (FP64,
 ! column-major, halo lower bound 0 where the reference has one).
 !
@@ -171,6 +173,56 @@ module tam_gpu
             import
             type(c_ptr), value :: ctx
             character(kind=c_char), intent(in) :: path(*)
+        end function
+        integer(c_int) function tam_device_errors(ctx, bits) bind(C)
+            import
+            type(c_ptr), value :: ctx
+            integer(c_int32_t), intent(out) :: bits       ! uint32 bit set
+        end function
+        integer(c_int) function tam_get_timing(ctx, transport_ms, heat_ms, heat_launches) bind(C)
+            import
+            type(c_ptr), value :: ctx
+            real(c_double), intent(out) :: transport_ms, heat_ms
+            integer(c_int64_t), intent(out) :: heat_launches
+        end function
+        integer(c_int) function tam_set_tuning(ctx, key, val) bind(C)
+            import
+            type(c_ptr), value :: ctx
+            character(kind=c_char), intent(in) :: key(*)  ! e.g. "heat.zchunk"//c_null_char
+            integer(c_int64_t), value :: val
+        end function
+        integer(c_int) function tam_autotune(ctx, packets, steps, chosen, nchosen) bind(C)
+            import
+            type(c_ptr), value :: ctx
+            integer(c_int64_t), value :: packets
+            integer(c_int32_t), value :: steps, nchosen
+            integer(c_int64_t), intent(out) :: chosen(*)
+        end function
+        ! batches: ctxs is an array of the instances' c_ptr handles
+        integer(c_int) function tam_batch_step_coupled(ctxs, n, iters, seeds) bind(C)
+            import
+            type(c_ptr), intent(in) :: ctxs(*)
+            integer(c_int32_t), value :: n, iters
+            integer(c_int64_t), intent(in) :: seeds(*)    ! the bits of uint64 seeds
+        end function
+        integer(c_int) function tam_batch_heat_steps(ctxs, n, nsteps) bind(C)
+            import
+            type(c_ptr), intent(in) :: ctxs(*)
+            integer(c_int32_t), value :: n, nsteps
+        end function
+        integer(c_int) function tam_batch_run(ctxs, n, seeds, max_iters, iters) bind(C)
+            import
+            type(c_ptr), intent(in) :: ctxs(*)
+            integer(c_int32_t), value :: n
+            integer(c_int64_t), intent(in) :: seeds(*)
+            integer(c_int64_t), value :: max_iters
+            integer(c_int64_t), intent(out) :: iters(*)
+        end function
+        integer(c_int) function tam_batch_autotune(ctxs, n, steps, chosen, nchosen) bind(C)
+            import
+            type(c_ptr), intent(in) :: ctxs(*)
+            integer(c_int32_t), value :: n, steps, nchosen
+            integer(c_int64_t), intent(out) :: chosen(*)
         end function
     end interface
 end module tam_gpu

@@ -172,3 +172,73 @@ def c5(scale=1.0, seed=5, packets=1_000_000_000, steps=100_000):
     cfg = _config(mats, retrace_fraction=1e-9, retrace_check=0)
     return Workload("C5 vessels and inclusions", p, cfg, grid, packets, steps,
                     {"grid": (n, n, n), "cylinders": len(cyl), "spheres": len(sph)})
+
+
+# ------------------------------------------------------------ command line --
+def _run_batch(a) -> None:
+    """Configuration 4 at any instance count: one MC pass per instance, warm-up
+    batched heat steps, then `steps` batched steps timed on the host clock
+    (each batched call returns after the device has finished)."""
+    import time
+
+    ws = c4(n=a.instances, packets=a.packets, steps=a.warm + a.steps)
+    ctxs = [w.context() for w in ws]
+    try:
+        nvox = sum(c.nx * c.ny * c.nz for c in ctxs)
+        for c in ctxs:
+            c.mc_pass(a.packets, seed=1)
+        if a.autotune:
+            print("batch autotune:", api.batch_autotune(ctxs, steps=20), flush=True)
+        if a.warm:
+            api.batch_heat_steps(ctxs, a.warm)
+        t0 = time.perf_counter()
+        api.batch_heat_steps(ctxs, a.steps)
+        dt = time.perf_counter() - t0
+        print(f"C4 batch: {len(ctxs)} instances, {nvox} voxels; {a.steps} batched steps after {a.warm}: "
+              f"{dt * 1e3:.2f} ms = {nvox * a.steps / dt:.3e} voxel updates/s; "
+              f"device errors {sum(c.device_errors() for c in ctxs)}", flush=True)
+    finally:
+        for c in ctxs:
+            c.close()
+
+
+def _run_vessels(a) -> None:
+    """Configuration 5's grid at `scale`: a warm-up MC pass, then one pass of
+    `packets` timed with the library's CUDA events."""
+    w = c5(scale=a.scale, packets=a.packets)
+    with w.context() as ctx:
+        ctx.set_tuning("transport.tally32", a.tally32)
+        ctx.mc_pass(a.warm_packets, seed=1)
+        ctx.mc_pass(a.packets, seed=2)
+        tr, _, _ = ctx.timing()
+        tl = ctx.tallies()
+        n = w.params.nxg
+        print(f"C5 grid {n}^3 (FP64 tally {n ** 3 * 8 / 1e6:.0f} MB), transport.tally32={a.tally32}: "
+              f"{a.packets} packets in {tr:.2f} ms = {a.packets / (tr * 1e-3):.3e} photons/s, "
+              f"{tl['voxel_steps']:.4e} voxel steps = {tl['voxel_steps'] / (tr * 1e-3):.3e} steps/s; "
+              f"device errors {ctx.device_errors()}", flush=True)
+
+
+def main(argv=None) -> None:
+    import argparse
+
+    ap = argparse.ArgumentParser(prog="python -m tam_gb300.workloads",
+                                 description="Run parts of benchmark configurations 4 and 5 and print their timings.")
+    sub = ap.add_subparsers(dest="cmd", required=True)
+    b = sub.add_parser("batch", help="configuration 4: batched heat steps of seeded instances")
+    b.add_argument("--instances", type=int, default=64)
+    b.add_argument("--packets", type=int, default=100_000, help="packets of each instance's MC pass")
+    b.add_argument("--warm", type=int, default=200, help="untimed batched steps first")
+    b.add_argument("--steps", type=int, default=200, help="timed batched steps")
+    b.add_argument("--autotune", action="store_true")
+    v = sub.add_parser("vessels", help="configuration 5: MC transport on the vessel grid")
+    v.add_argument("--scale", type=float, default=1.0, help="grid edge = 512 * scale")
+    v.add_argument("--packets", type=int, default=10_000_000)
+    v.add_argument("--warm-packets", type=int, default=1_000_000)
+    v.add_argument("--tally32", type=int, default=-1, choices=[-1, 0, 1])
+    a = ap.parse_args(argv)
+    (_run_batch if a.cmd == "batch" else _run_vessels)(a)
+
+
+if __name__ == "__main__":
+    main()
