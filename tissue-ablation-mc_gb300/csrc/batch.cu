@@ -234,14 +234,10 @@ __device__ __forceinline__ void issue_plane(const Src &d, const Offs &o, int p, 
 }
 
 // Sum of the ghost terms of the boundary faces in mask gm (bit f = face f).
-__device__ __noinline__ float ghost_sum(const FusedArgs &a, const ClassLut &L, unsigned gm, int kc, float Tc,
-                                        float ec)
+__device__ __forceinline__ float ghost_sum(const FusedArgs &a, const ClassLut &L, unsigned gm, int kc, float Tc,
+                                           float ec)
 {
-    const float kk = L.k[kc], rr = L.rho[kc], hh = L.c[kc];
-    float g = 0.f;
-    for (int f = 0; f < 6; ++f)
-        if (gm >> f & 1u) g += ghost_term<float>(a, f, Tc, ec, kk, rr, hh);
-    return g;
+    return ghost_faces(a, gm, Tc, ec, L.k[kc], L.rho[kc], L.c[kc]);
 }
 
 constexpr int ARGS_WORDS = (int)(sizeof(FusedArgs) / 4), LUT_WORDS = (int)(sizeof(ClassLut) / 4);

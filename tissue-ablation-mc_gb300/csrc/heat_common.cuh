@@ -57,6 +57,17 @@ __device__ __noinline__ Real ghost_term(const FusedArgs &a, int f, Real T, Real 
     return cst<Real>(a, f < 2 ? FC_CX : (f < 4 ? FC_CY : FC_CZ)) * (k / (r * h)) * d;
 }
 
+// Sum of the ghost terms of the boundary faces in mask gm (bit f = face f),
+// one out-of-line call for all of a voxel's boundary faces.
+__device__ __noinline__ float ghost_faces(const FusedArgs &a, unsigned gm, float T, float e, float k, float r,
+                                          float h)
+{
+    float g = 0.f;
+    for (int f = 0; f < 6; ++f)
+        if (gm >> f & 1u) g += ghost_term<float>(a, f, T, e, k, r, h);
+    return g;
+}
+
 // Arrhenius damage (FP64 exponent ln A - Ea/RT, src/3dFD.f90:450-461 with
 // every crossed threshold stamped) and ablation of the optics for one voxel
 // whose new true temperature is Tt.  Kept out of line so that no FP64 work is

@@ -487,9 +487,11 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
 // before the tile, so a pair sits at an even offset).  Per voxel it issues
 // half the shared-memory loads, stores and per-plane work of the one-voxel
 // form.  Needs nx even (the pair never straddles a row end).
-// 6 resident blocks of 128 threads per SM (80 registers) measured fastest
+// 7 resident blocks of 128 threads per SM (72 registers) measured fastest;
+// the boundary faces' ghost terms and the pair's damage updates each go
+// through one out-of-line call site, which keeps the spill at 8 bytes
 #ifndef TAM_CLS2_MINB
-#define TAM_CLS2_MINB 6
+#define TAM_CLS2_MINB 7
 #endif
 template <bool UNIFORM>
 __global__ void __launch_bounds__(FX / 2 * FY, TAM_CLS2_MINB)
@@ -598,6 +600,7 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_CLS2_MINB)
             const float2 Jv = *reinterpret_cast<const float2 *>((const float *)(P + Lay::J_OFF) + o);
             const int64_t v = (int64_t)x + sy * y + sz * z;
             float Tnew[2], Enew[2];
+            unsigned hot = 0;
             // voxels near the damage window: load their damage integrals now so
             // the loads overlap the update below
             const bool near0 = Tc.x >= a.fc[FC_SCREEN], near1 = Tc.y >= a.fc[FC_SCREEN];
@@ -636,13 +639,15 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_CLS2_MINB)
                 if (xx > 0 && xx < a.nx - 1 && y > 0 && y < a.ny - 1 && z > 0 && has_n) {
                     lap = ((azm * tzm + azp * tzp) + (aym * tym + ayp * typ)) + (axm * txm + axp * txp);
                 } else {
-                    const float kk = L.k[k], rr = L.rho[k], hh = L.c[k];
-                    lap = z > 0 ? azm * tzm : ghost_term<float>(a, 4, tc, e0, kk, rr, hh);
-                    lap += has_n ? azp * tzp : ghost_term<float>(a, 5, tc, e0, kk, rr, hh);
-                    lap += y > 0 ? aym * tym : ghost_term<float>(a, 2, tc, e0, kk, rr, hh);
-                    lap += y < a.ny - 1 ? ayp * typ : ghost_term<float>(a, 3, tc, e0, kk, rr, hh);
-                    lap += xx > 0 ? axm * txm : ghost_term<float>(a, 0, tc, e0, kk, rr, hh);
-                    lap += xx < a.nx - 1 ? axp * txp : ghost_term<float>(a, 1, tc, e0, kk, rr, hh);
+                    // boundary faces (bit f: x-, x+, y-, y+, z-, z+) take the ghost
+                    // term, summed by one out-of-line call
+                    const unsigned gm = (unsigned)(xx == 0) | (unsigned)(xx >= a.nx - 1) << 1 | (unsigned)(y == 0) << 2 |
+                                        (unsigned)(y == a.ny - 1) << 3 | (unsigned)(z == 0) << 4 |
+                                        (unsigned)(!has_n) << 5;
+                    lap = ((gm & 16 ? 0.f : azm * tzm) + (gm & 32 ? 0.f : azp * tzp)) +
+                          ((gm & 4 ? 0.f : aym * tym) + (gm & 8 ? 0.f : ayp * typ)) +
+                          ((gm & 1 ? 0.f : axm * txm) + (gm & 2 ? 0.f : axp * txp));
+                    if (inh) lap += ghost_faces(a, gm, tc, e0, L.k[k], L.rho[k], L.c[k]);
                 }
                 const float dT = dt * lap;
                 const float sPJ = Pdt * (h ? Jv.y : Jv.x);
@@ -674,8 +679,15 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_CLS2_MINB)
                 const float Ts = tn - en_;
                 if (inh) {
                     errbits |= (Ts == Ts) ? (Ts < 0.f ? (unsigned)DEVERR_NEG_T : 0u) : (unsigned)DEVERR_NAN;
-                    if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v + h, ni, tn, en_, a.t_new, h ? near1 : near0, o_pre[h]);
+                    if (Ts >= a.fc[FC_SCREEN]) hot |= 1u << h;
                 }
+            }
+            // damage and ablation of the pair's voxels in the window, from one call site
+#pragma unroll 1
+            for (unsigned m = hot; m; m &= m - 1) {
+                const int h = __ffs(m) - 1;
+                rare_update_f32(a, v + h, ni, h ? Tnew[1] : Tnew[0], h ? Enew[1] : Enew[0], a.t_new,
+                                h ? near1 : near0, h ? o_pre[1] : o_pre[0]);
             }
             if (in1) {
                 *reinterpret_cast<float2 *>(To + v) = make_float2(Tnew[0], Tnew[1]);
