@@ -499,7 +499,7 @@ __device__ __forceinline__ void issue_plane2(const Src &d, const Offs2 &o, int p
 }
 
 #ifndef TAM_PAIRS_MINB
-#define TAM_PAIRS_MINB 4  // 125 registers: more resident blocks spill, and spills cost more than warps
+#define TAM_PAIRS_MINB 5  // 96 registers without spills; 6 blocks spill and run 25 % slower
 #endif
 // GRID: K steps of every instance (persistent cooperative launch).  !GRID:
 // one step of one instance, one block per item; the step (`one`) and the
@@ -614,21 +614,22 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_PAIRS_MINB)
                     if (near1) o_pre[1] = A.omega[v + 1];
                     const float cx = A.fc[FC_CX], cy = A.fc[FC_CY], cz = A.fc[FC_CZ];
                     const bool yz_inner = y > 0 && y < d.ny - 1 && z > 0 && has_n;
-                    float Tnew[2], Enew[2];
-                    unsigned hot = 0;
+                    // the pair's Laplacians; boundary faces, the latent-heat clamp and
+                    // the damage update are rare and go through one call site each
+                    float lap[2], tcs[2] = {Tc.x, Tc.y}, e0s[2] = {ec.x, ec.y};
+                    int kks[2] = {kc0, kc1};
+                    unsigned gms = 0;
 #pragma unroll
                     for (int h = 0; h < 2; ++h) {
-                        const bool inh = h == 0 || in1;
                         const int xx = x + h;
-                        const float tc = h ? Tc.y : Tc.x, e0 = h ? ec.y : ec.x;
+                        const float tc = tcs[h], e0 = e0s[h];
                         const float tzm = ((h ? Tp.y : Tp.x) - tc) - ((h ? ep.y : ep.x) - e0);
                         const float tzp = ((h ? Tn.y : Tn.x) - tc) - ((h ? en.y : en.x) - e0);
                         const float txm = ((h ? Tc.x : Txl) - tc) - ((h ? ec.x : Exl) - e0);
                         const float txp = ((h ? Txr : Tc.y) - tc) - ((h ? Exr : ec.y) - e0);
                         const float tym = ((h ? Ty0.y : Ty0.x) - tc) - ((h ? Ey0.y : Ey0.x) - e0);
                         const float typ = ((h ? Ty1.y : Ty1.x) - tc) - ((h ? Ey1.y : Ey1.x) - e0);
-                        const int kk = h ? kc1 : kc0;
-                        const float *row = L.fa + kk * MAX_MAT;
+                        const float *row = L.fa + kks[h] * MAX_MAT;
                         float axm, axp, aym, ayp;
                         if (uc >= 0) {
                             axm = axp = aym = ayp = row[uc];
@@ -640,26 +641,44 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_PAIRS_MINB)
                             ayp = row[PC[qc + h + ACP] & (MAX_MAT - 1)];
                         }
                         const float azm = row[h ? kp1 : kp0], azp = row[h ? kn1 : kn0];
-                        float lap;
                         if (yz_inner && xx > 0 && xx < d.nx - 1) {
-                            lap = (cz * (azm * tzm + azp * tzp) + cy * (aym * tym + ayp * typ)) +
-                                  cx * (axm * txm + axp * txp);
+                            lap[h] = (cz * (azm * tzm + azp * tzp) + cy * (aym * tym + ayp * typ)) +
+                                     cx * (axm * txm + axp * txp);
                         } else {
                             const unsigned gm = (unsigned)(xx == 0) | (unsigned)(xx >= d.nx - 1) << 1 |
                                                 (unsigned)(y == 0) << 2 | (unsigned)(y == d.ny - 1) << 3 |
                                                 (unsigned)(z == 0) << 4 | (unsigned)(!has_n) << 5;
-                            lap = (cz * ((gm & 16 ? 0.f : azm * tzm) + (gm & 32 ? 0.f : azp * tzp)) +
-                                   cy * ((gm & 4 ? 0.f : aym * tym) + (gm & 8 ? 0.f : ayp * typ))) +
-                                  cx * ((gm & 1 ? 0.f : axm * txm) + (gm & 2 ? 0.f : axp * txp));
-                            if (inh) lap += ghost_sum(A, L, gm, kk, tc, e0);
+                            lap[h] = (cz * ((gm & 16 ? 0.f : azm * tzm) + (gm & 32 ? 0.f : azp * tzp)) +
+                                      cy * ((gm & 4 ? 0.f : aym * tym) + (gm & 8 ? 0.f : ayp * typ))) +
+                                     cx * ((gm & 1 ? 0.f : axm * txm) + (gm & 2 ? 0.f : axp * txp));
+                            if (h == 0 || in1) gms |= gm << (8 * h);
                         }
-                        const float dT = A.fc[FC_DT] * lap;
+                    }
+#pragma unroll 1
+                    for (int h = 0; h < 2; ++h)
+                        if ((gms >> (8 * h)) & 0xffu)
+                            (h ? lap[1] : lap[0]) += ghost_sum(A, L, (gms >> (8 * h)) & 0xffu, h ? kc1 : kc0,
+                                                               h ? Tc.y : Tc.x, h ? ec.y : ec.x);
+                    const float dt = A.fc[FC_DT], tboil = A.fc[FC_TBOIL];
+                    float Tnew[2], Enew[2];
+                    unsigned boil = 0, hot = 0;
+#pragma unroll
+                    for (int h = 0; h < 2; ++h)
+                        if ((h == 0 || in1) && A.boil && tcs[h] >= tboil) boil |= 1u << h;
+                    unsigned clamped = 0;
+#pragma unroll 1
+                    for (unsigned m = boil; m; m &= m - 1) {
+                        const int h = __ffs(m) - 1;
+                        if (boil_clamp(A, L, h ? kc1 : kc0, v + h, d.pdt * (h ? Jv.y : Jv.x), dt * (h ? lap[1] : lap[0])))
+                            clamped |= 1u << h;
+                    }
+#pragma unroll
+                    for (int h = 0; h < 2; ++h) {
+                        const float tc = tcs[h], e0 = e0s[h];
                         const float sPJ = d.pdt * (h ? Jv.y : Jv.x);
-                        const float srcT = sPJ * L.irc[kk];
-                        float tn = A.fc[FC_TBOIL], en_ = 0.f;
-                        const bool clamped = inh && A.boil && tc >= tn && boil_clamp(A, L, kk, v + h, sPJ, dT);
-                        if (!clamped) {
-                            const float inc = dT + srcT;
+                        float tn = tboil, en_ = 0.f;
+                        if (!(clamped >> h & 1u)) {
+                            const float inc = dt * lap[h] + sPJ * L.irc[kks[h]];
                             const float yk = inc - e0;
                             const float t = tc + yk;
                             en_ = (t - tc) - yk;
@@ -668,7 +687,7 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_PAIRS_MINB)
                         Tnew[h] = tn;
                         Enew[h] = en_;
                         const float Ts = tn - en_;
-                        if (inh) {
+                        if (h == 0 || in1) {
                             errbits |= (Ts == Ts) ? (Ts < 0.f ? (unsigned)DEVERR_NEG_T : 0u) : (unsigned)DEVERR_NAN;
                             if (Ts >= screen) hot |= 1u << h;
                         }
