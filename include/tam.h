@@ -247,8 +247,8 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
 /* Kernel tuning knobs (no reference counterpart; defaults are tuned for
  * GB300).  Keys: "transport.scat_min" (lanes of a warp that wait at an
  * interaction before the warp scatters, 1..32), "transport.tally32" (FP32
- * transport: -1 (default) deposits into an FP32 tally flushed into the FP64
- * jmean when the FP64 tally exceeds 256 MB, 0 never, 1 always),
+ * config-mode transport: -1 (default) deposits into an FP32 tally flushed
+ * into the FP64 jmean when the FP64 tally exceeds 256 MB, 0 never, 1 always),
  * "transport.tally32_chunk" (packets per flush, default 16777216), "heat.zchunk" (z planes per
  * thread column of the fused step, 0 = automatic), "heat.tma" (1: stage the
  * FP32 fused step's planes with TMA where the row pitch allows, 0: cp.async),

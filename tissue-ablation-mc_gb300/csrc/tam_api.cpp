@@ -555,7 +555,8 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream)
     // FP32 tally for grids whose FP64 tally is far larger than L2: deposits in
     // FP32, flushed into the FP64 jmean after every chunk of packets, so each
     // voxel's FP32 partial sum stays short
-    const bool t32 = !ctx->fp64 && (ctx->tally32 > 0 || (ctx->tally32 < 0 && ctx->ni * 8 > ((int64_t)256 << 20)));
+    const bool t32 = ctx->config && !ctx->fp64 &&
+                     (ctx->tally32 > 0 || (ctx->tally32 < 0 && ctx->ni * 8 > ((int64_t)256 << 20)));
     if (t32 && !ctx->d_j32) {
         RC(dalloc_t(ctx, &ctx->d_j32, ctx->ni));
         CK(cudaMemsetAsync(ctx->d_j32, 0, ctx->ni * sizeof(float), s));

@@ -176,9 +176,9 @@ template <typename Real> __device__ __forceinline__ Real fresnel(Real n1, Real n
 // for grids up to ~16 M voxels), or an FP32 reduction into the half-size
 // scratch tally that the host flushes into jmean every few million packets
 // (grids whose FP64 tally is far larger than L2).
-template <typename Real> __device__ __forceinline__ void deposit(const TransportArgs &a, int cidx, Real dep)
+template <bool T32, typename Real> __device__ __forceinline__ void deposit(const TransportArgs &a, int cidx, Real dep)
 {
-    if (a.jmean32) atomicAdd(a.jmean32 + cidx, (float)dep);
+    if constexpr (T32) atomicAdd(a.jmean32 + cidx, (float)dep);
     else atomicAdd(a.jmean + cidx, (double)dep);
 }
 
@@ -260,7 +260,7 @@ template <typename Real> __device__ __forceinline__ Real axis_pos(Real n, Real f
 // the next face of each axis and the cell width td along the ray; a crossing
 // moves tm of the crossed axis by td.  In-cell positions are reconstructed
 // only at events (interaction, outer face).
-template <typename Real, int MED>
+template <typename Real, int MED, bool T32>
 __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) transport_kernel(const TransportArgs a, int scat_min)
 {
     __shared__ MatR<Real> lut[MAX_MAT];
@@ -390,7 +390,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
         // -------------------------- one voxel step (src/inttau2.f90:37-63) --
         if (mode == M_FLY) {
             if (++nsteps > max_steps) {
-                if (dep != (Real)0) deposit(a, cidx, dep);
+                if (dep != (Real)0) deposit<T32>(a, cidx, dep);
                 dep = (Real)0;
                 atomicAdd(a.tally + T_OVERFLOW, 1.0);
                 atomicOr(&s_err, (unsigned)DEVERR_STEP_CAP);
@@ -428,7 +428,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     const int sg = cx ? sgx : (cy ? sgy : sgz);
                     const int j = (cx ? ix : (cy ? iy : iz)) + sg;
                     const int N = cx ? NX : (cy ? NY : NZ);
-                    deposit(a, cidx, dep);
+                    deposit<T32>(a, cidx, dep);
                     dep = (Real)0;
                     if ((unsigned)j < (unsigned)N) {
                         // step into the next cell (branch-free over the axis); the
@@ -577,7 +577,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     if (!die) mode = M_FLY;
                 }
                 if (die) {
-                    if (dep != (Real)0) deposit(a, cidx, dep);
+                    if (dep != (Real)0) deposit<T32>(a, cidx, dep);
                     dep = (Real)0;
                     atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
                     mode = M_DEAD;
@@ -655,10 +655,11 @@ int grid_for(int64_t n, int tpb)
     return (int)(b > 0 ? b : 1);
 }
 
-template <typename Real, int MED> cudaError_t launch_t(const TransportArgs &a, int sm_count, cudaStream_t s)
+template <typename Real, int MED, bool T32 = false>
+cudaError_t launch_t(const TransportArgs &a, int sm_count, cudaStream_t s)
 {
     int per_sm = 0;
-    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<Real, MED>, TPB, 0);
+    cudaError_t e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, transport_kernel<Real, MED, T32>, TPB, 0);
     const int scat_min = a.scat_min > 0 ? a.scat_min : 20;
     if (e != cudaSuccess) return e;
     if (per_sm < 1) per_sm = 1;
@@ -667,7 +668,7 @@ template <typename Real, int MED> cudaError_t launch_t(const TransportArgs &a, i
     if (blocks > need) blocks = need;
     if (blocks < 1) blocks = 1;
     count_launch();
-    transport_kernel<Real, MED><<<(unsigned)blocks, TPB, 0, s>>>(a, scat_min);
+    transport_kernel<Real, MED, T32><<<(unsigned)blocks, TPB, 0, s>>>(a, scat_min);
     return cudaGetLastError();
 }
 
@@ -679,13 +680,19 @@ cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cu
     cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     if (fp64) {
+        if (a.jmean32) return cudaErrorInvalidValue;  // FP64 transport keeps the FP64 tally
         if (a.medium == MED_RHOKAP) return launch_t<double, MED_RHOKAP>(a, sm_count, s);
         if (a.uniform_id >= 0) return launch_t<double, MED_UNIFORM>(a, sm_count, s);
         return launch_t<double, MED_MATERIAL>(a, sm_count, s);
     }
-    if (a.medium == MED_RHOKAP) return launch_t<float, MED_RHOKAP>(a, sm_count, s);
-    if (a.uniform_id >= 0) return launch_t<float, MED_UNIFORM>(a, sm_count, s);
-    return launch_t<float, MED_MATERIAL>(a, sm_count, s);
+    if (a.medium == MED_RHOKAP) {
+        if (a.jmean32) return cudaErrorInvalidValue;  // the FP32 tally is a config-mode form
+        return launch_t<float, MED_RHOKAP>(a, sm_count, s);
+    }
+    // the tally's precision is a template parameter: no per-deposit branch
+    if (a.uniform_id >= 0)
+        return a.jmean32 ? launch_t<float, MED_UNIFORM, true>(a, sm_count, s) : launch_t<float, MED_UNIFORM>(a, sm_count, s);
+    return a.jmean32 ? launch_t<float, MED_MATERIAL, true>(a, sm_count, s) : launch_t<float, MED_MATERIAL>(a, sm_count, s);
 }
 
 cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s)
