@@ -207,3 +207,38 @@ def test_batch_autotune_restores_state(tam):
     finally:
         for c in ctxs:
             c.close()
+
+
+def test_batch_run_uneven_lengths_matches_single_runs(tam):
+    # instances whose loops end after different numbers of iterations: the
+    # batched launches keep stepping the live ones while the finished ones
+    # stay put; each ends where it ends when run alone
+    F = tam._abi
+
+    def make(shp, total_time):
+        nx, ny, nz, layered, power = shp
+        half = 0.0025 * nx
+        p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half * ny / nx, zmax=half * nz / nx, mode=1,
+                               precision=1, nphotons=20000, pulse_type=1, power=power, energy_per_pixel=power * 1e3,
+                               total_time=total_time, loops=1)
+        return tam.Context(p, tam.default_config(retrace_fraction=0.0, source_radius=0.05))
+
+    times = [0.05, 0.12, 0.08]
+    seeds = [7, 8, 9]
+    want = []
+    for shp, tt, sd in zip(SHAPES, times, seeds):
+        with make(shp, tt) as ctx:
+            its = ctx.run(seed=sd)
+            want.append((its, ctx.download(F.TAM_F_TEMP), ctx.state().time))
+    ctxs = [make(shp, tt) for shp, tt in zip(SHAPES, times)]
+    try:
+        its = tam.batch_run(ctxs, seeds)
+        assert len(set(its)) == 3  # three different loop lengths
+        for ctx, n, (its1, T, t) in zip(ctxs, its, want):
+            assert n == its1
+            assert ctx.state().time == pytest.approx(t, rel=1e-12)
+            assert np.abs(ctx.download(F.TAM_F_TEMP) - T).max() <= 1e-4
+            assert ctx.device_errors() == 0
+    finally:
+        for c in ctxs:
+            c.close()

@@ -52,6 +52,16 @@ def test_workload_vessels_geometry(tam):
     assert counts[0] == 0 and counts[1] > 0.9 * x.grid.size and counts[2] > 0 and counts[3] > 0
 
 
+def test_workload_command_line(tam):
+    p = _w().parser()
+    a = p.parse_args(["batch", "--instances", "8", "--warm", "200", "--steps", "4"])
+    assert (a.cmd, a.instances, a.warm, a.steps, a.autotune) == ("batch", 8, 200, 4, False)
+    a = p.parse_args(["vessels", "--scale", "0.6", "--tally32", "1"])
+    assert (a.cmd, a.scale, a.tally32, a.packets) == ("vessels", 0.6, 1, 10_000_000)
+    with pytest.raises(SystemExit):
+        p.parse_args(["vessels", "--tally32", "2"])
+
+
 # ------------------------------------------------------------------ GPU --
 def _batches(ctx, F, n, nb, seed, stream0):
     out = []

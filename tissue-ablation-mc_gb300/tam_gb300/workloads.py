@@ -219,7 +219,8 @@ def _run_vessels(a) -> None:
               f"device errors {ctx.device_errors()}", flush=True)
 
 
-def main(argv=None) -> None:
+def parser():
+    """The command line of `python -m tam_gb300.workloads`."""
     import argparse
 
     ap = argparse.ArgumentParser(prog="python -m tam_gb300.workloads",
@@ -236,7 +237,11 @@ def main(argv=None) -> None:
     v.add_argument("--packets", type=int, default=10_000_000)
     v.add_argument("--warm-packets", type=int, default=1_000_000)
     v.add_argument("--tally32", type=int, default=-1, choices=[-1, 0, 1])
-    a = ap.parse_args(argv)
+    return ap
+
+
+def main(argv=None) -> None:
+    a = parser().parse_args(argv)
     (_run_batch if a.cmd == "batch" else _run_vessels)(a)
 
 
