@@ -122,7 +122,8 @@ typedef struct tam_config {
     double A, Ea, Rgas, T_lo, T_hi;
     double thr[3];
     double retrace_fraction;     /* re-run MC when newly ablated > fraction of grid; <=0 never */
-    int32_t retrace_check;       /* heat steps between re-trace checks */
+    int32_t retrace_check;       /* heat steps between re-trace checks, counted across calls
+                                  * (0: at the end of every heat-step call) */
     int64_t max_steps;           /* per-packet loop cap */
 } tam_config;
 
@@ -224,9 +225,12 @@ int tam_heat_steps(struct tam_ctx *ctx, int32_t nsteps, double *temp_out);
 int tam_arrhenius(struct tam_ctx *ctx);
 /* setupThermalCoeff (src/3dFD.f90:312-361), reference mode. */
 int tam_update_props(struct tam_ctx *ctx, double ablate_temp);
-/* n iterations of the outer loop of src/mcpolar.f90:148-186. */
+/* n iterations of the outer loop of src/mcpolar.f90:148-186.  The device
+ * error word is checked every 64 iterations and after the last, so the loop
+ * runs ahead of the device in between. */
 int tam_step_coupled(struct tam_ctx *ctx, int32_t n, uint64_t seed);
-/* The whole outer loop while time <= total_time (at most max_iters, <=0 no cap). */
+/* The whole outer loop while time <= total_time (at most max_iters, <=0 no
+ * cap), with the same error checks. */
 int tam_run(struct tam_ctx *ctx, uint64_t seed, int64_t max_iters, int64_t *iters);
 /* tissue(rhokap <= 0.1) = -1 (src/mcpolar.f90:196-204). */
 int tam_finalize(struct tam_ctx *ctx);

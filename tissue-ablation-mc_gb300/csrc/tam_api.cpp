@@ -92,6 +92,7 @@ struct tam_ctx {
     double cdt = 0;            // config-mode step
     bool need_trace = true;
     long long nabl_at_trace = 0;
+    int32_t since_check = 0;   // heat steps since the last re-trace check (config mode)
 
     // tuning knobs
     int scat_min = 20;
@@ -765,7 +766,18 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
         ctx->fcur = 1 - ctx->fcur;
         const bool on = pulse_update(ctx, ctx->cdt);
         const bool last = it + 1 == nsteps;
-        if (ctx->cfg.retrace_fraction > 0 && ((check && (it + 1) % check == 0) || last || on)) {
+        // re-trace checks every `check` heat steps, counted across calls (so a
+        // loop of one-step calls does not read the counter back every step),
+        // or at the end of each call when no interval is set; and whenever the
+        // source switches on
+        bool due = false;
+        if (ctx->cfg.retrace_fraction > 0) {
+            if (check) due = ++ctx->since_check >= check;
+            else due = last;
+            due = due || on;
+        }
+        if (due) {
+            ctx->since_check = 0;
             unsigned long long n = 0;
             CK(cudaMemcpyAsync(&n, ctx->d_nabl, sizeof n, cudaMemcpyDeviceToHost, ctx->stream));
             CK(cudaStreamSynchronize(ctx->stream));
@@ -780,7 +792,12 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
     return TAM_OK;
 }
 
-int outer_iteration(tam_ctx *ctx, uint64_t seed)
+constexpr int ERR_EVERY = 64;  // iterations between device-error checks of the driver loops
+
+// One outer iteration of the driver loop (src/mcpolar.f90:148-186).  sync:
+// wait for the stream and fold the device error word into the status (loops
+// do so every ERR_EVERY iterations and at their end).
+int outer_iteration(tam_ctx *ctx, uint64_t seed, bool sync = true)
 {
     const int64_t n = ctx->p.nphotons * (int64_t)ctx->p.numproc;
     if (ctx->config) {
@@ -800,6 +817,10 @@ int outer_iteration(tam_ctx *ctx, uint64_t seed)
         RC(ref_props(ctx, ctx->p.ablate_temp));
     }
     ctx->counter += 1;
+    if (!sync) {
+        CK(cudaGetLastError());
+        return TAM_OK;
+    }
     return finish(ctx, "tam_step_coupled");
 }
 
@@ -1436,7 +1457,7 @@ int tam_step_coupled(tam_ctx *ctx, int32_t n, uint64_t seed)
     if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
     if (n < 0) return fail(ctx, TAM_E_INVALID, "n must be >= 0");
     CK(cudaSetDevice(ctx->device));
-    for (int32_t i = 0; i < n; ++i) RC(outer_iteration(ctx, seed));
+    for (int32_t i = 0; i < n; ++i) RC(outer_iteration(ctx, seed, i + 1 == n || (i + 1) % ERR_EVERY == 0));
     return TAM_OK;
 }
 
@@ -1447,11 +1468,11 @@ int tam_run(tam_ctx *ctx, uint64_t seed, int64_t max_iters, int64_t *iters)
     int64_t it = 0;
     while (ctx->time <= ctx->total_time) {
         if (max_iters > 0 && it >= max_iters) break;
-        RC(outer_iteration(ctx, seed));
+        RC(outer_iteration(ctx, seed, (it + 1) % ERR_EVERY == 0));
         ++it;
     }
     if (iters) *iters = it;
-    return TAM_OK;
+    return finish(ctx, "tam_run");
 }
 
 // ------------------------------------------------------------ batches --
@@ -1743,7 +1764,7 @@ int tam_batch_step_coupled(tam_ctx *const *ctxs, int32_t n, int32_t iters, const
             ctxs, n, seeds, [&](tam_ctx *, int64_t it) { return it < iters; }, its);
     }
     return run_batch(ctxs, n, [&](tam_ctx *c, int32_t i) {
-        for (int32_t k = 0; k < iters; ++k) RC(outer_iteration(c, seeds[i]));
+        for (int32_t k = 0; k < iters; ++k) RC(outer_iteration(c, seeds[i], k + 1 == iters || (k + 1) % ERR_EVERY == 0));
         return (int)TAM_OK;
     });
 }
@@ -1765,11 +1786,11 @@ int tam_batch_run(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, int64_
         int64_t it = 0;
         while (c->time <= c->total_time) {
             if (max_iters > 0 && it >= max_iters) break;
-            RC(outer_iteration(c, seeds[i]));
+            RC(outer_iteration(c, seeds[i], (it + 1) % ERR_EVERY == 0));
             ++it;
         }
         if (iters) iters[i] = it;
-        return (int)TAM_OK;
+        return finish(c, "tam_batch_run");
     });
 }
 
@@ -1945,7 +1966,7 @@ std::vector<std::pair<void *, size_t>> state_buffers(tam_ctx *ctx)
 struct Scalars {
     double time, pulseCount, repetitionCount, laserOn, delt, total_time, cdt;
     int32_t laser_flag, pulseFlag, pulsesDone, counter, tcur, rcur, fcur, need_trace, uniform_id, cls_uniform,
-        thermal_by_class, pad;
+        thermal_by_class, since_check;
     int64_t mc_passes, nabl_at_trace, nabl_at_uniform, last_n;
     uint32_t errbits_seen, pad2;
 };
@@ -1971,6 +1992,7 @@ void get_scalars(const tam_ctx *c, Scalars &S)
     S.uniform_id = c->uniform_id;
     S.cls_uniform = c->cls_uniform;
     S.thermal_by_class = c->thermal_by_class;
+    S.since_check = c->since_check;
     S.mc_passes = c->mc_passes;
     S.nabl_at_trace = c->nabl_at_trace;
     S.nabl_at_uniform = c->nabl_at_uniform;
@@ -1998,6 +2020,7 @@ void set_scalars(tam_ctx *c, const Scalars &S)
     c->uniform_id = S.uniform_id;
     c->cls_uniform = S.cls_uniform;
     c->thermal_by_class = S.thermal_by_class != 0;
+    c->since_check = S.since_check;
     c->clut.uniform = S.cls_uniform;
     c->mc_passes = S.mc_passes;
     c->nabl_at_trace = S.nabl_at_trace;
@@ -2085,7 +2108,7 @@ struct Snapshot {
     std::vector<std::pair<void *, void *>> bufs;  // (saved copy, live buffer)
     std::vector<size_t> bytes;
     double time = 0, pulseCount = 0, repetitionCount = 0, laserOn = 0;
-    int laser_flag = 0, pulseFlag = 0, pulsesDone = 0, counter = 0, fcur = 0;
+    int laser_flag = 0, pulseFlag = 0, pulsesDone = 0, counter = 0, fcur = 0, since_check = 0;
     int64_t mc_passes = 0;
     bool need_trace = false;
     int uniform_id = -1;
@@ -2131,6 +2154,7 @@ int snap_take(tam_ctx *ctx, Snapshot &S)
     S.pulsesDone = ctx->pulsesDone;
     S.counter = ctx->counter;
     S.fcur = ctx->fcur;
+    S.since_check = ctx->since_check;
     S.mc_passes = ctx->mc_passes;
     S.need_trace = ctx->need_trace;
     S.uniform_id = ctx->uniform_id;
@@ -2152,6 +2176,7 @@ int snap_restore(tam_ctx *ctx, const Snapshot &S)
     ctx->pulsesDone = S.pulsesDone;
     ctx->counter = S.counter;
     ctx->fcur = S.fcur;
+    ctx->since_check = S.since_check;
     ctx->mc_passes = S.mc_passes;
     ctx->need_trace = S.need_trace;
     ctx->uniform_id = S.uniform_id;
