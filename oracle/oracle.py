@@ -1,7 +1,7 @@
 """ctypes binding of the CPU oracle liboracle.so (TEST INFRASTRUCTURE ONLY).
 
 Only tests/, __graft_entry__.smoke() and the CPU legs of bench.py use this
-module, and only as the checker / CPU baseline: the product library never
+module, and only to check results / as the CPU baseline: the product library never
 imports it.  See tam_oracle.h for what the oracle restates and how it is
 pinned.
 """

@@ -2,8 +2,8 @@
  * tam_oracle.h -- CPU oracle for the two hot paths of Tissue-Ablation-MC.
  *
  * TEST INFRASTRUCTURE ONLY.  This is a plain-C FP64 restatement of the
- * reference Fortran (lewisfish/Tissue-Ablation-MC) used as the checker for
- * the CUDA library.  Only tests/, __graft_entry__.smoke() and the CPU legs of
+ * reference Fortran (lewisfish/Tissue-Ablation-MC) that the tests check the
+ * CUDA library against.  Only tests/, __graft_entry__.smoke() and the CPU legs of
  * bench.py may load it; the product library never links or calls it.
  *
  * Parity status: parity unpinned.  The reference cannot be compiled (no
