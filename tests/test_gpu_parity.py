@@ -503,17 +503,27 @@ def test_autotune_restores_state(tam):
         assert ctx.device_errors() == 0
 
 
-def test_fp32_tally_flushed_matches_fp64_tally(tam):
+@pytest.mark.parametrize("layered", [False, True])
+def test_fp32_tally_flushed_matches_fp64_tally(tam, layered):
     # FP32 transport with deposits into the FP32 tally, flushed into the FP64
     # jmean every 30000 packets (four flushes), against FP64 deposits on the
-    # same Philox streams: only the rounding of the accumulation differs
+    # same Philox streams: only the rounding of the accumulation differs.
+    # Uniform medium and a per-voxel material grid (two kernel forms).
     nx = 40
     half = 0.0025 * nx
     p = tam.default_params(nxg=nx, nyg=nx, nzg=nx, xmax=half, ymax=half, zmax=half, mode=1, precision=1,
                            nphotons=100000)
+    c = tam.default_config(source_radius=0.03, nmat=3)
+    tam.set_material(c, 1, 0.3, 100.0, 0.9, 1.38, 0.56, 1070.0, 3400.0)
+    tam.set_material(c, 2, 3.0, 200.0, 0.8, 1.40, 0.52, 1060.0, 3770.0)
+    grid = np.ones((nx, nx, nx), dtype=np.uint8, order="F")
+    if layered:
+        grid[:, :, nx - 6:] = 2
+        grid[10:25, 12:30, 5:20] = 2
     out = []
     for t32 in (0, 1):
-        with tam.Context(p, tam.default_config(source_radius=0.03)) as ctx:
+        with tam.Context(p, c) as ctx:
+            ctx.upload(F.TAM_F_MATERIAL, grid)
             ctx.set_tuning("transport.tally32", t32)
             ctx.set_tuning("transport.tally32_chunk", 30000)
             J = ctx.mc_pass(100000, seed=4, stream=1, want=True)
