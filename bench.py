@@ -133,6 +133,17 @@ class Clocks:
 
 
 # ------------------------------------------------------------ GPU arm --
+def max_over_ranks(ms: float, dist, device: str) -> float:
+    """The largest of the ranks' times (all ranks get it); `dist` None: one rank."""
+    if dist is None:
+        return ms
+    import torch
+
+    t = torch.tensor([float(ms)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def run_gpu(args):
     import numpy as np
     import torch
@@ -184,11 +195,7 @@ def run_gpu(args):
         ev1.record(stream)
         torch.cuda.synchronize()
     launches = tam.kernel_launches() - l0
-    ms = ev0.elapsed_time(ev1)
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), dist, f"cuda:{local}")
     value = world * packets * args.steps / (ms * 1e-3)
     tr_ms = statistics.mean(t_tr)
     heat_ms = statistics.mean(t_heat)
@@ -233,11 +240,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     e2e_ms = ev0.elapsed_time(ev1)
     e2e_wall = (time.perf_counter() - w0) * 1e3
-    e2e_ms = max(e2e_ms, e2e_wall)
-    if dist:
-        t = torch.tensor([e2e_ms], device=f"cuda:{local}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_ms = float(t.item())
+    e2e_ms = max_over_ranks(max(e2e_ms, e2e_wall), dist, f"cuda:{local}")
     e2e_val = world * packets * args.steps / (e2e_ms * 1e-3)
     h2d = mat_h.nbytes + temp_h.nbytes
     d2h = out_T.nbytes + out_O.nbytes + out_J.nbytes
