@@ -2196,22 +2196,38 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
     Snapshot S;
     RC(snap_take(ctx, S));
     float ms = 0.f;
+    // on a failure the knobs and the state go back as they were
+    const int scat0 = ctx->scat_min, z0 = ctx->zchunk, rows0 = ctx->cls_rows;
+    auto undo = [&](int code) {
+        ctx->scat_min = scat0;
+        ctx->zchunk = z0;
+        ctx->cls_rows = rows0;
+        (void)cudaGetLastError();
+        (void)snap_restore(ctx, S);
+        return code;
+    };
+    auto timed = [&](int ev0, int ev1) -> int {
+        if (cudaEventSynchronize(ctx->ev[ev1]) != cudaSuccess ||
+            cudaEventElapsedTime(&ms, ctx->ev[ev0], ctx->ev[ev1]) != cudaSuccess)
+            return fail(ctx, TAM_E_CUDA, "autotune: timing events failed");
+        return TAM_OK;
+    };
+    int r = TAM_OK;
     // transport: lanes that must wait at an interaction before the warp's event batch
     if (packets > 0) {
         int best = ctx->scat_min;
         float best_ms = 1e30f;
         for (int cand : {12, 16, 20, 24, 28}) {
             ctx->scat_min = cand;
-            RC(mc_pass(ctx, packets, 0x5eedull, 0xA070u));
-            CK(cudaEventSynchronize(ctx->ev[1]));
-            CK(cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]));
+            if ((r = mc_pass(ctx, packets, 0x5eedull, 0xA070u)) != TAM_OK || (r = timed(0, 1)) != TAM_OK)
+                return undo(r);
             if (ms < best_ms) {
                 best_ms = ms;
                 best = cand;
             }
         }
         ctx->scat_min = best;
-        RC(snap_restore(ctx, S));
+        if ((r = snap_restore(ctx, S)) != TAM_OK) return undo(r);
     }
     // heat: z planes per thread column (and voxel rows per thread of the class-table step)
     if (steps > 0) {
@@ -2226,10 +2242,9 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
                 if (zc > ctx->nz) continue;
                 ctx->zchunk = zc;
                 ctx->cls_rows = rows;
-                RC(cfg_heat(ctx, steps));
-                CK(cudaEventSynchronize(ctx->ev[3]));
-                CK(cudaEventElapsedTime(&ms, ctx->ev[2], ctx->ev[3]));
-                RC(snap_restore(ctx, S));
+                if ((r = cfg_heat(ctx, steps)) != TAM_OK || (r = timed(2, 3)) != TAM_OK ||
+                    (r = snap_restore(ctx, S)) != TAM_OK)
+                    return undo(r);
                 if (ms < best_ms) {
                     best_ms = ms;
                     best_z = zc;
@@ -2270,18 +2285,30 @@ int tam_batch_autotune(tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *
         int form, z;
     };
     const Cand cands[] = {{2, 8}, {2, 16}, {2, 32}, {2, 64}, {1, 16}, {1, 32}};
+    // on a failure the settings and every instance's state go back as they were
+    auto undo = [&](int code) {
+        ctx->batch_staged = form0;
+        ctx->batch_zchunk = z0;
+        for (int32_t i = 0; i < n; ++i) (void)snap_restore(ctxs[i], *S[i]);
+        return code;
+    };
     for (const Cand &c : cands) {
         ctx->batch_staged = c.form;
         ctx->batch_zchunk = c.z;
         DevBatch B;
         const int K = std::min(batch_chunk(ctxs, n), (int)steps);
-        RC(batch_setup(B, ctxs, n, K));
-        RC(batch_heat_chunk(B, ctxs, n, K, active));  // warm-up (instruction cache, L2)
-        for (int32_t i = 0; i < n; ++i) RC(snap_restore(ctxs[i], *S[i]));
+        int r = batch_setup(B, ctxs, n, K);
+        if (r == TAM_OK) r = batch_heat_chunk(B, ctxs, n, K, active);  // warm-up (instruction cache, L2)
+        if (r != TAM_OK) return undo(r);
+        for (int32_t i = 0; i < n; ++i)
+            if ((r = snap_restore(ctxs[i], *S[i])) != TAM_OK) return undo(r);
         const auto t0 = std::chrono::steady_clock::now();
-        for (int32_t done = 0; done < steps; done += K) RC(batch_heat_chunk(B, ctxs, n, std::min(K, steps - done), active));
+        for (int32_t done = 0; done < steps && r == TAM_OK; done += K)
+            r = batch_heat_chunk(B, ctxs, n, std::min(K, steps - done), active);
         const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        for (int32_t i = 0; i < n; ++i) RC(snap_restore(ctxs[i], *S[i]));
+        if (r != TAM_OK) return undo(r);
+        for (int32_t i = 0; i < n; ++i)
+            if ((r = snap_restore(ctxs[i], *S[i])) != TAM_OK) return undo(r);
         if (dt < best) {
             best = dt;
             best_form = c.form;
