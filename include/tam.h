@@ -263,6 +263,9 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * step stages its planes with cp.async, two voxels per thread),
  * "heat.cls_rows" (class-table step: 0 = two x-adjacent voxels per thread,
  * the default; 1 or 2 = that many voxel rows per thread),
+ * "heat.graph" (config mode: 1 (default) replays chunks of 16 heat steps from
+ * CUDA graphs when no step but a chunk's last needs the host (re-trace check,
+ * source switching on); 0 launches every step),
  * "heat.arrhenius_fp64" (FP32 form: 1 evaluates the Arrhenius exponent
  * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits),
  * "batch.zchunk" (batched heat steps, read from the first context of the

@@ -534,3 +534,37 @@ def test_fp32_tally_flushed_matches_fp64_tally(tam, layered):
     assert np.abs(Ja - Jb).sum() / np.abs(Ja).sum() < 1e-6
     sig = Ja > 1e-3 * Ja.max()
     assert (np.abs(Ja - Jb)[sig] / Ja[sig]).max() < 1e-4
+
+
+@pytest.mark.parametrize("precision,check", [(1, 5), (1, 50), (0, 50)])
+def test_heat_graph_replay_matches_plain_launches(tam, precision, check):
+    # heat steps replayed from CUDA graphs (chunks of 16 whose step values come
+    # from a device table) against one launch per step: bit-identical fields,
+    # clock and pulse state, with a pulsed source switching on and off inside
+    # the run and re-trace checks every `check` steps
+    nx = 32
+    half = 0.0025 * nx
+    p = tam.default_params(nxg=nx, nyg=nx, nzg=nx, xmax=half, ymax=half, zmax=half, mode=1, precision=precision,
+                           nphotons=20000, pulse_type=1, power=20.0, energy_per_pixel=20.0 * 20.0,
+                           repetition_rate_1=0.1, pulses_to_do=3, total_time=10.0, loops=1)
+    # one absorbed-power field for both runs (an MC pass in FP64 sums its
+    # tally with atomics, so two passes differ in the last bits)
+    rng = np.random.default_rng(12)
+    J = np.asfortranarray(rng.uniform(0, 1, (nx, nx, nx)) ** 4 * 2e7)
+    out = []
+    for graph in (0, 1):
+        c = tam.default_config(source_radius=0.03, retrace_fraction=1e-3, retrace_check=check)
+        with tam.Context(p, c) as ctx:
+            ctx.set_tuning("heat.graph", graph)
+            ctx.upload(F.TAM_F_JMEAN_GLOBAL, J)
+            ctx.heat_steps(3)
+            ctx.heat_steps(197)
+            st = ctx.state()
+            out.append((ctx.download(F.TAM_F_TEMP), ctx.download(F.TAM_F_TISSUE), st.time, st.pulses_done,
+                        st.laser_flag, ctx.device_errors()))
+    (Ta, Oa, ta, pa, la, ea), (Tb, Ob, tb, pb, lb, eb) = out
+    assert ea == eb == 0
+    assert (Ta - 310.15).max() > 0.5
+    np.testing.assert_array_equal(Ta, Tb)
+    np.testing.assert_array_equal(Oa, Ob)
+    assert (ta, pa, la) == (tb, pb, lb) and pa >= 1

@@ -287,7 +287,8 @@ __global__ void __launch_bounds__(FX *FY, KAHAN ? 4 : 2) fused_kernel(const Fuse
     const float *E = a.Tc_in;
     float *Eo = a.Tc_out;
     const Real cx = cst<Real>(a, FC_CX), cy = cst<Real>(a, FC_CY), cz = cst<Real>(a, FC_CZ);
-    const Real dt = cst<Real>(a, FC_DT), Pdt = cst<Real>(a, FC_PDT);
+    const Real dt = cst<Real>(a, FC_DT), Pdt = step_pdt<Real>(a);
+    const double t_new = step_tnew(a);
     const bool src_on = Pdt != (Real)0;
     // halo cells this thread stages for every plane
     const bool hL = tx == 0 && x >= 1 && y < a.ny;
@@ -425,8 +426,8 @@ __global__ void __launch_bounds__(FX *FY, KAHAN ? 4 : 2) fused_kernel(const Fuse
             if (!(Ts == Ts)) errbits |= DEVERR_NAN;
             else if (Ts < (Real)0) errbits |= DEVERR_NEG_T;
             if (Ts >= cst<Real>(a, FC_SCREEN)) {
-                if constexpr (sizeof(Real) == 4) rare_update_f32(a, v, ni, Tn, (float)En, a.t_new);
-                else rare_update<Real>(a, v, ni, (double)Tn - (double)En, a.t_new);
+                if constexpr (sizeof(Real) == 4) rare_update_f32(a, v, ni, Tn, (float)En, t_new);
+                else rare_update<Real>(a, v, ni, (double)Tn - (double)En, t_new);
             }
         }
         prv = cur;

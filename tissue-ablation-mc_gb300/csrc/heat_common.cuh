@@ -44,6 +44,15 @@ template <typename Real> __device__ __forceinline__ Real cst(const FusedArgs &a,
 template <> __device__ __forceinline__ float cst<float>(const FusedArgs &a, int i) { return a.fc[i]; }
 template <> __device__ __forceinline__ double cst<double>(const FusedArgs &a, int i) { return a.dc[i]; }
 
+// The step's source multiplier x dt and end time: from the launch's constants,
+// or from device memory for steps replayed from a CUDA graph (the same values,
+// rounded the same way).
+template <typename Real> __device__ __forceinline__ Real step_pdt(const FusedArgs &a)
+{
+    return a.sv ? (Real)a.sv->pdt : cst<Real>(a, FC_PDT);
+}
+__device__ __forceinline__ double step_tnew(const FusedArgs &a) { return a.sv ? a.sv->t_new : a.t_new; }
+
 // Laplacian term of one boundary face f (x-, x+, y-, y+, z-, z+): the ghost
 // carries the voxel's own properties, so the face diffusivity is k/(rho c);
 // (ghost - true centre) is the Dirichlet value minus the true temperature, or

@@ -109,7 +109,8 @@ __global__ void __launch_bounds__(FX *FY, 4)
     const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, ni = sz * a.nz;
     float *To = (float *)a.T_out, *Q = (float *)a.Q;
     float *Eo = a.Tc_out;
-    const float dt = a.fc[FC_DT], Pdt = a.fc[FC_PDT];
+    const float dt = a.fc[FC_DT], Pdt = step_pdt<float>(a);
+    const double t_new = step_tnew(a);
     const bool src_on = Pdt != 0.f;
     const bool xy_inner = x > 0 && x < a.nx - 1 && y > 0 && y < a.ny - 1;
     const bool leader = tx == 0 && ty == 0;
@@ -243,7 +244,7 @@ __global__ void __launch_bounds__(FX *FY, 4)
             const float Ts = Tnew - Enew;
             if (!(Ts == Ts)) errbits |= DEVERR_NAN;
             else if (Ts < 0.f) errbits |= DEVERR_NEG_T;
-            if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew, a.t_new);
+            if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew, t_new);
         }
         __syncthreads();  // every thread is done with the stage the next issue overwrites
         Tp = Tc;
@@ -310,7 +311,8 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
     const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, ni = sz * a.nz;
     float *To = (float *)a.T_out, *Q = (float *)a.Q;
     float *Eo = a.Tc_out;
-    const float dt = a.fc[FC_DT], Pdt = a.fc[FC_PDT];
+    const float dt = a.fc[FC_DT], Pdt = step_pdt<float>(a);
+    const double t_new = step_tnew(a);
     const float cx = a.fc[FC_CX], cy = a.fc[FC_CY], cz = a.fc[FC_CZ];
     const bool leader = tx == 0 && ty == 0;
     const int gx = blockIdx.x * FX - 4, gy = blockIdx.y * FY * RY - 1, gx8 = blockIdx.x * FX - 16;
@@ -463,7 +465,7 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
                 Eo[v] = Enew;
                 const float Ts = Tnew - Enew;
                 errbits |= (Ts == Ts) ? (Ts < 0.f ? (unsigned)DEVERR_NEG_T : 0u) : (unsigned)DEVERR_NAN;
-                if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew, a.t_new, near, o_pre);
+                if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, v, ni, Tnew, Enew, t_new, near, o_pre);
             }
             Tp[r] = Tc[r];
             ep[r] = ec[r];
@@ -513,7 +515,8 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_CLS2_MINB)
     const int64_t sy = a.nx, sz = (int64_t)a.nx * a.ny, ni = sz * a.nz;
     float *To = (float *)a.T_out, *Q = (float *)a.Q;
     float *Eo = a.Tc_out;
-    const float dt = a.fc[FC_DT], Pdt = a.fc[FC_PDT];
+    const float dt = a.fc[FC_DT], Pdt = step_pdt<float>(a);
+    const double t_new = step_tnew(a);
     const float cx = a.fc[FC_CX], cy = a.fc[FC_CY], cz = a.fc[FC_CZ];
     const bool leader = tp == 0 && ty == 0;
     const int gx = blockIdx.x * FX - 4, gy = blockIdx.y * FY - 1, gx8 = blockIdx.x * FX - 16;
@@ -686,7 +689,7 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_CLS2_MINB)
 #pragma unroll 1
             for (unsigned m = hot; m; m &= m - 1) {
                 const int h = __ffs(m) - 1;
-                rare_update_f32(a, v + h, ni, h ? Tnew[1] : Tnew[0], h ? Enew[1] : Enew[0], a.t_new,
+                rare_update_f32(a, v + h, ni, h ? Tnew[1] : Tnew[0], h ? Enew[1] : Enew[0], t_new,
                                 h ? near1 : near0, h ? o_pre[1] : o_pre[0]);
             }
             if (in1) {

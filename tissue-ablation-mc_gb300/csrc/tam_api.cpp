@@ -109,6 +109,15 @@ struct tam_ctx {
     bool use_cls = true;
     int cls_rows = 0;                // class-table step: 0 = voxel pairs (measured fastest), 1 or 2 rows
     bool arr_fp64 = false;           // FP32 form: FP64 Arrhenius exponent instead of float-float
+    // heat steps replayed from CUDA graphs (single context, TMA and cp.async
+    // fused forms): chunks of GRAPH_STEPS steps whose P dt and end times come
+    // from a device table refreshed before each replay
+    bool use_graph = true;
+    bool heat_warm = false;                  // a step ran as an ordinary launch (kernel attributes set)
+    cudaStream_t cap_stream = nullptr;       // capture stream (replays run on `stream`)
+    tam::StepVals *d_sv = nullptr;           // the table
+    cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // by the buffer pair the chunk reads first
+    std::vector<unsigned char> gkey[2];      // what the graphs were captured with
     int batch_staged = 2;            // batched steps: staged voxel pairs (2), staged voxels (1), cached loads (0)
     int batch_zchunk = 0;            // batched steps: z planes per work item (0: heat.zchunk, else the default)
     // staged class-table step of this context alone (rows not aligned for TMA)
@@ -734,57 +743,184 @@ int staged_setup(tam_ctx *ctx)
     return TAM_OK;
 }
 
+// Forms of the config-mode heat step, by what the context's state allows.
+enum HeatForm { HF_CLS = 0, HF_STAGED, HF_TMA, HF_CPASYNC };
+
+HeatForm heat_form(const tam_ctx *ctx)
+{
+    if (ctx->fcls && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class) return HF_CLS;
+    if (!ctx->fp64 && ctx->use_cls && ctx->thermal_by_class && ctx->d_cls) return HF_STAGED;
+    if (ctx->tma && ctx->use_tma) return HF_TMA;
+    return HF_CPASYNC;
+}
+
+// Launch one heat step reading buffer pair `which` (a's buffers set here).
+int launch_heat(tam_ctx *ctx, tam::FusedArgs &a, HeatForm form, int which, cudaStream_t s)
+{
+    a.T_in = ctx->d_Tf[which];
+    a.T_out = ctx->d_Tf[1 - which];
+    a.Tc_in = ctx->fp64 ? nullptr : ctx->d_Tc[which];
+    a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[1 - which];
+    switch (form) {
+    case HF_CLS: CK(tam::launch_fused_cls(a, ctx->fcls, which, ctx->clut, ctx->cls_rows, s)); break;
+    case HF_STAGED: {
+        tam::BatchStep st{};
+        st.t_new = a.t_new;
+        st.pdt = (float)(a.P * ctx->cdt);
+        st.active = 1;
+        CK(tam::launch_staged_step(ctx->d_sinst, ctx->d_sprefix, ctx->s_items, st, which, s));
+        break;
+    }
+    case HF_TMA: CK(tam::launch_fused_tma(a, ctx->tma, which, s)); break;
+    default: CK(tam::launch_fused_step(a, ctx->fp64, s)); break;
+    }
+    return TAM_OK;
+}
+
+constexpr int GRAPH_STEPS = 16;  // heat steps per graph replay (even: a replay keeps the buffer pair)
+
+// What a graph depends on besides the per-step values: the launch arguments
+// (step values and buffer pointers masked), the class table and the knobs.
+std::vector<unsigned char> graph_key(const tam_ctx *ctx, const tam::FusedArgs &a0, HeatForm form)
+{
+    tam::FusedArgs a = a0;
+    a.P = 0.0;
+    a.t_new = 0.0;
+    a.sv = nullptr;
+    a.T_in = a.T_out = nullptr;
+    a.Tc_in = nullptr;
+    a.Tc_out = nullptr;
+    const int knobs[4] = {(int)form, ctx->cls_rows, ctx->zchunk, ctx->arr_fp64 ? 1 : 0};
+    std::vector<unsigned char> k(sizeof a + sizeof ctx->clut + sizeof knobs + 2 * sizeof(void *));
+    unsigned char *p = k.data();
+    std::memcpy(p, &a, sizeof a);
+    p += sizeof a;
+    std::memcpy(p, &ctx->clut, sizeof ctx->clut);
+    p += sizeof ctx->clut;
+    std::memcpy(p, knobs, sizeof knobs);
+    p += sizeof knobs;
+    std::memcpy(p, &ctx->fcls, sizeof(void *));
+    std::memcpy(p + sizeof(void *), &ctx->tma, sizeof(void *));
+    return k;
+}
+
+// Capture GRAPH_STEPS steps starting on buffer pair `which`, step j reading
+// its values from d_sv[j].  False (and graphs off for this context) when the
+// capture fails: the steps then run as ordinary launches.
+bool graph_capture(tam_ctx *ctx, const tam::FusedArgs &a0, HeatForm form, int which)
+{
+    if (!ctx->cap_stream && cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    if (!ctx->d_sv && dalloc_t(ctx, &ctx->d_sv, GRAPH_STEPS) != TAM_OK) return false;
+    if (ctx->gexec[which]) {
+        cudaGraphExecDestroy(ctx->gexec[which]);
+        ctx->gexec[which] = nullptr;
+    }
+    if (cudaStreamBeginCapture(ctx->cap_stream, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    bool ok = true;
+    for (int j = 0; j < GRAPH_STEPS && ok; ++j) {
+        tam::FusedArgs a = a0;
+        a.sv = ctx->d_sv + j;
+        ok = launch_heat(ctx, a, form, (which + j) & 1, ctx->cap_stream) == TAM_OK;
+    }
+    tam::count_launch(-GRAPH_STEPS);  // captured, not launched
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
+    ok = ok && e == cudaSuccess && g;
+    if (ok) ok = cudaGraphInstantiate(&ctx->gexec[which], g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        (void)cudaGetLastError();
+        ctx->gexec[which] = nullptr;
+        ctx->err.clear();
+    }
+    return ok;
+}
+
 int cfg_heat(tam_ctx *ctx, int32_t nsteps)
 {
     tam::FusedArgs a = fused_args(ctx);
     const int check = ctx->cfg.retrace_check > 0 ? ctx->cfg.retrace_check : 0;
-    const bool cls = ctx->fcls && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class;
-    const bool staged = !cls && !ctx->fp64 && ctx->use_cls && ctx->thermal_by_class && ctx->d_cls;
-    if (staged && nsteps > 0) RC(staged_setup(ctx));
-    if (!cls && !staged && ctx->tma && ctx->use_tma && ctx->coeff_dirty && nsteps > 0) {
+    const HeatForm form = heat_form(ctx);
+    if (form == HF_STAGED && nsteps > 0) RC(staged_setup(ctx));
+    if (form == HF_TMA && ctx->coeff_dirty && nsteps > 0) {
         CK(tam::launch_face_coeffs(a, ctx->d_ax, ctx->d_ay, ctx->d_az, ctx->d_irc, ctx->stream));
         ctx->coeff_dirty = false;
     }
+    const bool graphs = ctx->use_graph && form != HF_STAGED && nsteps >= GRAPH_STEPS;
+    std::vector<unsigned char> key;
+    if (graphs) key = graph_key(ctx, a, form);
+    // re-trace check after a step: every `check` heat steps, counted across
+    // calls (so a loop of one-step calls does not read the counter back every
+    // step), or at the end of each call when no interval is set; and whenever
+    // the source switches on
+    auto retrace_check = [&](bool on) -> int {
+        ctx->since_check = 0;
+        unsigned long long n = 0;
+        CK(cudaMemcpyAsync(&n, ctx->d_nabl, sizeof n, cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        const long long fresh = (long long)n - ctx->nabl_at_trace;
+        if ((double)fresh > ctx->cfg.retrace_fraction * (double)ctx->ni || (on && fresh > 0)) ctx->need_trace = true;
+        return TAM_OK;
+    };
+    const bool retrace = ctx->cfg.retrace_fraction > 0;
     CK(cudaEventRecord(ctx->ev[2], ctx->stream));
-    for (int32_t it = 0; it < nsteps; ++it) {
-        a.T_in = ctx->d_Tf[ctx->fcur];
-        a.T_out = ctx->d_Tf[1 - ctx->fcur];
-        a.Tc_in = ctx->fp64 ? nullptr : ctx->d_Tc[ctx->fcur];
-        a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[1 - ctx->fcur];
+    int32_t it = 0;
+    while (it < nsteps) {
+        // a chunk replays a graph when none of its steps but the last needs
+        // the host; the pulse machine is run ahead for the chunk and rolled
+        // back when it does
+        if (graphs && ctx->heat_warm && ctx->use_graph && nsteps - it >= GRAPH_STEPS) {
+            const double t0 = ctx->time, pc0 = ctx->pulseCount, rc0 = ctx->repetitionCount, lo0 = ctx->laserOn;
+            const int lf0 = ctx->laser_flag, pd0 = ctx->pulsesDone, sc0 = ctx->since_check;
+            tam::StepVals tab[GRAPH_STEPS];
+            bool fits = true, due = false, on = false;
+            for (int j = 0; j < GRAPH_STEPS && fits; ++j) {
+                tab[j].pdt = ctx->laserOn * get_pwr(ctx) * ctx->cdt;
+                tab[j].t_new = ctx->time + ctx->cdt;
+                on = pulse_update(ctx, ctx->cdt);
+                due = false;
+                if (retrace) due = (check ? ++ctx->since_check >= check : it + j + 1 == nsteps) || on;
+                if (due && j + 1 < GRAPH_STEPS) fits = false;
+            }
+            const int which = ctx->fcur;
+            if (fits && (ctx->gexec[which] == nullptr || ctx->gkey[which] != key)) {
+                fits = graph_capture(ctx, a, form, which);
+                if (fits) ctx->gkey[which] = key;
+                else ctx->use_graph = false;
+            }
+            if (fits) {
+                CK(cudaMemcpyAsync(ctx->d_sv, tab, sizeof tab, cudaMemcpyHostToDevice, ctx->stream));  // pageable: copied now
+                CK(cudaGraphLaunch(ctx->gexec[which], ctx->stream));
+                tam::count_launch(GRAPH_STEPS);
+                ctx->fcur = (ctx->fcur + GRAPH_STEPS) & 1;
+                it += GRAPH_STEPS;
+                if (due) RC(retrace_check(on));
+                continue;
+            }
+            ctx->time = t0;
+            ctx->pulseCount = pc0;
+            ctx->repetitionCount = rc0;
+            ctx->laserOn = lo0;
+            ctx->laser_flag = lf0;
+            ctx->pulsesDone = pd0;
+            ctx->since_check = sc0;
+        }
         a.P = ctx->laserOn * get_pwr(ctx);
         a.t_new = ctx->time + ctx->cdt;
-        if (cls) {
-            CK(tam::launch_fused_cls(a, ctx->fcls, ctx->fcur, ctx->clut, ctx->cls_rows, ctx->stream));
-        } else if (staged) {
-            tam::BatchStep st{};
-            st.t_new = a.t_new;
-            st.pdt = (float)(a.P * ctx->cdt);
-            st.active = 1;
-            CK(tam::launch_staged_step(ctx->d_sinst, ctx->d_sprefix, ctx->s_items, st, ctx->fcur, ctx->stream));
-        } else if (ctx->tma && ctx->use_tma) CK(tam::launch_fused_tma(a, ctx->tma, ctx->fcur, ctx->stream));
-        else CK(tam::launch_fused_step(a, ctx->fp64, ctx->stream));
+        RC(launch_heat(ctx, a, form, ctx->fcur, ctx->stream));
+        ctx->heat_warm = true;
         ctx->fcur = 1 - ctx->fcur;
         const bool on = pulse_update(ctx, ctx->cdt);
-        const bool last = it + 1 == nsteps;
-        // re-trace checks every `check` heat steps, counted across calls (so a
-        // loop of one-step calls does not read the counter back every step),
-        // or at the end of each call when no interval is set; and whenever the
-        // source switches on
         bool due = false;
-        if (ctx->cfg.retrace_fraction > 0) {
-            if (check) due = ++ctx->since_check >= check;
-            else due = last;
-            due = due || on;
-        }
-        if (due) {
-            ctx->since_check = 0;
-            unsigned long long n = 0;
-            CK(cudaMemcpyAsync(&n, ctx->d_nabl, sizeof n, cudaMemcpyDeviceToHost, ctx->stream));
-            CK(cudaStreamSynchronize(ctx->stream));
-            const long long fresh = (long long)n - ctx->nabl_at_trace;
-            if ((double)fresh > ctx->cfg.retrace_fraction * (double)ctx->ni || (on && fresh > 0))
-                ctx->need_trace = true;
-        }
+        if (retrace) due = (check ? ++ctx->since_check >= check : it + 1 == nsteps) || on;
+        if (due) RC(retrace_check(on));
+        ++it;
     }
     CK(cudaEventRecord(ctx->ev[3], ctx->stream));
     ctx->have_heat_time = true;
@@ -1154,6 +1290,9 @@ int tam_destroy(tam_ctx *ctx)
         if (e) cudaEventDestroy(e);
     if (ctx->tma) tam::fused_tma_destroy(ctx->tma);
     if (ctx->fcls) tam::fused_cls_destroy(ctx->fcls);
+    for (cudaGraphExec_t &g : ctx->gexec)
+        if (g) cudaGraphExecDestroy(g);
+    if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
     return TAM_OK;
@@ -1899,6 +2038,8 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
     } else if (k == "heat.cls_rows") {
         if (value < 0 || value > 2) return fail(ctx, TAM_E_INVALID, "heat.cls_rows must be 0 (voxel pairs), 1 or 2");
         ctx->cls_rows = (int)value;
+    } else if (k == "heat.graph") {
+        ctx->use_graph = value != 0;
     } else if (k == "heat.arrhenius_fp64") {
         ctx->arr_fp64 = value != 0;
     } else if (k == "batch.zchunk") {

@@ -131,6 +131,13 @@ enum FusedConst : int {
     FC_N = 39
 };
 
+// Values of one heat step that change from step to step, read by the fused
+// kernels from device memory when FusedArgs::sv is set (graph-captured steps).
+struct StepVals {
+    double pdt;                       // source multiplier x dt of the step
+    double t_new;                     // time stamp at the end of the step
+};
+
 struct FusedArgs {
     int32_t nx, ny, nz;
     double dx, dy, dz;                // m
@@ -143,6 +150,7 @@ struct FusedArgs {
     double bc_T[6], bc_h[6], bc_Tamb[6];
     double P;                         // source multiplier for this step
     double t_new;                     // time stamp of this step's end
+    const StepVals *sv;               // non-null: P dt and t_new of this step come from here
     const void *T_in;                 // interior, Real
     void *T_out;
     const float *Tc_in;               // Kahan compensation (FP32 form only)
