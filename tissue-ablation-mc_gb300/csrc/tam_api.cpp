@@ -141,6 +141,7 @@ struct tam_ctx {
 
     // last pass
     double tally[tam::N_TALLY] = {0};
+    bool tally_stale = false;  // the host copy lags the device tallies (read back on demand)
     int64_t last_n = 0;
     int64_t mc_passes = 0;
     unsigned errbits_seen = 0;
@@ -501,7 +502,10 @@ tam::FusedArgs fused_args(tam_ctx *ctx)
 }
 
 // ------------------------------------------------------------ MC pass --
-int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream)
+// One MC pass.  sync: wait for it and read its tallies back (API calls);
+// the driver loops do not, so the host runs ahead of the device, and the
+// tallies are read back when asked for.
+int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, bool sync = true)
 {
     cudaStream_t s = ctx->stream;
     tam::TransportArgs a{};
@@ -604,8 +608,24 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream)
         const double f = n > 0 ? (pw / 81.0) / den : 0.0;
         CK(tam::launch_scale_f64(ctx->d_jglob, ctx->d_jmean, f, ctx->ni, false, s));
     }
+    if (!sync) {
+        ctx->tally_stale = true;
+        CK(cudaGetLastError());
+        return TAM_OK;
+    }
     CK(cudaMemcpyAsync(ctx->tally, ctx->d_tally, sizeof(ctx->tally), cudaMemcpyDeviceToHost, s));
+    ctx->tally_stale = false;
     return finish(ctx, "tam_mc_pass");
+}
+
+// Bring the host copy of the last pass's tallies up to date.
+int refresh_tallies(tam_ctx *ctx)
+{
+    if (!ctx->tally_stale) return TAM_OK;
+    CK(cudaMemcpyAsync(ctx->tally, ctx->d_tally, sizeof(ctx->tally), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    ctx->tally_stale = false;
+    return TAM_OK;
 }
 
 // ------------------------------------------------------ heat (reference) --
@@ -938,7 +958,7 @@ int outer_iteration(tam_ctx *ctx, uint64_t seed, bool sync = true)
     const int64_t n = ctx->p.nphotons * (int64_t)ctx->p.numproc;
     if (ctx->config) {
         if (ctx->need_trace) {
-            RC(mc_pass(ctx, n, seed, (uint32_t)ctx->mc_passes));
+            RC(mc_pass(ctx, n, seed, (uint32_t)ctx->mc_passes, false));
             unsigned long long nab = 0;
             CK(cudaMemcpy(&nab, ctx->d_nabl, sizeof nab, cudaMemcpyDeviceToHost));
             ctx->nabl_at_trace = (long long)nab;
@@ -947,7 +967,7 @@ int outer_iteration(tam_ctx *ctx, uint64_t seed, bool sync = true)
         RC(cfg_heat(ctx, ctx->p.loops));
     } else {
         // src/mcpolar.f90:149-185
-        if (ctx->laser_flag) RC(mc_pass(ctx, n, seed, (uint32_t)ctx->counter));
+        if (ctx->laser_flag) RC(mc_pass(ctx, n, seed, (uint32_t)ctx->counter, false));
         RC(ref_heat(ctx, ctx->p.loops));
         RC(ref_arrhenius(ctx));
         RC(ref_props(ctx, ctx->p.ablate_temp));
@@ -1774,7 +1794,7 @@ int batch_traces(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, const s
     for (int32_t i = 0; i < n; ++i) {
         tam_ctx *c = ctxs[i];
         if (!active[i] || !c->need_trace) continue;
-        RC(mc_pass(c, c->p.nphotons * (int64_t)c->p.numproc, seeds[i], (uint32_t)c->mc_passes));
+        RC(mc_pass(c, c->p.nphotons * (int64_t)c->p.numproc, seeds[i], (uint32_t)c->mc_passes, false));
         traced[i] = 1;
     }
     for (int32_t i = 0; i < n; ++i) {
@@ -1951,6 +1971,7 @@ int tam_finalize(tam_ctx *ctx)
 int tam_get_tallies(tam_ctx *ctx, double *absorbed, double *reflected, double *transmitted)
 {
     if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
+    RC(refresh_tallies(ctx));
     const double n = ctx->last_n > 0 ? (double)ctx->last_n : 1.0;
     if (absorbed) *absorbed = ctx->tally[tam::T_ABSORBED] / n;
     if (reflected) *reflected = (ctx->tally[tam::T_SPECULAR] + ctx->tally[tam::T_REFLECTED]) / n;
@@ -1961,6 +1982,7 @@ int tam_get_tallies(tam_ctx *ctx, double *absorbed, double *reflected, double *t
 int tam_get_tallies_ex(tam_ctx *ctx, double *out, int32_t n)
 {
     if (!ctx || !out || n < 0) return fail(ctx, TAM_E_INVALID, "bad argument");
+    RC(refresh_tallies(ctx));
     const double np = ctx->last_n > 0 ? (double)ctx->last_n : 1.0;
     for (int i = 0; i < n && i < tam::N_TALLY; ++i) {
         const bool count = i == tam::T_STEPS || i == tam::T_SCATTERS || i == tam::T_OVERFLOW;
@@ -2179,6 +2201,7 @@ int tam_save_state(tam_ctx *ctx, const char *path)
     if (!ctx || !path) return fail(ctx, TAM_E_INVALID, "null argument");
     CK(cudaSetDevice(ctx->device));
     CK(cudaStreamSynchronize(ctx->stream));
+    RC(refresh_tallies(ctx));
     std::ofstream f(path, std::ios::binary);
     if (!f) return fail(ctx, TAM_E_IO, std::string("cannot open ") + path);
     Scalars S;
@@ -2239,6 +2262,7 @@ int tam_load_state(tam_ctx *ctx, const char *path)
     }
     set_scalars(ctx, S);
     std::memcpy(ctx->tally, tally, sizeof tally);
+    ctx->tally_stale = false;
     return finish(ctx, "tam_load_state");
 }
 
@@ -2299,6 +2323,7 @@ int snap_take(tam_ctx *ctx, Snapshot &S)
     S.mc_passes = ctx->mc_passes;
     S.need_trace = ctx->need_trace;
     S.uniform_id = ctx->uniform_id;
+    RC(refresh_tallies(ctx));
     std::memcpy(S.tally, ctx->tally, sizeof S.tally);
     S.last_n = ctx->last_n;
     return TAM_OK;
@@ -2322,6 +2347,7 @@ int snap_restore(tam_ctx *ctx, const Snapshot &S)
     ctx->need_trace = S.need_trace;
     ctx->uniform_id = S.uniform_id;
     std::memcpy(ctx->tally, S.tally, sizeof S.tally);
+    ctx->tally_stale = false;
     ctx->last_n = S.last_n;
     CK(cudaStreamSynchronize(ctx->stream));
     return TAM_OK;
