@@ -568,3 +568,32 @@ def test_heat_graph_replay_matches_plain_launches(tam, precision, check):
     np.testing.assert_array_equal(Ta, Tb)
     np.testing.assert_array_equal(Oa, Ob)
     assert (ta, pa, la) == (tb, pb, lb) and pa >= 1
+
+
+def test_ref_props_reuse_matches_full_update(tam, tmp_path):
+    # a property update that keeps the skin properties of voxels whose water
+    # content did not change since the previous update, against a full
+    # update from the same state (restored from a checkpoint): bit-identical
+    nx, ny, nz = 20, 16, 12
+    p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, precision=0)
+    rng = np.random.default_rng(4)
+    T = np.full((nx + 2, ny + 2, nz + 2), 310.15, order="F")
+    T[1:-1, 1:-1, 1:-1] = rng.uniform(300.0, 380.0, (nx, ny, nz))
+    fields = (F.TAM_F_KAPPA, F.TAM_F_DENSITY, F.TAM_F_HEATCAP, F.TAM_F_COEFF, F.TAM_F_ALPHA, F.TAM_F_RHOKAP,
+              F.TAM_F_WATER)
+    with tam.Context(p) as a:
+        qv = a.state().qvapor
+        a.upload(F.TAM_F_TEMP, T)
+        a.upload(F.TAM_F_Q, np.asfortranarray(rng.uniform(0.0, 1.1 * qv, (nx, ny, nz))))
+        a.update_props(80.0)  # ablation at 80 C: the hottest voxels take air properties
+        a.save_state(str(tmp_path / "state"))
+        a.update_props(80.0)  # water contents unchanged: the skin properties are kept
+        got = [a.download(f) for f in fields]
+        assert a.device_errors() == 0
+    with tam.Context(p) as b:
+        b.load_state(str(tmp_path / "state"))
+        b.update_props(80.0)  # every voxel recomputed
+        want = [b.download(f) for f in fields]
+    assert (want[5][1:-1, 1:-1, 1:-1] == 0).any() and (want[5][1:-1, 1:-1, 1:-1] > 0).any()
+    for g, w in zip(got, want):
+        np.testing.assert_array_equal(g, w)

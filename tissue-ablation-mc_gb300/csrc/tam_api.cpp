@@ -93,6 +93,7 @@ struct tam_ctx {
     bool need_trace = true;
     long long nabl_at_trace = 0;
     int32_t since_check = 0;   // heat steps since the last re-trace check (config mode)
+    double props_delt = -1.0;  // delt of the last property update whose results are intact (<0: none)
 
     // tuning knobs
     int scat_min = 20;
@@ -303,6 +304,7 @@ void reset_scalars(tam_ctx *ctx)
 int ref_setup(tam_ctx *ctx)
 {
     reset_scalars(ctx);
+    ctx->props_delt = -1.0;  // properties set here, not by the update kernel
     const tam_params &p = ctx->p;
     const int nx = ctx->nx, ny = ctx->ny, nz = ctx->nz;
     cudaStream_t s = ctx->stream;
@@ -704,8 +706,10 @@ int ref_props(tam_ctx *ctx, double ablate_temp)
     a.Q = ctx->d_Q;
     a.water = ctx->d_water;
     a.err = ctx->d_err;
+    a.reuse = ctx->props_delt == ctx->delt ? 1 : 0;
     CK(tam::launch_ref_props(a, ctx->stream));
     ctx->rcur = 1 - ctx->rcur;
+    ctx->props_delt = ctx->delt;
     return TAM_OK;
 }
 
@@ -1350,6 +1354,7 @@ int tam_init_opt(tam_ctx *ctx)
 {
     if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
     if (ctx->config) return fail(ctx, TAM_E_STATE, "init_opt1 applies to reference mode");
+    ctx->props_delt = -1.0;  // the absorption constants enter the property update
     ctx->hgg = 0.9;
     ctx->g2 = ctx->hgg * ctx->hgg;
     ctx->mu_water = 510.0;
@@ -1366,6 +1371,7 @@ int tam_gridset(tam_ctx *ctx, double xmax, double ymax, double zmax)
     if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
     if (!(xmax > 0) || !(ymax > 0) || !(zmax > 0)) return fail(ctx, TAM_E_INVALID, "half-widths must be > 0");
     CK(cudaSetDevice(ctx->device));
+    ctx->props_delt = -1.0;
     ctx->p.xmax = xmax;
     ctx->p.ymax = ymax;
     ctx->p.zmax = zmax;
@@ -1404,6 +1410,7 @@ int tam_field_bytes(tam_ctx *ctx, int field, int64_t *nbytes)
 int tam_upload(tam_ctx *ctx, int field, const void *host, int64_t nbytes)
 {
     if (!ctx || !host) return fail(ctx, TAM_E_INVALID, "null argument");
+    ctx->props_delt = -1.0;  // an uploaded field may be one the property update reads or keeps
     const FieldInfo fi = field_info(ctx, field);
     if (!fi.ok) return fail(ctx, TAM_E_STATE, "field " + std::to_string(field) + " not available in this mode");
     if (nbytes != fi.count * fi.esize) return fail(ctx, TAM_E_INVALID, "size mismatch for field " + std::to_string(field));
@@ -2229,6 +2236,7 @@ int tam_save_state(tam_ctx *ctx, const char *path)
 int tam_load_state(tam_ctx *ctx, const char *path)
 {
     if (!ctx || !path) return fail(ctx, TAM_E_INVALID, "null argument");
+    ctx->props_delt = -1.0;
     CK(cudaSetDevice(ctx->device));
     std::ifstream f(path, std::ios::binary);
     if (!f) return fail(ctx, TAM_E_IO, std::string("cannot open ") + path);

@@ -108,6 +108,7 @@ struct RefPropsArgs {
     const double *Q;                  // interior
     double *water;                    // interior
     unsigned *err;
+    int32_t reuse;                    // 1: the previous call's skin properties are intact (same delt)
 };
 cudaError_t launch_ref_props(const RefPropsArgs &a, cudaStream_t s);
 
