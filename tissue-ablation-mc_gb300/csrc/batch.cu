@@ -12,9 +12,13 @@
 // The per-voxel arithmetic is that of the class-table FP32 step: thermal
 // properties by material class, face coefficients k_f/(rho_f c_f) from the
 // per-instance class table, Kahan-compensated temperature, latent-heat clamp,
-// Arrhenius damage and ablation (rare_update_f32).  Neighbours are read with
-// cached global loads (any row pitch: the instances' edges need not be
-// multiples of four), the z column stays in registers.
+// Arrhenius damage and ablation (rare_update_f32).  Three forms, chosen by
+// "batch.staged": the default stages each tile's planes in shared memory with
+// 4-byte cp.async copies (any row pitch: the instances' edges need not be
+// multiples of four) and updates two x-adjacent voxels per thread
+// (batch_pairs_kernel, whose one-step form also serves single contexts with
+// such rows); batch_staged_kernel does the same with one voxel per thread;
+// batch_heat_kernel reads neighbours with cached global loads.
 #include <cstdint>
 
 #include "heat_common.cuh"

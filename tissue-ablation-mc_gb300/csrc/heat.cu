@@ -10,8 +10,10 @@
 //    ln A - Ea/RT in FP64, or float-float in the FP32 form) + ablation in one
 //    pass, with FP32 storage and a Kahan-compensated temperature, or plain
 //    FP64.  Each thread marches a (x, y) column through a z-chunk keeping the
-//    z-neighbours in registers; this cp.async form serves the FP64 step and
-//    FP32 grids whose rows are not 16-byte aligned for TMA (heat_tma.cu).
+//    z-neighbours in registers; this cp.async form with per-voxel k, rho, c
+//    serves the FP64 step and FP32 grids whose properties were uploaded per
+//    voxel on rows TMA cannot copy (class-table steps: heat_tma.cu with TMA,
+//    batch.cu with cp.async staging for any row pitch).
 #include <algorithm>
 #include <atomic>
 #include <cstdio>
