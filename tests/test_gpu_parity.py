@@ -85,6 +85,40 @@ def test_ref_stencil_fp64_matches_oracle(tam, orc):
     o.close()
 
 
+@pytest.mark.parametrize("case,n", [("boiling", 6), ("smooth", 200)])
+def test_ref_stencil_fp32_form_within_1mK(tam, orc, case, n):
+    # reference mode with FP32 precision: the stencil's arithmetic in FP32 on
+    # the FP64 temperatures (neighbour differences and the update in FP64),
+    # against the FP64 oracle.  "boiling": random properties, temperatures up
+    # to 380 K and Q around QVapor, a few steps (its diffusivity exceeds what
+    # delt was set for, so it is not run long).  "smooth": the default
+    # properties, 300-340 K and a source of up to 0.04 K per step, 200 steps,
+    # all below boiling.  The latent-heat branch is a threshold: a voxel whose
+    # FP32 and FP64 temperatures straddle 373 K enters it a step apart, and the
+    # two then differ by that step's increment, so the long run is kept off it.
+    ctx, o = ref_pair(tam, orc, 20, 16, 12, precision=1)
+    rng = np.random.default_rng(1)
+    if case == "boiling":
+        _randomise_ref(o, ctx, rng)
+    else:
+        nx, ny, nz = o.nx, o.ny, o.nz
+        o.arr("temp")[1:nx + 1, 1:ny + 1, 1:nz + 1] = rng.uniform(300.0, 340.0, (nx, ny, nz))
+        o.arr("jmeanGLOBAL")[...] = rng.uniform(0.0, 5e7, (nx, ny, nz))
+        for f, name in ((F.TAM_F_TEMP, "temp"), (F.TAM_F_JMEAN_GLOBAL, "jmeanGLOBAL")):
+            ctx.upload(f, o.arr(name))
+    o.st.p.loops = n
+    assert o.heat_sim(nthreads=1) == 0
+    T = ctx.heat_steps(n, want=True)
+    To = o.arr("temp")
+    dT = np.abs(T - To).max()
+    assert 0.0 < dT <= 1e-3, dT
+    assert (To > 373.0).any() if case == "boiling" else To.max() < 373.0
+    np.testing.assert_allclose(ctx.download(F.TAM_F_Q), o.arr("Q"), rtol=1e-5, atol=1e-6 * o.arr("Q").max())
+    assert ctx.state().time == o.st.time and ctx.device_errors() == 0
+    ctx.close()
+    o.close()
+
+
 def test_ref_arrhenius_fp64_matches_oracle(tam, orc):
     ctx, o = ref_pair(tam, orc, 11, 9, 7)
     rng = np.random.default_rng(2)

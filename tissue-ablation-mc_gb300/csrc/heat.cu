@@ -78,6 +78,63 @@ __device__ __forceinline__ void ref_update(const RefHeatArgs &a, int64_t c, int6
     a.tn[c] = tn;
 }
 
+// The FP32 form of the same update: the step's increment and source term in
+// FP32, added to the FP64 temperature in FP64 (so no compensation is
+// needed); the latent-heat branch, rare, stays FP64.
+__device__ __forceinline__ void ref_update_f32(const RefHeatArgs &a, int64_t c, int64_t q, double T, double cc,
+                                               float u_xx, float u_yy, float u_zz)
+{
+    const double J = a.J[q];
+    const float inc = (float)a.delt * ((u_xx + u_yy) + u_zz);
+    const float src = (float)a.laserOn * (float)a.coeff[c] * (float)J;
+    const double heat = T + (double)(inc + src);
+    double tn = heat;
+    const double Qv = a.Q[q];
+    if (T >= 373.0 && Qv < a.qvapor) {
+        const double energyIncrease = a.laserOn * J * a.delt * a.vvox + cc * a.mvox * (double)inc;
+        if (energyIncrease > 0.0) {
+            const double qn = Qv + energyIncrease;
+            a.Q[q] = qn < a.qvapor ? qn : a.qvapor;
+            tn = 373.0;
+        }
+    } else if (T < 0.0) {
+        atomicOr(a.err, DEVERR_NEG_T);
+    }
+    if (tn != tn) atomicOr(a.err, DEVERR_NAN);
+    a.tn[c] = tn;
+}
+
+// Face terms and axis sums of the reference stencil in the working precision
+// F: double keeps the Fortran's operations and order (bit parity); float is
+// the precision form (face coefficients and sums in FP32 from the FP64
+// properties, neighbour differences formed in FP64).
+template <typename F> struct RefOps;
+template <> struct RefOps<double> {
+    static __device__ __forceinline__ double face(double kc, double kn, double dc, double dn, double cc, double cn,
+                                                  double id2)
+    {
+        return ref_face(kc, kn, dc, dn, cc, cn, id2);
+    }
+    static __device__ __forceinline__ double axis(double a, double d, double tm, double t, double tp)
+    {
+        return ref_axis(a, d, tm, t, tp);
+    }
+};
+template <> struct RefOps<float> {
+    static __device__ __forceinline__ float face(double kc, double kn, double dc, double dn, double cc, double cn,
+                                                 double id2)
+    {
+        const float kh = 0.5f * ((float)kc + (float)kn), dh = 0.5f * ((float)dc + (float)dn),
+                    ch = 0.5f * ((float)cc + (float)cn);
+        return 0.5f * __fdividef(kh, dh * ch) * (float)id2;
+    }
+    // a (T- - T) + d (T+ - T): the reference's a T- - 2b T + d T+ with b = (a + d)/2
+    static __device__ __forceinline__ float axis(float a, float d, double tm, double t, double tp)
+    {
+        return a * (float)(tm - t) + d * (float)(tp - t);
+    }
+};
+
 // The reference stencil (src/3dFD.f90:113-187) with every face coefficient
 // computed once: a face term is symmetric in its two voxels (IEEE addition
 // and multiplication commute), so a voxel's plus face is its neighbour's
@@ -85,11 +142,13 @@ __device__ __forceinline__ void ref_update(const RefHeatArgs &a, int64_t c, int6
 // the x plus face comes from the next lane (shuffle), the y plus face from
 // the next row (shared memory), the z plus face becomes the next plane's
 // minus face; only the tile's last lane, last row and last plane compute
-// theirs.  Three FP64 divisions per voxel instead of six.
+// theirs.  Three divisions per voxel instead of six.  F = double: the parity
+// form; F = float: the FP32 form of reference mode.
 constexpr int REF_ZC = 8;
-__global__ void __launch_bounds__(256) ref_stencil_kernel(const RefHeatArgs a)
+template <typename F> __global__ void __launch_bounds__(256) ref_stencil_kernel(const RefHeatArgs a)
 {
-    __shared__ double s_fy[8][32];
+    using O = RefOps<F>;
+    __shared__ F s_fy[8][32];
     const int tx = threadIdx.x, ty = threadIdx.y;
     const int i = blockIdx.x * 32 + tx + 1, j = blockIdx.y * 8 + ty + 1;
     const bool in = i <= a.nx && j <= a.ny;
@@ -102,27 +161,28 @@ __global__ void __launch_bounds__(256) ref_stencil_kernel(const RefHeatArgs a)
     int64_t c = I(ic, jc, k0);
     const int64_t sz = (int64_t)(a.nx + 2) * (a.ny + 2), sy = a.nx + 2;
     double kc = K[c], dc = D[c], cc = C[c];
-    double fzm = ref_face(kc, K[c - sz], dc, D[c - sz], cc, C[c - sz], a.idz2);
+    F fzm = O::face(kc, K[c - sz], dc, D[c - sz], cc, C[c - sz], a.idz2);
     for (int k = k0; k <= k1; ++k, c += sz) {
         const double kp = K[c + sz], dp = D[c + sz], cp = C[c + sz];
-        const double fzp = ref_face(kc, kp, dc, dp, cc, cp, a.idz2);
-        const double fym = ref_face(kc, K[c - sy], dc, D[c - sy], cc, C[c - sy], a.idy2);
-        const double fxm = ref_face(kc, K[c - 1], dc, D[c - 1], cc, C[c - 1], a.idx2);
+        const F fzp = O::face(kc, kp, dc, dp, cc, cp, a.idz2);
+        const F fym = O::face(kc, K[c - sy], dc, D[c - sy], cc, C[c - sy], a.idy2);
+        const F fxm = O::face(kc, K[c - 1], dc, D[c - 1], cc, C[c - 1], a.idx2);
         s_fy[ty][tx] = fym;
-        double fxp = __shfl_down_sync(0xffffffffu, fxm, 1);
-        if (tx == 31 && ic <= a.nx) fxp = ref_face(kc, K[c + 1], dc, D[c + 1], cc, C[c + 1], a.idx2);
+        F fxp = __shfl_down_sync(0xffffffffu, fxm, 1);
+        if (tx == 31 && ic <= a.nx) fxp = O::face(kc, K[c + 1], dc, D[c + 1], cc, C[c + 1], a.idx2);
         __syncthreads();
-        double fyp = 0.0;
+        F fyp = 0;
         if (ty < 7) fyp = s_fy[ty + 1][tx];
-        else if (jc <= a.ny) fyp = ref_face(kc, K[c + sy], dc, D[c + sy], cc, C[c + sy], a.idy2);
+        else if (jc <= a.ny) fyp = O::face(kc, K[c + sy], dc, D[c + sy], cc, C[c + sy], a.idy2);
         __syncthreads();  // the row is read before the next plane overwrites it
         if (in) {
             const double T = t0[c];
-            const double u_zz = ref_axis(fzm, fzp, t0[c - sz], T, t0[c + sz]);
-            const double u_yy = ref_axis(fym, fyp, t0[c - sy], T, t0[c + sy]);
-            const double u_xx = ref_axis(fxm, fxp, t0[c - 1], T, t0[c + 1]);
+            const F u_zz = O::axis(fzm, fzp, t0[c - sz], T, t0[c + sz]);
+            const F u_yy = O::axis(fym, fyp, t0[c - sy], T, t0[c + sy]);
+            const F u_xx = O::axis(fxm, fxp, t0[c - 1], T, t0[c + 1]);
             const int64_t q = (int64_t)(i - 1) + (int64_t)a.nx * ((int64_t)(j - 1) + (int64_t)a.ny * (int64_t)(k - 1));
-            ref_update(a, c, q, T, cc, u_xx, u_yy, u_zz);
+            if constexpr (sizeof(F) == 8) ref_update(a, c, q, T, cc, u_xx, u_yy, u_zz);
+            else ref_update_f32(a, c, q, T, cc, u_xx, u_yy, u_zz);
         }
         fzm = fzp;
         kc = kp;
@@ -605,7 +665,9 @@ __global__ void from_halo_kernel(const FusedArgs a, const double *halo)
 cudaError_t launch_ref_stencil(const RefHeatArgs &a, cudaStream_t s)
 {
     count_launch();
-    ref_stencil_kernel<<<dim3((a.nx + 31) / 32, (a.ny + 7) / 8, (a.nz + REF_ZC - 1) / REF_ZC), dim3(32, 8), 0, s>>>(a);
+    const dim3 grid((a.nx + 31) / 32, (a.ny + 7) / 8, (a.nz + REF_ZC - 1) / REF_ZC);
+    if (a.f32) ref_stencil_kernel<float><<<grid, dim3(32, 8), 0, s>>>(a);
+    else ref_stencil_kernel<double><<<grid, dim3(32, 8), 0, s>>>(a);
     return cudaGetLastError();
 }
 

@@ -653,6 +653,7 @@ int ref_heat(tam_ctx *ctx, int32_t loops)
     a.J = ctx->d_jglob;
     a.Q = ctx->d_Q;
     a.err = ctx->d_err;
+    a.f32 = ctx->fp64 ? 0 : 1;  // the precision form: FP32 stencil arithmetic, FP64 temperatures
     for (int32_t it = 0; it < loops; ++it) {
         a.delt = ctx->delt;
         a.laserOn = ctx->laserOn;

@@ -87,6 +87,7 @@ struct RefHeatArgs {
     const double *J;                  // interior jmeanGLOBAL
     double *Q;                        // interior
     unsigned *err;
+    int32_t f32;                      // 1: FP32 arithmetic on the FP64 fields (precision form)
 };
 cudaError_t launch_ref_stencil(const RefHeatArgs &a, cudaStream_t s);
 
