@@ -83,7 +83,8 @@ typedef struct tam_params {
     int32_t nxg, nyg, nzg;       /* grid */
     int32_t numproc;             /* normalisation divisor, >= 1 */
     int32_t mode;                /* enum tam_mode */
-    int32_t precision;           /* enum tam_precision: transport and fused heat step */
+    int32_t precision;           /* enum tam_precision: transport and heat step (reference mode:
+                                    FP32 face/axis arithmetic on FP64 temperatures) */
     int32_t device;              /* CUDA device ordinal */
 } tam_params;
 
