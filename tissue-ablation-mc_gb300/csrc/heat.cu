@@ -19,12 +19,22 @@
 #include <cstdio>
 
 #include "heat_common.cuh"
+#include "ieee_bits.h"
 
 namespace tam {
 
 namespace {
 
 // ------------------------------------------------------- reference path --
+// Bit patterns of the positive constants the reference kernels compare
+// against (ieee::ge_pos / lt_pos).
+constexpr uint64_t B_0_53 = 0x3FE0F5C28F5C28F6ull;  // 0.53
+constexpr uint64_t B_0_75 = 0x3FE8000000000000ull;  // 0.75
+constexpr uint64_t B_1 = 0x3FF0000000000000ull;     // 1.0
+constexpr uint64_t B_316 = 0x4073C00000000000ull;   // 316.0
+constexpr uint64_t B_373 = 0x4077500000000000ull;   // 373.0
+constexpr uint64_t B_1E4 = 0x40C3880000000000ull;   // 10000.0
+
 struct H {
     int64_t hx, hy;
     __device__ __forceinline__ int64_t operator()(int i, int j, int k) const
@@ -60,21 +70,19 @@ __device__ __forceinline__ void ref_update(const RefHeatArgs &a, int64_t c, int6
     const double energyIncrease =
         ADD(MUL(MUL(MUL(a.laserOn, J), a.delt), a.vvox), MUL(MUL(cc, a.mvox), tempIncrease));
     const double heat = ADD(ADD(T, tempIncrease), MUL(MUL(a.laserOn, a.coeff[c]), J));
-    double tn;
-    const double Qv = a.Q[q];
-    if (T >= 373.0 && Qv < a.qvapor) {
-        if (energyIncrease > 0.0) {
+    double tn = heat;
+    // compares on the bit patterns (ieee_bits.h); Q is read only at 373 K and above
+    if (ieee::ge_pos(T, B_373)) {
+        const double Qv = a.Q[q];
+        if (ieee::lt(Qv, a.qvapor) && ieee::gt_zero(energyIncrease)) {
             const double qn = ADD(Qv, energyIncrease);
-            a.Q[q] = qn < a.qvapor ? qn : a.qvapor;
+            a.Q[q] = ieee::lt(qn, a.qvapor) ? qn : a.qvapor;
             tn = 373.0;
-        } else {
-            tn = heat;
         }
-    } else {
-        tn = heat;
-        if (T < 0.0) atomicOr(a.err, DEVERR_NEG_T);
+    } else if (ieee::lt_zero(T)) {
+        atomicOr(a.err, DEVERR_NEG_T);
     }
-    if (tn != tn) atomicOr(a.err, DEVERR_NAN);
+    if (ieee::is_nan(tn)) atomicOr(a.err, DEVERR_NAN);
     a.tn[c] = tn;
 }
 
@@ -89,18 +97,20 @@ __device__ __forceinline__ void ref_update_f32(const RefHeatArgs &a, int64_t c, 
     const float src = (float)a.laserOn * (float)a.coeff[c] * (float)J;
     const double heat = T + (double)(inc + src);
     double tn = heat;
-    const double Qv = a.Q[q];
-    if (T >= 373.0 && Qv < a.qvapor) {
-        const double energyIncrease = a.laserOn * J * a.delt * a.vvox + cc * a.mvox * (double)inc;
-        if (energyIncrease > 0.0) {
-            const double qn = Qv + energyIncrease;
-            a.Q[q] = qn < a.qvapor ? qn : a.qvapor;
-            tn = 373.0;
+    if (ieee::ge_pos(T, B_373)) {
+        const double Qv = a.Q[q];
+        if (ieee::lt(Qv, a.qvapor)) {
+            const double energyIncrease = a.laserOn * J * a.delt * a.vvox + cc * a.mvox * (double)inc;
+            if (ieee::gt_zero(energyIncrease)) {
+                const double qn = Qv + energyIncrease;
+                a.Q[q] = ieee::lt(qn, a.qvapor) ? qn : a.qvapor;
+                tn = 373.0;
+            }
         }
-    } else if (T < 0.0) {
+    } else if (ieee::lt_zero(T)) {
         atomicOr(a.err, DEVERR_NEG_T);
     }
-    if (tn != tn) atomicOr(a.err, DEVERR_NAN);
+    if (ieee::is_nan(tn)) atomicOr(a.err, DEVERR_NAN);
     a.tn[c] = tn;
 }
 
@@ -202,16 +212,17 @@ __global__ void ref_arrhenius_kernel(const RefArrheniusArgs a)
     const int64_t q = (int64_t)(x - 1) + (int64_t)a.nx * ((int64_t)(y - 1) + (int64_t)a.ny * (int64_t)(z - 1));
     const double T = a.temp[I(x, y, z)];
     double om = a.tissue[q];
-    // src/3dFD.f90:450-452 with A=3.1d98, dE=6.3d5, R=8.314d0
-    if (T >= 316.0 && T < 373.0 && a.rhokap[I(x, y, z)] >= 0.0) {
+    // src/3dFD.f90:450-452 with A=3.1d98, dE=6.3d5, R=8.314d0 (compares on
+    // the bit patterns, ieee_bits.h)
+    if (ieee::ge_pos(T, B_316) && ieee::lt_pos(T, B_373) && ieee::ge_zero(a.rhokap[I(x, y, z)])) {
         om = ADD(om, MUL(MUL(a.delt, 3.1e98), exp(-DIV(6.3e5, MUL(8.314, T)))));
         a.tissue[q] = om;
     }
     // src/3dFD.f90:455-461
     double *t1 = a.thres + q, *t2 = a.thres + q + ni, *t3 = a.thres + q + 2 * ni;
-    if (*t1 == 0.0 && om >= 0.53) *t1 = a.time;
-    else if (*t2 == 0.0 && om >= 1.0) *t2 = a.time;
-    else if (*t3 == 0.0 && om >= 10000.0) *t3 = a.time;
+    if (ieee::is_zero(*t1) && ieee::ge_pos(om, B_0_53)) *t1 = a.time;
+    else if (ieee::is_zero(*t2) && ieee::ge_pos(om, B_1)) *t2 = a.time;
+    else if (ieee::is_zero(*t3) && ieee::ge_pos(om, B_1E4)) *t3 = a.time;
 }
 
 // src/thermalConst_mod.f90 with explicit rounding (the reference evaluates
@@ -247,34 +258,41 @@ __global__ void ref_props_kernel(const RefPropsArgs a)
     const H I{a.nx + 2, a.ny + 2};
     const int64_t c = I(i, j, k);
     const int64_t q = (int64_t)(i - 1) + (int64_t)a.nx * ((int64_t)(j - 1) + (int64_t)a.ny * (int64_t)(k - 1));
-    const double abl_T = ADD(a.ablate_temp, 273.0);
+    const double abl_T = a.abl_T;
     const double T = a.temp[c];
-    // WaterContent = getWaterContent(Q, watercontent)  (src/3dFD.f90:328)
-    const double wa = SUB(0.75, MUL(0.75, DIV(a.Q[q], a.qvapor)));
-    double w = wa < 0.75 ? wa : 0.75;
+    // WaterContent = getWaterContent(Q, watercontent)  (src/3dFD.f90:328).
+    // Compares run on the bit patterns (ieee_bits.h), and a zero Q gives
+    // 0.75 - 0.75 * (0 / qvapor) = 0.75 exactly unless qvapor is 0 or NaN,
+    // so the FP64 division is skipped for it.
+    const double Qv = a.Q[q];
+    double wa = 0.75;
+    if (!ieee::is_zero(Qv) || ieee::is_zero(a.qvapor) || ieee::is_nan(a.qvapor))
+        wa = SUB(0.75, MUL(0.75, DIV(Qv, a.qvapor)));
+    double w = ieee::lt_pos(wa, B_0_75) ? wa : 0.75;
     const double wo = a.water[q];
-    w = w < wo ? w : wo;
-    w = w > 0.0 ? w : 0.0;
+    w = ieee::lt(w, wo) ? w : wo;
+    w = ieee::gt_zero(w) ? w : 0.0;
     a.water[q] = w;
 
     const double *rk = a.rk_old;
-    const bool abl = T >= abl_T;
-    bool zero = abl || !(rk[c] > 0.0);
+    const bool abl = ieee::le(abl_T, T);
+    bool zero = abl || !ieee::gt_zero(rk[c]);
     if (!zero) {
         // backward neighbours (already swept): zero if zero before or ablated now
         bool iso = true;
-        if (i > 1) iso = iso && (rk[I(i - 1, j, k)] == 0.0 || a.temp[I(i - 1, j, k)] >= abl_T);
-        else iso = iso && (rk[I(i - 1, j, k)] == 0.0);
-        if (j > 1) iso = iso && (rk[I(i, j - 1, k)] == 0.0 || a.temp[I(i, j - 1, k)] >= abl_T);
-        else iso = iso && (rk[I(i, j - 1, k)] == 0.0);
-        if (k > 1) iso = iso && (rk[I(i, j, k - 1)] == 0.0 || a.temp[I(i, j, k - 1)] >= abl_T);
-        else iso = iso && (rk[I(i, j, k - 1)] == 0.0);
+        if (i > 1) iso = iso && (ieee::is_zero(rk[I(i - 1, j, k)]) || ieee::le(abl_T, a.temp[I(i - 1, j, k)]));
+        else iso = iso && ieee::is_zero(rk[I(i - 1, j, k)]);
+        if (j > 1) iso = iso && (ieee::is_zero(rk[I(i, j - 1, k)]) || ieee::le(abl_T, a.temp[I(i, j - 1, k)]));
+        else iso = iso && ieee::is_zero(rk[I(i, j - 1, k)]);
+        if (k > 1) iso = iso && (ieee::is_zero(rk[I(i, j, k - 1)]) || ieee::le(abl_T, a.temp[I(i, j, k - 1)]));
+        else iso = iso && ieee::is_zero(rk[I(i, j, k - 1)]);
         // forward neighbours (not yet swept): old values
-        iso = iso && rk[I(i + 1, j, k)] == 0.0 && rk[I(i, j + 1, k)] == 0.0 && rk[I(i, j, k + 1)] == 0.0;
+        iso = iso && ieee::is_zero(rk[I(i + 1, j, k)]) && ieee::is_zero(rk[I(i, j + 1, k)]) &&
+              ieee::is_zero(rk[I(i, j, k + 1)]);
         zero = iso;
     }
     if (!zero) {
-        if (a.reuse && w == wo) {
+        if (a.reuse && ieee::eq(w, wo)) {
             // the water content is what the previous call's skin branch saw:
             // its properties are still in place and would come out bit for bit
             // the same, so only the ping-pong copy of rhokap is written
@@ -289,7 +307,7 @@ __global__ void ref_props_kernel(const RefPropsArgs a)
         a.kappa[c] = skin_cond(w, dn);
         a.coeff[c] = DIV(a.delt, MUL(dn, hc));
     } else {
-        if (T < 0.0) atomicOr(a.err, DEVERR_NEG_T);
+        if (ieee::lt_zero(T)) atomicOr(a.err, DEVERR_NEG_T);
         const double dn = air_dens(T);
         const double hc = 1.006e3;
         const double kk = air_cond(T);

@@ -594,21 +594,22 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, bool sync =
     }
     CK(cudaEventRecord(ctx->ev[1], s));
     ctx->have_mc_time = true;
-    CK(tam::launch_sum_f64(ctx->d_jmean, ctx->ni, ctx->d_tally + tam::T_ABSORBED, s));
     ctx->last_n = n;
     ctx->mc_passes += 1;
     // normalisation (src/mcpolar.f90:174)
     if (ctx->config) {
         const double f = n > 0 ? 1.0 / ((double)n * ctx->volumeVoxel) : 0.0;
-        if (ctx->fp64) CK(tam::launch_scale_f64((double *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s));
-        else CK(tam::launch_scale_to_f32((float *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s));
+        // the total absorbed weight (zeroed with the tallies above) is summed in the same pass
+        double *absorbed = ctx->d_tally + tam::T_ABSORBED;
+        if (ctx->fp64) CK(tam::launch_scale_f64((double *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s, absorbed));
+        else CK(tam::launch_scale_to_f32((float *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s, absorbed));
     } else {
         const tam_params &p = ctx->p;
         const double pw = get_pwr(ctx);
         const double den = (double)n * (2. * p.xmax * 1.e-2 / p.nxg) * (2. * p.ymax * 1.e-2 / p.nyg) *
                            (2. * p.zmax * 1.e-2 / p.nzg);
         const double f = n > 0 ? (pw / 81.0) / den : 0.0;
-        CK(tam::launch_scale_f64(ctx->d_jglob, ctx->d_jmean, f, ctx->ni, false, s));
+        CK(tam::launch_scale_f64(ctx->d_jglob, ctx->d_jmean, f, ctx->ni, false, s, ctx->d_tally + tam::T_ABSORBED));
     }
     if (!sync) {
         ctx->tally_stale = true;
@@ -691,7 +692,7 @@ int ref_props(tam_ctx *ctx, double ablate_temp)
     a.nx = ctx->nx;
     a.ny = ctx->ny;
     a.nz = ctx->nz;
-    a.ablate_temp = ablate_temp;
+    a.abl_T = ablate_temp + 273.0;  // src/3dFD.f90: ablateTemp + 273 (one IEEE add, as on the device)
     a.delt = ctx->delt;
     a.qvapor = ctx->QVapor;
     a.mu_water = ctx->mu_water;

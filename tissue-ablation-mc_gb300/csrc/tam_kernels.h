@@ -67,8 +67,11 @@ cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cu
 cudaError_t launch_flush_f32(double *acc, float *part, int64_t n, cudaStream_t s);
 
 // out[q] = in[q] * f for q < n; in is then zeroed when zero_in is set.
-cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s);
-cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s);
+// out = in * f; with `sum`, also *sum += the total of in (the caller zeroes *sum)
+cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s,
+                             double *sum = nullptr);
+cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s,
+                                double *sum = nullptr);
 
 // Philox self-test: out_mine / out_curand hold 4 words per input; in holds 6
 // words per input {c0, c1, c2, c3, k0, k1}.
@@ -101,7 +104,7 @@ cudaError_t launch_ref_arrhenius(const RefArrheniusArgs &a, cudaStream_t s);
 
 struct RefPropsArgs {
     int32_t nx, ny, nz;
-    double ablate_temp, delt, qvapor, mu_water, mu_protein;
+    double abl_T, delt, qvapor, mu_water, mu_protein;  // abl_T: ablation temperature + 273 (kelvin)
     const double *temp;               // halo
     const double *rk_old;             // halo
     double *rk_new;                   // halo (interior written)

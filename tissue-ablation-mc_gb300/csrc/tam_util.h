@@ -25,7 +25,6 @@ cudaError_t launch_interior_to_halo(const void *src, bool fp64, double *halo, in
 cudaError_t launch_halo_to_interior(const double *halo, void *dst, bool fp64, int nx, int ny, int nz, cudaStream_t s);
 cudaError_t launch_rhokap_from_mat(const uint8_t *mat, int nmat, const MatThermal &lut, double *halo, int nx, int ny,
                                    int nz, cudaStream_t s);
-cudaError_t launch_sum_f64(const double *p, int64_t n, double *out, cudaStream_t s);
 cudaError_t launch_count_negative(const double *p, int64_t n, unsigned long long *out, cudaStream_t s);
 
 }  // namespace tam

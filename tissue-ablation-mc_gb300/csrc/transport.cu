@@ -602,19 +602,31 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
     }
 }
 
-__global__ void scale_f64_kernel(double *out, double *in, double f, int64_t n, int zero_in)
+// out = in * f (normalisation of the tally), and with `sum` the total of
+// `in` added to *sum: one FP64 atomic per block, so the grid is kept to a few
+// thousand blocks
+template <typename Out>
+__global__ void scale_kernel(Out *out, double *in, double f, int64_t n, int zero_in, double *sum)
 {
+    double acc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        out[q] = in[q] * f;
+        const double v = in[q];
+        out[q] = (Out)(v * f);
+        acc += v;
         if (zero_in) in[q] = 0.0;
     }
-}
-
-__global__ void scale_f32_kernel(float *out, double *in, double f, int64_t n, int zero_in)
-{
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        out[q] = (float)(in[q] * f);
-        if (zero_in) in[q] = 0.0;
+    if (!sum) return;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    __shared__ double ws[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) ws[wid] = acc;
+    __syncthreads();
+    if (wid == 0) {
+        acc = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+        if (lane == 0) atomicAdd(sum, acc);
     }
 }
 
@@ -695,11 +707,19 @@ cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cu
     return a.jmean32 ? launch_t<float, MED_MATERIAL, true>(a, sm_count, s) : launch_t<float, MED_MATERIAL>(a, sm_count, s);
 }
 
-cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s)
+// at least four elements per thread, at most 152 x 16 blocks (atomics on *sum)
+static int scale_grid(int64_t n)
+{
+    int64_t b = (n + 1023) / 1024;
+    if (b > 152 * 16) b = 152 * 16;
+    return (int)(b > 0 ? b : 1);
+}
+
+cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s, double *sum)
 {
     if (n <= 0) return cudaSuccess;
     count_launch();
-    scale_f64_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0);
+    scale_kernel<double><<<scale_grid(n), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0, sum);
     return cudaGetLastError();
 }
 
@@ -711,11 +731,11 @@ cudaError_t launch_flush_f32(double *acc, float *part, int64_t n, cudaStream_t s
     return cudaGetLastError();
 }
 
-cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s)
+cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s, double *sum)
 {
     if (n <= 0) return cudaSuccess;
     count_launch();
-    scale_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0);
+    scale_kernel<float><<<scale_grid(n), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0, sum);
     return cudaGetLastError();
 }
 

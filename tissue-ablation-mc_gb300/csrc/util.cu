@@ -134,24 +134,6 @@ __global__ void rhokap_from_mat_kernel(const uint8_t *mat, int nmat, MatThermal 
     }
 }
 
-__global__ void sum_f64_kernel(const double *p, int64_t n, double *out)
-{
-    double s = 0.0;
-    GRID_STRIDE(q, n) s += p[q];
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    __shared__ double ws[32];
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) ws[wid] = s;
-    __syncthreads();
-    if (wid == 0) {
-        s = lane < (int)(blockDim.x >> 5) ? ws[lane] : 0.0;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-        if (lane == 0) atomicAdd(out, s);
-    }
-}
-
 // min / max of rhokap-like halo array over the interior (validation helper)
 __global__ void count_negative_kernel(const double *p, int64_t n, unsigned long long *out)
 {
@@ -250,14 +232,6 @@ cudaError_t launch_rhokap_from_mat(const uint8_t *mat, int nmat, const MatTherma
     const int64_t n = (int64_t)(nx + 2) * (ny + 2) * (nz + 2);
     count_launch();
     rhokap_from_mat_kernel<<<blocks_for(n, 256), 256, 0, s>>>(mat, nmat, lut, halo, nx, ny, nz);
-    return cudaGetLastError();
-}
-cudaError_t launch_sum_f64(const double *p, int64_t n, double *out, cudaStream_t s)
-{
-    cudaError_t e = cudaMemsetAsync(out, 0, sizeof(double), s);
-    if (e != cudaSuccess || n <= 0) return e;
-    count_launch();
-    sum_f64_kernel<<<blocks_for(n, 256), 256, 0, s>>>(p, n, out);
     return cudaGetLastError();
 }
 cudaError_t launch_count_negative(const double *p, int64_t n, unsigned long long *out, cudaStream_t s)
