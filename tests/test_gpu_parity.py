@@ -106,6 +106,16 @@ def test_ref_stencil_fp32_form_within_1mK(tam, orc, case, n):
         o.arr("jmeanGLOBAL")[...] = rng.uniform(0.0, 5e7, (nx, ny, nz))
         for f, name in ((F.TAM_F_TEMP, "temp"), (F.TAM_F_JMEAN_GLOBAL, "jmeanGLOBAL")):
             ctx.upload(f, o.arr(name))
+    if case == "smooth":
+        # the FP32 copies of the fields are rebuilt after an upload: halfway,
+        # a 20 K hot block is written into the temperatures on both sides
+        n //= 2
+        o.st.p.loops = n
+        assert o.heat_sim(nthreads=1) == 0
+        ctx.heat_steps(n)
+        To = o.arr("temp")
+        To[5:10, 4:8, 3:6] += 20.0
+        ctx.upload(F.TAM_F_TEMP, To)
     o.st.p.loops = n
     assert o.heat_sim(nthreads=1) == 0
     T = ctx.heat_steps(n, want=True)
@@ -117,6 +127,39 @@ def test_ref_stencil_fp32_form_within_1mK(tam, orc, case, n):
     assert ctx.state().time == o.st.time and ctx.device_errors() == 0
     ctx.close()
     o.close()
+
+
+def test_ref_fp32_form_follows_property_updates(tam):
+    # the property update writes the FP32 copies of kappa, density, heatcap
+    # and coeff beside the FP64 fields: a random Q lowers the water content,
+    # and with it the properties of every voxel, on the first update, and
+    # the FP32 form (which reads only the copies) stays within 1 mK of the
+    # FP64 form over 100 coupled heat steps and property updates below boiling
+    nx, ny, nz = 20, 16, 12
+    rng = np.random.default_rng(3)
+    ctxs = [tam.Context(tam.default_params(nxg=nx, nyg=ny, nzg=nz, precision=p)) for p in (0, 1)]
+    T = ctxs[0].download(F.TAM_F_TEMP)
+    T[1:nx + 1, 1:ny + 1, 1:nz + 1] = rng.uniform(300.0, 340.0, (nx, ny, nz))
+    J = rng.uniform(0.0, 5e7, (nx, ny, nz))
+    Q = rng.uniform(0.0, ctxs[0].state().qvapor, (nx, ny, nz))
+    for c in ctxs:
+        c.upload(F.TAM_F_TEMP, T)
+        c.upload(F.TAM_F_JMEAN_GLOBAL, J)
+        c.upload(F.TAM_F_Q, Q)
+    k0 = ctxs[0].download(F.TAM_F_KAPPA)
+    for _ in range(100):
+        for c in ctxs:
+            c.heat_steps(1)
+            c.update_props(500.0)
+    k1 = ctxs[0].download(F.TAM_F_KAPPA)
+    assert np.abs(k1 - k0).max() > 0.1 * np.abs(k0).max()  # the properties did change
+    T64, T32 = (c.download(F.TAM_F_TEMP) for c in ctxs)
+    assert T64.max() < 373.0
+    dT = np.abs(T32 - T64).max()
+    assert 0.0 < dT <= 1e-3, dT
+    assert all(c.device_errors() == 0 for c in ctxs)
+    for c in ctxs:
+        c.close()
 
 
 def test_ref_arrhenius_fp64_matches_oracle(tam, orc):

@@ -88,19 +88,20 @@ __device__ __forceinline__ void ref_update(const RefHeatArgs &a, int64_t c, int6
 
 // The FP32 form of the same update: the step's increment and source term in
 // FP32, added to the FP64 temperature in FP64 (so no compensation is
-// needed); the latent-heat branch, rare, stays FP64.
-__device__ __forceinline__ void ref_update_f32(const RefHeatArgs &a, int64_t c, int64_t q, double T, double cc,
+// needed), and the FP32 copy of the result written beside it; the
+// latent-heat branch, rare, stays FP64.
+__device__ __forceinline__ void ref_update_f32(const RefHeatArgs &a, int64_t c, int64_t q, double T, float cc,
                                                float u_xx, float u_yy, float u_zz)
 {
     const double J = a.J[q];
     const float inc = (float)a.delt * ((u_xx + u_yy) + u_zz);
-    const float src = (float)a.laserOn * (float)a.coeff[c] * (float)J;
+    const float src = (float)a.laserOn * a.p32[3 * a.nh + c] * (float)J;
     const double heat = T + (double)(inc + src);
     double tn = heat;
     if (ieee::ge_pos(T, B_373)) {
         const double Qv = a.Q[q];
         if (ieee::lt(Qv, a.qvapor)) {
-            const double energyIncrease = a.laserOn * J * a.delt * a.vvox + cc * a.mvox * (double)inc;
+            const double energyIncrease = a.laserOn * J * a.delt * a.vvox + (double)cc * a.mvox * (double)inc;
             if (ieee::gt_zero(energyIncrease)) {
                 const double qn = Qv + energyIncrease;
                 a.Q[q] = ieee::lt(qn, a.qvapor) ? qn : a.qvapor;
@@ -112,12 +113,12 @@ __device__ __forceinline__ void ref_update_f32(const RefHeatArgs &a, int64_t c, 
     }
     if (ieee::is_nan(tn)) atomicOr(a.err, DEVERR_NAN);
     a.tn[c] = tn;
+    a.sn[c] = (float)tn;
 }
 
 // Face terms and axis sums of the reference stencil in the working precision
 // F: double keeps the Fortran's operations and order (bit parity); float is
-// the precision form (face coefficients and sums in FP32 from the FP64
-// properties, neighbour differences formed in FP64).
+// the precision form, on FP32 copies of the properties and temperatures.
 template <typename F> struct RefOps;
 template <> struct RefOps<double> {
     static __device__ __forceinline__ double face(double kc, double kn, double dc, double dn, double cc, double cn,
@@ -131,17 +132,15 @@ template <> struct RefOps<double> {
     }
 };
 template <> struct RefOps<float> {
-    static __device__ __forceinline__ float face(double kc, double kn, double dc, double dn, double cc, double cn,
-                                                 double id2)
+    static __device__ __forceinline__ float face(float kc, float kn, float dc, float dn, float cc, float cn, float id2)
     {
-        const float kh = 0.5f * ((float)kc + (float)kn), dh = 0.5f * ((float)dc + (float)dn),
-                    ch = 0.5f * ((float)cc + (float)cn);
-        return 0.5f * __fdividef(kh, dh * ch) * (float)id2;
+        const float kh = 0.5f * (kc + kn), dh = 0.5f * (dc + dn), ch = 0.5f * (cc + cn);
+        return 0.5f * __fdividef(kh, dh * ch) * id2;
     }
     // a (T- - T) + d (T+ - T): the reference's a T- - 2b T + d T+ with b = (a + d)/2
-    static __device__ __forceinline__ float axis(float a, float d, double tm, double t, double tp)
+    static __device__ __forceinline__ float axis(float a, float d, float tm, float t, float tp)
     {
-        return a * (float)(tm - t) + d * (float)(tp - t);
+        return a * (tm - t) + d * (tp - t);
     }
 };
 
@@ -167,32 +166,40 @@ template <typename F> __global__ void __launch_bounds__(256) ref_stencil_kernel(
     const int ic = min(i, a.nx + 1), jc = min(j, a.ny + 1);
     const int k0 = blockIdx.z * REF_ZC + 1, k1 = min(a.nz, k0 + REF_ZC - 1);
     const H I{a.nx + 2, a.ny + 2};
-    const double *K = a.kappa, *D = a.density, *C = a.heatcap, *t0 = a.t0;
+    // the fields the stencil reads: FP64 for the parity form, the FP32
+    // copies for the precision form (whose update still adds to the FP64 T)
+    const F *K, *D, *C, *tt;
+    if constexpr (sizeof(F) == 8) {
+        K = a.kappa, D = a.density, C = a.heatcap, tt = a.t0;
+    } else {
+        K = a.p32, D = a.p32 + a.nh, C = a.p32 + 2 * a.nh, tt = a.s0;
+    }
+    const F idx2 = (F)a.idx2, idy2 = (F)a.idy2, idz2 = (F)a.idz2;
     int64_t c = I(ic, jc, k0);
     const int64_t sz = (int64_t)(a.nx + 2) * (a.ny + 2), sy = a.nx + 2;
-    double kc = K[c], dc = D[c], cc = C[c];
-    F fzm = O::face(kc, K[c - sz], dc, D[c - sz], cc, C[c - sz], a.idz2);
+    F kc = K[c], dc = D[c], cc = C[c];
+    F fzm = O::face(kc, K[c - sz], dc, D[c - sz], cc, C[c - sz], idz2);
     for (int k = k0; k <= k1; ++k, c += sz) {
-        const double kp = K[c + sz], dp = D[c + sz], cp = C[c + sz];
-        const F fzp = O::face(kc, kp, dc, dp, cc, cp, a.idz2);
-        const F fym = O::face(kc, K[c - sy], dc, D[c - sy], cc, C[c - sy], a.idy2);
-        const F fxm = O::face(kc, K[c - 1], dc, D[c - 1], cc, C[c - 1], a.idx2);
+        const F kp = K[c + sz], dp = D[c + sz], cp = C[c + sz];
+        const F fzp = O::face(kc, kp, dc, dp, cc, cp, idz2);
+        const F fym = O::face(kc, K[c - sy], dc, D[c - sy], cc, C[c - sy], idy2);
+        const F fxm = O::face(kc, K[c - 1], dc, D[c - 1], cc, C[c - 1], idx2);
         s_fy[ty][tx] = fym;
         F fxp = __shfl_down_sync(0xffffffffu, fxm, 1);
-        if (tx == 31 && ic <= a.nx) fxp = O::face(kc, K[c + 1], dc, D[c + 1], cc, C[c + 1], a.idx2);
+        if (tx == 31 && ic <= a.nx) fxp = O::face(kc, K[c + 1], dc, D[c + 1], cc, C[c + 1], idx2);
         __syncthreads();
         F fyp = 0;
         if (ty < 7) fyp = s_fy[ty + 1][tx];
-        else if (jc <= a.ny) fyp = O::face(kc, K[c + sy], dc, D[c + sy], cc, C[c + sy], a.idy2);
+        else if (jc <= a.ny) fyp = O::face(kc, K[c + sy], dc, D[c + sy], cc, C[c + sy], idy2);
         __syncthreads();  // the row is read before the next plane overwrites it
         if (in) {
-            const double T = t0[c];
-            const F u_zz = O::axis(fzm, fzp, t0[c - sz], T, t0[c + sz]);
-            const F u_yy = O::axis(fym, fyp, t0[c - sy], T, t0[c + sy]);
-            const F u_xx = O::axis(fxm, fxp, t0[c - 1], T, t0[c + 1]);
+            const F t = tt[c];
+            const F u_zz = O::axis(fzm, fzp, tt[c - sz], t, tt[c + sz]);
+            const F u_yy = O::axis(fym, fyp, tt[c - sy], t, tt[c + sy]);
+            const F u_xx = O::axis(fxm, fxp, tt[c - 1], t, tt[c + 1]);
             const int64_t q = (int64_t)(i - 1) + (int64_t)a.nx * ((int64_t)(j - 1) + (int64_t)a.ny * (int64_t)(k - 1));
-            if constexpr (sizeof(F) == 8) ref_update(a, c, q, T, cc, u_xx, u_yy, u_zz);
-            else ref_update_f32(a, c, q, T, cc, u_xx, u_yy, u_zz);
+            if constexpr (sizeof(F) == 8) ref_update(a, c, q, t, cc, u_xx, u_yy, u_zz);
+            else ref_update_f32(a, c, q, a.t0[c], cc, u_xx, u_yy, u_zz);
         }
         fzm = fzp;
         kc = kp;
@@ -249,6 +256,15 @@ __device__ __forceinline__ double skin_cond(double w, double rho)
 //   zero_new(v) = abl(v) | !(rk_old(v) > 0) |
 //                 [AND_back (rk_old(b)==0 | abl(b))] & [AND_fwd rk_old(f)==0]
 // with ghost neighbours counting as zero.  rhokap is double-buffered.
+// FP32 copies of one voxel's new properties, for the FP32 form of the stencil
+__device__ __forceinline__ void store_p32(const RefPropsArgs &a, int64_t c, double kk, double dn, double hc, double cf)
+{
+    a.p32[c] = (float)kk;
+    a.p32[a.nh + c] = (float)dn;
+    a.p32[2 * a.nh + c] = (float)hc;
+    a.p32[3 * a.nh + c] = (float)cf;
+}
+
 __global__ void ref_props_kernel(const RefPropsArgs a)
 {
     const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
@@ -301,11 +317,13 @@ __global__ void ref_props_kernel(const RefPropsArgs a)
         }
         const double dn = skin_dens(w);
         const double hc = skin_cap(w);
+        const double kk = skin_cond(w, dn), cf = DIV(a.delt, MUL(dn, hc));
         a.density[c] = dn;
         a.rk_new[c] = ADD(MUL(w, a.mu_water), a.mu_protein);
         a.heatcap[c] = hc;
-        a.kappa[c] = skin_cond(w, dn);
-        a.coeff[c] = DIV(a.delt, MUL(dn, hc));
+        a.kappa[c] = kk;
+        a.coeff[c] = cf;
+        if (a.p32) store_p32(a, c, kk, dn, hc, cf);
     } else {
         if (ieee::lt_zero(T)) atomicOr(a.err, DEVERR_NEG_T);
         const double dn = air_dens(T);
@@ -316,7 +334,25 @@ __global__ void ref_props_kernel(const RefPropsArgs a)
         a.rk_new[c] = 0.0;
         a.kappa[c] = kk;
         a.alpha[c] = DIV(kk, MUL(dn, hc));
-        a.coeff[c] = DIV(a.delt, MUL(air_dens(T), hc));
+        const double cf = DIV(a.delt, MUL(air_dens(T), hc));
+        a.coeff[c] = cf;
+        if (a.p32) store_p32(a, c, kk, dn, hc, cf);
+    }
+}
+
+// FP32 copies of the temperature (into both ping-pong buffers, halo
+// included) and of the four properties the FP32 stencil reads.
+__global__ void ref_shadow_kernel(int64_t nh, const double *T, float *ta, float *tb, const double *kappa,
+                                  const double *density, const double *heatcap, const double *coeff, float *p32)
+{
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < nh; c += (int64_t)gridDim.x * blockDim.x) {
+        const float t = (float)T[c];
+        ta[c] = t;
+        tb[c] = t;
+        p32[c] = (float)kappa[c];
+        p32[nh + c] = (float)density[c];
+        p32[2 * nh + c] = (float)heatcap[c];
+        p32[3 * nh + c] = (float)coeff[c];
     }
 }
 
@@ -700,6 +736,18 @@ cudaError_t launch_ref_props(const RefPropsArgs &a, cudaStream_t s)
 {
     count_launch();
     ref_props_kernel<<<ref_grid(a.nx, a.ny, a.nz), dim3(32, 8), 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ref_shadow(int64_t nh, const double *T, float *t32a, float *t32b, const double *kappa,
+                              const double *density, const double *heatcap, const double *coeff, float *p32,
+                              cudaStream_t s)
+{
+    if (nh <= 0) return cudaSuccess;
+    int64_t b = (nh + 255) / 256;
+    if (b > 152 * 16) b = 152 * 16;
+    count_launch();
+    ref_shadow_kernel<<<(int)b, 256, 0, s>>>(nh, T, t32a, t32b, kappa, density, heatcap, coeff, p32);
     return cudaGetLastError();
 }
 

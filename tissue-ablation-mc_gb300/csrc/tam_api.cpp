@@ -94,6 +94,13 @@ struct tam_ctx {
     long long nabl_at_trace = 0;
     int32_t since_check = 0;   // heat steps since the last re-trace check (config mode)
     double props_delt = -1.0;  // delt of the last property update whose results are intact (<0: none)
+    // reference mode, FP32 form: FP32 copies of the temperatures (ping-pong
+    // with d_T) and of kappa, density, heatcap and coeff (4 x nh, in that
+    // order), kept by the heat step and the property update; rebuilt from the
+    // FP64 fields when anything else has written those (shadow_ok false)
+    float *d_t32[2] = {nullptr, nullptr};
+    float *d_p32 = nullptr;
+    bool shadow_ok = false;
 
     // tuning knobs
     int scat_min = 20;
@@ -147,6 +154,18 @@ struct tam_ctx {
     int64_t mc_passes = 0;
     unsigned errbits_seen = 0;
 };
+
+namespace {
+// The fields were written by something other than the heat step and the
+// property update (set-up, an upload, a checkpoint load, new constants): the
+// property update recomputes every voxel next time and the FP32 copies are
+// rebuilt before the next heat step.
+void fields_changed(tam_ctx *ctx)
+{
+    ctx->props_delt = -1.0;
+    ctx->shadow_ok = false;
+}
+}  // namespace
 
 namespace {
 
@@ -304,7 +323,7 @@ void reset_scalars(tam_ctx *ctx)
 int ref_setup(tam_ctx *ctx)
 {
     reset_scalars(ctx);
-    ctx->props_delt = -1.0;  // properties set here, not by the update kernel
+    fields_changed(ctx);  // properties set here, not by the update kernel
     const tam_params &p = ctx->p;
     const int nx = ctx->nx, ny = ctx->ny, nz = ctx->nz;
     cudaStream_t s = ctx->stream;
@@ -654,12 +673,25 @@ int ref_heat(tam_ctx *ctx, int32_t loops)
     a.J = ctx->d_jglob;
     a.Q = ctx->d_Q;
     a.err = ctx->d_err;
-    a.f32 = ctx->fp64 ? 0 : 1;  // the precision form: FP32 stencil arithmetic, FP64 temperatures
+    // the precision form: FP32 stencil arithmetic on FP32 copies of the
+    // temperatures and properties, the update added to the FP64 temperatures
+    a.f32 = ctx->fp64 ? 0 : 1;
+    if (a.f32) {
+        if (!ctx->shadow_ok) {
+            CK(tam::launch_ref_shadow(ctx->nh, ctx->d_T[ctx->tcur], ctx->d_t32[0], ctx->d_t32[1], ctx->d_kappa,
+                                      ctx->d_density, ctx->d_heatcap, ctx->d_coeff, ctx->d_p32, ctx->stream));
+            ctx->shadow_ok = true;
+        }
+        a.p32 = ctx->d_p32;
+        a.nh = ctx->nh;
+    }
     for (int32_t it = 0; it < loops; ++it) {
         a.delt = ctx->delt;
         a.laserOn = ctx->laserOn;
         a.t0 = ctx->d_T[ctx->tcur];
         a.tn = ctx->d_T[1 - ctx->tcur];
+        a.s0 = ctx->d_t32[ctx->tcur];
+        a.sn = ctx->d_t32[1 - ctx->tcur];
         CK(tam::launch_ref_stencil(a, ctx->stream));
         ctx->tcur = 1 - ctx->tcur;  // t0 = tn (src/3dFD.f90:187)
         pulse_update(ctx, ctx->delt);
@@ -709,6 +741,8 @@ int ref_props(tam_ctx *ctx, double ablate_temp)
     a.water = ctx->d_water;
     a.err = ctx->d_err;
     a.reuse = ctx->props_delt == ctx->delt ? 1 : 0;
+    a.p32 = ctx->fp64 ? nullptr : ctx->d_p32;  // FP32 copies written beside the FP64 properties
+    a.nh = ctx->nh;
     CK(tam::launch_ref_props(a, ctx->stream));
     ctx->rcur = 1 - ctx->rcur;
     ctx->props_delt = ctx->delt;
@@ -1248,6 +1282,11 @@ int tam_create(const tam_params *p, const tam_config *cfg, tam_ctx **out)
         AL(ctx->d_alpha, ctx->nh);
         AL(ctx->d_Q, ctx->ni);
         AL(ctx->d_water, ctx->ni);
+        if (!ctx->fp64) {
+            AL(ctx->d_t32[0], ctx->nh);
+            AL(ctx->d_t32[1], ctx->nh);
+            AL(ctx->d_p32, 4 * ctx->nh);
+        }
     } else {
         const size_t rs = ctx->fp64 ? 8 : 4;
         for (int b = 0; b < 2 && r == TAM_OK; ++b) {
@@ -1356,7 +1395,7 @@ int tam_init_opt(tam_ctx *ctx)
 {
     if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
     if (ctx->config) return fail(ctx, TAM_E_STATE, "init_opt1 applies to reference mode");
-    ctx->props_delt = -1.0;  // the absorption constants enter the property update
+    fields_changed(ctx);  // the absorption constants enter the property update
     ctx->hgg = 0.9;
     ctx->g2 = ctx->hgg * ctx->hgg;
     ctx->mu_water = 510.0;
@@ -1373,7 +1412,7 @@ int tam_gridset(tam_ctx *ctx, double xmax, double ymax, double zmax)
     if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
     if (!(xmax > 0) || !(ymax > 0) || !(zmax > 0)) return fail(ctx, TAM_E_INVALID, "half-widths must be > 0");
     CK(cudaSetDevice(ctx->device));
-    ctx->props_delt = -1.0;
+    fields_changed(ctx);
     ctx->p.xmax = xmax;
     ctx->p.ymax = ymax;
     ctx->p.zmax = zmax;
@@ -1412,7 +1451,7 @@ int tam_field_bytes(tam_ctx *ctx, int field, int64_t *nbytes)
 int tam_upload(tam_ctx *ctx, int field, const void *host, int64_t nbytes)
 {
     if (!ctx || !host) return fail(ctx, TAM_E_INVALID, "null argument");
-    ctx->props_delt = -1.0;  // an uploaded field may be one the property update reads or keeps
+    fields_changed(ctx);  // an uploaded field may be one the property update reads or keeps
     const FieldInfo fi = field_info(ctx, field);
     if (!fi.ok) return fail(ctx, TAM_E_STATE, "field " + std::to_string(field) + " not available in this mode");
     if (nbytes != fi.count * fi.esize) return fail(ctx, TAM_E_INVALID, "size mismatch for field " + std::to_string(field));
@@ -2238,7 +2277,7 @@ int tam_save_state(tam_ctx *ctx, const char *path)
 int tam_load_state(tam_ctx *ctx, const char *path)
 {
     if (!ctx || !path) return fail(ctx, TAM_E_INVALID, "null argument");
-    ctx->props_delt = -1.0;
+    fields_changed(ctx);
     CK(cudaSetDevice(ctx->device));
     std::ifstream f(path, std::ios::binary);
     if (!f) return fail(ctx, TAM_E_IO, std::string("cannot open ") + path);

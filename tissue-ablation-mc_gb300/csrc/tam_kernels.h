@@ -90,7 +90,11 @@ struct RefHeatArgs {
     const double *J;                  // interior jmeanGLOBAL
     double *Q;                        // interior
     unsigned *err;
-    int32_t f32;                      // 1: FP32 arithmetic on the FP64 fields (precision form)
+    int32_t f32;                      // 1: the FP32 form, on the FP32 copies below
+    int64_t nh;                       // halo cells per field
+    const float *p32;                 // FP32 kappa, density, heatcap, coeff (4 x nh)
+    const float *s0;                  // FP32 copy of t0
+    float *sn;                        // FP32 copy of tn, written with it
 };
 cudaError_t launch_ref_stencil(const RefHeatArgs &a, cudaStream_t s);
 
@@ -113,8 +117,16 @@ struct RefPropsArgs {
     double *water;                    // interior
     unsigned *err;
     int32_t reuse;                    // 1: the previous call's skin properties are intact (same delt)
+    float *p32;                       // null, or FP32 copies of kappa, density, heatcap, coeff (4 x nh)
+    int64_t nh;
 };
 cudaError_t launch_ref_props(const RefPropsArgs &a, cudaStream_t s);
+
+// FP32 copies for the FP32 form of the reference stencil: T into both
+// t32a and t32b (halo included), kappa, density, heatcap, coeff into p32
+cudaError_t launch_ref_shadow(int64_t nh, const double *T, float *t32a, float *t32b, const double *kappa,
+                              const double *density, const double *heatcap, const double *coeff, float *p32,
+                              cudaStream_t s);
 
 // tissue(rhokap <= 0.1) = -1 (src/mcpolar.f90:196-204)
 cudaError_t launch_ref_finalize(int nx, int ny, int nz, const double *rhokap, double *tissue, cudaStream_t s);
