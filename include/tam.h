@@ -84,7 +84,7 @@ typedef struct tam_params {
     int32_t numproc;             /* normalisation divisor, >= 1 */
     int32_t mode;                /* enum tam_mode */
     int32_t precision;           /* enum tam_precision: transport and heat step (reference mode:
-                                    FP32 face/axis arithmetic on FP64 temperatures) */
+                                    FP32 stencil, increments added to FP64 temperatures) */
     int32_t device;              /* CUDA device ordinal */
 } tam_params;
 
