@@ -36,7 +36,11 @@ constexpr uint64_t PINF = 0x7FF0000000000000ull;  // +inf; |x| bits above this a
 TAM_HD uint64_t bits(double x)
 {
 #if defined(__CUDA_ARCH__)
-    return (uint64_t)__double_as_longlong(x);
+    // an opaque move: the compiler would otherwise fold the integer tests
+    // below back into FP64 compares
+    uint64_t b;
+    asm("mov.b64 %0, %1;" : "=l"(b) : "d"(x));
+    return b;
 #else
     uint64_t b;
     std::memcpy(&b, &x, sizeof b);

@@ -32,6 +32,19 @@ struct OptMat {
 };
 
 // One transport pass (packets [p0, p0 + n)).
+// Per-launch constants of the transport kernel in the working precision,
+// computed once on the host by launch_transport (its IEEE double operations
+// give the bits a thread would compute), so no thread spends FP64 divisions
+// on them.
+template <typename Real> struct TrConst {
+    Real hx, hy, hz;                  // cell widths 2 max / n
+    Real knx, kny, knz;               // 1 - nudge / h: a crossed axis's next face after the nudge
+    Real w2x, w2y;                    // 2 xmax, 2 ymax
+    Real xmax, ymax;
+    Real wmin, rm, inv_rm;            // roulette threshold, survival factor and its inverse
+    Real namb, rhokap_n, src_r;       // ambient and rhokap-medium refractive indices, source radius
+};
+
 struct TransportArgs {
     int32_t nx, ny, nz;
     double xmax, ymax, zmax;          // half-widths, cm
@@ -58,6 +71,8 @@ struct TransportArgs {
     double *tally;                    // N_TALLY doubles
     unsigned long long *work;         // dynamic packet counter (zeroed by the launcher)
     unsigned *err;                    // device error word
+    TrConst<double> cd;               // filled by launch_transport
+    TrConst<float> cf;
 };
 
 // Launch the transport kernel in FP32 (fp64 == false) or FP64.

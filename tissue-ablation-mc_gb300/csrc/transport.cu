@@ -260,6 +260,12 @@ template <typename Real> __device__ __forceinline__ Real axis_pos(Real n, Real f
 // the next face of each axis and the cell width td along the ray; a crossing
 // moves tm of the crossed axis by td.  In-cell positions are reconstructed
 // only at events (interaction, outer face).
+template <typename Real> __device__ __forceinline__ const TrConst<Real> &consts(const TransportArgs &a)
+{
+    if constexpr (sizeof(Real) == 4) return a.cf;
+    else return a.cd;
+}
+
 template <typename Real, int MED, bool T32>
 __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) transport_kernel(const TransportArgs a, int scat_min)
 {
@@ -285,19 +291,19 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
     __syncthreads();
 
     const unsigned FULL = 0xffffffffu;
-    const Real hx = (Real)(2.0 * a.xmax / a.nx), hy = (Real)(2.0 * a.ymax / a.ny), hz = (Real)(2.0 * a.zmax / a.nz);
+    const TrConst<Real> &K = consts<Real>(a);
+    const Real hx = K.hx, hy = K.hy, hz = K.hz;
     const Real BIG = (Real)1.0e30;
     const Real TWOPI = (Real)TWOPI_R;
     // after a crossing the next face along the crossed axis is (h - nudge)
     // away along the axis: tm advances by td * (1 - nudge / h)
-    const Real knx = (Real)(1.0 - a.nudge / (2.0 * a.xmax / a.nx)), kny = (Real)(1.0 - a.nudge / (2.0 * a.ymax / a.ny)),
-               knz = (Real)(1.0 - a.nudge / (2.0 * a.zmax / a.nz));
+    const Real knx = K.knx, kny = K.kny, knz = K.knz;
     const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
     const unsigned lane = threadIdx.x & 31u;
-    const Real wmin = (Real)a.roulette_w, rm = (Real)a.roulette_m, inv_rm = (Real)(1.0 / a.roulette_m);
+    const Real wmin = K.wmin, rm = K.rm, inv_rm = K.inv_rm;
     const int NX = a.nx, NY = a.ny, NZ = a.nz, SY = a.nx, SZ = a.nx * a.ny;
     const uint32_t max_steps = a.max_steps > 0xfffffff0ll ? 0xfffffff0u : (uint32_t)a.max_steps;
-    const Real namb = (Real)a.n_ambient;
+    const Real namb = K.namb;
     // FP32 in a uniform medium: the flight is tracked by distance (tau / mut
     // once per flight) instead of optical depth per voxel step
     constexpr bool DIST = sizeof(Real) == 4 && MED == MED_UNIFORM;
@@ -334,22 +340,22 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     ev = 1;
                     const Real u0 = Uniform<Real>::from(r.x), u1 = Uniform<Real>::from(r.y);
                     const Real u2 = Uniform<Real>::from(r.z), u3 = Uniform<Real>::from(r.w);
-                    const Real R = (Real)a.source_radius;
+                    const Real R = K.src_r;
                     const Real rad = a.source == SRC_DISK ? M<Real>::sqrt(u0 * (R * R))
                                                           : R * M<Real>::sqrt((Real)0.5 * M<Real>::neglog(u0));
                     Real st, ct, sp, cp;
                     M<Real>::sincos(u1 * TWOPI, &st, &ct);
-                    const Real X = rad * ct + (Real)a.xmax, Y = rad * st + (Real)a.ymax;
+                    const Real X = rad * ct + K.xmax, Y = rad * st + K.ymax;
                     phi = TWOPI * u2;
                     M<Real>::sincos(phi, &sp, &cp);
                     cpv = cp;
                     spv = sp;
                     sint = (Real)0;
-                    if (!(X >= (Real)0 && X < (Real)(2.0 * a.xmax) && Y >= (Real)0 && Y < (Real)(2.0 * a.ymax))) {
+                    if (!(X >= (Real)0 && X < K.w2x && Y >= (Real)0 && Y < K.w2y)) {
                         atomicAdd(a.tally + T_MISSED, 1.0);
                     } else {
-                        ix = (int)((Real)NX * X / (Real)(2.0 * a.xmax));
-                        iy = (int)((Real)NY * Y / (Real)(2.0 * a.ymax));
+                        ix = (int)((Real)NX * X / K.w2x);
+                        iy = (int)((Real)NY * Y / K.w2y);
                         ix = ix > NX - 1 ? NX - 1 : ix;
                         iy = iy > NY - 1 ? NY - 1 : iy;
                         iz = NZ - 1;
@@ -360,7 +366,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                         fetch<Real, MED>(a, lut, ix, iy, iz, cidx, mut, mua, mid);
                         w = (Real)1;
                         if (a.fresnel) {
-                            const Real nt = MED == MED_RHOKAP ? (Real)a.rhokap_n : lut[mid].n;
+                            const Real nt = MED == MED_RHOKAP ? K.rhokap_n : lut[mid].n;
                             Real rsp = (namb - nt) / (namb + nt);
                             rsp = rsp * rsp;
                             atomicAdd(&s_tal[0], (double)rsp);
@@ -489,7 +495,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                 if (face) {
                     const bool cx = fax == 0, cy = fax == 1;
                     const Real nc = cx ? nx : (cy ? ny : nz);
-                    const Real nt = MED == MED_RHOKAP ? (Real)a.rhokap_n : lut[mid].n;
+                    const Real nt = MED == MED_RHOKAP ? K.rhokap_n : lut[mid].n;
                     if (Uniform<Real>::from(r.x) < fresnel<Real>(nt, namb, M<Real>::abs(nc))) {
                         // reflect: mirror the crossed direction component; the
                         // next face along it is one cell width back
@@ -686,9 +692,41 @@ cudaError_t launch_t(const TransportArgs &a, int sm_count, cudaStream_t s)
 
 }  // namespace
 
-cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cudaStream_t s)
+// The per-launch constants, in the order of operations a thread used to
+// evaluate them in FP64 (so the FP64 form's values are unchanged), and their
+// FP32 roundings.
+static void fill_consts(TransportArgs &a)
 {
-    if (a.n <= 0) return cudaSuccess;
+    TrConst<double> &d = a.cd;
+    d.hx = 2.0 * a.xmax / a.nx;
+    d.hy = 2.0 * a.ymax / a.ny;
+    d.hz = 2.0 * a.zmax / a.nz;
+    d.knx = 1.0 - a.nudge / (2.0 * a.xmax / a.nx);
+    d.kny = 1.0 - a.nudge / (2.0 * a.ymax / a.ny);
+    d.knz = 1.0 - a.nudge / (2.0 * a.zmax / a.nz);
+    d.w2x = 2.0 * a.xmax;
+    d.w2y = 2.0 * a.ymax;
+    d.xmax = a.xmax;
+    d.ymax = a.ymax;
+    d.wmin = a.roulette_w;
+    d.rm = a.roulette_m;
+    d.inv_rm = 1.0 / a.roulette_m;
+    d.namb = a.n_ambient;
+    d.rhokap_n = a.rhokap_n;
+    d.src_r = a.source_radius;
+    TrConst<float> &f = a.cf;
+    f.hx = (float)d.hx, f.hy = (float)d.hy, f.hz = (float)d.hz;
+    f.knx = (float)d.knx, f.kny = (float)d.kny, f.knz = (float)d.knz;
+    f.w2x = (float)d.w2x, f.w2y = (float)d.w2y, f.xmax = (float)d.xmax, f.ymax = (float)d.ymax;
+    f.wmin = (float)d.wmin, f.rm = (float)d.rm, f.inv_rm = (float)d.inv_rm;
+    f.namb = (float)d.namb, f.rhokap_n = (float)d.rhokap_n, f.src_r = (float)d.src_r;
+}
+
+cudaError_t launch_transport(const TransportArgs &args, bool fp64, int sm_count, cudaStream_t s)
+{
+    if (args.n <= 0) return cudaSuccess;
+    TransportArgs a = args;
+    fill_consts(a);
     cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     if (fp64) {
