@@ -129,6 +129,30 @@ def test_ref_stencil_fp32_form_within_1mK(tam, orc, case, n):
     o.close()
 
 
+def test_ref_fp32_coupled_loop_within_mc_noise(tam):
+    # the whole FP32 reference loop (FP32 transport, FP32 stencil on the FP32
+    # copies, fused FP64 Arrhenius and property update) against the FP64 loop
+    # on the reference's own input, 1000 outer iterations.  FP32 draws its
+    # uniforms in FP32, so its packets are independent of the FP64 ones: the
+    # difference must stay within the seed-to-seed Monte Carlo noise of two
+    # FP64 runs plus the FP32 form's 1 mK precision target, with no offset
+    def run(prec, seed):
+        c = tam.Context(tam.default_params(precision=prec))
+        assert c.run(seed=seed, max_iters=1000) == 1000
+        T, Om = c.download(F.TAM_F_TEMP), c.download(F.TAM_F_TISSUE)
+        assert c.device_errors() == 0
+        c.close()
+        return T, Om
+    (a, oa), (b, ob), (f, of) = run(0, 1), run(0, 2), run(1, 3)
+    noise = np.abs(a - b)
+    assert noise.max() > 0.0
+    d = np.abs(f - a)
+    assert d.max() <= 3.0 * noise.max() + 1e-3, (d.max(), noise.max())
+    assert d.mean() <= 2.0 * noise.mean() + 1e-4, (d.mean(), noise.mean())
+    assert abs(f.mean() - a.mean()) <= 3.0 * abs(a.mean() - b.mean()) + 1e-4
+    assert np.abs(of - oa).max() <= 3.0 * np.abs(oa - ob).max() + 1e-9
+
+
 def test_ref_fp32_form_follows_property_updates(tam):
     # the property update writes the FP32 copies of kappa, density, heatcap
     # and coeff beside the FP64 fields: a random Q lowers the water content,

@@ -208,20 +208,15 @@ template <typename F> __global__ void __launch_bounds__(256) ref_stencil_kernel(
     }
 }
 
-__global__ void ref_arrhenius_kernel(const RefArrheniusArgs a)
+// Arrhenius damage of one voxel: T and rk its temperature and extinction,
+// q its interior index.
+__device__ __forceinline__ void arrhenius_voxel(const RefArrheniusArgs &a, int64_t q, double T, double rk)
 {
-    const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int z = blockIdx.z + 1;
-    if (x > a.nx || y > a.ny) return;
-    const H I{a.nx + 2, a.ny + 2};
     const int64_t ni = (int64_t)a.nx * a.ny * a.nz;
-    const int64_t q = (int64_t)(x - 1) + (int64_t)a.nx * ((int64_t)(y - 1) + (int64_t)a.ny * (int64_t)(z - 1));
-    const double T = a.temp[I(x, y, z)];
     double om = a.tissue[q];
     // src/3dFD.f90:450-452 with A=3.1d98, dE=6.3d5, R=8.314d0 (compares on
     // the bit patterns, ieee_bits.h)
-    if (ieee::ge_pos(T, B_316) && ieee::lt_pos(T, B_373) && ieee::ge_zero(a.rhokap[I(x, y, z)])) {
+    if (ieee::ge_pos(T, B_316) && ieee::lt_pos(T, B_373) && ieee::ge_zero(rk)) {
         om = ADD(om, MUL(MUL(a.delt, 3.1e98), exp(-DIV(6.3e5, MUL(8.314, T)))));
         a.tissue[q] = om;
     }
@@ -230,6 +225,18 @@ __global__ void ref_arrhenius_kernel(const RefArrheniusArgs a)
     if (ieee::is_zero(*t1) && ieee::ge_pos(om, B_0_53)) *t1 = a.time;
     else if (ieee::is_zero(*t2) && ieee::ge_pos(om, B_1)) *t2 = a.time;
     else if (ieee::is_zero(*t3) && ieee::ge_pos(om, B_1E4)) *t3 = a.time;
+}
+
+__global__ void ref_arrhenius_kernel(const RefArrheniusArgs a)
+{
+    const int x = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int z = blockIdx.z + 1;
+    if (x > a.nx || y > a.ny) return;
+    const H I{a.nx + 2, a.ny + 2};
+    const int64_t q = (int64_t)(x - 1) + (int64_t)a.nx * ((int64_t)(y - 1) + (int64_t)a.ny * (int64_t)(z - 1));
+    const int64_t c = I(x, y, z);
+    arrhenius_voxel(a, q, a.temp[c], a.rhokap[c]);
 }
 
 // src/thermalConst_mod.f90 with explicit rounding (the reference evaluates
@@ -265,17 +272,12 @@ __device__ __forceinline__ void store_p32(const RefPropsArgs &a, int64_t c, doub
     a.p32[3 * a.nh + c] = (float)cf;
 }
 
-__global__ void ref_props_kernel(const RefPropsArgs a)
+// The property update of voxel (i, j, k): c its halo index, q its interior
+// index, T its temperature.
+__device__ __forceinline__ void props_voxel(const RefPropsArgs &a, int i, int j, int k, int64_t c, int64_t q, double T)
 {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
-    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
-    const int k = blockIdx.z + 1;
-    if (i > a.nx || j > a.ny) return;
     const H I{a.nx + 2, a.ny + 2};
-    const int64_t c = I(i, j, k);
-    const int64_t q = (int64_t)(i - 1) + (int64_t)a.nx * ((int64_t)(j - 1) + (int64_t)a.ny * (int64_t)(k - 1));
     const double abl_T = a.abl_T;
-    const double T = a.temp[c];
     // WaterContent = getWaterContent(Q, watercontent)  (src/3dFD.f90:328).
     // Compares run on the bit patterns (ieee_bits.h), and a zero Q gives
     // 0.75 - 0.75 * (0 / qvapor) = 0.75 exactly unless qvapor is 0 or NaN,
@@ -338,6 +340,34 @@ __global__ void ref_props_kernel(const RefPropsArgs a)
         a.coeff[c] = cf;
         if (a.p32) store_p32(a, c, kk, dn, hc, cf);
     }
+}
+
+__global__ void ref_props_kernel(const RefPropsArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > a.nx || j > a.ny) return;
+    const H I{a.nx + 2, a.ny + 2};
+    const int64_t c = I(i, j, k);
+    const int64_t q = (int64_t)(i - 1) + (int64_t)a.nx * ((int64_t)(j - 1) + (int64_t)a.ny * (int64_t)(k - 1));
+    props_voxel(a, i, j, k, c, q, a.temp[c]);
+}
+
+// Arrhenius then the property update, voxel by voxel: the coupled loop's
+// order, one read of T and rhokap for both
+__global__ void ref_damage_props_kernel(const RefArrheniusArgs d, const RefPropsArgs a)
+{
+    const int i = blockIdx.x * blockDim.x + threadIdx.x + 1;
+    const int j = blockIdx.y * blockDim.y + threadIdx.y + 1;
+    const int k = blockIdx.z + 1;
+    if (i > a.nx || j > a.ny) return;
+    const H I{a.nx + 2, a.ny + 2};
+    const int64_t c = I(i, j, k);
+    const int64_t q = (int64_t)(i - 1) + (int64_t)a.nx * ((int64_t)(j - 1) + (int64_t)a.ny * (int64_t)(k - 1));
+    const double T = a.temp[c];
+    arrhenius_voxel(d, q, T, a.rk_old[c]);
+    props_voxel(a, i, j, k, c, q, T);
 }
 
 // FP32 copies of the temperature (into both ping-pong buffers, halo
@@ -736,6 +766,13 @@ cudaError_t launch_ref_props(const RefPropsArgs &a, cudaStream_t s)
 {
     count_launch();
     ref_props_kernel<<<ref_grid(a.nx, a.ny, a.nz), dim3(32, 8), 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_ref_damage_props(const RefArrheniusArgs &d, const RefPropsArgs &a, cudaStream_t s)
+{
+    count_launch();
+    ref_damage_props_kernel<<<ref_grid(a.nx, a.ny, a.nz), dim3(32, 8), 0, s>>>(d, a);
     return cudaGetLastError();
 }
 

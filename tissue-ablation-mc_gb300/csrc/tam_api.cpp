@@ -702,7 +702,7 @@ int ref_heat(tam_ctx *ctx, int32_t loops)
     return TAM_OK;
 }
 
-int ref_arrhenius(tam_ctx *ctx)
+tam::RefArrheniusArgs arrhenius_args(const tam_ctx *ctx)
 {
     tam::RefArrheniusArgs a{};
     a.nx = ctx->nx;
@@ -714,11 +714,10 @@ int ref_arrhenius(tam_ctx *ctx)
     a.rhokap = ctx->d_rk[ctx->rcur];
     a.tissue = ctx->d_tissue;
     a.thres = ctx->d_thres;
-    CK(tam::launch_ref_arrhenius(a, ctx->stream));
-    return TAM_OK;
+    return a;
 }
 
-int ref_props(tam_ctx *ctx, double ablate_temp)
+tam::RefPropsArgs props_args(const tam_ctx *ctx, double ablate_temp)
 {
     tam::RefPropsArgs a{};
     a.nx = ctx->nx;
@@ -743,9 +742,35 @@ int ref_props(tam_ctx *ctx, double ablate_temp)
     a.reuse = ctx->props_delt == ctx->delt ? 1 : 0;
     a.p32 = ctx->fp64 ? nullptr : ctx->d_p32;  // FP32 copies written beside the FP64 properties
     a.nh = ctx->nh;
-    CK(tam::launch_ref_props(a, ctx->stream));
+    return a;
+}
+
+// rhokap ping-pong and the delt whose skin properties are now in place
+void props_done(tam_ctx *ctx)
+{
     ctx->rcur = 1 - ctx->rcur;
     ctx->props_delt = ctx->delt;
+}
+
+int ref_arrhenius(tam_ctx *ctx)
+{
+    CK(tam::launch_ref_arrhenius(arrhenius_args(ctx), ctx->stream));
+    return TAM_OK;
+}
+
+int ref_props(tam_ctx *ctx, double ablate_temp)
+{
+    CK(tam::launch_ref_props(props_args(ctx, ablate_temp), ctx->stream));
+    props_done(ctx);
+    return TAM_OK;
+}
+
+// Arrhenius followed by the property update, as the coupled loop calls them
+// (src/mcpolar.f90:149-185), in one pass over the voxels
+int ref_damage_props(tam_ctx *ctx, double ablate_temp)
+{
+    CK(tam::launch_ref_damage_props(arrhenius_args(ctx), props_args(ctx, ablate_temp), ctx->stream));
+    props_done(ctx);
     return TAM_OK;
 }
 
@@ -1009,8 +1034,7 @@ int outer_iteration(tam_ctx *ctx, uint64_t seed, bool sync = true)
         // src/mcpolar.f90:149-185
         if (ctx->laser_flag) RC(mc_pass(ctx, n, seed, (uint32_t)ctx->counter, false));
         RC(ref_heat(ctx, ctx->p.loops));
-        RC(ref_arrhenius(ctx));
-        RC(ref_props(ctx, ctx->p.ablate_temp));
+        RC(ref_damage_props(ctx, ctx->p.ablate_temp));
     }
     ctx->counter += 1;
     if (!sync) {

@@ -136,6 +136,9 @@ struct RefPropsArgs {
     int64_t nh;
 };
 cudaError_t launch_ref_props(const RefPropsArgs &a, cudaStream_t s);
+// Arrhenius and then the property update of every voxel in one pass (their
+// outputs are disjoint and the update reads no damage)
+cudaError_t launch_ref_damage_props(const RefArrheniusArgs &d, const RefPropsArgs &a, cudaStream_t s);
 
 // FP32 copies for the FP32 form of the reference stencil: T into both
 // t32a and t32b (halo included), kappa, density, heatcap, coeff into p32
