@@ -5,7 +5,11 @@
 //    src/3dFD.f90:113-187, Arrhenius of src/3dFD.f90:424-466 and the property
 //    / ablation update of src/3dFD.f90:312-361, each evaluated with explicit
 //    round-to-nearest operations in the reference's order of evaluation so
-//    the result matches the Fortran arithmetic (no FMA contraction);
+//    the result matches the Fortran arithmetic (no FMA contraction), with
+//    compares on the integer pipe (ieee_bits.h) because these kernels are
+//    bound by GB300's narrow FP64 pipe; an FP32 form of the stencil reads
+//    FP32 copies of the fields and adds its increments to the FP64
+//    temperatures;
 //  * fused config-mode step: stencil + latent-heat clamp + Arrhenius (exponent
 //    ln A - Ea/RT in FP64, or float-float in the FP32 form) + ablation in one
 //    pass, with FP32 storage and a Kahan-compensated temperature, or plain
