@@ -85,6 +85,74 @@ def test_ref_stencil_fp64_matches_oracle(tam, orc):
     o.close()
 
 
+def _ref_step_numpy(T, K, D, C, coeff, J, Q, st):
+    """One FP64 reference heat step (src/3dFD.f90:113-187) in numpy, in the
+    kernel's order of operations: float64 arithmetic is IEEE round-to-nearest
+    without contraction, so the result is the kernel's, bit for bit."""
+    c = (slice(1, -1),) * 3
+
+    def sh(A, ax, o):
+        idx = [slice(1, -1)] * 3
+        idx[ax] = slice(1 + o, A.shape[ax] - 1 + o)
+        return A[tuple(idx)]
+
+    def face(ax, o, id2):
+        kh = 0.5 * (K[c] + sh(K, ax, o))
+        dh = 0.5 * (D[c] + sh(D, ax, o))
+        ch = 0.5 * (C[c] + sh(C, ax, o))
+        return (0.5 * (kh / (dh * ch))) * id2
+
+    u = []
+    for ax, dd in enumerate((st.dx, st.dy, st.dz)):
+        id2 = 1.0 / (dd * dd)
+        a, d = face(ax, -1, id2), face(ax, 1, id2)
+        b = 0.5 * (a + d)
+        u.append(((a * sh(T, ax, -1)) - ((2.0 * b) * T[c])) + (d * sh(T, ax, 1)))
+    inc = st.delt * ((u[0] + u[1]) + u[2])
+    energy = (((st.laser_on * J) * st.delt) * st.volume_voxel) + ((C[c] * st.mass_voxel) * inc)
+    heat = (T[c] + inc) + ((st.laser_on * coeff[c]) * J)
+    boil = (T[c] >= 373.0) & (Q < st.qvapor) & (energy > 0.0)
+    qn = Q + energy
+    Qn = np.where(boil, np.where(qn < st.qvapor, qn, st.qvapor), Q)
+    Tn = T.copy()
+    Tn[c] = np.where(boil, 373.0, heat)
+    return Tn, Qn
+
+
+def test_ref_stencil_fp64_bitwise_vs_numpy(tam):
+    # the FP64 reference step (its exact halvings and compares on the bit
+    # pattern included) against a numpy restatement of the same IEEE
+    # operations: every voxel bit-identical, boiling branch active
+    nx, ny, nz = 20, 16, 12
+    ctx = tam.Context(tam.default_params(nxg=nx, nyg=ny, nzg=nz))
+    rng = np.random.default_rng(11)
+    inter = (slice(1, nx + 1), slice(1, ny + 1), slice(1, nz + 1))
+    f = {}
+    for fld, lo, hi in ((F.TAM_F_TEMP, 300.0, 380.0), (F.TAM_F_KAPPA, 0.3, 0.7), (F.TAM_F_DENSITY, 900.0, 1200.0),
+                        (F.TAM_F_HEATCAP, 2500.0, 4000.0)):
+        A = ctx.download(fld)
+        A[inter] = rng.uniform(lo, hi, (nx, ny, nz))
+        f[fld] = A
+    # a uniform block at 375 K: inside it diffusion is small and the source
+    # drives the latent-heat branch (Q grows, T held at 373 K)
+    f[F.TAM_F_TEMP][6:14, 5:11, 4:9] = 375.0
+    st = ctx.state()
+    coeff = ctx.download(F.TAM_F_COEFF)
+    coeff[inter] = st.delt / (f[F.TAM_F_DENSITY][inter] * f[F.TAM_F_HEATCAP][inter])
+    J = rng.uniform(0.0, 5e9, (nx, ny, nz))
+    Q = rng.uniform(0.0, st.qvapor * 1.1, (nx, ny, nz))
+    for fld, A in list(f.items()) + [(F.TAM_F_COEFF, coeff), (F.TAM_F_JMEAN_GLOBAL, J), (F.TAM_F_Q, Q)]:
+        ctx.upload(fld, A)
+    T = ctx.heat_steps(1, want=True)
+    assert ctx.state().delt == st.delt and ctx.device_errors() == 0
+    Tn, Qn = _ref_step_numpy(f[F.TAM_F_TEMP], f[F.TAM_F_KAPPA], f[F.TAM_F_DENSITY], f[F.TAM_F_HEATCAP], coeff,
+                             J, Q, st)
+    assert (Qn != Q).any() and (Tn[inter] == 373.0).any()
+    assert np.array_equal(T.view(np.uint64), Tn.view(np.uint64)), np.mean(T == Tn)
+    assert np.array_equal(ctx.download(F.TAM_F_Q).view(np.uint64), Qn.view(np.uint64))
+    ctx.close()
+
+
 @pytest.mark.parametrize("case,n", [("boiling", 6), ("smooth", 200)])
 def test_ref_stencil_fp32_form_within_1mK(tam, orc, case, n):
     # reference mode with FP32 precision: the stencil's arithmetic in FP32 on

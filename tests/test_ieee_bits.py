@@ -1,5 +1,6 @@
-"""The bit-pattern comparisons of csrc/ieee_bits.h against the compiler's
-own IEEE double comparisons, on the host (the header is plain C++ too).
+"""The bit-pattern comparisons and scalings of csrc/ieee_bits.h against the
+compiler's own IEEE double comparisons and multiplies by 0.5 and 2.0, on the
+host (the header is plain C++ too).
 
 The reference-mode kernels use these predicates in place of FP64 compares,
 and must return exactly what the FP64 compare returns, so the check runs
@@ -31,8 +32,22 @@ static void check(bool got, bool want, const char *what, double a, double b)
     if (got != want && bad++ < 20)
         std::printf("MISMATCH %s a=%a (%016llx) b=%a\n", what, a, (unsigned long long)bits(a), b);
 }
+static void scaled(double x)
+{
+    // exact halving and doubling against the host's IEEE multiply (NaN: stays NaN)
+    const double h = 0.5 * x, t = 2.0 * h;
+    const double hh = half(x), tt = twice_half(x, hh);
+    if (x != x) {
+        check(hh != hh, true, "half nan", x, 0);
+        check(tt != tt, true, "twice_half nan", x, 0);
+    } else {
+        check(bits(hh) == bits(h), true, "half", x, h);
+        check(bits(tt) == bits(t), true, "twice_half", x, t);
+    }
+}
 static void one(double x, const std::vector<double> &cs)
 {
+    scaled(x);
     check(is_nan(x), x != x, "is_nan", x, 0);
     check(is_zero(x), x == 0.0, "is_zero", x, 0);
     check(gt_zero(x), x > 0.0, "gt_zero", x, 0);
@@ -73,6 +88,8 @@ int main()
         // half the draws near the constants' exponents, half anywhere
         const uint64_t b = (n & 1) ? r : ((r & 0x800FFFFFFFFFFFFFull) | ((uint64_t)(1016 + (r >> 52) % 16) << 52));
         one(from(b), cs);
+        // denormals and the two lowest binades, where halving rounds
+        scaled(from((r & 0x800FFFFFFFFFFFFFull) | ((uint64_t)((r >> 52) % 3) << 52)));
         const double y = from(g());
         check(lt(from(b), y), from(b) < y, "lt r", from(b), y);
         check(eq(from(b), y), from(b) == y, "eq r", from(b), y);

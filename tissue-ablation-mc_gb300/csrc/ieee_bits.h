@@ -87,6 +87,46 @@ TAM_HD bool lt(double a, double b) { return !is_nan(a) && !is_nan(b) && key(a) <
 TAM_HD bool le(double a, double b) { return !is_nan(a) && !is_nan(b) && key(a) <= key(b); }
 TAM_HD bool eq(double a, double b) { return !is_nan(a) && !is_nan(b) && key(a) == key(b); }
 
+TAM_HD double from_bits(uint64_t b)
+{
+#if defined(__CUDA_ARCH__)
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    std::memcpy(&x, &b, sizeof x);
+    return x;
+#endif
+}
+
+// 0.5 * x with IEEE round-to-nearest-even, on the bit pattern.  A biased
+// exponent of 2..2046 is lowered by one (exact); zeros, denormals and the
+// smallest normal binade shift their significand right by one and round
+// half to even (the significand and the exponent field are contiguous, so
+// the shift covers both); infinities pass through.  Bit-identical to the
+// FP64 multiply for every non-NaN input; a NaN stays a NaN.
+TAM_HD double half(double x)
+{
+    const uint64_t b = bits(x), s = b & SIGN, m = b & ~SIGN;
+    const uint64_t e = m >> 52;
+    uint64_t r;
+    if (e >= 2u) r = e == 0x7FFu ? m : m - (1ull << 52);
+    else r = (m >> 1) + (m & (m >> 1) & 1u);
+    return from_bits(s | r);
+}
+
+// 2.0 * half(s), given h = half(s), on the bit pattern.  When half(s) was
+// exact (biased exponent of s at least 2, or s infinite) it is s itself;
+// otherwise h is a denormal or zero and its doubling shifts the
+// significand left by one (exact).  Bit-identical to the FP64 multiply for
+// every non-NaN input.
+TAM_HD double twice_half(double s, double h)
+{
+    const uint64_t sb = bits(s);
+    if (((sb & ~SIGN) >> 52) >= 2u) return s;
+    const uint64_t hb = bits(h);
+    return from_bits((hb & SIGN) | ((hb & ~SIGN) << 1));
+}
+
 }  // namespace ieee
 }  // namespace tam
 
