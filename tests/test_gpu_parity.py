@@ -1,9 +1,11 @@
 """Parity of the CUDA library (through its C ABI) with the CPU oracle.
 
 Tolerances, stated per test:
-  * reference-mode FP64 heat path (stencil, Arrhenius, property update):
-    1e-12 relative (the kernels evaluate the reference's operations in its
-    order with explicit round-to-nearest, so most values are bit-identical);
+  * reference-mode FP64 heat path: the stencil bit-identical (the kernel
+    evaluates the reference's operations in its order with explicit
+    round-to-nearest), Arrhenius and the property update 1e-13 relative (the
+    device exp, in the damage integral and in air's conductivity, and the C
+    library's can differ in the last bit);
   * FP64 transport vs the oracle on identical Philox streams: 1e-9 relative
     per voxel (summation order of the tally differs; the reference's
     absolute-coordinate arithmetic differs from the cell-relative DDA in the
@@ -74,11 +76,10 @@ def test_ref_stencil_fp64_matches_oracle(tam, orc):
     assert o.heat_sim(nthreads=1) == 0
     T = ctx.heat_steps(n, want=True)
     To = o.arr("temp")
-    np.testing.assert_allclose(T, To, rtol=1e-12, atol=0)
-    np.testing.assert_allclose(ctx.download(F.TAM_F_Q), o.arr("Q"), rtol=1e-12, atol=0)
+    # bit-identical: both evaluate the Fortran's IEEE operations in its order
+    assert np.array_equal(T.view(np.uint64), To.view(np.uint64)), np.mean(T == To)
+    assert np.array_equal(ctx.download(F.TAM_F_Q).view(np.uint64), o.arr("Q").view(np.uint64))
     assert (o.arr("Q") > 0).any()
-    exact = np.mean(T == To)
-    assert exact > 0.99, f"bit-identical fraction {exact}"
     st = ctx.state()
     assert st.time == o.st.time and st.delt == o.st.delt and st.laser_flag == o.st.laser_flag
     ctx.close()

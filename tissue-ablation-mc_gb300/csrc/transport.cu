@@ -347,7 +347,17 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     M<Real>::sincos(u1 * TWOPI, &st, &ct);
                     const Real X = rad * ct + K.xmax, Y = rad * st + K.ymax;
                     phi = TWOPI * u2;
-                    M<Real>::sincos(phi, &sp, &cp);
+                    if constexpr (MED == MED_RHOKAP) {
+                        // reference medium: a pure absorber (any interaction
+                        // ends the packet) launched straight down, so the
+                        // azimuth only enters nx = ny = sint * (cos, sin) phi
+                        // = +-0, which the walk treats alike; its sincos (an
+                        // FP64 one in the parity form) is skipped
+                        cp = (Real)1;
+                        sp = (Real)0;
+                    } else {
+                        M<Real>::sincos(phi, &sp, &cp);
+                    }
                     cpv = cp;
                     spv = sp;
                     sint = (Real)0;
