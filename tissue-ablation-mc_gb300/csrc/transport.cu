@@ -220,9 +220,17 @@ enum : int { M_DEAD = 0, M_FLY = 1, M_SCAT = 2, M_FACE = 3 };  // M_SCAT, M_FACE
 template <typename Real>
 __device__ __forceinline__ void axis_setup(Real n, Real f, Real h, Real BIG, Real &td, Real &tm, int &sg)
 {
-    const Real inv = M<Real>::rcp(n);
-    td = n != (Real)0 ? h * M<Real>::abs(inv) : BIG;
-    tm = n > (Real)0 ? (h - f) * inv : (n < (Real)0 ? -f * inv : BIG);
+    // the reciprocal only for a component that is not zero: an FP64 1/0
+    // takes the division's slow special-case path, and the reference medium
+    // launches every packet with x and y components of zero
+    if (n != (Real)0) {
+        const Real inv = M<Real>::rcp(n);
+        td = h * M<Real>::abs(inv);
+        tm = n > (Real)0 ? (h - f) * inv : (n < (Real)0 ? -f * inv : BIG);
+    } else {
+        td = BIG;
+        tm = BIG;
+    }
     tm = tm < (Real)0 ? (Real)0 : tm;
     sg = n > (Real)0 ? 1 : -1;
 }
