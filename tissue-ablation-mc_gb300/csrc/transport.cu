@@ -326,6 +326,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
     Real w = 0, tau = 0, dep = 0, mut = 0, mua = 0;
     uint32_t ev = 0, plo = 0, phi32 = 0, nsteps = 0;
     uint32_t cScat = 0;
+    uint64_t cSteps = 0;  // voxel steps of this thread's finished packets (reduced once at the end)
 
     for (;;) {
         // ---------------------------------------------- refill dead lanes --
@@ -418,7 +419,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                 dep = (Real)0;
                 atomicAdd(a.tally + T_OVERFLOW, 1.0);
                 atomicOr(&s_err, (unsigned)DEVERR_STEP_CAP);
-                atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
+                cSteps += nsteps;
                 mode = M_DEAD;
             } else {
                 // nearest face; ties go z over y over x (src/inttau2.f90:116-118)
@@ -474,7 +475,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     } else {
                         // outer face without Fresnel: escape
                         atomicAdd(&s_tal[cz ? (sgz > 0 ? 1 : 2) : 3], (double)w);
-                        atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
+                        cSteps += nsteps;
                         mode = M_DEAD;
                     }
                 } else {
@@ -553,7 +554,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                         mode = M_FLY;
                     } else {
                         atomicAdd(&s_tal[(!cx && !cy) ? (sgz > 0 ? 1 : 2) : 3], (double)w);
-                        atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
+                        cSteps += nsteps;
                         mode = M_DEAD;
                     }
                 } else if (!die) {
@@ -603,7 +604,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                 if (die) {
                     if (dep != (Real)0) deposit<T32>(a, cidx, dep);
                     dep = (Real)0;
-                    atomicAdd(&s_cnt[0], (unsigned long long)nsteps);
+                    cSteps += nsteps;
                     mode = M_DEAD;
                 }
             }
@@ -612,7 +613,12 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
 
     // ---- block reduction of the tallies ----
     const unsigned c1 = __reduce_add_sync(FULL, cScat);
-    if (lane == 0) atomicAdd(&s_cnt[1], (unsigned long long)c1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) cSteps += __shfl_xor_sync(FULL, cSteps, o);
+    if (lane == 0) {
+        atomicAdd(&s_cnt[1], (unsigned long long)c1);
+        atomicAdd(&s_cnt[0], (unsigned long long)cSteps);
+    }
     __syncthreads();
     if (threadIdx.x == 0) {
         atomicAdd(a.tally + T_SPECULAR, s_tal[0]);
