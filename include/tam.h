@@ -275,7 +275,11 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * "batch.staged" (batched heat steps, read from the first context of the
  * batch: 2 (default) stages each tile's planes in shared memory with
  * cp.async and updates two x-adjacent voxels per thread, 1 the same with one
- * voxel per thread, 0 reads neighbours with cached global loads). */
+ * voxel per thread, 0 reads neighbours with cached global loads),
+ * "batch.streams" (batched heat steps, read from the first context: 1 runs
+ * each instance's own single-context steps on its own stream, issued
+ * round-robin in chunks of 256 steps so the instances overlap, instead of
+ * the one cooperative launch of 0, the default). */
 int tam_set_tuning(struct tam_ctx *ctx, const char *key, int64_t value);
 /*
  * Batches of independent instances (no reference counterpart: the reference
@@ -323,7 +327,8 @@ int tam_autotune(struct tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *c
  * contexts (as tam_batch_heat_steps requires them) for each candidate form
  * and z-chunk length ("batch.staged" 2 or 1, "batch.zchunk" 8..64), keeps the
  * fastest on ctxs[0] (whose settings the batch reads) and puts every
- * instance's state back.  chosen (nullable): staged form, z-chunk. */
+ * instance's state back.  The candidates include the streams form
+ * ("batch.streams" 1).  chosen (nullable): staged form, z-chunk, streams. */
 int tam_batch_autotune(struct tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *chosen, int32_t nchosen);
 
 /* Kernels this library has launched in this process (all contexts). */

@@ -85,16 +85,24 @@ def _fp32_instance(tam, nx, ny, nz, layered, power):
 SHAPES = [(37, 29, 23, True, 1.0), (48, 40, 36, False, 2.0), (64, 20, 18, True, 3.0)]
 
 
-def test_batch_heat_steps_matches_single_contexts(tam):
+@pytest.mark.parametrize("streams", [0, 1])
+def test_batch_heat_steps_matches_single_contexts(tam, streams):
+    # streams 0: the batched cooperative kernel; 1: each instance's own
+    # single-context steps on its stream, issued round-robin (bit-identical
+    # to the single runs, so held to the same bound here)
     F = tam._abi
     want = []
     for shp in SHAPES:
         with _fp32_instance(tam, *shp) as ctx:
-            ctx.heat_steps(150)
+            ctx.heat_steps(300)
             want.append((ctx.download(F.TAM_F_TEMP), ctx.download(F.TAM_F_TISSUE), ctx.state().time))
     ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
     try:
-        tam.batch_heat_steps(ctxs, 150)
+        ctxs[0].set_tuning("batch.streams", streams)
+        tam.batch_heat_steps(ctxs, 300)
+        if streams:
+            for ctx, (T, _, _) in zip(ctxs, want):
+                assert np.array_equal(ctx.download(F.TAM_F_TEMP), T)
         for ctx, (T, om, t) in zip(ctxs, want):
             assert ctx.device_errors() == 0
             got_T = ctx.download(F.TAM_F_TEMP)
@@ -189,8 +197,9 @@ def test_batch_staged_matches_cached_loads(tam, zchunk):
 
 
 def test_batch_autotune_restores_state(tam):
-    # the batch autotuner times forms and z-chunks on the instances, keeps the
-    # fastest and leaves every instance's fields and clock as they were
+    # the batch autotuner times forms and z-chunks (and the streams form) on
+    # the instances, keeps the fastest and leaves every instance's fields and
+    # clock as they were
     F = tam._abi
     ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
     try:
@@ -198,6 +207,7 @@ def test_batch_autotune_restores_state(tam):
         before = [(c.download(F.TAM_F_TEMP), c.download(F.TAM_F_TISSUE), c.state().time) for c in ctxs]
         chosen = tam.batch_autotune(ctxs, steps=8)
         assert chosen["batch.staged"] in (1, 2) and chosen["batch.zchunk"] in (8, 16, 32, 64)
+        assert chosen["batch.streams"] in (0, 1)
         for c, (T, om, t) in zip(ctxs, before):
             np.testing.assert_array_equal(c.download(F.TAM_F_TEMP), T)
             np.testing.assert_array_equal(c.download(F.TAM_F_TISSUE), om)

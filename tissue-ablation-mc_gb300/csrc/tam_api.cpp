@@ -127,6 +127,7 @@ struct tam_ctx {
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // by the buffer pair the chunk reads first
     std::vector<unsigned char> gkey[2];      // what the graphs were captured with
     int batch_staged = 2;            // batched steps: staged voxel pairs (2), staged voxels (1), cached loads (0)
+    int batch_streams = 0;           // 1: batched steps as each instance's own steps on its stream, overlapped
     int batch_zchunk = 0;            // batched steps: z planes per work item (0: heat.zchunk, else the default)
     // staged class-table step of this context alone (rows not aligned for TMA)
     tam::BatchInst *d_sinst = nullptr;
@@ -1893,6 +1894,16 @@ int tam_batch_heat_steps(tam_ctx *const *ctxs, int32_t n, int32_t nsteps)
                                            "thermal properties by material class");
     tam_ctx *const ctx = ctxs[0];
     CK(cudaSetDevice(ctx->device));
+    if (ctx->batch_streams) {
+        // each instance's own steps (its single-context kernel, replayed from
+        // its CUDA graphs) on its own stream, issued round-robin in chunks so
+        // the instances overlap on the device; one wait at the end
+        constexpr int32_t RR = 256;
+        for (int32_t done = 0; done < nsteps; done += RR)
+            for (int32_t i = 0; i < n; ++i) RC(cfg_heat(ctxs[i], std::min(RR, nsteps - done)));
+        for (int32_t i = 0; i < n; ++i) RC(finish(ctxs[i], "tam_batch_heat_steps"));
+        return TAM_OK;
+    }
     DevBatch B;
     const int kmax = std::min(batch_chunk(ctxs, n), std::max(nsteps, 1));
     RC(batch_setup(B, ctxs, n, kmax));
@@ -2142,6 +2153,8 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
     } else if (k == "batch.staged") {
         if (value < 0 || value > 2) return fail(ctx, TAM_E_INVALID, "batch.staged must be 0, 1 or 2");
         ctx->batch_staged = (int)value;
+    } else if (k == "batch.streams") {
+        ctx->batch_streams = value != 0;
     } else if (k == "heat.zchunk") {
         if (value < 0 || value > ctx->nz) return fail(ctx, TAM_E_INVALID, "heat.zchunk must be in 0..nz");
         ctx->zchunk = (int)value;
@@ -2517,8 +2530,8 @@ int tam_batch_autotune(tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *
         RC(snap_take(ctxs[i], *S[i]));
         CK(cudaStreamSynchronize(ctxs[i]->stream));
     }
-    const int form0 = ctx->batch_staged, z0 = ctx->batch_zchunk;
-    int best_form = form0, best_z = z0;
+    const int form0 = ctx->batch_staged, z0 = ctx->batch_zchunk, streams0 = ctx->batch_streams;
+    int best_form = form0, best_z = z0, best_streams = 0;
     double best = 1e300;
     const std::vector<int> active(n, 1);
     struct Cand {
@@ -2529,9 +2542,11 @@ int tam_batch_autotune(tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *
     auto undo = [&](int code) {
         ctx->batch_staged = form0;
         ctx->batch_zchunk = z0;
+        ctx->batch_streams = streams0;
         for (int32_t i = 0; i < n; ++i) (void)snap_restore(ctxs[i], *S[i]);
         return code;
     };
+    ctx->batch_streams = 0;
     for (const Cand &c : cands) {
         ctx->batch_staged = c.form;
         ctx->batch_zchunk = c.z;
@@ -2555,10 +2570,33 @@ int tam_batch_autotune(tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *
             best_z = c.z;
         }
     }
+    // the streams form: each instance's own steps on its stream, issued as
+    // tam_batch_heat_steps issues them (a short warm-up call captures graphs)
+    {
+        auto run = [&](int32_t nsteps) -> int {
+            for (int32_t done = 0; done < nsteps; done += 256)
+                for (int32_t i = 0; i < n; ++i) RC(cfg_heat(ctxs[i], std::min(256, nsteps - done)));
+            for (int32_t i = 0; i < n; ++i) CK(cudaStreamSynchronize(ctxs[i]->stream));
+            return TAM_OK;
+        };
+        int r = run(std::min(32, (int)steps));
+        for (int32_t i = 0; i < n && r == TAM_OK; ++i) r = snap_restore(ctxs[i], *S[i]);
+        if (r != TAM_OK) return undo(r);
+        const auto t0 = std::chrono::steady_clock::now();
+        r = run(steps);
+        const double dt = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        for (int32_t i = 0; i < n && r == TAM_OK; ++i) r = snap_restore(ctxs[i], *S[i]);
+        if (r != TAM_OK) return undo(r);
+        if (dt < best) {
+            best = dt;
+            best_streams = 1;
+        }
+    }
     ctx->batch_staged = best_form;
     ctx->batch_zchunk = best_z;
-    const int64_t v[2] = {best_form, best_z};
-    for (int32_t i = 0; i < nchosen && i < 2 && chosen; ++i) chosen[i] = v[i];
+    ctx->batch_streams = best_streams;
+    const int64_t v[3] = {best_form, best_z, best_streams};
+    for (int32_t i = 0; i < nchosen && i < 3 && chosen; ++i) chosen[i] = v[i];
     for (int32_t i = 0; i < n; ++i) RC(finish(ctxs[i], "tam_batch_autotune"));
     return TAM_OK;
 }

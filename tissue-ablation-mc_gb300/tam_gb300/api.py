@@ -230,12 +230,14 @@ def batch_heat_steps(contexts, nsteps: int) -> None:
 
 
 def batch_autotune(contexts, steps: int = 20) -> dict:
-    """Pick the fastest batched-step form and z-chunk on these contexts; their state is restored."""
+    """Pick the fastest batched-step form (cooperative kernel form and z-chunk,
+    or each instance's own steps on its stream) on these contexts; their
+    state is restored."""
     n = len(contexts)
     hs = (_abi._P * n)(*[c._h for c in contexts])
-    out = (C.c_int64 * 2)()
-    check(lib().tam_batch_autotune(hs, n, int(steps), out, 2))
-    return {"batch.staged": out[0], "batch.zchunk": out[1]}
+    out = (C.c_int64 * 3)()
+    check(lib().tam_batch_autotune(hs, n, int(steps), out, 3))
+    return {"batch.staged": out[0], "batch.zchunk": out[1], "batch.streams": out[2]}
 
 
 def kernel_launches() -> int:
