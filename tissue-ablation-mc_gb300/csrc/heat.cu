@@ -229,11 +229,13 @@ __device__ __forceinline__ void arrhenius_voxel(const RefArrheniusArgs &a, int64
         om = ADD(om, MUL(MUL(a.delt, 3.1e98), exp(-DIV(6.3e5, MUL(8.314, T)))));
         a.tissue[q] = om;
     }
-    // src/3dFD.f90:455-461
+    // src/3dFD.f90:455-461, with the damage tested before each threshold
+    // time is loaded (the conditions are pure, so the order of the two tests
+    // changes nothing): below 0.53 no threshold time is read at all
     double *t1 = a.thres + q, *t2 = a.thres + q + ni, *t3 = a.thres + q + 2 * ni;
-    if (ieee::is_zero(*t1) && ieee::ge_pos(om, B_0_53)) *t1 = a.time;
-    else if (ieee::is_zero(*t2) && ieee::ge_pos(om, B_1)) *t2 = a.time;
-    else if (ieee::is_zero(*t3) && ieee::ge_pos(om, B_1E4)) *t3 = a.time;
+    if (ieee::ge_pos(om, B_0_53) && ieee::is_zero(*t1)) *t1 = a.time;
+    else if (ieee::ge_pos(om, B_1) && ieee::is_zero(*t2)) *t2 = a.time;
+    else if (ieee::ge_pos(om, B_1E4) && ieee::is_zero(*t3)) *t3 = a.time;
 }
 
 __global__ void ref_arrhenius_kernel(const RefArrheniusArgs a)
@@ -302,13 +304,17 @@ __device__ __forceinline__ void props_voxel(const RefPropsArgs &a, int i, int j,
     a.water[q] = w;
 
     const double *rk = a.rk_old;
+    // the loads the common case needs (this voxel's extinction, the -x
+    // neighbour's extinction and temperature; all inside the halo) issued
+    // together instead of one after another
+    const double rkc = rk[c], rkxm = rk[I(i - 1, j, k)], txm = a.temp[I(i - 1, j, k)];
     const bool abl = ieee::le(abl_T, T);
-    bool zero = abl || !ieee::gt_zero(rk[c]);
+    bool zero = abl || !ieee::gt_zero(rkc);
     if (!zero) {
         // backward neighbours (already swept): zero if zero before or ablated now
         bool iso = true;
-        if (i > 1) iso = iso && (ieee::is_zero(rk[I(i - 1, j, k)]) || ieee::le(abl_T, a.temp[I(i - 1, j, k)]));
-        else iso = iso && ieee::is_zero(rk[I(i - 1, j, k)]);
+        if (i > 1) iso = iso && (ieee::is_zero(rkxm) || ieee::le(abl_T, txm));
+        else iso = iso && ieee::is_zero(rkxm);
         if (j > 1) iso = iso && (ieee::is_zero(rk[I(i, j - 1, k)]) || ieee::le(abl_T, a.temp[I(i, j - 1, k)]));
         else iso = iso && ieee::is_zero(rk[I(i, j - 1, k)]);
         if (k > 1) iso = iso && (ieee::is_zero(rk[I(i, j, k - 1)]) || ieee::le(abl_T, a.temp[I(i, j, k - 1)]));
@@ -323,7 +329,7 @@ __device__ __forceinline__ void props_voxel(const RefPropsArgs &a, int i, int j,
             // the water content is what the previous call's skin branch saw:
             // its properties are still in place and would come out bit for bit
             // the same, so only the ping-pong copy of rhokap is written
-            a.rk_new[c] = rk[c];
+            a.rk_new[c] = rkc;
             return;
         }
         const double dn = skin_dens(w);
