@@ -21,8 +21,9 @@ roofline: the dominant kernel (transport): 12 B per voxel step (rhokap /
           HBM copy bandwidth; the stencil's 36 B per voxel update likewise.
 
 --impl reference runs the CPU oracle (the C restatement of the reference,
-OpenMP on all host cores) on a bounded sample of the same workload, scaled to
-the same metric.  With --gpus N > 1 every rank runs an independent replica
+OpenMP on all host cores) on bounded samples of the same workload, scaled to
+the same metric, in a fresh process; the GPU arm's cpu_baseline times the same
+samples the same way.  Both also time configuration 1 in full.  With --gpus N > 1 every rank runs an independent replica
 (the path has no exchange step on one instance).
 """
 from __future__ import annotations
@@ -288,10 +289,42 @@ def run_gpu(args):
             },
         }
 
-    # ---- CPU baseline (oracle port, all host cores) ----
+    # ---- configuration 1 in full (1e6 packets on 100^3 + 103 steps), both forms ----
+    c1 = None
+    if rank == 0 and not args.no_c1:
+        from tam_gb300 import workloads
+
+        c1 = {"workload": "configuration 1: 100^3 cube, 1e6 packets + 103 heat steps (1 W for 1 s)"}
+        for prec, name in ((tam._abi.TAM_FP64, "fp64"), (tam._abi.TAM_FP32, "fp32")):
+            w = workloads.c1()
+            w.params.precision = prec
+            w.params.device = local
+            with w.context() as cc:
+                cc.set_stream(stream.cuda_stream)
+                cc.mc_pass(w.packets, seed=1, stream=1)  # warm-up
+                cc.heat_steps(w.heat_steps)
+                cc.init_thermal()
+                torch.cuda.synchronize()
+                ev0.record(stream)
+                cc.mc_pass(w.packets, seed=1, stream=0)
+                cc.heat_steps(w.heat_steps)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+                sec = ev0.elapsed_time(ev1) * 1e-3
+                c1[name] = {"seconds": sec, "photons_per_s": w.packets / sec, "heat_steps": w.heat_steps}
+
+    # ---- CPU baseline (oracle port, all host cores, in a fresh process) ----
     cpu = None
     if rank == 0 and not args.no_cpu:
-        cpu = cpu_measure(args.cpu_seconds)
+        res = cpu_subprocess(args.cpu_samples, args.cpu_seconds, args.cpu_heat_seconds, c1=not args.no_c1)
+        smp = res["samples"]
+        cpu = dict(smp[-1])
+        cpu["value"] = statistics.mean(r["value"] for r in smp)
+        cpu["spread"] = [min(r["value"] for r in smp), max(r["value"] for r in smp)]
+        cpu["transport_photons_per_s"] = statistics.mean(r["transport_photons_per_s"] for r in smp)
+        cpu["voxel_updates_per_s"] = statistics.mean(r["voxel_updates_per_s"] for r in smp)
+        cpu["sample"] = f"mean of {len(smp)} samples; last: " + cpu["sample"]
+        cpu["c1_full"] = res.get("c1_full")
 
     ctx.close()
     if rank != 0:
@@ -312,16 +345,7 @@ def run_gpu(args):
         "vs_baseline": None,
         "dtype": "f32 transport + f64 tally; f32+Kahan stencil, float-float Arrhenius exponent + f64 damage sum",
         "data": "synthetic (homogeneous tissue cube built from the workload parameters)",
-        "config": {
-            "workload": f"precision form: {GRID}^3 homogeneous cube 1x1x1 cm, {packets:.0e} packets "
-                        f"(Gaussian beam w=0.1 cm, Fresnel, roulette 1e-4) + {nsteps} fused FP32 heat steps "
-                        f"(2 W for 2 s, Arrhenius, ablation at 100 C)",
-            "grid": [GRID, GRID, GRID],
-            "packets_per_step": packets,
-            "heat_steps_per_step": nsteps,
-            "l2": "inputs larger than L2 (working set ~0.4 GB); no flush",
-            "parallelism": f"replicas x{world}",
-        },
+        "config": workload_config(packets, nsteps, world),
         "voxel_updates_per_s": world * nvox * nsteps / (heat_ms * 1e-3),
         "transport": {
             "photons_per_s": world * packets / (tr_ms * 1e-3),
@@ -371,6 +395,7 @@ def run_gpu(args):
         "gpu_launches": launches,
         "clocks": clk_s,
         "fp64": fp64,
+        "c1_full": c1,
         "cpu_baseline": cpu,
     }
     traffic = profile_traffic(vs)
@@ -413,9 +438,46 @@ def profile_traffic(voxel_steps):
 
 
 # ------------------------------------------------------- CPU (oracle) --
-def cpu_measure(seconds, threads=0):
-    """Oracle port (C, FP64, OpenMP) on a bounded sample of the workload,
-    scaled to photons/s of transport + heat for the full step."""
+def workload_config(packets, nsteps, world):
+    """The `config` object of both arms' JSON lines."""
+    return {
+        "workload": f"precision form: {GRID}^3 homogeneous cube 1x1x1 cm, {packets:.0e} packets "
+                    f"(Gaussian beam w=0.1 cm, Fresnel, roulette 1e-4) + {nsteps} fused heat steps "
+                    f"(2 W for 2 s, Arrhenius, ablation at 100 C)",
+        "grid": [GRID, GRID, GRID],
+        "packets_per_step": packets,
+        "heat_steps_per_step": nsteps,
+        "l2": "inputs larger than L2 (working set ~0.4 GB); no flush",
+        "parallelism": f"replicas x{world}",
+    }
+
+
+def cpu_nsteps():
+    dxm = 2 * HALF * 1e-2 / GRID
+    alpha = 0.56 / (1070 * 3400)
+    dt = 0.9 * dxm * dxm / (6 * alpha)
+    return dt, int(math.ceil(SIM_TIME / dt - 1e-9))
+
+
+def host_cores():
+    try:
+        return len(os.sched_getaffinity(0))
+    except AttributeError:
+        return os.cpu_count() or 1
+
+
+def cpu_samples(nsamples, mc_seconds, heat_seconds, c1=False):
+    """The oracle port (C, FP64, OpenMP on every host core) on bounded samples
+    of the workload.  Runs in a process of its own (see cpu_subprocess).
+
+    Transport: one oracle call has a fixed cost (per-thread tallies of the
+    whole grid are allocated, zeroed and summed, as the reference's per-rank
+    tallies and all-reduce), measured with an empty call; each sample times
+    about `mc_seconds` of packets (sized from the previous sample's rate), and
+    the full pass is that fixed cost plus the sample's per-packet time x 1e8.
+    Heat: consecutive fused steps from the initial state, on the sample's own
+    normalised tally as the absorbed-power field, for about `heat_seconds`,
+    scaled to the full step count."""
     import numpy as np
 
     import build_oracle
@@ -423,77 +485,143 @@ def cpu_measure(seconds, threads=0):
     build_oracle.build()
     import oracle as orc
 
-    ncores = threads or os.cpu_count() or 1
+    ncores = host_cores()
     mats = [(0.0, 0.0, 0.0, 1.0), (0.3, 100.0, 0.9, 1.38)]
     d = orc.mc_desc(GRID, GRID, GRID, HALF, HALF, HALF, materials=mats, source_radius=0.1)
     grid = np.ones((GRID, GRID, GRID), dtype=np.uint8, order="F")
-    # calibrate the packet sample to about half the budget
-    n = 2000
-    t0 = time.perf_counter()
-    orc.mc_transport(d, grid, n, seed=SEED, nthreads=ncores)
-    t_cal = time.perf_counter() - t0
-    n_mc = max(2000, int(n * (0.5 * seconds) / max(t_cal, 1e-3)))
-    t0 = time.perf_counter()
-    _, tal = orc.mc_transport(d, grid, n_mc, seed=SEED, stream=1, nthreads=ncores)
-    t_mc = time.perf_counter() - t0
+    fix = []
+    for _ in range(2):
+        t0 = time.perf_counter()
+        orc.mc_transport(d, grid, 0, seed=SEED, nthreads=ncores)
+        fix.append(time.perf_counter() - t0)
+    t_fix = min(fix)
+    n = 8000
+    while True:
+        t0 = time.perf_counter()
+        orc.mc_transport(d, grid, n, seed=SEED, stream=99, nthreads=ncores)
+        t = time.perf_counter() - t0 - t_fix
+        if t >= 0.4 * mc_seconds or n >= 1 << 24:
+            break
+        n *= 2
+    rate = n / max(t, 1e-6)  # packets/s, re-measured by every sample
+    dt, nsteps = cpu_nsteps()
     dxm = 2 * HALF * 1e-2 / GRID
-    alpha = 0.56 / (1070 * 3400)
-    h = orc.heat_desc(GRID, GRID, GRID, dxm, dxm, dxm, dt=0.9 * dxm * dxm / (6 * alpha))
-    nsteps = int(math.ceil(SIM_TIME / h.dt - 1e-9))
+    h = orc.heat_desc(GRID, GRID, GRID, dxm, dxm, dxm, dt=dt)
     sh = (GRID, GRID, GRID)
+    out = []
+    for i in range(nsamples):
+        n_mc = max(8000, int(rate * mc_seconds))
+        t0 = time.perf_counter()
+        jm, tal = orc.mc_transport(d, grid, n_mc, seed=SEED, stream=1 + i, nthreads=ncores)
+        t_mc = time.perf_counter() - t0
+        per_packet = max(t_mc - t_fix, 1e-9) / n_mc
+        rate = 1.0 / per_packet
+        t_mc_full = t_fix + per_packet * PACKETS
+        J = np.asfortranarray(jm * (1.0 / (n_mc * dxm ** 3)))
+        T = np.full(sh, 310.15, order="F")
+        k = np.full(sh, 0.56, order="F")
+        rho = np.full(sh, 1070.0, order="F")
+        c = np.full(sh, 3400.0, order="F")
+        Q = np.zeros(sh, order="F")
+        om = np.zeros(sh, order="F")
+        thr = np.zeros(sh + (3,), order="F")
+        mat = np.ones(sh, dtype=np.uint8, order="F")
+        t0 = time.perf_counter()
+        s = 0
+        while s < 2 or ((time.perf_counter() - t0) < heat_seconds and s < nsteps):
+            T, _ = orc.fused_step(h, POWER, (s + 1) * h.dt, T, k, rho, c, J, Q, om, thr, mat, nthreads=ncores)
+            s += 1
+        t_heat = time.perf_counter() - t0
+        t_step = t_mc_full + t_heat * (nsteps / s)
+        out.append({
+            "value": PACKETS / t_step,
+            "unit": "photons/s",
+            "cores": ncores,
+            "kind": "port",
+            "sample": f"extrapolated: {n_mc} packets ({t_mc:.2f} s, of which {t_fix:.2f} s is the fixed per-call "
+                      f"cost of the per-thread tallies) and {s} of {nsteps} heat steps ({t_heat:.2f} s) of the "
+                      f"{GRID}^3 workload, FP64 oracle on {ncores} threads, scaled linearly to {PACKETS:.0e} packets "
+                      f"+ {nsteps} steps",
+            "transport_photons_per_s": 1.0 / per_packet,
+            "voxel_updates_per_s": GRID ** 3 * s / t_heat,
+            "voxel_steps_per_packet": tal["voxel_steps"] / n_mc,
+        })
+    res = {"samples": out}
+    if c1:
+        res["c1_full"] = cpu_c1_full(orc, ncores)
+    return res
+
+
+def cpu_c1_full(orc, ncores):
+    """Configuration 1 in full on the oracle: one pass of 1e6 packets on the
+    100^3 cube and its 103 heat steps of 1 s at 1 W (FP64)."""
+    import numpy as np
+
+    edge, n, P, secs = 100, 1_000_000, 1.0, 1.0
+    mats = [(0.0, 0.0, 0.0, 1.0), (0.3, 100.0, 0.9, 1.38)]
+    d = orc.mc_desc(edge, edge, edge, HALF, HALF, HALF, materials=mats, source_radius=0.1)
+    grid = np.ones((edge,) * 3, dtype=np.uint8, order="F")
+    dxm = 2 * HALF * 1e-2 / edge
+    alpha = 0.56 / (1070 * 3400)
+    dt = 0.9 * dxm * dxm / (6 * alpha)
+    nsteps = int(math.ceil(secs / dt - 1e-9))
+    h = orc.heat_desc(edge, edge, edge, dxm, dxm, dxm, dt=dt)
+    sh = (edge,) * 3
+    t0 = time.perf_counter()
+    jm, _ = orc.mc_transport(d, grid, n, seed=1, nthreads=ncores)
+    t_mc = time.perf_counter() - t0
+    J = np.asfortranarray(jm * (1.0 / (n * dxm ** 3)))
     T = np.full(sh, 310.15, order="F")
-    k = np.full(sh, 0.56, order="F")
-    rho = np.full(sh, 1070.0, order="F")
-    c = np.full(sh, 3400.0, order="F")
-    J = np.asfortranarray(np.random.default_rng(0).uniform(0, 1e6, sh))
-    Q = np.zeros(sh, order="F")
-    om = np.zeros(sh, order="F")
+    k, rho, c = (np.full(sh, v, order="F") for v in (0.56, 1070.0, 3400.0))
+    Q, om = np.zeros(sh, order="F"), np.zeros(sh, order="F")
     thr = np.zeros(sh + (3,), order="F")
     mat = np.ones(sh, dtype=np.uint8, order="F")
-    t0 = time.perf_counter()
-    s = 0
-    while s < 2 or (time.perf_counter() - t0) < 0.4 * seconds:
-        T, _ = orc.fused_step(h, POWER, (s + 1) * h.dt, T, k, rho, c, J, Q, om, thr, mat, nthreads=ncores)
-        s += 1
-    t_heat = time.perf_counter() - t0
-    t_step = t_mc * (PACKETS / n_mc) + t_heat * (nsteps / s)
-    return {
-        "value": PACKETS / t_step,
-        "unit": "photons/s",
-        "cores": ncores,
-        "kind": "port",
-        "sample": f"{n_mc} packets ({t_mc:.1f} s) and {s} of {nsteps} heat steps ({t_heat:.1f} s) of the "
-                  f"{GRID}^3 workload, FP64 oracle on {ncores} threads, scaled linearly to {PACKETS:.0e} packets "
-                  f"+ {nsteps} steps",
-        "transport_photons_per_s": n_mc / t_mc,
-        "voxel_updates_per_s": GRID ** 3 * s / t_heat,
-        "voxel_steps_per_packet": tal["voxel_steps"] / n_mc,
-    }
+    t1 = time.perf_counter()
+    for s in range(nsteps):
+        T, _ = orc.fused_step(h, P, (s + 1) * dt, T, k, rho, c, J, Q, om, thr, mat, nthreads=ncores)
+    t_heat = time.perf_counter() - t1
+    return {"workload": f"configuration 1: {edge}^3 cube, {n:.0e} packets + {nsteps} heat steps (FP64)",
+            "seconds": t_mc + t_heat, "transport_s": t_mc, "heat_s": t_heat, "photons_per_s": n / (t_mc + t_heat),
+            "cores": ncores}
+
+
+def cpu_subprocess(nsamples, mc_seconds, heat_seconds, c1=False):
+    """cpu_samples in a fresh Python process, so that no thread pool or CUDA
+    state of the calling process competes with the oracle's threads."""
+    cmd = [sys.executable, os.path.abspath(__file__), "--cpu-leg", "--cpu-samples", str(nsamples),
+           "--cpu-seconds", str(mc_seconds), "--cpu-heat-seconds", str(heat_seconds)]
+    if c1:
+        cmd.append("--cpu-c1")
+    r = subprocess.run(cmd, capture_output=True, text=True, cwd=ROOT)
+    if r.returncode != 0:
+        raise RuntimeError("CPU leg failed:\n" + r.stdout[-2000:] + r.stderr[-2000:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
 
 
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    vals = []
-    last = None
-    for i in range(args.warmup + args.steps):
-        r = cpu_measure(args.cpu_seconds)
-        if i >= args.warmup:
-            vals.append(r["value"])
-            last = r
-    v = statistics.mean(vals)
+    res = cpu_subprocess(args.warmup + args.steps, args.cpu_seconds, args.cpu_heat_seconds, c1=not args.no_c1)
+    timed = res["samples"][args.warmup:]
+    v = statistics.mean(r["value"] for r in timed)
+    last = timed[-1]
+    _, nsteps = cpu_nsteps()
     line = {
         "metric": METRIC, "value": v, "unit": "photons/s", "n_gpus": int(os.environ.get("WORLD_SIZE", "1")),
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * PACKETS / v, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "impl": "reference",
-        "config": {"workload": f"precision form: {GRID}^3 homogeneous cube, {PACKETS:.0e} packets + 2 s of heat steps"},
+        "config": workload_config(PACKETS, nsteps, int(os.environ.get("WORLD_SIZE", "1"))),
         "cpu_baseline": {"value": v, "unit": "photons/s", "cores": last["cores"], "kind": "port",
-                         "sample": last["sample"]},
+                         "sample": last["sample"],
+                         "spread": [min(r["value"] for r in timed), max(r["value"] for r in timed)],
+                         "transport_photons_per_s": statistics.mean(r["transport_photons_per_s"] for r in timed),
+                         "voxel_updates_per_s": statistics.mean(r["voxel_updates_per_s"] for r in timed),
+                         "c1_full": res.get("c1_full")},
         "e2e": {"value": v, "unit": "photons/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference is Fortran + MPI and no Fortran compiler exists on either machine; "
-                "its C restatement (oracle/) is timed instead",
+                "its C restatement (oracle/) is timed instead; each step is one extrapolated sample",
     }
     print(json.dumps(line), flush=True)
 
@@ -507,12 +635,18 @@ def main():
     ap.add_argument("--packets", type=int, default=PACKETS, help="profiling only: packets per step")
     ap.add_argument("--heat-steps", type=int, default=0, help="profiling only: heat steps per step")
     ap.add_argument("--fp64-packets", type=int, default=2_000_000)
-    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--cpu-seconds", type=float, default=3.0, help="seconds of packets per CPU sample")
+    ap.add_argument("--cpu-heat-seconds", type=float, default=1.5, help="seconds of heat steps per CPU sample")
+    ap.add_argument("--cpu-samples", type=int, default=3, help="CPU samples of the GPU arm's baseline")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-c1", action="store_true", help="skip the full run of configuration 1")
+    ap.add_argument("--cpu-leg", action="store_true", help=argparse.SUPPRESS)
+    ap.add_argument("--cpu-c1", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
-    if args.impl == "reference":
-        args.cpu_seconds = min(args.cpu_seconds, 8.0)
+    if args.cpu_leg:
+        print(json.dumps(cpu_samples(args.cpu_samples, args.cpu_seconds, args.cpu_heat_seconds, c1=args.cpu_c1)))
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_gpu(args)

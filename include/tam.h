@@ -341,23 +341,28 @@ int tam_write_output(struct tam_ctx *ctx, const char *dir);
  * Allocation-free MC pass.  No counterpart in the reference: the reference
  * allocates its module arrays itself and never runs on a GPU.  Some callers
  * cannot let this library call cudaMalloc -- a Fortran host whose device
- * arrays belong to another runtime (OpenACC, CUDA Fortran), a host working
- * within a fixed device-memory budget, or code that must not allocate inside
- * a stream capture or a real-time loop.  This entry point allocates nothing:
- * the caller passes the reference-mode parameters, `rhokap` as a device
- * pointer in the halo layout ((nx+2)(ny+2)(nz+2) doubles, input) and
- * `jmean_global` as a device pointer (nx*ny*nz doubles, output), plus the
- * laser power `power` (W) of the normalisation of src/mcpolar.f90:174.  It
- * runs the same photon loop as tam_mc_pass in reference mode, on
- * `cuda_stream` (NULL: the legacy default stream), and returns after that
+ * arrays belong to another runtime (OpenACC, CUDA Fortran) that must not see
+ * the device heap change behind its back, or a host working within a fixed
+ * device-memory budget.  This entry point allocates nothing: the caller
+ * passes the reference-mode parameters, `rhokap` as a device pointer in the
+ * halo layout ((nx+2)(ny+2)(nz+2) doubles, input) and `jmean_global` as a
+ * device pointer (nx*ny*nz doubles, output), plus the laser power `power` (W)
+ * of the normalisation of src/mcpolar.f90:174.  It runs the same photon loop
+ * as tam_mc_pass in reference mode (p->precision selects the FP64 or FP32
+ * transport), on `cuda_stream` (NULL: the legacy default stream), and is
+ * synchronous: it reads the pass's error word back and returns after that
  * stream has finished the pass.
+ * The device is the caller's current device, and p->device must name it
+ * (otherwise TAM_E_INVALID); the library does not change the current device.
  * The pass's scratch lives in one file-scope device array sized for grids of
  * at most TAM_NOALLOC_MAX_VOXELS voxels (about 16 MiB, held by every GPU that
  * loads the library until the process exits); larger grids are rejected with
  * TAM_E_INVALID.  The first call on a device looks up the array's device
- * address, so make that first call before any stream capture.  All calls
- * share the array (it is cleared at the start of each call): calls that
- * overlap on the GPU race.  Errors are reported by tam_last_error(NULL).
+ * address and keeps it for the rest of the process, so make that first call
+ * before any stream capture, and do not reset that device (cudaDeviceReset)
+ * afterwards.  All calls share the array (it is cleared at the start of each
+ * call): calls that overlap on the GPU race.  Errors are reported by
+ * tam_last_error(NULL).
  */
 #define TAM_NOALLOC_MAX_VOXELS 2097152
 int tam_mc_pass_noalloc(const tam_params *p, const double *rhokap, double *jmean_global, int64_t nphotons,

@@ -2,14 +2,14 @@
 //
 // Some callers cannot call cudaMalloc: a Fortran host whose device arrays are
 // owned by another runtime (OpenACC / CUDA Fortran) and that must not grow the
-// device heap behind that runtime's back, a host running under a fixed device
-// memory budget, or code that must not allocate while a stream capture or a
-// real-time loop is in progress.  tam_mc_pass_noalloc serves them: the caller
+// device heap behind that runtime's back, or a host running under a fixed
+// device-memory budget.  tam_mc_pass_noalloc serves them: the caller
 // passes the input (rhokap) and output (jmeanGLOBAL) as device pointers, and
 // the pass's scratch -- the FP64 tally in packet units, the escape tallies,
 // the packet work counter and the device error word -- lives in the
 // file-scope array below, which every GPU that loads this library holds until
-// the process exits.
+// the process exits.  The call is synchronous: it reads the pass's error word
+// back before it returns.
 #include <atomic>
 #include <cstdio>
 #include <cstring>
@@ -42,8 +42,10 @@ int fail(int code, const std::string &m)
 }
 
 // Device address of the scratch array on the current device.  The first call
-// on a device looks it up (cudaGetSymbolAddress); the host-side symbol itself
-// is only a stand-in and must never be handed to a kernel.
+// on a device looks it up (cudaGetSymbolAddress) and keeps it for the rest of
+// the process, so a cudaDeviceReset of that device afterwards is not
+// supported; the host-side symbol itself is only a stand-in and must never be
+// handed to a kernel.
 int scratch_on_current_device(double **out)
 {
     int dev = 0;
@@ -81,6 +83,16 @@ extern "C" int tam_mc_pass_noalloc(const tam_params *p, const double *rhokap, do
         (void)cudaGetLastError();
         return fail(TAM_E_NODEV, "no CUDA device");
     }
+    // the caller's runtime owns the choice of device: run on the current one,
+    // which p->device must name, rather than switching devices behind its back
+    int cur = -1;
+    if (cudaGetDevice(&cur) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return fail(TAM_E_CUDA, "cudaGetDevice failed");
+    }
+    if (p->device != cur)
+        return fail(TAM_E_INVALID, "p->device (" + std::to_string(p->device) + ") is not the current device (" +
+                                       std::to_string(cur) + ")");
     double *base = nullptr;
     int r = scratch_on_current_device(&base);
     if (r != TAM_OK) return r;
@@ -93,9 +105,8 @@ extern "C" int tam_mc_pass_noalloc(const tam_params *p, const double *rhokap, do
     cudaError_t e = cudaMemsetAsync(base, 0, (size_t)(HEAD + ni) * sizeof(double), s);
     if (e != cudaSuccess) return fail(TAM_E_CUDA, std::string("cudaMemsetAsync: ") + cudaGetErrorString(e));
 
-    int dev = 0, sms = 152;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    int sms = 152;
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, cur);
     // sourcephCO2 + tauint1 of the reference (pure absorber, uniform disk of
     // diameter 250 um, no Fresnel, no roulette), as tam_mc_pass in reference mode
     tam::TransportArgs a{};

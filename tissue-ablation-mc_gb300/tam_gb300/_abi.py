@@ -2,8 +2,8 @@
 
 This module mirrors the header one-to-one: the same struct layouts, enum
 values and entry points.  It is the binding a Python caller (or the tests)
-uses; a Fortran caller would use the iso_c_binding interface shown in
-INTEGRATION.md instead.
+uses; a Fortran caller would use the iso_c_binding interface module
+include/tam.f90 instead.
 """
 from __future__ import annotations
 
