@@ -262,8 +262,13 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * per-voxel coefficient arrays; 0: always read the arrays; with TMA off or
  * rows whose pitch TMA cannot take (nx not a multiple of 4) the class-table
  * step stages its planes with cp.async, two voxels per thread),
- * "heat.cls_rows" (class-table step: 0 = two x-adjacent voxels per thread,
- * the default; 1 or 2 = that many voxel rows per thread),
+ * "heat.slab" (class-table step with TMA: 1 (default) runs the slab form --
+ * tiles of 32 x 8 voxels, two x-adjacent voxels per thread, one block
+ * barrier per plane, boundary faces as ghost neighbours, boiling, damage and
+ * ablation done for the listed voxels after the planes; 0 runs the form
+ * chosen by "heat.cls_rows"),
+ * "heat.cls_rows" (class-table step without the slab form: 0 = two
+ * x-adjacent voxels per thread; 1 or 2 = that many voxel rows per thread),
  * "heat.graph" (config mode: 1 (default) replays chunks of 16 heat steps from
  * CUDA graphs when no step but a chunk's last needs the host (re-trace check,
  * source switching on); 0 launches every step),
@@ -317,10 +322,11 @@ int tam_load_state(struct tam_ctx *ctx, const char *path);
 /*
  * Autotuner (no reference counterpart).  Config mode: times the context's own
  * workload under candidate settings of "transport.scat_min" (an MC pass of
- * `packets`) and of "heat.zchunk" / "heat.cls_rows" (`steps` heat steps),
- * keeps the fastest and puts the context's state back as it was (fields,
- * clock, pulse state, tallies).  0 packets or 0 steps skips that part.
- * chosen (nullable) receives up to nchosen values: scat_min, zchunk, cls_rows.
+ * `packets`) and of "heat.zchunk" / "heat.slab" / "heat.cls_rows" (`steps`
+ * heat steps), keeps the fastest and puts the context's state back as it was
+ * (fields, clock, pulse state, tallies).  0 packets or 0 steps skips that
+ * part.  chosen (nullable) receives up to nchosen values: scat_min, zchunk,
+ * cls_rows, slab.
  */
 int tam_autotune(struct tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, int32_t nchosen);
 /* Autotuner of the batched heat step: times `steps` batched steps of the n

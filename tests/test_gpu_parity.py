@@ -560,7 +560,7 @@ def test_writer_files(tam, orc, tmp_path):
 
 
 # ------------------------------------------- class-table fused heat step --
-def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats, rows=2, tma=1):
+def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats, rows=2, tma=1, slab=0):
     half = 0.0025 * nx  # cm: 50 um voxels
     p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half * ny / nx, zmax=half * nz / nx, mode=1,
                            precision=precision, pulse_type=1, power=1.0, energy_per_pixel=1e6, total_time=10.0)
@@ -571,6 +571,7 @@ def _layered_heat_ctx(tam, nx, ny, nz, precision, cls, dt, J, grid, mats, rows=2
     ctx.set_tuning("heat.cls", cls)
     ctx.set_tuning("heat.cls_rows", rows)
     ctx.set_tuning("heat.tma", tma)
+    ctx.set_tuning("heat.slab", slab)
     ctx.upload(F.TAM_F_MATERIAL, grid)
     ctx.upload(F.TAM_F_JMEAN_GLOBAL, J)
     return ctx
@@ -596,9 +597,10 @@ def test_fused_class_table_matches_coefficient_arrays(tam, nx):
     alpha = max(k / (r * c) for k, r, c in mats[1:])
     dt = 0.9 / (2 * alpha * 3 / d ** 2)
     out = {}
-    for name, prec, cls, rows, tma in (("cls", 1, 1, 2, 1), ("cls1", 1, 1, 1, 1), ("cls0", 1, 1, 0, 1),
-                                       ("arr", 1, 0, 1, 1), ("f64", 0, 1, 1, 1), ("stg", 1, 1, 0, 0)):
-        ctx = _layered_heat_ctx(tam, nx, ny, nz, prec, cls, dt, J, grid, mats, rows, tma)
+    for name, prec, cls, rows, tma, slab in (("cls", 1, 1, 2, 1, 0), ("cls1", 1, 1, 1, 1, 0), ("cls0", 1, 1, 0, 1, 0),
+                                             ("arr", 1, 0, 1, 1, 0), ("f64", 0, 1, 1, 1, 0), ("stg", 1, 1, 0, 0, 0),
+                                             ("slab", 1, 1, 0, 1, 1)):
+        ctx = _layered_heat_ctx(tam, nx, ny, nz, prec, cls, dt, J, grid, mats, rows, tma, slab)
         T = ctx.heat_steps(300, want=True)
         out[name] = (T, ctx.download(F.TAM_F_TISSUE), ctx.device_errors())
         ctx.close()
@@ -611,6 +613,48 @@ def test_fused_class_table_matches_coefficient_arrays(tam, nx):
     assert np.abs(out["cls"][0] - out["f64"][0]).max() <= 1e-3
     assert np.abs(out["stg"][0] - out["cls"][0]).max() <= 1e-4 and out["stg"][2] == 0
     assert np.abs(out["stg"][1] - out["cls"][1]).max() <= 1e-4 * max(out["cls"][1].max(), 1e-30)
+    # the slab form (rows of 44 and 48: TMA; 45: not 16-byte aligned, the staged step runs)
+    assert out["slab"][2] == 0
+    assert np.abs(out["slab"][0] - out["cls"][0]).max() <= 1e-4
+    assert np.abs(out["slab"][0] - out["f64"][0]).max() <= 1e-3
+    assert np.abs(out["slab"][1] - out["f64"][1]).max() <= 1e-3 * max(out["f64"][1].max(), 1e-30)
+
+
+@pytest.mark.parametrize("nx,layered", [(40, False), (96, False), (64, False), (40, True), (96, True), (64, True)])
+def test_slab_step_matches_pair_step_and_fp64(tam, nx, layered):
+    # the slab form of the class-table step (tiles of 32 x 8, so nx = 40 and 96
+    # leave a partly filled last tile), uniform and layered grids, against the
+    # voxel-pair form (1e-4 K) and the FP64 step (1e-3 K), 300 steps with a hot
+    # spot at the convective top face that boils and ablates
+    ny, nz = 24, 20
+    mats = [(0.026, 1.2, 1005.0), (0.56, 1070.0, 3400.0), (0.21, 911.0, 2348.0)]
+    grid = np.ones((nx, ny, nz), dtype=np.uint8, order="F")
+    if layered:
+        grid[:, :, :8] = 2
+        grid[5:15, 3:12, 10:16] = 2
+    rng = np.random.default_rng(nx)
+    J = np.asfortranarray(rng.uniform(0, 1, (nx, ny, nz)) ** 2 * 5e8)
+    J[nx // 2 - 2:nx // 2 + 2, 10:14, nz - 4:] = 5e10
+    d = 5e-5
+    alpha = max(k / (r * c) for k, r, c in mats[1:])
+    dt = 0.9 / (2 * alpha * 3 / d ** 2)
+    out = {}
+    for name, prec, rows, slab in (("slab", 1, 0, 1), ("pair", 1, 0, 0), ("f64", 0, 1, 0)):
+        ctx = _layered_heat_ctx(tam, nx, ny, nz, prec, 1, dt, J, grid, mats, rows, 1, slab)
+        T = ctx.heat_steps(300, want=True)
+        out[name] = (T, ctx.download(F.TAM_F_TISSUE), ctx.device_errors(), ctx.download(F.TAM_F_Q),
+                     ctx.download(F.TAM_F_MATERIAL))
+        ctx.close()
+    assert out["slab"][2] == 0 and out["pair"][2] == 0
+    # the latent-heat branch ran and the hot spot ablated (its source then stops, so it cools again)
+    assert (out["f64"][3] > 0).any() and (out["f64"][4] == 0).any()
+    np.testing.assert_array_equal(out["slab"][4], out["f64"][4])
+    hot = out["f64"][0] - 373.15
+    away = np.abs(hot) > 0.05  # voxels straddling the boiling threshold enter the clamp a step apart
+    assert np.abs(out["slab"][0] - out["pair"][0])[away].max() <= 1e-4
+    assert np.abs(out["slab"][0] - out["f64"][0])[away].max() <= 1e-3
+    om = out["f64"][1]
+    assert np.abs(out["slab"][1] - om).max() <= 1e-3 * max(om.max(), 1e-30)
 
 
 def test_fused_class_table_off_after_per_voxel_properties(tam):
@@ -664,7 +708,8 @@ def test_autotune_restores_state(tam):
         t0, passes0 = st0.time, st0.mc_passes
         chosen = ctx.autotune(packets=50000, steps=10)
         assert chosen["transport.scat_min"] in (12, 16, 20, 24, 28)
-        assert chosen["heat.zchunk"] in (2, 3, 4, 8, 16) and chosen["heat.cls_rows"] in (0, 1)
+        assert chosen["heat.zchunk"] in (2, 3, 4, 5, 8, 16) and chosen["heat.cls_rows"] in (0, 1)
+        assert chosen["heat.slab"] in (0, 1)
         for f, arr in before.items():
             np.testing.assert_array_equal(ctx.download(f), arr)
         st = ctx.state()

@@ -385,7 +385,7 @@ __global__ void __launch_bounds__(FX *FY, TAM_STAGED_MINB)
                     const float dT = A.fc[FC_DT] * lap;
                     const float sPJ = d.pdt * Jv;
                     const float srcT = sPJ * L.irc[kc];
-                    float Tnew = A.fc[FC_TBOIL], Enew = 0.f;
+                    float Tnew = A.fc[FC_TBOIL], Enew = A.fc[FC_TBOIL_E];
                     const bool clamped = A.boil && Tc >= Tnew && boil_clamp(A, L, kc, v, sPJ, dT);
                     if (!clamped) {
                         const float inc = dT + srcT;
@@ -680,7 +680,7 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_PAIRS_MINB)
                     for (int h = 0; h < 2; ++h) {
                         const float tc = tcs[h], e0 = e0s[h];
                         const float sPJ = d.pdt * (h ? Jv.y : Jv.x);
-                        float tn = tboil, en_ = 0.f;
+                        float tn = tboil, en_ = A.fc[FC_TBOIL_E];
                         if (!(clamped >> h & 1u)) {
                             const float inc = dt * lap[h] + sPJ * L.irc[kks[h]];
                             const float yk = inc - e0;
@@ -835,7 +835,7 @@ __global__ void __launch_bounds__(FX *FY, 4)
                 const float dT = dt * lap;
                 const float sPJ = Pdt != 0.f ? Pdt * __ldg(J + v) : 0.f;
                 const float srcT = sPJ * I.L.irc[kc];
-                float Tnew = a.fc[FC_TBOIL], Enew = 0.f;
+                float Tnew = a.fc[FC_TBOIL], Enew = a.fc[FC_TBOIL_E];
                 const bool clamped = a.boil && Tc >= a.fc[FC_TBOIL] && boil_clamp(a, I.L, kc, v, sPJ, dT);
                 if (!clamped) {
                     const float inc = dT + srcT;

@@ -601,6 +601,7 @@ __global__ void __launch_bounds__(FX *FY, KAHAN ? 4 : 2) fused_kernel(const Fuse
                         const Real qn = Qv + Ein;
                         Q[v] = qn < qv ? qn : qv;
                         Tn = cst<Real>(a, FC_TBOIL);
+                        if (KAHAN) En = cst<Real>(a, FC_TBOIL_E);
                         clamped = true;
                     }
                 }
@@ -665,12 +666,14 @@ void fill_fused_consts(FusedArgs &a)
     d[FC_TLO] = a.T_lo;
     d[FC_THI] = a.T_hi;
     d[FC_TABL] = a.T_abl;
+    d[FC_TBOIL_E] = 0.0;  // the FP64 forms clamp to T_boil itself
     for (int i = 0; i < FC_N; ++i) a.fc[i] = (float)d[i];
     a.fc[FC_LNA_LO] = (float)(d[FC_LNA_HI] - (double)a.fc[FC_LNA_HI]);
     a.fc[FC_EAR_LO] = (float)(d[FC_EAR_HI] - (double)a.fc[FC_EAR_HI]);
     a.fc[FC_TLO_LO] = (float)(d[FC_TLO] - (double)a.fc[FC_TLO]);
     a.fc[FC_THI_LO] = (float)(d[FC_THI] - (double)a.fc[FC_THI]);
     a.fc[FC_TABL_LO] = (float)(d[FC_TABL] - (double)a.fc[FC_TABL]);
+    a.fc[FC_TBOIL_E] = (float)((double)a.fc[FC_TBOIL] - d[FC_TBOIL]);
 }
 
 namespace {

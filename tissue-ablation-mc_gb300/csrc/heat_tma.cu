@@ -20,6 +20,7 @@
 #include <atomic>
 
 #include "heat_common.cuh"
+#include "tma_common.cuh"
 
 namespace tam {
 
@@ -40,7 +41,6 @@ constexpr int OWN_BYTES = FY * FX * 4;                 // 1024: Az, 1/(rho c), J
 constexpr int STAGE_BYTES = 4 * ARR_BYTES + 3 * OWN_BYTES;  // 9728
 constexpr uint32_t TX_BYTES = 4u * TROWS * TPITCH * 4 + 3u * FY * FX * 4;  // bytes landed per plane
 constexpr int SMEM_BYTES = TS * STAGE_BYTES + TS * 8 + 128;
-constexpr long long WAIT_CYCLES = 4000000000ll;        // ~2 s at 2 GHz: give up and flag
 
 static_assert(STAGE_BYTES % 128 == 0, "stage alignment");
 
@@ -48,47 +48,6 @@ struct Maps {  // the seven maps of one launch
     CUtensorMap T, E, ax, ay, az, irc, J;
 };
 
-__device__ __forceinline__ uint32_t su32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count)
-{
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(su32(bar)), "r"(count) : "memory");
-}
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes)
-{
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(su32(bar)), "r"(bytes) : "memory");
-}
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity)
-{
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}\n"
-        : "=r"(ok)
-        : "r"(su32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-// Bounded wait for phase `parity` of a stage barrier; false on time-out.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity)
-{
-    if (mbar_try_wait(bar, parity)) return true;
-    const long long t0 = clock64();
-    while (!mbar_try_wait(bar, parity))
-        if (clock64() - t0 > WAIT_CYCLES) return false;
-    return true;
-}
-__device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar)
-{
-    asm volatile(
-        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::
-            "r"(su32(dst)),
-        "l"(map), "r"(x), "r"(y), "r"(z), "r"(su32(bar))
-        : "memory");
-}
-__device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
-__device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }
 
 struct View {  // one staged plane
     const float *T, *E, *ax, *ay, *az, *irc, *J;
@@ -228,6 +187,7 @@ __global__ void __launch_bounds__(FX *FY, 4)
                         const float qn = Qv + Ein;
                         Q[v] = qn < qv ? qn : qv;
                         Tnew = a.fc[FC_TBOIL];
+                        Enew = a.fc[FC_TBOIL_E];
                         clamped = true;
                     }
                 }
@@ -450,6 +410,7 @@ __global__ void __launch_bounds__(FX *FY, RY == 1 ? 4 : 3)
                             const float qn = Qv + Ein;
                             Q[v] = qn < qv ? qn : qv;
                             Tnew = a.fc[FC_TBOIL];
+                            Enew = a.fc[FC_TBOIL_E];
                             clamped = true;
                         }
                     }
@@ -655,7 +616,7 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_CLS2_MINB)
                 const float dT = dt * lap;
                 const float sPJ = Pdt * (h ? Jv.y : Jv.x);
                 const float src = sPJ * (UNIFORM ? irc_u : L.irc[k]);
-                float tn = a.fc[FC_TBOIL], en_ = 0.f;
+                float tn = a.fc[FC_TBOIL], en_ = a.fc[FC_TBOIL_E];
                 bool clamped = false;
                 if (inh && a.boil && tc >= a.fc[FC_TBOIL]) {
                     const float rr = L.rho[k], rc = rr * L.c[k];
@@ -717,46 +678,6 @@ __global__ void __launch_bounds__(FX / 2 * FY, TAM_CLS2_MINB)
     if (errbits) atomicOr(a.err, errbits);
 }
 
-CUresult (*p_encode)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *, const cuuint64_t *,
-                     const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                     CUtensorMapL2promotion, CUtensorMapFloatOOBfill) = nullptr;
-
-cudaError_t encoder()
-{
-    if (p_encode) return cudaSuccess;
-    void *fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q);
-    if (e != cudaSuccess) return e;
-    if (q != cudaDriverEntryPointSuccess || !fn) return cudaErrorNotSupported;
-    p_encode = reinterpret_cast<decltype(p_encode)>(fn);
-    return cudaSuccess;
-}
-
-cudaError_t encode(CUtensorMap *m, const float *base, int nx, int ny, int nz, int bx, int by)
-{
-    const cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, (cuuint64_t)nz};
-    const cuuint64_t strides[2] = {(cuuint64_t)nx * 4, (cuuint64_t)nx * ny * 4};
-    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    const CUresult r = p_encode(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void *)base, dims, strides, box, estr,
-                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
-}
-
-// Tensor map of the u8 class grid, rows of `pitch` bytes (a multiple of 16).
-cudaError_t encode_u8(CUtensorMap *m, const uint8_t *base, int pitch, int ny, int nz, int bx, int by)
-{
-    const cuuint64_t dims[3] = {(cuuint64_t)pitch, (cuuint64_t)ny, (cuuint64_t)nz};
-    const cuuint64_t strides[2] = {(cuuint64_t)pitch, (cuuint64_t)pitch * ny};
-    const cuuint32_t box[3] = {(cuuint32_t)bx, (cuuint32_t)by, 1};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    const CUresult r = p_encode(m, CU_TENSOR_MAP_DATA_TYPE_UINT8, 3, (void *)base, dims, strides, box, estr,
-                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
-                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    return r == CUDA_SUCCESS ? cudaSuccess : cudaErrorInvalidValue;
-}
 
 // Class grid (row pitch `pitch`) from the material ids; ids beyond the table
 // map to 0 as in the property fill.

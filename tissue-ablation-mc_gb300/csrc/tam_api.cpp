@@ -135,6 +135,8 @@ struct tam_ctx {
     tam::BatchInst h_sinst{};
     int s_items = 0;
     tam::FusedCls *fcls = nullptr;
+    tam::FusedSlab *fslab = nullptr;
+    bool use_slab = true;            // class-table step: the slab form where the grid allows it
     uint8_t *d_cls = nullptr;
     int cls_pitch = 0;
     bool thermal_by_class = false;
@@ -830,10 +832,11 @@ int staged_setup(tam_ctx *ctx)
 }
 
 // Forms of the config-mode heat step, by what the context's state allows.
-enum HeatForm { HF_CLS = 0, HF_STAGED, HF_TMA, HF_CPASYNC };
+enum HeatForm { HF_CLS = 0, HF_STAGED, HF_TMA, HF_CPASYNC, HF_SLAB };
 
 HeatForm heat_form(const tam_ctx *ctx)
 {
+    if (ctx->fslab && ctx->use_slab && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class) return HF_SLAB;
     if (ctx->fcls && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class) return HF_CLS;
     if (!ctx->fp64 && ctx->use_cls && ctx->thermal_by_class && ctx->d_cls) return HF_STAGED;
     if (ctx->tma && ctx->use_tma) return HF_TMA;
@@ -848,6 +851,7 @@ int launch_heat(tam_ctx *ctx, tam::FusedArgs &a, HeatForm form, int which, cudaS
     a.Tc_in = ctx->fp64 ? nullptr : ctx->d_Tc[which];
     a.Tc_out = ctx->fp64 ? nullptr : ctx->d_Tc[1 - which];
     switch (form) {
+    case HF_SLAB: CK(tam::launch_fused_slab(a, ctx->fslab, which, ctx->clut, s)); break;
     case HF_CLS: CK(tam::launch_fused_cls(a, ctx->fcls, which, ctx->clut, ctx->cls_rows, s)); break;
     case HF_STAGED: {
         tam::BatchStep st{};
@@ -885,7 +889,8 @@ std::vector<unsigned char> graph_key(const tam_ctx *ctx, const tam::FusedArgs &a
     p += sizeof ctx->clut;
     std::memcpy(p, knobs, sizeof knobs);
     p += sizeof knobs;
-    std::memcpy(p, &ctx->fcls, sizeof(void *));
+    const void *maps = form == HF_SLAB ? (const void *)ctx->fslab : (const void *)ctx->fcls;
+    std::memcpy(p, &maps, sizeof(void *));
     std::memcpy(p + sizeof(void *), &ctx->tma, sizeof(void *));
     return k;
 }
@@ -1359,6 +1364,12 @@ int tam_create(const tam_params *p, const tam_config *cfg, tam_ctx **out)
             (void)cudaGetLastError();
             ctx->fcls = nullptr;
         }
+        if (tam::fused_slab_supported(ctx->nx, ctx->ny, ctx->nz) &&
+            tam::fused_slab_create(&ctx->fslab, ctx->nx, ctx->ny, ctx->nz, T2, E2, (const float *)ctx->d_J,
+                                   ctx->d_cls, ctx->cls_pitch) != cudaSuccess) {
+            (void)cudaGetLastError();
+            ctx->fslab = nullptr;
+        }
     }
     r = ctx->config ? cfg_setup(ctx) : ref_setup(ctx);
     if (r == TAM_OK) r = finish(ctx, "tam_create");
@@ -1380,6 +1391,7 @@ int tam_destroy(tam_ctx *ctx)
         if (e) cudaEventDestroy(e);
     if (ctx->tma) tam::fused_tma_destroy(ctx->tma);
     if (ctx->fcls) tam::fused_cls_destroy(ctx->fcls);
+    if (ctx->fslab) tam::fused_slab_destroy(ctx->fslab);
     for (cudaGraphExec_t &g : ctx->gexec)
         if (g) cudaGraphExecDestroy(g);
     if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
@@ -2140,6 +2152,8 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
         ctx->use_tma = value != 0;
     } else if (k == "heat.cls") {
         ctx->use_cls = value != 0;
+    } else if (k == "heat.slab") {
+        ctx->use_slab = value != 0;
     } else if (k == "heat.cls_rows") {
         if (value < 0 || value > 2) return fail(ctx, TAM_E_INVALID, "heat.cls_rows must be 0 (voxel pairs), 1 or 2");
         ctx->cls_rows = (int)value;
@@ -2451,10 +2465,12 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
     float ms = 0.f;
     // on a failure the knobs and the state go back as they were
     const int scat0 = ctx->scat_min, z0 = ctx->zchunk, rows0 = ctx->cls_rows;
+    const bool slab0 = ctx->use_slab;
     auto undo = [&](int code) {
         ctx->scat_min = scat0;
         ctx->zchunk = z0;
         ctx->cls_rows = rows0;
+        ctx->use_slab = slab0;
         (void)cudaGetLastError();
         (void)snap_restore(ctx, S);
         return code;
@@ -2482,34 +2498,41 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
         ctx->scat_min = best;
         if ((r = snap_restore(ctx, S)) != TAM_OK) return undo(r);
     }
-    // heat: z planes per thread column (and voxel rows per thread of the class-table step)
+    // heat: z planes per thread column, and the form of the class-table step
+    // (slab form, voxel pairs or rows of voxels)
     if (steps > 0) {
         int best_z = ctx->zchunk, best_r = ctx->cls_rows;
+        bool best_s = ctx->use_slab;
         float best_ms = 1e30f;
         const bool cls = ctx->fcls && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class;
-        const bool staged = !cls && !ctx->fp64 && ctx->use_cls && ctx->thermal_by_class && ctx->d_cls;
-        const std::vector<int> zcs = staged ? std::vector<int>{4, 8, 16, 32} : std::vector<int>{2, 3, 4, 8, 16};
-        for (int rows : {0, 1}) {
-            if (rows == 0 && !cls) continue;
+        const bool slab = ctx->fslab && ctx->use_tma && ctx->use_cls && ctx->thermal_by_class;
+        const bool staged = !cls && !slab && !ctx->fp64 && ctx->use_cls && ctx->thermal_by_class && ctx->d_cls;
+        const std::vector<int> zcs = staged ? std::vector<int>{4, 8, 16, 32} : std::vector<int>{2, 3, 4, 5, 8, 16};
+        for (int form : {2, 0, 1}) {  // 2: slab form; 0 / 1: class-table voxel pairs / rows
+            if (form == 2 && !slab) continue;
+            if (form == 0 && !cls) continue;
             for (int zc : zcs) {
                 if (zc > ctx->nz) continue;
                 ctx->zchunk = zc;
-                ctx->cls_rows = rows;
+                ctx->use_slab = form == 2;
+                if (form != 2) ctx->cls_rows = form;
                 if ((r = cfg_heat(ctx, steps)) != TAM_OK || (r = timed(2, 3)) != TAM_OK ||
                     (r = snap_restore(ctx, S)) != TAM_OK)
                     return undo(r);
                 if (ms < best_ms) {
                     best_ms = ms;
                     best_z = zc;
-                    best_r = rows;
+                    best_s = form == 2;
+                    if (form != 2) best_r = form;
                 }
             }
         }
         ctx->zchunk = best_z;
         ctx->cls_rows = best_r;
+        ctx->use_slab = best_s;
     }
-    const int64_t v[3] = {ctx->scat_min, ctx->zchunk, ctx->cls_rows};
-    for (int32_t i = 0; i < nchosen && i < 3 && chosen; ++i) chosen[i] = v[i];
+    const int64_t v[4] = {ctx->scat_min, ctx->zchunk, ctx->cls_rows, ctx->use_slab ? 1 : 0};
+    for (int32_t i = 0; i < nchosen && i < 4 && chosen; ++i) chosen[i] = v[i];
     return finish(ctx, "tam_autotune");
 }
 

@@ -163,7 +163,10 @@ enum FusedConst : int {
     // pairs (high part, low part), exact window and ablation temperatures
     FC_LNA_HI = 29, FC_LNA_LO, FC_EAR_HI, FC_EAR_LO, FC_TLO, FC_THI, FC_TABL,
     FC_TLO_LO, FC_THI_LO, FC_TABL_LO, // low parts of the three temperatures
-    FC_N = 39
+    // FP32 Kahan term of the clamped boiling temperature: the pair
+    // (FC_TBOIL, FC_TBOIL_E) has the true value T_boil (true T = T - e)
+    FC_TBOIL_E = 39,
+    FC_N = 40
 };
 
 // Values of one heat step that change from step to step, read by the fused
@@ -239,6 +242,19 @@ void fused_cls_destroy(FusedCls *m);
 // rows: voxel rows per thread (1 or 2).
 cudaError_t launch_fused_cls(const FusedArgs &a, const FusedCls *m, int which, const ClassLut &L, int rows,
                              cudaStream_t s);
+
+// Slab form of the FP32 class-table step (heat_slab.cu): tiles of 32 x 8
+// voxels, voxel pairs, one block barrier per plane, boundary faces as ghost
+// neighbours in the staged planes, rare voxels (boiling, damage window,
+// ablation) redone from a per-block list after the planes.  Same layout
+// requirements as the class-table form (nx a multiple of 4, class rows of a
+// 16-byte pitch) and fewer than 2^31 voxels.
+struct FusedSlab;  // opaque: tensor maps of T[2], Tc[2], J and the class grid
+bool fused_slab_supported(int nx, int ny, int nz);
+cudaError_t fused_slab_create(FusedSlab **out, int nx, int ny, int nz, float *const T[2], float *const Tc[2],
+                              const float *J, const uint8_t *cls, int pitch);
+void fused_slab_destroy(FusedSlab *m);
+cudaError_t launch_fused_slab(const FusedArgs &a, const FusedSlab *m, int which, const ClassLut &L, cudaStream_t s);
 
 // Batched FP32 heat step of many instances in one persistent cooperative
 // launch (batch.cu).  BatchInst lives in device memory, one per instance.

@@ -191,9 +191,9 @@ class Context:
 
     def autotune(self, packets: int = 1_000_000, steps: int = 20) -> dict:
         """Pick the fastest kernel settings on this context's workload; state is restored."""
-        out = (C.c_int64 * 3)()
-        self._ck(self._lib.tam_autotune(self._h, int(packets), int(steps), out, 3))
-        return {"transport.scat_min": out[0], "heat.zchunk": out[1], "heat.cls_rows": out[2]}
+        out = (C.c_int64 * 4)()
+        self._ck(self._lib.tam_autotune(self._h, int(packets), int(steps), out, 4))
+        return {"transport.scat_min": out[0], "heat.zchunk": out[1], "heat.cls_rows": out[2], "heat.slab": out[3]}
 
     def write_output(self, directory: str) -> None:
         self._ck(self._lib.tam_write_output(self._h, directory.encode()))
