@@ -374,6 +374,13 @@ int tam_write_output(struct tam_ctx *ctx, const char *dir);
 int tam_mc_pass_noalloc(const tam_params *p, const double *rhokap, double *jmean_global, int64_t nphotons,
                         uint64_t seed, uint32_t stream, double power, void *cuda_stream);
 
+/* Measurement (no reference counterpart): the current device's rate of
+ * fire-and-forget atomic adds (FP64, or FP32 with fp32 != 0) into a tally of
+ * `cells` entries at cells drawn from Philox inside the kernel, launched as
+ * the transport kernel is (4 blocks of 256 threads per SM): the ceiling of
+ * the transport's tally updates.  Allocates and frees its own tally. */
+int tam_measure_tally_atomics(int64_t cells, int32_t fp32, double *per_second);
+
 /* Self-test: Philox4x32-10 of this library against cuRAND's device Philox on
  * n inputs of 6 words {c0,c1,c2,c3,k0,k1}; outputs 4 words each. */
 int tam_selftest_philox(const uint32_t *in, uint32_t *out_mine, uint32_t *out_curand, int64_t n);

@@ -2690,6 +2690,46 @@ int tam_write_output(tam_ctx *ctx, const char *dir)
     return TAM_OK;
 }
 
+int tam_measure_tally_atomics(int64_t cells, int32_t fp32, double *per_second)
+{
+    tam_ctx *ctx = nullptr;
+    if (!per_second || cells < 1 || cells > ((int64_t)1 << 32) - 1)
+        return fail(nullptr, TAM_E_INVALID, "cells must be in 1 .. 2^32 - 1 and per_second non-null");
+    int ndev = 0, dev = 0, sms = 152;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev < 1) {
+        (void)cudaGetLastError();
+        return fail(nullptr, TAM_E_NODEV, "no CUDA device");
+    }
+    CK(cudaGetDevice(&dev));
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    const size_t bytes = (size_t)cells * (fp32 ? 4 : 8);
+    void *acc = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    cudaError_t e = cudaMalloc(&acc, bytes);
+    if (e == cudaSuccess) e = cudaMemset(acc, 0, bytes);
+    if (e == cudaSuccess) e = cudaEventCreate(&e0);
+    if (e == cudaSuccess) e = cudaEventCreate(&e1);
+    // the transport's launch shape: 4 resident blocks of 256 threads per SM
+    const int blocks = 4 * sms, per_thread = 512;
+    const double ops = (double)blocks * 256.0 * per_thread;
+    double best = 0.0;
+    for (int rep = 0; rep < 6 && e == cudaSuccess; ++rep) {
+        e = cudaEventRecord(e0);
+        if (e == cudaSuccess) e = tam::launch_atomic_peak(acc, fp32 != 0, (uint32_t)cells, blocks, per_thread, rep, nullptr);
+        if (e == cudaSuccess) e = cudaEventRecord(e1);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 0.f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e == cudaSuccess && rep > 0 && ms > 0.f) best = std::max(best, ops / (ms * 1e-3));  // rep 0 warms up
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (acc) cudaFree(acc);
+    if (e != cudaSuccess) return fail(nullptr, TAM_E_CUDA, cudaGetErrorString(e));
+    *per_second = best;
+    return TAM_OK;
+}
+
 int tam_selftest_philox(const uint32_t *in, uint32_t *out_mine, uint32_t *out_curand, int64_t n)
 {
     tam_ctx *ctx = nullptr;

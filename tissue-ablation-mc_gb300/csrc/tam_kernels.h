@@ -88,6 +88,11 @@ cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool 
 cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s,
                                 double *sum = nullptr);
 
+// Atomic-add ceiling of the tally: blocks x 256 threads, per_thread (a
+// multiple of 4) adds of 1 each at Philox-drawn cells of acc[0, cells).
+cudaError_t launch_atomic_peak(void *acc, bool fp32, uint32_t cells, int blocks, int per_thread, uint32_t seed,
+                               cudaStream_t s);
+
 // Philox self-test: out_mine / out_curand hold 4 words per input; in holds 6
 // words per input {c0, c1, c2, c3, k0, k1}.
 cudaError_t launch_philox_selftest(const uint32_t *in, uint32_t *out_mine, uint32_t *out_curand, int64_t n,

@@ -801,6 +801,34 @@ cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, boo
     return cudaGetLastError();
 }
 
+namespace {
+// Ceiling of the tally updates: `per_thread` fire-and-forget atomic adds per
+// thread (red.global.add, the result unused, as the transport's deposits) at
+// cells drawn from Philox inside the kernel, so no index stream is read; four
+// cells per Philox block, mapped to [0, cells) by a 32 x 32 high product.
+template <typename Real>
+__global__ void __launch_bounds__(256) atomic_peak_kernel(Real *acc, uint32_t cells, int per_thread, uint32_t seed)
+{
+    const uint32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+    for (int i = 0; i < per_thread; i += 4) {
+        const U4 r = philox4x32_10((uint32_t)i, t, 0x7a11u, 0u, seed, 0x5eedu);
+        atomicAdd(acc + __umulhi(r.x, cells), (Real)1);
+        atomicAdd(acc + __umulhi(r.y, cells), (Real)1);
+        atomicAdd(acc + __umulhi(r.z, cells), (Real)1);
+        atomicAdd(acc + __umulhi(r.w, cells), (Real)1);
+    }
+}
+}  // namespace
+
+cudaError_t launch_atomic_peak(void *acc, bool fp32, uint32_t cells, int blocks, int per_thread, uint32_t seed,
+                               cudaStream_t s)
+{
+    count_launch();
+    if (fp32) atomic_peak_kernel<float><<<blocks, 256, 0, s>>>((float *)acc, cells, per_thread, seed);
+    else atomic_peak_kernel<double><<<blocks, 256, 0, s>>>((double *)acc, cells, per_thread, seed);
+    return cudaGetLastError();
+}
+
 cudaError_t launch_philox_selftest(const uint32_t *in, uint32_t *mine, uint32_t *ref, int64_t n, cudaStream_t s)
 {
     if (n <= 0) return cudaSuccess;

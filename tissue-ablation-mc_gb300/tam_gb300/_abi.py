@@ -138,6 +138,7 @@ SIGNATURES = [
     ("tam_kernel_launches", C.c_int64, []),
     ("tam_set_tuning", C.c_int, [_P, C.c_char_p, C.c_int64]),
     ("tam_write_output", C.c_int, [_P, C.c_char_p]),
+    ("tam_measure_tally_atomics", C.c_int, [C.c_int64, C.c_int32, C.POINTER(C.c_double)]),
     ("tam_selftest_philox", C.c_int, [_U32, _U32, _U32, C.c_int64]),
     ("tam_mc_pass_noalloc", C.c_int, [C.POINTER(Params), _P, _P, C.c_int64, C.c_uint64, C.c_uint32, C.c_double, _P]),
 ]

@@ -240,6 +240,14 @@ def batch_autotune(contexts, steps: int = 20) -> dict:
     return {"batch.staged": out[0], "batch.zchunk": out[1], "batch.streams": out[2]}
 
 
+def tally_atomics_per_second(cells: int, fp32: bool = False) -> float:
+    """Rate of the device's atomic adds into a tally of `cells` entries (the
+    transport's tally-update ceiling; tam_measure_tally_atomics)."""
+    v = C.c_double(0)
+    check(lib().tam_measure_tally_atomics(int(cells), 1 if fp32 else 0, C.byref(v)))
+    return v.value
+
+
 def kernel_launches() -> int:
     return int(lib().tam_kernel_launches())
 
