@@ -316,6 +316,12 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
     // once per flight) instead of optical depth per voxel step
     constexpr bool DIST = sizeof(Real) == 4 && MED == MED_UNIFORM;
     const Real inv_mut = DIST ? (Real)1 / lut[a.uniform_id >= 0 ? a.uniform_id : 0].mut : (Real)0;
+    // a uniform medium's properties stay in registers (no fetch per crossing)
+    const int mid_u = MED == MED_UNIFORM ? (a.uniform_id >= 0 ? a.uniform_id : 0) : 0;
+    const Real mut_u = lut[mid_u].mut, mua_u = lut[mid_u].mua;
+    // only the reference medium nudges a crossed coordinate past the face
+    // (config mode's factor is exactly 1)
+    constexpr bool NUDGE = MED == MED_RHOKAP;
 
     int mode = M_DEAD;
     bool exhausted = false;
@@ -327,6 +333,15 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
     uint32_t ev = 0, plo = 0, phi32 = 0, nsteps = 0;
     uint32_t cScat = 0;
     uint64_t cSteps = 0;  // voxel steps of this thread's finished packets (reduced once at the end)
+    auto props = [&]() {
+        if constexpr (MED == MED_UNIFORM) {
+            mid = mid_u;
+            mut = mut_u;
+            mua = mua_u;
+        } else {
+            fetch<Real, MED>(a, lut, ix, iy, iz, cidx, mut, mua, mid);
+        }
+    };
 
     for (;;) {
         // ---------------------------------------------- refill dead lanes --
@@ -382,7 +397,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                         fx = X - (Real)ix * hx;
                         fy = Y - (Real)iy * hy;
                         fz = hz - (Real)1.e-8 * hz;
-                        fetch<Real, MED>(a, lut, ix, iy, iz, cidx, mut, mua, mid);
+                        props();
                         w = (Real)1;
                         if (a.fresnel) {
                             const Real nt = MED == MED_RHOKAP ? K.rhokap_n : lut[mid].n;
@@ -411,8 +426,8 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
         // voxel steps of the flying lanes until enough lanes wait to scatter,
         // no lane flies, or a lane needs a new packet
         unsigned sc, fl;
-        for (;;) {
         // -------------------------- one voxel step (src/inttau2.f90:37-63) --
+        auto vstep = [&]() {
         if (mode == M_FLY) {
             if (++nsteps > max_steps) {
                 if (dep != (Real)0) deposit<T32>(a, cidx, dep);
@@ -463,10 +478,10 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                         iy = cy ? j : iy;
                         iz = cz ? j : iz;
                         cidx += cx ? sg : (cy ? sg * SY : sg * SZ);
-                        tmx = cx ? tmx + tdx * knx : tmx;
-                        tmy = cy ? tmy + tdy * kny : tmy;
-                        tmz = cz ? tmz + tdz * knz : tmz;
-                        fetch<Real, MED>(a, lut, ix, iy, iz, cidx, mut, mua, mid);
+                        tmx = cx ? tmx + (NUDGE ? tdx * knx : tdx) : tmx;
+                        tmy = cy ? tmy + (NUDGE ? tdy * kny : tdy) : tmy;
+                        tmz = cz ? tmz + (NUDGE ? tdz * knz : tdz) : tmz;
+                        props();
                     } else if (a.fresnel) {
                         // outer face: the packet sits on it; the Fresnel draw
                         // waits for the event batch
@@ -490,7 +505,14 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                 }
             }
         }
-
+        };
+        for (;;) {
+            // two voxel steps per vote: the votes are a sizeable share of a
+            // step, and a lane that stops after the first step only idles
+            // for the second (its packet's walk does not depend on when the
+            // event batch runs)
+            vstep();
+            vstep();
             sc = __ballot_sync(FULL, mode >= M_SCAT);
             fl = __ballot_sync(FULL, mode == M_FLY);
             if (fl == 0 || __popc(sc) >= scat_min || (!exhausted && (sc | fl) != FULL)) break;
