@@ -219,12 +219,29 @@ def _run_vessels(a) -> None:
               f"device errors {ctx.device_errors()}", flush=True)
 
 
+def _run_heat(a) -> None:
+    """The heat step of the homogeneous cube (configuration 2 at edge 200):
+    one MC pass for the absorbed-power field, then `steps` steps of each
+    requested form launched one by one (no graph replay), timed with the
+    library's CUDA events; the form used by profiles of the heat kernels."""
+    w = homogeneous(a.edge, a.packets, 2.0, 2.0, precision=1)
+    with w.context() as ctx:
+        ctx.mc_pass(a.packets, seed=1)
+        ctx.set_tuning("heat.graph", 0)
+        for form in a.forms.split(","):
+            ctx.set_tuning("heat.slab", 1 if form == "slab" else 0)
+            ctx.heat_steps(a.steps)
+            _, hm, _ = ctx.timing()
+            print(f"heat {form}: {a.steps} steps of {a.edge}^3 in {hm:.3f} ms; device errors {ctx.device_errors()}",
+                  flush=True)
+
+
 def parser():
     """The command line of `python -m tam_gb300.workloads`."""
     import argparse
 
     ap = argparse.ArgumentParser(prog="python -m tam_gb300.workloads",
-                                 description="Run parts of benchmark configurations 4 and 5 and print their timings.")
+                                 description="Run parts of the benchmark configurations and print their timings.")
     sub = ap.add_subparsers(dest="cmd", required=True)
     b = sub.add_parser("batch", help="configuration 4: batched heat steps of seeded instances")
     b.add_argument("--instances", type=int, default=64)
@@ -237,12 +254,17 @@ def parser():
     v.add_argument("--packets", type=int, default=10_000_000)
     v.add_argument("--warm-packets", type=int, default=1_000_000)
     v.add_argument("--tally32", type=int, default=-1, choices=[-1, 0, 1])
+    h = sub.add_parser("heat", help="the homogeneous cube's FP32 heat step, one launch per step")
+    h.add_argument("--edge", type=int, default=200)
+    h.add_argument("--packets", type=int, default=1_000_000)
+    h.add_argument("--steps", type=int, default=4)
+    h.add_argument("--forms", default="slab,pair", help="comma list of slab / pair")
     return ap
 
 
 def main(argv=None) -> None:
     a = parser().parse_args(argv)
-    (_run_batch if a.cmd == "batch" else _run_vessels)(a)
+    {"batch": _run_batch, "vessels": _run_vessels, "heat": _run_heat}[a.cmd](a)
 
 
 if __name__ == "__main__":
