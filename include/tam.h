@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define TAM_ABI_VERSION 1
+#define TAM_ABI_VERSION 2
 
 /* ---- status codes ---- */
 enum tam_status {
@@ -126,6 +126,9 @@ typedef struct tam_config {
     int32_t retrace_check;       /* heat steps between re-trace checks, counted across calls
                                   * (0: at the end of every heat-step call) */
     int64_t max_steps;           /* per-packet loop cap */
+    int32_t isolation;           /* 1: after every heat step a tissue voxel whose six neighbours are all air
+                                  * (outside the grid counts as air) turns to air, the rule of
+                                  * src/3dFD.f90:347-349; 0 (default): no such rule */
 } tam_config;
 
 /* Mutable module scalars of the reference (module Heat, src/3dFD.f90:7-12). */
@@ -254,7 +257,12 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * interaction before the warp scatters, 1..32), "transport.tally32" (FP32
  * config-mode transport: -1 (default) deposits into an FP32 tally flushed
  * into the FP64 jmean when the FP64 tally exceeds 256 MB, 0 never, 1 always),
- * "transport.tally32_chunk" (packets per flush, default 16777216), "heat.zchunk" (z planes per
+ * "transport.tally32_chunk" (packets per flush, default 16777216),
+ * "transport.tally32_box" (cells of the FP32 tally at most, default 25165824
+ * = 96 MB: larger grids get a box of that many cells centred on the beam axis
+ * and reaching down from the top face, whose deposits are tallied in FP32;
+ * deposits outside it go to the FP64 jmean directly; FP64 contexts use the
+ * FP32 tally only with "transport.tally32" 1), "heat.zchunk" (z planes per
  * thread column of the fused step, 0 = automatic), "heat.tma" (1: stage the
  * FP32 fused step's planes with TMA where the row pitch allows, 0: cp.async),
  * "heat.cls" (1: while the thermal properties are those of the material

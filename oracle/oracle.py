@@ -127,6 +127,8 @@ def load() -> C.CDLL:
     L.orc_fused_step.restype = C.c_int64
     L.orc_fused_step.argtypes = [C.POINTER(HeatDesc), C.c_double, C.c_double, _DP, _DP, _DP, _DP, _DP, _DP, _DP,
                                  _DP, _DP, C.POINTER(C.c_uint8), C.c_int]
+    L.orc_isolate.restype = C.c_int64
+    L.orc_isolate.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_uint8), _DP]
     L.orc_stable_dt.restype = C.c_double
     L.orc_stable_dt.argtypes = [C.POINTER(HeatDesc), C.c_double]
     _lib = L
@@ -288,3 +290,13 @@ def fused_step(h: HeatDesc, P, t_new, T, k, rho, c, J, Q, omega, thres, mat, nth
     n = L.orc_fused_step(C.byref(h), P, t_new, dp(T), dp(Tn), dp(k), dp(rho), dp(c), dp(J), dp(Q), dp(omega),
                          dp(thres), mat.ctypes.data_as(C.POINTER(C.c_uint8)), nthreads)
     return Tn, n
+
+
+def isolate(mat, J):
+    """The isolation rule (src/3dFD.f90:347-349) in place on a u8 material
+    grid and its FP64 source field (both Fortran order); returns the count."""
+    L = load()
+    if not mat.flags.f_contiguous or mat.dtype != np.uint8:
+        raise ValueError("mat must be uint8 and Fortran-ordered")
+    nx, ny, nz = mat.shape
+    return L.orc_isolate(nx, ny, nz, mat.ctypes.data_as(C.POINTER(C.c_uint8)), dp(J))

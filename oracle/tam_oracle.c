@@ -1045,3 +1045,30 @@ int64_t orc_fused_step(const orc_heat_desc *h, double P, double t_new, const dou
             }
     return nabl;
 }
+
+/* src/3dFD.f90:330-349: do k / do j / do i, summ of the six neighbours,
+ * in place (the backward neighbours are already updated). */
+int64_t orc_isolate(int nx, int ny, int nz, uint8_t *mat, double *J)
+{
+    const int64_t sy = nx, sz = (int64_t)nx * ny;
+    int64_t n = 0;
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                const int64_t v = i + sy * j + sz * k;
+                if (mat[v] == 0) continue;
+                int summ = 0;
+                summ += k + 1 < nz ? mat[v + sz] : 0;
+                summ += j + 1 < ny ? mat[v + sy] : 0;
+                summ += i + 1 < nx ? mat[v + 1] : 0;
+                summ += k > 0 ? mat[v - sz] : 0;
+                summ += j > 0 ? mat[v - sy] : 0;
+                summ += i > 0 ? mat[v - 1] : 0;
+                if (summ == 0) {
+                    mat[v] = 0;
+                    J[v] = 0.0;
+                    n += 1;
+                }
+            }
+    return n;
+}

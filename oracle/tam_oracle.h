@@ -211,6 +211,14 @@ int64_t orc_fused_step(const orc_heat_desc *h, double P, double t_new,
                        const double *c, double *J, double *Q, double *omega, double *thres,
                        uint8_t *mat, int nthreads);
 
+/* The isolation rule of src/3dFD.f90:347-349 on a config-mode material grid
+ * (u8, x fastest): the reference's sequential sweep (k, j, i) with its
+ * in-place updates, where a voxel that is not air (id != 0) and whose six
+ * neighbours are air -- outside the grid counting as air, as the
+ * reference's zero halo -- becomes air and its source J goes to zero.
+ * Returns the number of voxels turned to air. */
+int64_t orc_isolate(int nx, int ny, int nz, uint8_t *mat, double *J);
+
 /* Stability-limited step of the config-mode operator: 1/(2 opscale amax sum 1/d^2). */
 double orc_stable_dt(const orc_heat_desc *h, double alpha_max);
 

@@ -37,7 +37,7 @@ def test_struct_layouts_match(tam):
     assert lib.tam_struct_size(2) == C.sizeof(tam.State)
     assert lib.tam_struct_size(3) == C.sizeof(tam._abi.Material)
     assert lib.tam_struct_size(9) == -1
-    assert lib.tam_abi_version() == 1
+    assert lib.tam_abi_version() == 2
     assert b"sm_103a" in lib.tam_version()
 
 

@@ -718,12 +718,14 @@ def test_autotune_restores_state(tam):
         assert ctx.device_errors() == 0
 
 
-@pytest.mark.parametrize("layered", [False, True])
-def test_fp32_tally_flushed_matches_fp64_tally(tam, layered):
+@pytest.mark.parametrize("layered,box", [(False, 0), (True, 0), (False, 20 * 20 * 16), (True, 20 * 20 * 16)])
+def test_fp32_tally_flushed_matches_fp64_tally(tam, layered, box):
     # FP32 transport with deposits into the FP32 tally, flushed into the FP64
     # jmean every 30000 packets (four flushes), against FP64 deposits on the
     # same Philox streams: only the rounding of the accumulation differs.
-    # Uniform medium and a per-voxel material grid (two kernel forms).
+    # Uniform medium and a per-voxel material grid (two kernel forms); the
+    # tally either covers the grid or is a 20 x 20 x 16 box below the beam,
+    # the deposits outside it going to the FP64 jmean directly.
     nx = 40
     half = 0.0025 * nx
     p = tam.default_params(nxg=nx, nyg=nx, nzg=nx, xmax=half, ymax=half, zmax=half, mode=1, precision=1,
@@ -741,6 +743,8 @@ def test_fp32_tally_flushed_matches_fp64_tally(tam, layered):
             ctx.upload(F.TAM_F_MATERIAL, grid)
             ctx.set_tuning("transport.tally32", t32)
             ctx.set_tuning("transport.tally32_chunk", 30000)
+            if box:
+                ctx.set_tuning("transport.tally32_box", box)
             J = ctx.mc_pass(100000, seed=4, stream=1, want=True)
             out.append((J, ctx.tallies(), ctx.device_errors()))
     (Ja, ta, ea), (Jb, tb, eb) = out
@@ -749,6 +753,41 @@ def test_fp32_tally_flushed_matches_fp64_tally(tam, layered):
     assert np.abs(Ja - Jb).sum() / np.abs(Ja).sum() < 1e-6
     sig = Ja > 1e-3 * Ja.max()
     assert (np.abs(Ja - Jb)[sig] / Ja[sig]).max() < 1e-4
+    if box:
+        # a sizeable share of the deposits on either side of the box: both paths ran
+        inside = np.zeros(Ja.shape, dtype=bool)
+        inside[10:30, 10:30, nx - 16:] = True
+        assert Ja[~inside].sum() > 0.1 * Ja.sum() and Ja[inside].sum() > 0.1 * Ja.sum()
+
+
+def test_box_tally_fp64_transport_matches_oracle(tam, orc):
+    # the FP32 box tally on the FP64 transport (a 16 x 16 x 12 box under the
+    # beam of a 32^3 layered grid) against the oracle on the same Philox
+    # streams: paths identical, deposits summed in FP32 inside the box
+    # (flushed every 5000 packets) and in FP64 outside it
+    mats = [(0.0, 0.0, 0.0, 1.0), (1.0, 200.0, 0.8, 1.4), (0.3, 120.0, 0.9, 1.4), (0.1, 80.0, 0.9, 1.4)]
+    n = 32
+    ctx, d = cfg_pair(tam, orc, n, n, n, 0.2, mats=mats, radius=0.06)
+    grid = np.full((n, n, n), 3, dtype=np.uint8, order="F")
+    grid[:, :, n - 4:] = 1
+    grid[:, :, 12:n - 4] = 2
+    ctx.upload(F.TAM_F_MATERIAL, grid)
+    ctx.set_tuning("transport.tally32", 1)
+    ctx.set_tuning("transport.tally32_box", 16 * 16 * 12)
+    ctx.set_tuning("transport.tally32_chunk", 5000)
+    npk = 20000
+    ctx.mc_pass(npk, seed=8, stream=2)
+    J = ctx.download(F.TAM_F_JMEAN)
+    t = ctx.tallies()
+    Jo, to = orc.mc_transport(d, grid, npk, seed=8, stream=2, nthreads=0)
+    assert t["scatters"] == to["scatters"] and t["voxel_steps"] == to["voxel_steps"]
+    assert np.abs(J - Jo).sum() / np.abs(Jo).sum() < 1e-6
+    sig = Jo > 1e-3 * Jo.max()
+    assert (np.abs(J - Jo)[sig] / Jo[sig]).max() < 1e-4
+    inside = np.zeros(J.shape, dtype=bool)
+    inside[8:24, 8:24, n - 12:] = True
+    assert Jo[~inside].sum() > 0 and Jo[inside].sum() > 0.5 * Jo.sum()
+    ctx.close()
 
 
 @pytest.mark.parametrize("precision,check", [(1, 5), (1, 50), (0, 50)])
@@ -812,3 +851,57 @@ def test_ref_props_reuse_matches_full_update(tam, tmp_path):
     assert (want[5][1:-1, 1:-1, 1:-1] == 0).any() and (want[5][1:-1, 1:-1, 1:-1] > 0).any()
     for g, w in zip(got, want):
         np.testing.assert_array_equal(g, w)
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_isolation_rule_on_cratered_slab(tam, orc, precision):
+    # config.isolation = 1: after every heat step, tissue whose six neighbours
+    # are air (outside the grid counts as air) turns to air and loses its
+    # source (src/3dFD.f90:347-349).  A crater open to the top face holds
+    # single tissue voxels (removed, one of them on the top face) and a pair
+    # (kept); against the oracle's step + sequential sweep, FP64 to 1e-12 and
+    # FP32 (slab form) to 1e-3 K, the material grids equal
+    nx, ny, nz = 24, 20, 16
+    half = 0.12
+    dt = 2e-3
+    p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half, zmax=half, mode=1, precision=precision,
+                           pulse_type=1, power=1.0, energy_per_pixel=1e6, total_time=10.0)
+    c = tam.default_config(dt=dt, nmat=2, isolation=1)
+    tam.set_material(c, 0, 0.0, 0.0, 0.0, 1.0, 0.56, 1070.0, 3400.0)
+    tam.set_material(c, 1, 0.3, 100.0, 0.9, 1.38, 0.56, 1070.0, 3400.0)
+    grid = np.ones((nx, ny, nz), dtype=np.uint8, order="F")
+    grid[6:18, 5:15, 8:] = 0
+    grid[10, 9, 12] = 1
+    grid[14, 11, 10] = 1
+    grid[12, 10, nz - 1] = 1
+    grid[8, 8, 13] = grid[9, 8, 13] = 1
+    rng = np.random.default_rng(31)
+    J = np.asfortranarray(rng.uniform(0, 1, (nx, ny, nz)) ** 2 * 2e9)
+    nsteps = 6
+    with tam.Context(p, c) as ctx:
+        ctx.upload(F.TAM_F_MATERIAL, grid)
+        ctx.upload(F.TAM_F_JMEAN_GLOBAL, J)
+        T = ctx.heat_steps(nsteps, want=True)
+        mat = ctx.download(F.TAM_F_MATERIAL)
+        Jg = ctx.download(F.TAM_F_JMEAN_GLOBAL)
+        assert ctx.device_errors() == 0
+    h = orc.heat_desc(nx, ny, nz, 2 * half * 1e-2 / nx, 2 * half * 1e-2 / ny, 2 * half * 1e-2 / nz, dt=dt)
+    sh = (nx, ny, nz)
+    To = np.full(sh, 310.15, order="F")
+    k, rho, cc = (np.full(sh, v, order="F") for v in (0.56, 1070.0, 3400.0))
+    Q, om = np.zeros(sh, order="F"), np.zeros(sh, order="F")
+    thres = np.zeros(sh + (3,), order="F")
+    mo = grid.copy(order="F")
+    Jo = J.copy(order="F")
+    removed = 0
+    for s in range(nsteps):
+        To, _ = orc.fused_step(h, 1.0, (s + 1) * dt, To, k, rho, cc, Jo, Q, om, thres, mo)
+        removed += orc.isolate(mo, Jo)
+    assert removed == 3
+    assert mo[10, 9, 12] == mo[14, 11, 10] == mo[12, 10, nz - 1] == 0 and mo[8, 8, 13] == mo[9, 8, 13] == 1
+    np.testing.assert_array_equal(mat, mo)
+    np.testing.assert_array_equal(Jg == 0, Jo == 0)
+    if precision == 0:
+        np.testing.assert_allclose(T[1:-1, 1:-1, 1:-1], To, rtol=1e-12, atol=0)
+    else:
+        assert np.abs(T[1:-1, 1:-1, 1:-1] - To).max() <= 1e-3

@@ -356,3 +356,23 @@ def test_fused_arrhenius_and_ablation(orc):
                             st["thres"], st["mat"])
     assert nab >= 1 and st["mat"][1, 2, 3] == 0 and st["J"][1, 2, 3] == 0.0
     assert st["mat"].sum() == N ** 3 - nab
+
+
+def test_isolation_sweep_equals_parallel_rule(orc):
+    # src/3dFD.f90:347-349 sweeps k, j, i in place; the library applies the rule
+    # to every voxel at once from the old grid.  The two agree because a voxel
+    # that turns to air has only air around it, so no other test depends on it.
+    rng = np.random.default_rng(21)
+    for frac in (0.05, 0.2, 0.5):
+        mat = np.asfortranarray((rng.random((13, 11, 9)) < frac).astype(np.uint8) * rng.integers(1, 4, (13, 11, 9),
+                                                                                                 dtype=np.uint8))
+        J = np.asfortranarray(rng.random(mat.shape))
+        P = np.pad(mat, 1)  # outside the grid counts as air
+        nb = (P[:-2, 1:-1, 1:-1] | P[2:, 1:-1, 1:-1] | P[1:-1, :-2, 1:-1] | P[1:-1, 2:, 1:-1] |
+              P[1:-1, 1:-1, :-2] | P[1:-1, 1:-1, 2:])
+        want = (mat != 0) & (nb == 0)
+        m2, J2 = mat.copy(order="F"), J.copy(order="F")
+        n = orc.isolate(m2, J2)
+        assert n == want.sum() and want.sum() > 0
+        np.testing.assert_array_equal(m2, np.where(want, 0, mat))
+        np.testing.assert_array_equal(J2, np.where(want, 0.0, J))

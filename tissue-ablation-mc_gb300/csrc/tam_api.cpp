@@ -106,6 +106,8 @@ struct tam_ctx {
     int scat_min = 20;
     int tally32 = -1;                // FP32 transport: -1 auto (FP32 tally when the FP64 one exceeds 256 MB), 0 off, 1 on
     int64_t tally32_chunk = (int64_t)1 << 24;  // packets per flush of the FP32 tally (each launch ends in a tail)
+    int64_t tally32_box = (int64_t)24 << 20;   // cells of the FP32 box tally at most (96 MB: L2-resident)
+    int64_t j32_cells = 0;                     // cells allocated for the FP32 box tally
     float *d_j32 = nullptr;
     int zchunk = 0;
     bool use_tma = true;
@@ -593,11 +595,40 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, bool sync =
     // FP32 tally for grids whose FP64 tally is far larger than L2: deposits in
     // FP32, flushed into the FP64 jmean after every chunk of packets, so each
     // voxel's FP32 partial sum stays short
-    const bool t32 = ctx->config && !ctx->fp64 &&
-                     (ctx->tally32 > 0 || (ctx->tally32 < 0 && ctx->ni * 8 > ((int64_t)256 << 20)));
-    if (t32 && !ctx->d_j32) {
-        RC(dalloc_t(ctx, &ctx->d_j32, ctx->ni));
-        CK(cudaMemsetAsync(ctx->d_j32, 0, ctx->ni * sizeof(float), s));
+    // (FP64 contexts use it only when asked, for checks on the same streams)
+    const bool t32 = ctx->config && (ctx->tally32 > 0 || (!ctx->fp64 && ctx->tally32 < 0 &&
+                                                          ctx->ni * 8 > ((int64_t)256 << 20)));
+    if (t32) {
+        // the box: the whole grid if it fits the cap, else a block centred on
+        // the beam axis (the source is centred on the top face) reaching down
+        // from the top face, as near a cube as the grid allows
+        const int64_t cap = ctx->tally32_box;
+        int bn[3] = {ctx->nx, ctx->ny, ctx->nz};
+        if (ctx->ni > cap) {
+            const int side = std::max(1, (int)std::floor(std::cbrt((double)cap)));
+            bn[0] = std::min(ctx->nx, side);
+            bn[1] = std::min(ctx->ny, side);
+            bn[2] = (int)std::max<int64_t>(1, std::min<int64_t>(ctx->nz, cap / ((int64_t)bn[0] * bn[1])));
+        }
+        a.bnx = bn[0];
+        a.bny = bn[1];
+        a.bnz = bn[2];
+        a.bx0 = (ctx->nx - bn[0]) / 2;
+        a.by0 = (ctx->ny - bn[1]) / 2;
+        a.bz0 = ctx->nz - bn[2];
+        const int64_t cells = (int64_t)bn[0] * bn[1] * bn[2];
+        if (cells > ctx->j32_cells) {
+            if (ctx->d_j32) {
+                ctx->allocs.erase(std::remove(ctx->allocs.begin(), ctx->allocs.end(), (void *)ctx->d_j32),
+                                  ctx->allocs.end());
+                cudaFree(ctx->d_j32);
+            }
+            ctx->d_j32 = nullptr;
+            ctx->j32_cells = 0;
+            RC(dalloc_t(ctx, &ctx->d_j32, cells));
+            CK(cudaMemsetAsync(ctx->d_j32, 0, cells * sizeof(float), s));
+            ctx->j32_cells = cells;
+        }
     }
     a.jmean32 = t32 ? ctx->d_j32 : nullptr;
     CK(cudaMemsetAsync(ctx->d_jmean, 0, ctx->ni * sizeof(double), s));
@@ -609,7 +640,8 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, bool sync =
             a.p0 = p0;
             a.n = std::min(ctx->tally32_chunk, n - p0);
             CK(tam::launch_transport(a, ctx->fp64, ctx->sm_count, s));
-            CK(tam::launch_flush_f32(ctx->d_jmean, ctx->d_j32, ctx->ni, s));
+            CK(tam::launch_flush_f32(ctx->d_jmean, ctx->d_j32, ctx->nx, ctx->ny, a.bx0, a.by0, a.bz0, a.bnx, a.bny,
+                                     a.bnz, s));
         }
     } else {
         CK(tam::launch_transport(a, ctx->fp64, ctx->sm_count, s));
@@ -864,6 +896,9 @@ int launch_heat(tam_ctx *ctx, tam::FusedArgs &a, HeatForm form, int which, cudaS
     case HF_TMA: CK(tam::launch_fused_tma(a, ctx->tma, which, s)); break;
     default: CK(tam::launch_fused_step(a, ctx->fp64, s)); break;
     }
+    // tissue left with six air neighbours turns to air (src/3dFD.f90:347-349)
+    if (ctx->cfg.isolation)
+        CK(tam::launch_isolate(ctx->d_mat, ctx->d_J, ctx->fp64, ctx->nx, ctx->ny, ctx->nz, ctx->d_nabl, s));
     return TAM_OK;
 }
 
@@ -1173,6 +1208,7 @@ int tam_config_default(tam_config *c)
     c->retrace_fraction = 1e-3;
     c->retrace_check = 50;
     c->max_steps = 10000000;
+    c->isolation = 0;
     return TAM_OK;
 }
 
@@ -1254,7 +1290,8 @@ int tam_create(const tam_params *p, const tam_config *cfg, tam_ctx **out)
         }
         if (!(cfg->n_ambient > 0) || !(cfg->source_radius > 0) || !(cfg->opscale > 0) ||
             (cfg->dt <= 0 && !(cfg->dt_factor > 0)) || (cfg->roulette && !(cfg->roulette_m > 1.0)) ||
-            cfg->max_steps < 1 || (cfg->arrhenius && (!(cfg->A > 0) || !(cfg->Rgas > 0))))
+            cfg->max_steps < 1 || (cfg->arrhenius && (!(cfg->A > 0) || !(cfg->Rgas > 0))) ||
+            (cfg->isolation != 0 && cfg->isolation != 1))
             return fail(nullptr, TAM_E_INVALID, "config value out of range");
     }
     int ndev = 0;
@@ -1769,7 +1806,7 @@ bool batchable(tam_ctx *const *ctxs, int32_t n)
     if (n < 1) return false;
     for (int32_t i = 0; i < n; ++i) {
         const tam_ctx *c = ctxs[i];
-        if (!c->config || c->fp64 || !c->d_cls || !c->thermal_by_class || !c->use_cls) return false;
+        if (!c->config || c->fp64 || !c->d_cls || !c->thermal_by_class || !c->use_cls || c->cfg.isolation) return false;
         if (c->device != ctxs[0]->device || c->ni >= ((int64_t)1 << 31)) return false;
     }
     return true;
@@ -2145,6 +2182,9 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
     } else if (k == "transport.tally32") {
         if (value < -1 || value > 1) return fail(ctx, TAM_E_INVALID, "transport.tally32 must be -1 (auto), 0 or 1");
         ctx->tally32 = (int)value;
+    } else if (k == "transport.tally32_box") {
+        if (value < 1) return fail(ctx, TAM_E_INVALID, "transport.tally32_box must be positive");
+        ctx->tally32_box = value;
     } else if (k == "transport.tally32_chunk") {
         if (value < 1) return fail(ctx, TAM_E_INVALID, "transport.tally32_chunk must be positive");
         ctx->tally32_chunk = value;

@@ -67,7 +67,10 @@ struct TransportArgs {
     int32_t scat_min;                 // lanes that must wait before a warp scatters (0: default)
     int32_t uniform_id;               // >= 0: every voxel holds this material (no per-cell fetch)
     double *jmean;                    // interior, packet units (sum of w*d*mua)
-    float *jmean32;                   // non-null: deposits go here in FP32 (the host flushes them into jmean)
+    float *jmean32;                   // non-null: deposits inside the box below go here in FP32 (the host
+                                      // flushes them into jmean); deposits outside it go to jmean in FP64
+    int32_t bx0, by0, bz0;            // the FP32 tally's box: first cell and extent per axis
+    int32_t bnx, bny, bnz;
     double *tally;                    // N_TALLY doubles
     unsigned long long *work;         // dynamic packet counter (zeroed by the launcher)
     unsigned *err;                    // device error word
@@ -78,8 +81,11 @@ struct TransportArgs {
 // Launch the transport kernel in FP32 (fp64 == false) or FP64.
 cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cudaStream_t s);
 
-// acc[q] += (double)part[q], part[q] = 0 for q < n (flush of an FP32 tally).
-cudaError_t launch_flush_f32(double *acc, float *part, int64_t n, cudaStream_t s);
+// acc[cell of q] += (double)part[q], part[q] = 0 for the bnx x bny x bnz box
+// of cells starting at (bx0, by0, bz0) in an nx x ny grid (flush of the
+// FP32 box tally; part is box-indexed, x fastest).
+cudaError_t launch_flush_f32(double *acc, float *part, int nx, int ny, int bx0, int by0, int bz0, int bnx, int bny,
+                             int bnz, cudaStream_t s);
 
 // out[q] = in[q] * f for q < n; in is then zeroed when zero_in is set.
 // out = in * f; with `sum`, also *sum += the total of in (the caller zeroes *sum)
@@ -294,6 +300,15 @@ cudaError_t launch_batch_heat(const BatchInst *insts, int n, const int *prefix, 
 // pitch.  fcur selects the buffer pair read by the step.
 cudaError_t launch_staged_step(const BatchInst *inst, const int *prefix, int items, const BatchStep &step, int fcur,
                                cudaStream_t s);
+
+// The isolation rule of src/3dFD.f90:347-349 on the config-mode material
+// grid: a voxel that is not air (id != 0) and whose six neighbours are air
+// (outside the grid counts as air) becomes air, its source J (Real: double
+// when fp64, else float) goes to zero and n_ablated counts it.  Updating in
+// place equals the reference's sequential sweep: a voxel that turns to air
+// here has only air around it, so no other voxel's test depends on it.
+cudaError_t launch_isolate(uint8_t *mat, void *J, bool fp64, int nx, int ny, int nz, unsigned long long *n_ablated,
+                           cudaStream_t s);
 
 // Halo (reference-layout) FP64 temperature from the interior state, with
 // ghosts filled from the boundary conditions.

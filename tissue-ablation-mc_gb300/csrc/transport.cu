@@ -173,13 +173,22 @@ template <typename Real> __device__ __forceinline__ Real fresnel(Real n1, Real n
 }
 
 // Tally update of one voxel visit: an FP64 reduction into jmean (L2-resident
-// for grids up to ~16 M voxels), or an FP32 reduction into the half-size
-// scratch tally that the host flushes into jmean every few million packets
-// (grids whose FP64 tally is far larger than L2).
-template <bool T32, typename Real> __device__ __forceinline__ void deposit(const TransportArgs &a, int cidx, Real dep)
+// for grids up to ~16 M voxels), or -- for grids whose FP64 tally is far
+// larger than L2 -- an FP32 reduction into a box-sized tally around the
+// beam's entry, which stays L2-resident and which the host flushes into
+// jmean every few million packets; the rare deposits outside the box go to
+// jmean directly.
+template <bool T32, typename Real>
+__device__ __forceinline__ void deposit(const TransportArgs &a, int cidx, int ix, int iy, int iz, Real dep)
 {
-    if constexpr (T32) atomicAdd(a.jmean32 + cidx, (float)dep);
-    else atomicAdd(a.jmean + cidx, (double)dep);
+    if constexpr (T32) {
+        const unsigned bx = (unsigned)(ix - a.bx0), by = (unsigned)(iy - a.by0), bz = (unsigned)(iz - a.bz0);
+        if (bx < (unsigned)a.bnx && by < (unsigned)a.bny && bz < (unsigned)a.bnz) {
+            atomicAdd(a.jmean32 + (bx + (unsigned)a.bnx * (by + (unsigned)a.bny * bz)), (float)dep);
+            return;
+        }
+    }
+    atomicAdd(a.jmean + cidx, (double)dep);
 }
 
 template <typename Real> __device__ __forceinline__ Real clamp0h(Real f, Real h)
@@ -430,7 +439,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
         auto vstep = [&]() {
         if (mode == M_FLY) {
             if (++nsteps > max_steps) {
-                if (dep != (Real)0) deposit<T32>(a, cidx, dep);
+                if (dep != (Real)0) deposit<T32>(a, cidx, ix, iy, iz, dep);
                 dep = (Real)0;
                 atomicAdd(a.tally + T_OVERFLOW, 1.0);
                 atomicOr(&s_err, (unsigned)DEVERR_STEP_CAP);
@@ -468,7 +477,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     const int sg = cx ? sgx : (cy ? sgy : sgz);
                     const int j = (cx ? ix : (cy ? iy : iz)) + sg;
                     const int N = cx ? NX : (cy ? NY : NZ);
-                    deposit<T32>(a, cidx, dep);
+                    deposit<T32>(a, cidx, ix, iy, iz, dep);
                     dep = (Real)0;
                     if ((unsigned)j < (unsigned)N) {
                         // step into the next cell (branch-free over the axis); the
@@ -624,7 +633,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     if (!die) mode = M_FLY;
                 }
                 if (die) {
-                    if (dep != (Real)0) deposit<T32>(a, cidx, dep);
+                    if (dep != (Real)0) deposit<T32>(a, cidx, ix, iy, iz, dep);
                     dep = (Real)0;
                     cSteps += nsteps;
                     mode = M_DEAD;
@@ -682,12 +691,14 @@ __global__ void scale_kernel(Out *out, double *in, double f, int64_t n, int zero
     }
 }
 
-__global__ void flush_f32_kernel(double *acc, float *part, int64_t n)
+__global__ void flush_f32_kernel(double *acc, float *part, int nx, int ny, int bx0, int by0, int bz0, int bnx, int bny,
+                                 int64_t n)
 {
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
         const float v = part[q];
         if (v != 0.f) {
-            acc[q] += (double)v;
+            const int64_t x = bx0 + q % bnx, y = by0 + (q / bnx) % bny, z = bz0 + q / ((int64_t)bnx * bny);
+            acc[x + (int64_t)nx * (y + (int64_t)ny * z)] += (double)v;
             part[q] = 0.f;
         }
     }
@@ -776,10 +787,15 @@ cudaError_t launch_transport(const TransportArgs &args, bool fp64, int sm_count,
     cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     if (fp64) {
-        if (a.jmean32) return cudaErrorInvalidValue;  // FP64 transport keeps the FP64 tally
-        if (a.medium == MED_RHOKAP) return launch_t<double, MED_RHOKAP>(a, sm_count, s);
-        if (a.uniform_id >= 0) return launch_t<double, MED_UNIFORM>(a, sm_count, s);
-        return launch_t<double, MED_MATERIAL>(a, sm_count, s);
+        // the FP32 box tally is a config-mode form; on the FP64 transport it
+        // serves its checks against the FP64 oracle on the same streams
+        if (a.medium == MED_RHOKAP) {
+            if (a.jmean32) return cudaErrorInvalidValue;
+            return launch_t<double, MED_RHOKAP>(a, sm_count, s);
+        }
+        if (a.uniform_id >= 0)
+            return a.jmean32 ? launch_t<double, MED_UNIFORM, true>(a, sm_count, s) : launch_t<double, MED_UNIFORM>(a, sm_count, s);
+        return a.jmean32 ? launch_t<double, MED_MATERIAL, true>(a, sm_count, s) : launch_t<double, MED_MATERIAL>(a, sm_count, s);
     }
     if (a.medium == MED_RHOKAP) {
         if (a.jmean32) return cudaErrorInvalidValue;  // the FP32 tally is a config-mode form
@@ -807,11 +823,13 @@ cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool 
     return cudaGetLastError();
 }
 
-cudaError_t launch_flush_f32(double *acc, float *part, int64_t n, cudaStream_t s)
+cudaError_t launch_flush_f32(double *acc, float *part, int nx, int ny, int bx0, int by0, int bz0, int bnx, int bny,
+                             int bnz, cudaStream_t s)
 {
+    const int64_t n = (int64_t)bnx * bny * bnz;
     if (n <= 0) return cudaSuccess;
     count_launch();
-    flush_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(acc, part, n);
+    flush_f32_kernel<<<grid_for(n, 256), 256, 0, s>>>(acc, part, nx, ny, bx0, by0, bz0, bnx, bny, n);
     return cudaGetLastError();
 }
 

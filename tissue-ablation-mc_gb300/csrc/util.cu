@@ -243,4 +243,36 @@ cudaError_t launch_count_negative(const double *p, int64_t n, unsigned long long
     return cudaGetLastError();
 }
 
+namespace {
+__global__ void isolate_kernel(uint8_t *mat, void *J, int fp64, int nx, int ny, int nz, unsigned long long *n_ablated)
+{
+    const int64_t sy = nx, sz = (int64_t)nx * ny, n = sz * nz;
+    GRID_STRIDE(v, n)
+    {
+        if (mat[v] == 0) continue;
+        const int x = (int)(v % nx), y = (int)((v / nx) % ny), z = (int)(v / sz);
+        // a neighbour outside the grid counts as air, as the reference's zero halo
+        const bool air = (x == 0 || mat[v - 1] == 0) && (x == nx - 1 || mat[v + 1] == 0) &&
+                         (y == 0 || mat[v - sy] == 0) && (y == ny - 1 || mat[v + sy] == 0) &&
+                         (z == 0 || mat[v - sz] == 0) && (z == nz - 1 || mat[v + sz] == 0);
+        if (air) {
+            mat[v] = 0;
+            if (fp64) ((double *)J)[v] = 0.0;
+            else ((float *)J)[v] = 0.f;
+            atomicAdd(n_ablated, 1ull);
+        }
+    }
+}
+}  // namespace
+
+cudaError_t launch_isolate(uint8_t *mat, void *J, bool fp64, int nx, int ny, int nz, unsigned long long *n_ablated,
+                           cudaStream_t s)
+{
+    const int64_t n = (int64_t)nx * ny * nz;
+    if (n <= 0) return cudaSuccess;
+    count_launch();
+    isolate_kernel<<<blocks_for(n, 256), 256, 0, s>>>(mat, J, fp64 ? 1 : 0, nx, ny, nz, n_ablated);
+    return cudaGetLastError();
+}
+
 }  // namespace tam

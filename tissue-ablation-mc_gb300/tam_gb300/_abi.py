@@ -82,6 +82,7 @@ class Config(C.Structure):
         ("retrace_fraction", C.c_double),
         ("retrace_check", C.c_int32),
         ("max_steps", C.c_int64),
+        ("isolation", C.c_int32),
     ]
 
 
