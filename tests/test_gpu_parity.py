@@ -905,3 +905,69 @@ def test_isolation_rule_on_cratered_slab(tam, orc, precision):
         np.testing.assert_allclose(T[1:-1, 1:-1, 1:-1], To, rtol=1e-12, atol=0)
     else:
         assert np.abs(T[1:-1, 1:-1, 1:-1] - To).max() <= 1e-3
+
+
+def _coupled_cfg(tam, retrace, check, precision=1):
+    nx = 32
+    half = 0.0025 * nx
+    p = tam.default_params(nxg=nx, nyg=nx, nzg=nx, xmax=half, ymax=half, zmax=half, mode=1, precision=precision,
+                           nphotons=20000, pulse_type=1, power=30.0, energy_per_pixel=30.0 * 40.0,
+                           repetition_rate_1=0.1, pulses_to_do=3, total_time=0.35, loops=1)
+    c = tam.default_config(source_radius=0.03, retrace_fraction=retrace, retrace_check=check)
+    return p, c
+
+
+def test_coupled_config_loop_batched_matches_one_iteration_at_a_time(tam):
+    # tam_run's config-mode loop runs the iterations between MC passes as one
+    # heat-step call (steps replayed from CUDA graphs); against one iteration
+    # per call with every step launched on its own: bit-identical fields,
+    # clock, pulse state and counters (pulsed source switching on and off, no
+    # re-trace, so no MC pass after the first and nothing summed atomically)
+    out = []
+    p, c = _coupled_cfg(tam, 0.0, 0)
+    with tam.Context(p, c) as ctx:
+        ctx.mc_pass(20000, seed=5)
+        J = ctx.download(F.TAM_F_JMEAN_GLOBAL)
+    for batched in (1, 0):
+        p, c = _coupled_cfg(tam, 0.0, 0)
+        with tam.Context(p, c) as ctx:
+            ctx.upload(F.TAM_F_JMEAN_GLOBAL, J)  # no MC pass inside the loop
+            if batched:
+                iters = ctx.run(seed=7)
+            else:
+                ctx.set_tuning("heat.graph", 0)
+                iters = 0
+                while ctx.state().time <= ctx.state().total_time:
+                    ctx.step_coupled(1, seed=7)
+                    iters += 1
+            st = ctx.state()
+            out.append((iters, ctx.download(F.TAM_F_TEMP), ctx.download(F.TAM_F_TISSUE), st.time, st.counter,
+                        st.pulses_done, st.mc_passes, ctx.device_errors()))
+    (ia, Ta, Oa, ta, ca, pa, ma, ea), (ib, Tb, Ob, tb, cb, pb, mb, eb) = out
+    assert ea == eb == 0 and ia == ib > 100 and pa == pb >= 2
+    np.testing.assert_array_equal(Ta, Tb)
+    np.testing.assert_array_equal(Oa, Ob)
+    assert (ta, ca, ma) == (tb, cb, mb)
+
+
+def test_coupled_config_loop_retrace_batched(tam):
+    # with ablation re-traces (a check every 10 steps) the batched loop stops
+    # its heat-step call after the check that asks for a new MC pass, as the
+    # one-iteration loop does: the same MC passes at the same iterations (the
+    # FP64 tally's atomic sums may differ in their last bits, so fields to 1e-4 K)
+    out = []
+    for batched in (1, 0):
+        p, c = _coupled_cfg(tam, 1e-4, 10)
+        c.T_abl = 320.0
+        with tam.Context(p, c) as ctx:
+            if not batched:
+                ctx.set_tuning("heat.graph", 0)
+            for _ in range(150 if not batched else 6):
+                ctx.step_coupled(1 if not batched else 25, seed=9)
+            st = ctx.state()
+            out.append((ctx.download(F.TAM_F_TEMP), st.mc_passes, st.n_ablated, st.counter, ctx.device_errors()))
+    (Ta, ma, na, ca, ea), (Tb, mb, nb, cb, eb) = out
+    assert ea == eb == 0 and ca == cb
+    assert ma == mb >= 3, (ma, mb)
+    assert abs(na - nb) <= 2 and na > 0
+    assert np.abs(Ta - Tb).max() <= 1e-4

@@ -968,10 +968,15 @@ bool graph_capture(tam_ctx *ctx, const tam::FusedArgs &a0, HeatForm form, int wh
     return ok;
 }
 
-int cfg_heat(tam_ctx *ctx, int32_t nsteps)
+// nsteps config-mode heat steps.  With stop_on_trace the call returns as
+// soon as a re-trace check has asked for a new MC pass (the driver loop then
+// runs it before the next step), and a retrace_check of 0 (a check at the end
+// of every call) means a check after every step, as the driver's
+// one-step-per-iteration calls make it; *done receives the steps taken.
+int cfg_heat(tam_ctx *ctx, int32_t nsteps, int32_t *done = nullptr, bool stop_on_trace = false)
 {
     tam::FusedArgs a = fused_args(ctx);
-    const int check = ctx->cfg.retrace_check > 0 ? ctx->cfg.retrace_check : 0;
+    const int check = ctx->cfg.retrace_check > 0 ? ctx->cfg.retrace_check : (stop_on_trace ? 1 : 0);
     const HeatForm form = heat_form(ctx);
     if (form == HF_STAGED && nsteps > 0) RC(staged_setup(ctx));
     if (form == HF_TMA && ctx->coeff_dirty && nsteps > 0) {
@@ -1027,6 +1032,7 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
                 ctx->fcur = (ctx->fcur + GRAPH_STEPS) & 1;
                 it += GRAPH_STEPS;
                 if (due) RC(retrace_check(on));
+                if (stop_on_trace && ctx->need_trace) break;
                 continue;
             }
             ctx->time = t0;
@@ -1047,10 +1053,12 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps)
         if (retrace) due = (check ? ++ctx->since_check >= check : it + 1 == nsteps) || on;
         if (due) RC(retrace_check(on));
         ++it;
+        if (stop_on_trace && ctx->need_trace) break;
     }
     CK(cudaEventRecord(ctx->ev[3], ctx->stream));
     ctx->have_heat_time = true;
-    ctx->heat_launches = nsteps;
+    ctx->heat_launches = it;
+    if (done) *done = it;
     return TAM_OK;
 }
 
@@ -1733,11 +1741,59 @@ int tam_update_props(tam_ctx *ctx, double ablate_temp)
     return finish(ctx, "tam_update_props");
 }
 
+}  // extern "C"
+namespace {
+// Config-mode driver loop (src/mcpolar.f90:148-186 with one heat step per
+// iteration): the iterations between two MC passes run as one heat-step call,
+// so its steps replay from CUDA graphs, in batches that end where the
+// one-iteration-at-a-time loop would stop -- at the next multiple of
+// ERR_EVERY iterations (error fold), at max_iters, at the time limit
+// (until_time: an iteration runs while time <= total_time, the host's own
+// clock advanced step by step as pulse_update advances it), or right after a
+// re-trace check that calls for a new MC pass.  The kernels, their order and
+// the host state are those of the one-at-a-time loop.
+int cfg_run(tam_ctx *ctx, uint64_t seed, int64_t max_iters, bool until_time, int64_t *iters)
+{
+    int64_t it = 0;
+    for (;;) {
+        if (until_time && !(ctx->time <= ctx->total_time)) break;
+        if (max_iters > 0 && it >= max_iters) break;
+        if (ctx->need_trace) {
+            const int64_t n = ctx->p.nphotons * (int64_t)ctx->p.numproc;
+            RC(mc_pass(ctx, n, seed, (uint32_t)ctx->mc_passes, false));
+            unsigned long long nab = 0;
+            CK(cudaMemcpy(&nab, ctx->d_nabl, sizeof nab, cudaMemcpyDeviceToHost));
+            ctx->nabl_at_trace = (long long)nab;
+            ctx->need_trace = false;
+        }
+        int64_t k = ERR_EVERY - (it % ERR_EVERY);
+        if (max_iters > 0) k = std::min(k, max_iters - it);
+        if (until_time) {
+            int64_t m = 0;
+            for (double t = ctx->time; m < k && t <= ctx->total_time; ++m) t += ctx->cdt;
+            k = std::max<int64_t>(m, 1);
+        }
+        int32_t done = 0;
+        RC(cfg_heat(ctx, (int32_t)k, &done, true));
+        ctx->counter += done;
+        it += done;
+        if (it % ERR_EVERY == 0) RC(finish(ctx, "tam_run"));
+    }
+    if (iters) *iters = it;
+    return TAM_OK;
+}
+}  // namespace
+extern "C" {
+
 int tam_step_coupled(tam_ctx *ctx, int32_t n, uint64_t seed)
 {
     if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
     if (n < 0) return fail(ctx, TAM_E_INVALID, "n must be >= 0");
     CK(cudaSetDevice(ctx->device));
+    if (ctx->config && ctx->p.loops == 1) {
+        if (n > 0) RC(cfg_run(ctx, seed, n, false, nullptr));
+        return finish(ctx, "tam_step_coupled");
+    }
     for (int32_t i = 0; i < n; ++i) RC(outer_iteration(ctx, seed, i + 1 == n || (i + 1) % ERR_EVERY == 0));
     return TAM_OK;
 }
@@ -1746,6 +1802,10 @@ int tam_run(tam_ctx *ctx, uint64_t seed, int64_t max_iters, int64_t *iters)
 {
     if (!ctx) return fail(nullptr, TAM_E_INVALID, "null context");
     CK(cudaSetDevice(ctx->device));
+    if (ctx->config && ctx->p.loops == 1) {
+        RC(cfg_run(ctx, seed, max_iters, true, iters));
+        return finish(ctx, "tam_run");
+    }
     int64_t it = 0;
     while (ctx->time <= ctx->total_time) {
         if (max_iters > 0 && it >= max_iters) break;

@@ -169,7 +169,7 @@ def c5(scale=1.0, seed=5, packets=1_000_000_000, steps=100_000):
     p = api.default_params(nxg=n, nyg=n, nzg=n, xmax=L / 2, ymax=L / 2, zmax=L / 2, mode=1, precision=1,
                            nphotons=packets, pulse_type=1, power=10.0, energy_per_pixel=10.0 * 50.0,
                            repetition_rate_1=1.0, pulses_to_do=10, total_time=10.0, loops=1)
-    cfg = _config(mats, retrace_fraction=1e-9, retrace_check=0)
+    cfg = _config(mats, retrace_fraction=1e-9, retrace_check=64)
     return Workload("C5 vessels and inclusions", p, cfg, grid, packets, steps,
                     {"grid": (n, n, n), "cylinders": len(cyl), "spheres": len(sph)})
 
