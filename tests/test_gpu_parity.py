@@ -971,3 +971,34 @@ def test_coupled_config_loop_retrace_batched(tam):
     assert ma == mb >= 3, (ma, mb)
     assert abs(na - nb) <= 2 and na > 0
     assert np.abs(Ta - Tb).max() <= 1e-4
+
+
+@pytest.mark.parametrize("precision", [0, 1])
+def test_reference_loop_graph_replay_matches_launches(tam, precision):
+    # reference mode on the reference's own input (80^3, 125k packets per
+    # pass): outer iterations replayed from CUDA graphs in runs of 16 (MC pass,
+    # normalisation, heat step, damage and property update; per-iteration
+    # stream, normalisation, laserOn and clock from a device table) against
+    # every kernel launched: the same clock, counters and pulse state, and the
+    # same fields up to the order of the tally's atomic sums (1e-12 relative)
+    out = []
+    for graph in (1, 0):
+        p = tam.default_params(precision=precision)
+        with tam.Context(p) as ctx:
+            ctx.set_tuning("heat.graph", graph)
+            l0 = tam.kernel_launches()
+            ctx.step_coupled(96, seed=11)
+            launches = tam.kernel_launches() - l0
+            st = ctx.state()
+            out.append(({f: ctx.download(f) for f in (F.TAM_F_TEMP, F.TAM_F_JMEAN_GLOBAL, F.TAM_F_Q, F.TAM_F_TISSUE,
+                                                         F.TAM_F_RHOKAP)},
+                        (st.time, st.counter, st.pulses_done, st.laser_flag, st.mc_passes), launches,
+                        ctx.device_errors()))
+    (fa, sa, la, ea), (fb, sb, lb, eb) = out
+    assert ea == eb == 0
+    assert sa == sb and sa[1] == 96 and sa[4] == 96
+    assert la == lb  # the same kernels, counted whether replayed or launched
+    for f in fa:
+        np.testing.assert_allclose(fa[f], fb[f], rtol=1e-12, atol=1e-12 * max(np.abs(fb[f]).max(), 1e-300),
+                                   err_msg=str(f))
+    assert fa[F.TAM_F_JMEAN_GLOBAL].max() > 0 and fa[F.TAM_F_TEMP][1:-1, 1:-1, 1:-1].max() > 279.0

@@ -163,8 +163,11 @@ template <> struct RefOps<float> {
 // theirs.  Three divisions per voxel instead of six.  F = double: the parity
 // form; F = float: the FP32 form of reference mode.
 constexpr int REF_ZC = 8;
-template <typename F> __global__ void __launch_bounds__(256) ref_stencil_kernel(const RefHeatArgs a)
+template <typename F> __global__ void __launch_bounds__(256) ref_stencil_kernel(const RefHeatArgs a0)
 {
+    // the iteration's laserOn from device memory when replayed from a graph
+    RefHeatArgs a = a0;
+    if (a0.laser_dev) a.laserOn = *a0.laser_dev;
     using O = RefOps<F>;
     __shared__ F s_fy[8][32];
     const int tx = threadIdx.x, ty = threadIdx.y;
@@ -233,9 +236,10 @@ __device__ __forceinline__ void arrhenius_voxel(const RefArrheniusArgs &a, int64
     // time is loaded (the conditions are pure, so the order of the two tests
     // changes nothing): below 0.53 no threshold time is read at all
     double *t1 = a.thres + q, *t2 = a.thres + q + ni, *t3 = a.thres + q + 2 * ni;
-    if (ieee::ge_pos(om, B_0_53) && ieee::is_zero(*t1)) *t1 = a.time;
-    else if (ieee::ge_pos(om, B_1) && ieee::is_zero(*t2)) *t2 = a.time;
-    else if (ieee::ge_pos(om, B_1E4) && ieee::is_zero(*t3)) *t3 = a.time;
+    auto now = [&]() { return a.time_dev ? *a.time_dev : a.time; };  // replayed from a graph: this iteration's clock
+    if (ieee::ge_pos(om, B_0_53) && ieee::is_zero(*t1)) *t1 = now();
+    else if (ieee::ge_pos(om, B_1) && ieee::is_zero(*t2)) *t2 = now();
+    else if (ieee::ge_pos(om, B_1E4) && ieee::is_zero(*t3)) *t3 = now();
 }
 
 __global__ void ref_arrhenius_kernel(const RefArrheniusArgs a)

@@ -128,6 +128,12 @@ struct tam_ctx {
     tam::StepVals *d_sv = nullptr;           // the table
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // by the buffer pair the chunk reads first
     std::vector<unsigned char> gkey[2];      // what the graphs were captured with
+    // reference-mode outer iterations replayed from CUDA graphs: chunks of
+    // REF_GRAPH_ITERS iterations whose changing values come from a device table
+    bool ref_warm = false;                   // an iteration ran as ordinary launches
+    tam::RefIterVals *d_iv = nullptr;
+    cudaGraphExec_t rexec[4] = {nullptr, nullptr, nullptr, nullptr};  // by (temperature, rhokap) buffers read first
+    std::vector<unsigned char> rkey[4];
     int batch_staged = 2;            // batched steps: staged voxel pairs (2), staged voxels (1), cached loads (0)
     int batch_streams = 0;           // 1: batched steps as each instance's own steps on its stream, overlapped
     int batch_zchunk = 0;            // batched steps: z planes per work item (0: heat.zchunk, else the default)
@@ -1084,6 +1090,7 @@ int outer_iteration(tam_ctx *ctx, uint64_t seed, bool sync = true)
         if (ctx->laser_flag) RC(mc_pass(ctx, n, seed, (uint32_t)ctx->counter, false));
         RC(ref_heat(ctx, ctx->p.loops));
         RC(ref_damage_props(ctx, ctx->p.ablate_temp));
+        ctx->ref_warm = true;
     }
     ctx->counter += 1;
     if (!sync) {
@@ -1439,6 +1446,8 @@ int tam_destroy(tam_ctx *ctx)
     if (ctx->fslab) tam::fused_slab_destroy(ctx->fslab);
     for (cudaGraphExec_t &g : ctx->gexec)
         if (g) cudaGraphExecDestroy(g);
+    for (cudaGraphExec_t &g : ctx->rexec)
+        if (g) cudaGraphExecDestroy(g);
     if (ctx->cap_stream) cudaStreamDestroy(ctx->cap_stream);
     if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
@@ -1743,6 +1752,215 @@ int tam_update_props(tam_ctx *ctx, double ablate_temp)
 
 }  // extern "C"
 namespace {
+constexpr int REF_GRAPH_ITERS = 16;  // reference iterations per graph replay (even: the buffers come back)
+
+// Normalisation factor of a reference-mode MC pass of n packets at power pw
+// (src/mcpolar.f90:174), as mc_pass forms it.
+double ref_norm(const tam_ctx *ctx, int64_t n, double pw)
+{
+    const tam_params &p = ctx->p;
+    const double den = (double)n * (2. * p.xmax * 1.e-2 / p.nxg) * (2. * p.ymax * 1.e-2 / p.nyg) *
+                       (2. * p.zmax * 1.e-2 / p.nzg);
+    return n > 0 ? (pw / 81.0) / den : 0.0;
+}
+
+// Capture REF_GRAPH_ITERS reference iterations with the laser on (MC pass,
+// normalisation, heat step, damage and property update), iteration j reading
+// its stream, normalisation, laserOn and clock from d_iv[j].  The buffers
+// alternate as in the launched loop, starting from the context's current pair.
+bool ref_graph_capture(tam_ctx *ctx, uint64_t seed, int slot)
+{
+    if (!ctx->cap_stream && cudaStreamCreateWithFlags(&ctx->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    if (!ctx->d_iv && dalloc_t(ctx, &ctx->d_iv, REF_GRAPH_ITERS) != TAM_OK) return false;
+    if (ctx->rexec[slot]) {
+        cudaGraphExecDestroy(ctx->rexec[slot]);
+        ctx->rexec[slot] = nullptr;
+    }
+    cudaStream_t s = ctx->cap_stream;
+    if (cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return false;
+    }
+    const int64_t n = ctx->p.nphotons * (int64_t)ctx->p.numproc;
+    int tcur = ctx->tcur, rcur = ctx->rcur;
+    bool ok = true;
+    for (int j = 0; j < REF_GRAPH_ITERS && ok; ++j) {
+        const tam::RefIterVals *iv = ctx->d_iv + j;
+        // MC pass (src/mcpolar.f90:151-174): sourcephCO2 + tauint1, normalisation
+        tam::TransportArgs a{};
+        a.nx = ctx->nx;
+        a.ny = ctx->ny;
+        a.nz = ctx->nz;
+        a.xmax = ctx->p.xmax;
+        a.ymax = ctx->p.ymax;
+        a.zmax = ctx->p.zmax;
+        a.medium = tam::MED_RHOKAP;
+        a.rhokap = ctx->d_rk[rcur];
+        a.rhokap_n = ctx->p.n2;
+        a.n_ambient = ctx->p.n1;
+        a.source = tam::SRC_DISK;
+        a.source_radius = 250e-4 / 2.;
+        a.roulette_m = 1.0;
+        a.max_steps = (int64_t)1 << 40;
+        a.nudge = ctx->delta;
+        a.scat_min = ctx->scat_min;
+        a.uniform_id = -1;
+        a.seed = seed;
+        a.stream_dev = &iv->stream;
+        a.n = n;
+        a.jmean = ctx->d_jmean;
+        a.tally = ctx->d_tally;
+        a.work = ctx->d_work;
+        a.err = ctx->d_err;
+        ok = cudaMemsetAsync(ctx->d_jmean, 0, ctx->ni * sizeof(double), s) == cudaSuccess &&
+             cudaMemsetAsync(ctx->d_tally, 0, tam::N_TALLY * sizeof(double), s) == cudaSuccess &&
+             tam::launch_transport(a, ctx->fp64, ctx->sm_count, s) == cudaSuccess &&
+             tam::launch_scale_f64(ctx->d_jglob, ctx->d_jmean, 0.0, ctx->ni, false, s,
+                                   ctx->d_tally + tam::T_ABSORBED, &iv->f) == cudaSuccess;
+        // heat step (src/3dFD.f90:113-187)
+        tam::RefHeatArgs h{};
+        h.nx = ctx->nx;
+        h.ny = ctx->ny;
+        h.nz = ctx->nz;
+        h.idx2 = 1.0 / (ctx->dx * ctx->dx);
+        h.idy2 = 1.0 / (ctx->dy * ctx->dy);
+        h.idz2 = 1.0 / (ctx->dz * ctx->dz);
+        h.vvox = ctx->volumeVoxel;
+        h.mvox = ctx->massVoxel;
+        h.qvapor = ctx->QVapor;
+        h.kappa = ctx->d_kappa;
+        h.density = ctx->d_density;
+        h.heatcap = ctx->d_heatcap;
+        h.coeff = ctx->d_coeff;
+        h.J = ctx->d_jglob;
+        h.Q = ctx->d_Q;
+        h.err = ctx->d_err;
+        h.f32 = ctx->fp64 ? 0 : 1;
+        h.p32 = ctx->fp64 ? nullptr : ctx->d_p32;
+        h.nh = ctx->nh;
+        h.delt = ctx->delt;
+        h.laser_dev = &iv->laser_on;
+        h.t0 = ctx->d_T[tcur];
+        h.tn = ctx->d_T[1 - tcur];
+        h.s0 = ctx->fp64 ? nullptr : ctx->d_t32[tcur];
+        h.sn = ctx->fp64 ? nullptr : ctx->d_t32[1 - tcur];
+        ok = ok && tam::launch_ref_stencil(h, s) == cudaSuccess;
+        tcur = 1 - tcur;
+        // Arrhenius and setupThermalCoeff (src/3dFD.f90:312-466)
+        tam::RefArrheniusArgs d = arrhenius_args(ctx);
+        d.time_dev = &iv->time;
+        d.temp = ctx->d_T[tcur];
+        d.rhokap = ctx->d_rk[rcur];
+        tam::RefPropsArgs pr = props_args(ctx, ctx->p.ablate_temp);
+        pr.temp = ctx->d_T[tcur];
+        pr.rk_old = ctx->d_rk[rcur];
+        pr.rk_new = ctx->d_rk[1 - rcur];
+        pr.reuse = 1;
+        ok = ok && tam::launch_ref_damage_props(d, pr, s) == cudaSuccess;
+        rcur = 1 - rcur;
+    }
+    tam::count_launch(-4 * REF_GRAPH_ITERS);  // captured, not launched (transport, scale, stencil, damage/props)
+    cudaGraph_t g = nullptr;
+    const cudaError_t e = cudaStreamEndCapture(s, &g);
+    ok = ok && e == cudaSuccess && g;
+    if (ok) ok = cudaGraphInstantiate(&ctx->rexec[slot], g, 0) == cudaSuccess;
+    if (g) cudaGraphDestroy(g);
+    if (!ok) {
+        (void)cudaGetLastError();
+        ctx->rexec[slot] = nullptr;
+        ctx->err.clear();
+    }
+    return ok;
+}
+
+// Reference-mode driver loop (src/mcpolar.f90:148-186).  Runs of
+// REF_GRAPH_ITERS iterations with the laser on replay one CUDA graph, their
+// stream ids, normalisations, laserOn values and clocks computed ahead by the
+// host's own pulse machine (advanced exactly as the launched iterations
+// advance it) and copied to a device table before the replay; a run that
+// would cross the time limit, max_iters, an error-fold point (every
+// ERR_EVERY iterations) or a laser switch, or the first iteration of a
+// context, runs as ordinary launches.
+int ref_run(tam_ctx *ctx, uint64_t seed, int64_t max_iters, bool until_time, int64_t *iters)
+{
+    const int G = REF_GRAPH_ITERS;
+    const int64_t n = ctx->p.nphotons * (int64_t)ctx->p.numproc;
+    int64_t it = 0;
+    std::vector<unsigned char> key;
+    for (;;) {
+        if (until_time && !(ctx->time <= ctx->total_time)) break;
+        if (max_iters > 0 && it >= max_iters) break;
+        bool replayed = false;
+        if (ctx->use_graph && ctx->ref_warm && ctx->p.loops == 1 && (it % ERR_EVERY) + G <= ERR_EVERY &&
+            (max_iters <= 0 || it + G <= max_iters) && ctx->props_delt == ctx->delt && !(ctx->pulseLength < ctx->delt) &&
+            (ctx->fp64 || ctx->shadow_ok)) {
+            // run the host state ahead; roll it back if the chunk does not fit
+            const double t0 = ctx->time, pc0 = ctx->pulseCount, rc0 = ctx->repetitionCount, lo0 = ctx->laserOn;
+            const int lf0 = ctx->laser_flag, pf0 = ctx->pulseFlag, pd0 = ctx->pulsesDone, ll0 = ctx->loops_left;
+            tam::RefIterVals tab[REF_GRAPH_ITERS];
+            bool fits = true;
+            for (int j = 0; j < G && fits; ++j) {
+                if ((until_time && !(ctx->time <= ctx->total_time)) || !ctx->laser_flag) {
+                    fits = false;
+                    break;
+                }
+                tab[j].stream = (uint32_t)(ctx->counter + j);
+                tab[j].f = ref_norm(ctx, n, get_pwr(ctx));
+                ctx->loops_left = (int)(ctx->total_time / ((double)ctx->p.loops * ctx->delt)) - (ctx->counter + j);
+                tab[j].laser_on = ctx->laserOn;
+                pulse_update(ctx, ctx->delt);
+                tab[j].time = ctx->time;
+            }
+            const int slot = ctx->tcur * 2 + ctx->rcur;
+            if (fits) {
+                key.assign(sizeof(uint64_t) * 3 + sizeof(double) + 2 * sizeof(int), 0);
+                unsigned char *q = key.data();
+                const uint64_t kk[3] = {seed, (uint64_t)n, (uint64_t)ctx->scat_min};
+                std::memcpy(q, kk, sizeof kk);
+                std::memcpy(q + sizeof kk, &ctx->delt, sizeof(double));
+                const int ff[2] = {ctx->fp64 ? 1 : 0, ctx->stream == nullptr ? 0 : 1};
+                std::memcpy(q + sizeof kk + sizeof(double), ff, sizeof ff);
+                if (ctx->rexec[slot] == nullptr || ctx->rkey[slot] != key) {
+                    fits = ref_graph_capture(ctx, seed, slot);
+                    if (fits) ctx->rkey[slot] = key;
+                    else ctx->use_graph = false;
+                }
+            }
+            if (fits) {
+                CK(cudaMemcpyAsync(ctx->d_iv, tab, sizeof tab, cudaMemcpyHostToDevice, ctx->stream));  // pageable: copied now
+                CK(cudaGraphLaunch(ctx->rexec[slot], ctx->stream));
+                tam::count_launch(4 * G);
+                ctx->counter += G;
+                ctx->mc_passes += G;
+                ctx->last_n = n;
+                ctx->tally_stale = true;
+                it += G;
+                replayed = true;
+            } else {
+                ctx->time = t0;
+                ctx->pulseCount = pc0;
+                ctx->repetitionCount = rc0;
+                ctx->laserOn = lo0;
+                ctx->laser_flag = lf0;
+                ctx->pulseFlag = pf0;
+                ctx->pulsesDone = pd0;
+                ctx->loops_left = ll0;
+            }
+        }
+        if (!replayed) {
+            RC(outer_iteration(ctx, seed, (it + 1) % ERR_EVERY == 0));
+            ++it;
+        } else if (it % ERR_EVERY == 0) {
+            RC(finish(ctx, "tam_run"));
+        }
+    }
+    if (iters) *iters = it;
+    return TAM_OK;
+}
+
 // Config-mode driver loop (src/mcpolar.f90:148-186 with one heat step per
 // iteration): the iterations between two MC passes run as one heat-step call,
 // so its steps replay from CUDA graphs, in batches that end where the
@@ -1794,6 +2012,10 @@ int tam_step_coupled(tam_ctx *ctx, int32_t n, uint64_t seed)
         if (n > 0) RC(cfg_run(ctx, seed, n, false, nullptr));
         return finish(ctx, "tam_step_coupled");
     }
+    if (!ctx->config) {
+        if (n > 0) RC(ref_run(ctx, seed, n, false, nullptr));
+        return finish(ctx, "tam_step_coupled");
+    }
     for (int32_t i = 0; i < n; ++i) RC(outer_iteration(ctx, seed, i + 1 == n || (i + 1) % ERR_EVERY == 0));
     return TAM_OK;
 }
@@ -1804,6 +2026,10 @@ int tam_run(tam_ctx *ctx, uint64_t seed, int64_t max_iters, int64_t *iters)
     CK(cudaSetDevice(ctx->device));
     if (ctx->config && ctx->p.loops == 1) {
         RC(cfg_run(ctx, seed, max_iters, true, iters));
+        return finish(ctx, "tam_run");
+    }
+    if (!ctx->config) {
+        RC(ref_run(ctx, seed, max_iters, true, iters));
         return finish(ctx, "tam_run");
     }
     int64_t it = 0;

@@ -31,6 +31,16 @@ struct OptMat {
     double mua, mus, g, n;
 };
 
+// Values of one reference-mode outer iteration that change from iteration to
+// iteration, read by the kernels from device memory when an iteration is
+// replayed from a CUDA graph (the pointers below are then set).
+struct RefIterVals {
+    double f;          // normalisation of the iteration's MC pass, (P/81)/(N V)
+    double laser_on;   // laserOn of its heat step
+    double time;       // clock after its heat step (threshold time stamps)
+    uint32_t stream;   // Philox stream of its MC pass (the iteration counter)
+};
+
 // One transport pass (packets [p0, p0 + n)).
 // Per-launch constants of the transport kernel in the working precision,
 // computed once on the host by launch_transport (its IEEE double operations
@@ -61,6 +71,7 @@ struct TransportArgs {
     double roulette_w, roulette_m;
     uint64_t seed;
     uint32_t stream;
+    const uint32_t *stream_dev;       // non-null: the stream is read from here
     int64_t p0, n;
     int64_t max_steps;
     double nudge;                     // offset past a crossed face (reference delta), 0 in config mode
@@ -90,7 +101,7 @@ cudaError_t launch_flush_f32(double *acc, float *part, int nx, int ny, int bx0, 
 // out[q] = in[q] * f for q < n; in is then zeroed when zero_in is set.
 // out = in * f; with `sum`, also *sum += the total of in (the caller zeroes *sum)
 cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s,
-                             double *sum = nullptr);
+                             double *sum = nullptr, const double *f_dev = nullptr);
 cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s,
                                 double *sum = nullptr);
 
@@ -121,12 +132,14 @@ struct RefHeatArgs {
     const float *p32;                 // FP32 kappa, density, heatcap, coeff (4 x nh)
     const float *s0;                  // FP32 copy of t0
     float *sn;                        // FP32 copy of tn, written with it
+    const double *laser_dev;          // non-null: laserOn is read from here
 };
 cudaError_t launch_ref_stencil(const RefHeatArgs &a, cudaStream_t s);
 
 struct RefArrheniusArgs {
     int32_t nx, ny, nz;
     double delt, time;
+    const double *time_dev;           // non-null: the time stamp is read from here
     const double *temp, *rhokap;      // halo
     double *tissue, *thres;           // interior, interior x 3
 };

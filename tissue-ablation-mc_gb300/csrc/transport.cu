@@ -316,6 +316,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
     // away along the axis: tm advances by td * (1 - nudge / h)
     const Real knx = K.knx, kny = K.kny, knz = K.knz;
     const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
+    const uint32_t strm = a.stream_dev ? *a.stream_dev : a.stream;
     const unsigned lane = threadIdx.x & 31u;
     const Real wmin = K.wmin, rm = K.rm, inv_rm = K.inv_rm;
     const int NX = a.nx, NY = a.ny, NZ = a.nz, SY = a.nx, SZ = a.nx * a.ny;
@@ -369,7 +370,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     const uint64_t pid = (uint64_t)a.p0 + my;
                     plo = (uint32_t)pid;
                     phi32 = (uint32_t)(pid >> 32);
-                    const U4 r = philox4x32_10(0u, plo, phi32, a.stream, k0, k1);
+                    const U4 r = philox4x32_10(0u, plo, phi32, strm, k0, k1);
                     ev = 1;
                     const Real u0 = Uniform<Real>::from(r.x), u1 = Uniform<Real>::from(r.y);
                     const Real u2 = Uniform<Real>::from(r.z), u3 = Uniform<Real>::from(r.w);
@@ -541,7 +542,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                 if (!face) w *= MED == MED_RHOKAP ? (Real)0 : lut[mid].alb;
                 bool die = !face && !(w > (Real)0);
                 U4 r{0u, 0u, 0u, 0u};
-                if (!die) r = philox4x32_10(ev++, plo, phi32, a.stream, k0, k1);
+                if (!die) r = philox4x32_10(ev++, plo, phi32, strm, k0, k1);
                 if (face) {
                     const bool cx = fax == 0, cy = fax == 1;
                     const Real nc = cx ? nx : (cy ? ny : nz);
@@ -667,8 +668,10 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
 // `in` added to *sum: one FP64 atomic per block, so the grid is kept to a few
 // thousand blocks
 template <typename Out>
-__global__ void scale_kernel(Out *out, double *in, double f, int64_t n, int zero_in, double *sum)
+__global__ void scale_kernel(Out *out, double *in, double f, int64_t n, int zero_in, double *sum,
+                             const double *f_dev)
 {
+    if (f_dev) f = *f_dev;
     double acc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
         const double v = in[q];
@@ -815,11 +818,12 @@ static int scale_grid(int64_t n)
     return (int)(b > 0 ? b : 1);
 }
 
-cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s, double *sum)
+cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool zero_in, cudaStream_t s, double *sum,
+                             const double *f_dev)
 {
     if (n <= 0) return cudaSuccess;
     count_launch();
-    scale_kernel<double><<<scale_grid(n), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0, sum);
+    scale_kernel<double><<<scale_grid(n), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0, sum, f_dev);
     return cudaGetLastError();
 }
 
@@ -837,7 +841,7 @@ cudaError_t launch_scale_to_f32(float *out, double *in, double f, int64_t n, boo
 {
     if (n <= 0) return cudaSuccess;
     count_launch();
-    scale_kernel<float><<<scale_grid(n), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0, sum);
+    scale_kernel<float><<<scale_grid(n), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0, sum, nullptr);
     return cudaGetLastError();
 }
 
