@@ -315,6 +315,20 @@ int tam_batch_step_coupled(struct tam_ctx *const *ctxs, int32_t n, int32_t iters
  * same batched heat step whenever every context qualifies; MC passes and
  * re-trace decisions then happen at chunk boundaries. */
 int tam_batch_heat_steps(struct tam_ctx *const *ctxs, int32_t n, int32_t nsteps);
+/* One MC pass of every instance (tam_mc_pass of each, without the output
+ * copy): nphotons[i] packets (nphotons NULL: each context's nphotons x
+ * numproc), Philox key seeds[i] and stream streams[i] (streams NULL: each
+ * context's count of passes so far, as the coupled loop uses).  The passes of
+ * FP32 config-mode instances in a uniform medium on ctxs[0]'s device, with
+ * the FP64 tally, run together in launches of a batched transport kernel (up
+ * to 64 instances each; "batch.transport" 0 on ctxs[0] turns this off): its
+ * packets draw from each instance's own Philox stream, so every instance's
+ * tallies equal those of its own pass up to the order of the atomic sums.
+ * The other instances' passes run one by one.  Waits for every instance and
+ * checks its device error word.  tam_batch_step_coupled and tam_batch_run
+ * run their passes the same way. */
+int tam_batch_mc_pass(struct tam_ctx *const *ctxs, int32_t n, const int64_t *nphotons, const uint64_t *seeds,
+                      const uint32_t *streams);
 int tam_batch_run(struct tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, int64_t max_iters, int64_t *iters);
 
 /*

@@ -252,3 +252,116 @@ def test_batch_run_uneven_lengths_matches_single_runs(tam):
     finally:
         for c in ctxs:
             c.close()
+
+
+# ------------------------------------------------- batched MC transport --
+def _c4_like(tam, n, packets, edge_range, seed=4):
+    from tam_gb300 import workloads
+
+    return [w.context() for w in workloads.c4(n=n, seed=seed, packets=packets, steps=1, edge_range=edge_range)]
+
+
+def _single_pass(tam, ctx, n, seed, stream):
+    F = tam._abi
+    ctx.mc_pass(n, seed=seed, stream=stream)
+    return ctx.download(F.TAM_F_JMEAN), ctx.download(F.TAM_F_JMEAN_GLOBAL), ctx.tallies()
+
+
+EXACT_TALLIES = ("voxel_steps", "scatters", "missed", "overflow")
+
+
+def _check_same_pass(got, want):
+    (Jm, Jg, tl), (Jm0, Jg0, tl0) = got, want
+    assert Jm0.max() > 0
+    np.testing.assert_allclose(Jm, Jm0, rtol=1e-9, atol=1e-9 * Jm0.max())
+    np.testing.assert_allclose(Jg, Jg0, rtol=1e-6, atol=1e-7 * Jg0.max())
+    for k, v in tl0.items():
+        if k in EXACT_TALLIES:
+            assert tl[k] == v, k
+        else:
+            assert tl[k] == pytest.approx(v, rel=1e-9, abs=1e-12), k
+
+
+def test_batch_mc_pass_matches_single_passes(tam):
+    # uneven uniform-medium instances (edges 24..56, the batched form's
+    # per-instance optics) in one launch of the batched transport, plus a
+    # layered instance and an FP64 one, whose passes run alone: every
+    # instance's tally equals its own pass's on the same Philox streams up to
+    # the order of the FP64 atomic sums
+    F = tam._abi
+    N = 30000
+    seeds = [101, 102, 103, 104, 105, 106, 107]
+    streams = [3, 0, 7, 1, 2, 9, 4]
+
+    def make():
+        ctxs = _c4_like(tam, 5, N, (24, 56))
+        ctxs.append(_fp32_instance(tam, 37, 29, 23, True, 1.0))
+        p = tam.default_params(nxg=24, nyg=24, nzg=20, xmax=0.06, ymax=0.06, zmax=0.05, mode=1, precision=0,
+                               nphotons=N, pulse_type=1, power=1.0, energy_per_pixel=1e3, total_time=1.0, loops=1)
+        ctxs.append(tam.Context(p, tam.default_config(retrace_fraction=0.0, source_radius=0.03)))
+        return ctxs
+
+    want = []
+    for i, c in enumerate(make()):
+        with c:
+            want.append(_single_pass(tam, c, N, seeds[i], streams[i]))
+    ctxs = make()
+    try:
+        l0 = tam.kernel_launches()
+        tam.batch_mc_pass(ctxs, seeds, nphotons=[N] * len(ctxs), streams=streams)
+        # one batched transport for the five uniform instances, a transport
+        # each for the other two, and a normalisation per instance
+        assert tam.kernel_launches() - l0 == 1 + 2 + len(ctxs)
+        for c, w in zip(ctxs, want):
+            assert c.device_errors() == 0
+            assert c.state().mc_passes == 1
+            _check_same_pass((c.download(F.TAM_F_JMEAN), c.download(F.TAM_F_JMEAN_GLOBAL), c.tallies()), w)
+    finally:
+        for c in ctxs:
+            c.close()
+
+
+def test_batch_mc_pass_more_instances_than_one_launch(tam):
+    # 70 small instances: two launches of the batched transport (64 + 6), the
+    # instances' own streams (their pass counts) and per-instance packet counts
+    F = tam._abi
+    n = 70
+    packets = [2000 + 37 * i for i in range(n)]
+    seeds = [1000 + i for i in range(n)]
+    want = []
+    for i, c in enumerate(_c4_like(tam, n, 2000, (12, 20), seed=9)):
+        with c:
+            want.append(_single_pass(tam, c, packets[i], seeds[i], 0))
+    ctxs = _c4_like(tam, n, 2000, (12, 20), seed=9)
+    try:
+        l0 = tam.kernel_launches()
+        tam.batch_mc_pass(ctxs, seeds, nphotons=packets)
+        assert tam.kernel_launches() - l0 == 2 + n
+        for c, w in zip(ctxs, want):
+            assert c.device_errors() == 0
+            _check_same_pass((c.download(F.TAM_F_JMEAN), c.download(F.TAM_F_JMEAN_GLOBAL), c.tallies()), w)
+    finally:
+        for c in ctxs:
+            c.close()
+
+
+def test_batch_loop_transport_switch(tam):
+    # the batched coupled loop's passes through the batched transport and
+    # through one launch per instance ("batch.transport" 0) agree
+    F = tam._abi
+    seeds = [21, 22, 23, 24]
+    res = []
+    for on in (1, 0):
+        ctxs = _c4_like(tam, 4, 20000, (24, 40), seed=11)
+        try:
+            ctxs[0].set_tuning("batch.transport", on)
+            tam.batch_step_coupled(ctxs, 3, seeds)
+            res.append([(c.download(F.TAM_F_JMEAN), c.download(F.TAM_F_TEMP), c.state().mc_passes) for c in ctxs])
+            assert all(c.device_errors() == 0 for c in ctxs)
+        finally:
+            for c in ctxs:
+                c.close()
+    for (Ja, Ta, pa), (Jb, Tb, pb) in zip(*res):
+        assert pa == pb == 1
+        np.testing.assert_allclose(Ja, Jb, rtol=1e-9, atol=1e-9 * Jb.max())
+        assert np.abs(Ta - Tb).max() <= 1e-4

@@ -136,6 +136,7 @@ struct tam_ctx {
     std::vector<unsigned char> rkey[4];
     int batch_staged = 2;            // batched steps: staged voxel pairs (2), staged voxels (1), cached loads (0)
     int batch_streams = 0;           // 1: batched steps as each instance's own steps on its stream, overlapped
+    int batch_transport = 1;         // batched loops: the instances' uniform-medium passes in one launch
     int batch_zchunk = 0;            // batched steps: z planes per work item (0: heat.zchunk, else the default)
     // staged class-table step of this context alone (rows not aligned for TMA)
     tam::BatchInst *d_sinst = nullptr;
@@ -537,10 +538,12 @@ tam::FusedArgs fused_args(tam_ctx *ctx)
 // One MC pass.  sync: wait for it and read its tallies back (API calls);
 // the driver loops do not, so the host runs ahead of the device, and the
 // tallies are read back when asked for.
-int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, bool sync = true)
+// The arguments of one pass (t32: the pass deposits into the FP32 box
+// tally, which is allocated here when it first grows).
+int pass_args(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, tam::TransportArgs &a, bool &t32)
 {
     cudaStream_t s = ctx->stream;
-    tam::TransportArgs a{};
+    a = tam::TransportArgs{};
     a.nx = ctx->nx;
     a.ny = ctx->ny;
     a.nz = ctx->nz;
@@ -602,8 +605,7 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, bool sync =
     // FP32, flushed into the FP64 jmean after every chunk of packets, so each
     // voxel's FP32 partial sum stays short
     // (FP64 contexts use it only when asked, for checks on the same streams)
-    const bool t32 = ctx->config && (ctx->tally32 > 0 || (!ctx->fp64 && ctx->tally32 < 0 &&
-                                                          ctx->ni * 8 > ((int64_t)256 << 20)));
+    t32 = ctx->config && (ctx->tally32 > 0 || (!ctx->fp64 && ctx->tally32 < 0 && ctx->ni * 8 > ((int64_t)256 << 20)));
     if (t32) {
         // the box: the whole grid if it fits the cap, else a block centred on
         // the beam axis (the source is centred on the top face) reaching down
@@ -637,6 +639,40 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, bool sync =
         }
     }
     a.jmean32 = t32 ? ctx->d_j32 : nullptr;
+    return TAM_OK;
+}
+
+// Bookkeeping and normalisation (src/mcpolar.f90:174) after a pass's
+// launches on stream s.
+int pass_normalise(tam_ctx *ctx, int64_t n, cudaStream_t s)
+{
+    ctx->have_mc_time = true;
+    ctx->last_n = n;
+    ctx->mc_passes += 1;
+    if (ctx->config) {
+        const double f = n > 0 ? 1.0 / ((double)n * ctx->volumeVoxel) : 0.0;
+        // the total absorbed weight (zeroed with the tallies) is summed in the same pass
+        double *absorbed = ctx->d_tally + tam::T_ABSORBED;
+        if (ctx->fp64) CK(tam::launch_scale_f64((double *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s, absorbed));
+        else CK(tam::launch_scale_to_f32((float *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s, absorbed));
+    } else {
+        const tam_params &p = ctx->p;
+        const double pw = get_pwr(ctx);
+        const double den = (double)n * (2. * p.xmax * 1.e-2 / p.nxg) * (2. * p.ymax * 1.e-2 / p.nyg) *
+                           (2. * p.zmax * 1.e-2 / p.nzg);
+        const double f = n > 0 ? (pw / 81.0) / den : 0.0;
+        CK(tam::launch_scale_f64(ctx->d_jglob, ctx->d_jmean, f, ctx->ni, false, s, ctx->d_tally + tam::T_ABSORBED));
+    }
+    ctx->tally_stale = true;
+    return TAM_OK;
+}
+
+int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, bool sync = true)
+{
+    cudaStream_t s = ctx->stream;
+    tam::TransportArgs a;
+    bool t32 = false;
+    RC(pass_args(ctx, n, seed, stream, a, t32));
     CK(cudaMemsetAsync(ctx->d_jmean, 0, ctx->ni * sizeof(double), s));
     CK(cudaMemsetAsync(ctx->d_tally, 0, tam::N_TALLY * sizeof(double), s));
     CK(cudaEventRecord(ctx->ev[0], s));
@@ -653,26 +689,8 @@ int mc_pass(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, bool sync =
         CK(tam::launch_transport(a, ctx->fp64, ctx->sm_count, s));
     }
     CK(cudaEventRecord(ctx->ev[1], s));
-    ctx->have_mc_time = true;
-    ctx->last_n = n;
-    ctx->mc_passes += 1;
-    // normalisation (src/mcpolar.f90:174)
-    if (ctx->config) {
-        const double f = n > 0 ? 1.0 / ((double)n * ctx->volumeVoxel) : 0.0;
-        // the total absorbed weight (zeroed with the tallies above) is summed in the same pass
-        double *absorbed = ctx->d_tally + tam::T_ABSORBED;
-        if (ctx->fp64) CK(tam::launch_scale_f64((double *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s, absorbed));
-        else CK(tam::launch_scale_to_f32((float *)ctx->d_J, ctx->d_jmean, f, ctx->ni, false, s, absorbed));
-    } else {
-        const tam_params &p = ctx->p;
-        const double pw = get_pwr(ctx);
-        const double den = (double)n * (2. * p.xmax * 1.e-2 / p.nxg) * (2. * p.ymax * 1.e-2 / p.nyg) *
-                           (2. * p.zmax * 1.e-2 / p.nzg);
-        const double f = n > 0 ? (pw / 81.0) / den : 0.0;
-        CK(tam::launch_scale_f64(ctx->d_jglob, ctx->d_jmean, f, ctx->ni, false, s, ctx->d_tally + tam::T_ABSORBED));
-    }
+    RC(pass_normalise(ctx, n, s));
     if (!sync) {
-        ctx->tally_stale = true;
         CK(cudaGetLastError());
         return TAM_OK;
     }
@@ -2098,12 +2116,88 @@ bool batchable(tam_ctx *const *ctxs, int32_t n)
     return true;
 }
 
+// Device copy of the batched transport's instance table and its packet counter.
+struct TrTable {
+    tam::BatchTrInst *d_tr = nullptr;
+    unsigned long long *d_work = nullptr;
+    ~TrTable()
+    {
+        cudaFree(d_tr);
+        cudaFree(d_work);
+    }
+};
+
+// One MC pass of every instance i with sel[i] set: np[i] packets, Philox key
+// seeds[i], stream streams[i].  Instances in a uniform medium with the FP64
+// tally (FP32 config mode on the first instance's device) share launches of
+// the batched transport, up to MAX_BATCH_TR per launch, on the first
+// instance's stream, which is waited for; every other pass runs alone on its
+// instance's stream and is not waited for.  Tallies are read back on demand.
+int multi_pass(TrTable &T, tam_ctx *const *ctxs, int32_t n, const std::vector<int> &sel,
+               const std::vector<int64_t> &np, const uint64_t *seeds, const std::vector<uint32_t> &streams)
+{
+    tam_ctx *const ctx = ctxs[0];  // CUDA errors of the batched launches are reported on the first instance
+    cudaStream_t s = ctx->stream;
+    std::vector<int32_t> grouped;
+    std::vector<tam::BatchTrInst> tab;
+    int64_t total = 0;
+    auto flush = [&]() -> int {
+        if (grouped.size() == 1) {
+            RC(mc_pass(ctxs[grouped[0]], np[grouped[0]], seeds[grouped[0]], streams[grouped[0]], false));
+        } else if (!grouped.empty()) {
+            if (!T.d_tr) {
+                CK(cudaMalloc(&T.d_tr, sizeof(tam::BatchTrInst) * tam::MAX_BATCH_TR));
+                CK(cudaMalloc(&T.d_work, sizeof(unsigned long long)));
+            }
+            for (int32_t i : grouped) {
+                tam_ctx *c = ctxs[i];
+                if (c->stream != s) CK(cudaStreamSynchronize(c->stream));
+                CK(cudaMemsetAsync(c->d_jmean, 0, c->ni * sizeof(double), s));
+                CK(cudaMemsetAsync(c->d_tally, 0, tam::N_TALLY * sizeof(double), s));
+            }
+            CK(cudaMemcpyAsync(T.d_tr, tab.data(), sizeof(tam::BatchTrInst) * tab.size(), cudaMemcpyHostToDevice, s));
+            for (int32_t i : grouped) CK(cudaEventRecord(ctxs[i]->ev[0], s));
+            CK(tam::launch_batch_transport(T.d_tr, (int)tab.size(), total, T.d_work, ctx->scat_min, ctx->sm_count, s));
+            for (int32_t i : grouped) CK(cudaEventRecord(ctxs[i]->ev[1], s));
+            for (size_t q = 0; q < grouped.size(); ++q) RC(pass_normalise(ctxs[grouped[q]], tab[q].count, s));
+            CK(cudaStreamSynchronize(s));
+        }
+        grouped.clear();
+        tab.clear();
+        total = 0;
+        return TAM_OK;
+    };
+    for (int32_t i = 0; i < n; ++i) {
+        if (!sel[i]) continue;
+        tam_ctx *c = ctxs[i];
+        if (ctx->batch_transport && np[i] > 0 && c->config && !c->fp64 && c->device == ctx->device) {
+            tam::TransportArgs a;
+            bool t32 = false;
+            RC(pass_args(c, np[i], seeds[i], streams[i], a, t32));
+            if (a.uniform_id >= 0 && !t32) {
+                tam::BatchTrInst b;
+                tam::fill_batch_inst(a, b);
+                b.first = total;
+                b.err = c->d_err;
+                total += np[i];
+                tab.push_back(b);
+                grouped.push_back(i);
+                if ((int)tab.size() == tam::MAX_BATCH_TR) RC(flush());
+                continue;
+            }
+        }
+        RC(mc_pass(c, np[i], seeds[i], streams[i], false));
+    }
+    return flush();
+}
+
 struct DevBatch {
     tam::BatchInst *d_inst = nullptr;
     int *d_prefix = nullptr;
     tam::BatchStep *d_steps = nullptr;
     tam::BatchSync *d_sync = nullptr;
     unsigned *d_err = nullptr;
+    TrTable tr;  // the batched transport's instance table
     std::vector<tam::BatchInst> inst;
     std::vector<int> prefix;
     std::vector<tam::BatchStep> steps;
@@ -2193,18 +2287,22 @@ int batch_chunk(tam_ctx *const *ctxs, int32_t n)
     return std::max(K, 1);
 }
 
-// MC passes of the instances that need one, each on its own stream so that
-// the passes (and their tails of long-lived packets) overlap.
-int batch_traces(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, const std::vector<int> &active)
+// MC passes of the instances that need one, each on the stream that
+// counts its passes (the batched transport where the instances qualify).
+int batch_traces(DevBatch &B, tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, const std::vector<int> &active)
 {
     std::vector<unsigned long long> nab(n, 0);
     std::vector<int> traced(n, 0);
+    std::vector<int64_t> np(n, 0);
+    std::vector<uint32_t> streams(n, 0);
     for (int32_t i = 0; i < n; ++i) {
         tam_ctx *c = ctxs[i];
         if (!active[i] || !c->need_trace) continue;
-        RC(mc_pass(c, c->p.nphotons * (int64_t)c->p.numproc, seeds[i], (uint32_t)c->mc_passes, false));
         traced[i] = 1;
+        np[i] = c->p.nphotons * (int64_t)c->p.numproc;
+        streams[i] = (uint32_t)c->mc_passes;
     }
+    RC(multi_pass(B.tr, ctxs, n, traced, np, seeds, streams));
     for (int32_t i = 0; i < n; ++i) {
         if (!traced[i]) continue;
         tam_ctx *const ctx = ctxs[i];
@@ -2217,6 +2315,31 @@ int batch_traces(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, const s
 }
 }  // namespace
 extern "C" {
+
+int tam_batch_mc_pass(tam_ctx *const *ctxs, int32_t n, const int64_t *nphotons, const uint64_t *seeds,
+                      const uint32_t *streams)
+{
+    if (n < 1 || !ctxs || !seeds) return fail(nullptr, TAM_E_INVALID, "bad batch arguments");
+    for (int32_t i = 0; i < n; ++i) {
+        if (!ctxs[i]) return fail(nullptr, TAM_E_INVALID, "null context in batch");
+        for (int32_t j = 0; j < i; ++j)
+            if (ctxs[j] == ctxs[i]) return fail(nullptr, TAM_E_INVALID, "context listed twice in batch");
+        if (nphotons && nphotons[i] < 0) return fail(ctxs[i], TAM_E_INVALID, "nphotons must be >= 0");
+    }
+    tam_ctx *const ctx = ctxs[0];
+    CK(cudaSetDevice(ctx->device));
+    std::vector<int> sel(n, 1);
+    std::vector<int64_t> np(n);
+    std::vector<uint32_t> st(n);
+    for (int32_t i = 0; i < n; ++i) {
+        np[i] = nphotons ? nphotons[i] : ctxs[i]->p.nphotons * (int64_t)ctxs[i]->p.numproc;
+        st[i] = streams ? streams[i] : (uint32_t)ctxs[i]->mc_passes;
+    }
+    TrTable T;
+    RC(multi_pass(T, ctxs, n, sel, np, seeds, st));
+    for (int32_t i = 0; i < n; ++i) RC(finish(ctxs[i], "tam_batch_mc_pass"));
+    return TAM_OK;
+}
 
 int tam_batch_heat_steps(tam_ctx *const *ctxs, int32_t n, int32_t nsteps)
 {
@@ -2286,7 +2409,7 @@ int batch_loop_device(tam_ctx *const *ctxs, int32_t n, const uint64_t *seeds, Mo
             any = true;
         }
         if (!any) break;
-        RC(batch_traces(ctxs, n, seeds, act));
+        RC(batch_traces(B, ctxs, n, seeds, act));
         // steps of this chunk: the instance's current iteration, then further
         // iterations while its loop condition holds (checked step by step)
         int k = 0;
@@ -2495,6 +2618,8 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
         ctx->batch_staged = (int)value;
     } else if (k == "batch.streams") {
         ctx->batch_streams = value != 0;
+    } else if (k == "batch.transport") {
+        ctx->batch_transport = value != 0;
     } else if (k == "heat.zchunk") {
         if (value < 0 || value > ctx->nz) return fail(ctx, TAM_E_INVALID, "heat.zchunk must be in 0..nz");
         ctx->zchunk = (int)value;

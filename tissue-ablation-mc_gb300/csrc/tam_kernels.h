@@ -89,6 +89,33 @@ struct TransportArgs {
     TrConst<float> cf;
 };
 
+// One instance of a batched FP32 transport pass (config mode, a uniform
+// medium, the FP64 tally): its grid, beam and material, its Philox key and
+// stream, and its packets' place in the batch's concatenated packet range.
+struct BatchTrInst {
+    int32_t nx, ny, nz;
+    int32_t source, fresnel, roulette;
+    float hx, hy, hz, w2x, w2y, xmax, ymax, src_r, namb;
+    float wmin, rm, inv_rm;
+    float mut, mua, alb, g, g2, n;    // the instance's material
+    uint64_t seed;
+    uint32_t stream, max_steps;
+    int64_t first, count;             // its packets are [first, first + count) of the batch
+    double *jmean;                    // interior, packet units
+    double *tally;                    // N_TALLY doubles
+    unsigned *err;                    // the instance's device error word
+};
+constexpr int MAX_BATCH_TR = 64;      // instances per batched launch
+// An instance's entry from the arguments of its own FP32 uniform-medium pass
+// (the batch's `first` is left 0 for the caller to set).
+void fill_batch_inst(const TransportArgs &a, BatchTrInst &b);
+// One launch for up to MAX_BATCH_TR instances (insts: a device copy of the
+// table): every packet sees the streams and the arithmetic of its instance's
+// own single pass (transport_kernel<float, uniform>), so the tallies agree up
+// to the order of their atomic sums.
+cudaError_t launch_batch_transport(const BatchTrInst *insts, int n, int64_t total, unsigned long long *work,
+                                   int scat_min, int sm_count, cudaStream_t s);
+
 // Launch the transport kernel in FP32 (fp64 == false) or FP64.
 cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cudaStream_t s);
 

@@ -132,6 +132,8 @@ SIGNATURES = [
     ("tam_batch_run", C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(C.c_uint64), C.c_int64,
                                 C.POINTER(C.c_int64)]),
     ("tam_batch_heat_steps", C.c_int, [C.POINTER(_P), C.c_int32, C.c_int32]),
+    ("tam_batch_mc_pass", C.c_int, [C.POINTER(_P), C.c_int32, C.POINTER(C.c_int64), C.POINTER(C.c_uint64),
+                                    C.POINTER(C.c_uint32)]),
     ("tam_batch_autotune", C.c_int, [C.POINTER(_P), C.c_int32, C.c_int32, C.POINTER(C.c_int64), C.c_int32]),
     ("tam_autotune", C.c_int, [_P, C.c_int64, C.c_int32, C.POINTER(C.c_int64), C.c_int32]),
     ("tam_save_state", C.c_int, [_P, C.c_char_p]),

@@ -222,6 +222,19 @@ def batch_run(contexts, seeds, max_iters: int = 0):
     return list(it)
 
 
+def batch_mc_pass(contexts, seeds, nphotons=None, streams=None) -> None:
+    """One MC pass of every context (tam_batch_mc_pass): the FP32 uniform-medium
+    instances' passes in shared launches of the batched transport, each packet
+    on its instance's own Philox stream.  nphotons / streams: one per context,
+    or None for each context's nphotons x numproc / its count of passes."""
+    n, hs, sd = _batch_args(contexts, seeds)
+    if (nphotons is not None and len(nphotons) != n) or (streams is not None and len(streams) != n):
+        raise ValueError("one value per context")
+    np_ = None if nphotons is None else (C.c_int64 * n)(*[int(x) for x in nphotons])
+    st = None if streams is None else (C.c_uint32 * n)(*[int(x) for x in streams])
+    check(lib().tam_batch_mc_pass(hs, n, np_, sd, st))
+
+
 def batch_heat_steps(contexts, nsteps: int) -> None:
     """`nsteps` FP32 heat steps of every context in persistent batched launches."""
     n = len(contexts)

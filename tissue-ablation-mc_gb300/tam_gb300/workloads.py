@@ -176,17 +176,27 @@ def c5(scale=1.0, seed=5, packets=1_000_000_000, steps=100_000):
 
 # ------------------------------------------------------------ command line --
 def _run_batch(a) -> None:
-    """Configuration 4 at any instance count: one MC pass per instance, warm-up
-    batched heat steps, then `steps` batched steps timed on the host clock
-    (each batched call returns after the device has finished)."""
+    """Configuration 4 at any instance count: one MC pass per instance (all of
+    them through tam_batch_mc_pass, timed), warm-up batched heat steps, then
+    `steps` batched steps, each part timed on the host clock (each batched call
+    returns after the device has finished)."""
     import time
 
     ws = c4(n=a.instances, packets=a.packets, steps=a.warm + a.steps)
     ctxs = [w.context() for w in ws]
     try:
         nvox = sum(c.nx * c.ny * c.nz for c in ctxs)
-        for c in ctxs:
-            c.mc_pass(a.packets, seed=1)
+        n = len(ctxs)
+        forms = [1, 0] if a.compare_mc else [1]
+        for on in forms:
+            # the instances' MC passes: the batched transport (1) or one launch each (0)
+            ctxs[0].set_tuning("batch.transport", on)
+            t0 = time.perf_counter()
+            api.batch_mc_pass(ctxs, [1] * n, nphotons=[a.packets] * n, streams=[0] * n)
+            dt = time.perf_counter() - t0
+            print(f"C4 MC ({'batched transport' if on else 'one launch per instance'}): {n} passes of {a.packets} "
+                  f"packets in {dt:.3f} s = {n * a.packets / dt:.3e} photons/s", flush=True)
+        ctxs[0].set_tuning("batch.transport", 1)
         if a.autotune:
             print("batch autotune:", api.batch_autotune(ctxs, steps=20), flush=True)
         if a.warm:
@@ -249,6 +259,7 @@ def parser():
     b.add_argument("--warm", type=int, default=200, help="untimed batched steps first")
     b.add_argument("--steps", type=int, default=200, help="timed batched steps")
     b.add_argument("--autotune", action="store_true")
+    b.add_argument("--compare-mc", action="store_true", help="also time the passes with one launch per instance")
     v = sub.add_parser("vessels", help="configuration 5: MC transport on the vessel grid")
     v.add_argument("--scale", type=float, default=1.0, help="grid edge = 512 * scale")
     v.add_argument("--packets", type=int, default=10_000_000)
