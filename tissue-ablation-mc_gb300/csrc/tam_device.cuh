@@ -61,7 +61,13 @@ template <> struct Uniform<double> {
 // u lies on a 2^-23 grid strictly inside (0,1), the largest value 1 - 2^-24.
 // (24 bits would round k + 0.5 to even above 2^23 and could give u = 1.)
 template <> struct Uniform<float> {
-    __device__ __forceinline__ static float from(uint32_t x) { return ((float)(x >> 9) + 0.5f) * 0x1p-23f; }
+    // (k + 1/2) 2^-23 for k = x >> 9, exactly: the float 1 + k 2^-23 built
+    // from its bits, minus 1 - 2^-24 (an exact difference), in place of an
+    // integer-to-float conversion
+    __device__ __forceinline__ static float from(uint32_t x)
+    {
+        return __uint_as_float(0x3f800000u | (x >> 9)) - 0x1.fffffep-1f;
+    }
 };
 
 // ------------------------------------------- exact FP64 helpers (no FMA) --

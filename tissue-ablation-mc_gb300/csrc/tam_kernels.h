@@ -98,6 +98,7 @@ struct BatchTrInst {
     float hx, hy, hz, w2x, w2y, xmax, ymax, src_r, namb;
     float wmin, rm, inv_rm;
     float mut, mua, alb, g, g2, n;    // the instance's material
+    float inv_mut;                    // 1 / mut (a flight's distance is its optical depth times this)
     uint64_t seed;
     uint32_t stream, max_steps;
     int64_t first, count;             // its packets are [first, first + count) of the batch

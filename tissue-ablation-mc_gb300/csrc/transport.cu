@@ -44,7 +44,7 @@ __device__ __forceinline__ void deposit(const TransportArgs &a, int cidx, int ix
             return;
         }
     }
-    atomicAdd(a.jmean + cidx, (double)dep);
+    atomicAdd(a.jmean + cidx, to_tally(dep));
 }
 
 // Optical properties of the current cell: extinction and absorption for the
@@ -609,6 +609,7 @@ void fill_batch_inst(const TransportArgs &args, BatchTrInst &b)
     b.g = (float)o.g;
     b.g2 = (float)(o.g * o.g);
     b.n = (float)o.n;
+    b.inv_mut = 1.0f / b.mut;  // IEEE single division: the bits of the single pass's 1 / mut
     b.seed = a.seed;
     b.stream = a.stream;
     b.max_steps = a.max_steps > 0xfffffff0ll ? 0xfffffff0u : (uint32_t)a.max_steps;

@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(BTPB, 4)
                             w = 1.f - rsp;
                         }
                         // the flight by distance: tau / mut once per flight
-                        tau = M<float>::neglog(u3) * (1.f / I.mut);
+                        tau = M<float>::neglog(u3) * I.inv_mut;
                         nx = sint * cp;
                         ny = sint * sp;
                         nz = -1.f;
@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(BTPB, 4)
         auto vstep = [&]() {
             if (mode != M_FLY) return;
             if (++nsteps > s_in[inst].max_steps) {
-                if (dep != 0.f) atomicAdd(s_in[inst].jmean + cidx, (double)dep);
+                if (dep != 0.f) atomicAdd(s_in[inst].jmean + cidx, to_tally(dep));
                 dep = 0.f;
                 atomicAdd(s_in[inst].tally + T_OVERFLOW, 1.0);
                 atomicOr(s_in[inst].err, (unsigned)DEVERR_STEP_CAP);
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(BTPB, 4)
             const int sg = cx ? sgx : (cy ? sgy : sgz);
             const int j = (cx ? ix : (cy ? iy : iz)) + sg;
             const int N = cx ? NX : (cy ? NY : NZ);
-            atomicAdd(s_in[inst].jmean + cidx, (double)dep);
+            atomicAdd(s_in[inst].jmean + cidx, to_tally(dep));
             dep = 0.f;
             if ((unsigned)j < (unsigned)N) {
                 ix = cx ? j : ix;
@@ -279,12 +279,12 @@ __global__ void __launch_bounds__(BTPB, 4)
                                 die = true;
                             }
                         }
-                        tau = M<float>::neglog(Uniform<float>::from(r.w)) * (1.f / I.mut);
+                        tau = M<float>::neglog(Uniform<float>::from(r.w)) * I.inv_mut;
                     }
                     if (!die) mode = M_FLY;
                 }
                 if (die) {
-                    if (dep != 0.f) atomicAdd(I.jmean + cidx, (double)dep);
+                    if (dep != 0.f) atomicAdd(I.jmean + cidx, to_tally(dep));
                     dep = 0.f;
                     retire();
                 }
