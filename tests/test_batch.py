@@ -85,11 +85,12 @@ def _fp32_instance(tam, nx, ny, nz, layered, power):
 SHAPES = [(37, 29, 23, True, 1.0), (48, 40, 36, False, 2.0), (64, 20, 18, True, 3.0)]
 
 
-@pytest.mark.parametrize("streams", [0, 1])
-def test_batch_heat_steps_matches_single_contexts(tam, streams):
-    # streams 0: the batched cooperative kernel; 1: each instance's own
-    # single-context steps on its stream, issued round-robin (bit-identical
-    # to the single runs, so held to the same bound here)
+@pytest.mark.parametrize("streams,staged", [(0, 2), (1, 2), (0, 3)])
+def test_batch_heat_steps_matches_single_contexts(tam, streams, staged):
+    # streams 0: the batched cooperative kernel (staged 2: 4-byte cp.async
+    # copies; 3: the slab form); 1: each instance's own single-context steps
+    # on its stream, issued round-robin (bit-identical to the single runs, so
+    # held to the same bound here)
     F = tam._abi
     want = []
     for shp in SHAPES:
@@ -99,6 +100,7 @@ def test_batch_heat_steps_matches_single_contexts(tam, streams):
     ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
     try:
         ctxs[0].set_tuning("batch.streams", streams)
+        ctxs[0].set_tuning("batch.staged", staged)
         tam.batch_heat_steps(ctxs, 300)
         if streams:
             for ctx, (T, _, _) in zip(ctxs, want):
@@ -171,13 +173,14 @@ def test_batch_device_path_with_mc_passes(tam):
 
 @pytest.mark.parametrize("zchunk", [0, 1, 7])
 def test_batch_staged_matches_cached_loads(tam, zchunk):
-    # the three forms of the batched step (neighbours by cached global loads;
+    # the four forms of the batched step (neighbours by cached global loads;
     # planes staged in shared memory by cp.async, one voxel or a pair of
-    # voxels per thread) on odd, layered and uniform instances, with z-chunks
-    # of one plane, a ragged last chunk and the default
+    # voxels per thread; the slab form) on odd, layered and uniform
+    # instances, with z-chunks of one plane, a ragged last chunk and the
+    # default
     F = tam._abi
     res = []
-    for staged in (0, 1, 2):
+    for staged in (0, 1, 2, 3):
         ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
         try:
             for c in ctxs:
@@ -206,7 +209,8 @@ def test_batch_autotune_restores_state(tam):
         tam.batch_heat_steps(ctxs, 5)
         before = [(c.download(F.TAM_F_TEMP), c.download(F.TAM_F_TISSUE), c.state().time) for c in ctxs]
         chosen = tam.batch_autotune(ctxs, steps=8)
-        assert chosen["batch.staged"] in (1, 2) and chosen["batch.zchunk"] in (8, 16, 32, 64)
+        assert (chosen["batch.staged"], chosen["batch.zchunk"]) in [(3, 4), (3, 6), (3, 8), (2, 8), (2, 16), (2, 32),
+                                                                    (2, 64), (1, 16), (1, 32)]
         assert chosen["batch.streams"] in (0, 1)
         for c, (T, om, t) in zip(ctxs, before):
             np.testing.assert_array_equal(c.download(F.TAM_F_TEMP), T)
@@ -365,3 +369,64 @@ def test_batch_loop_transport_switch(tam):
         assert pa == pb == 1
         np.testing.assert_allclose(Ja, Jb, rtol=1e-9, atol=1e-9 * Jb.max())
         assert np.abs(Ta - Tb).max() <= 1e-4
+
+
+# ------------------------------------------- slab form through the rare paths --
+HOT = [(45, 24, 20, True), (37, 29, 21, False), (64, 20, 18, False)]
+
+
+def _hot_ctx(tam, nx, ny, nz, layered, precision):
+    # three thermal classes (air, tissue, a second tissue), random sources
+    # plus a hot spot at the convective top face that boils and ablates
+    mats = [(0.026, 1.2, 1005.0), (0.56, 1070.0, 3400.0), (0.21, 911.0, 2348.0)]
+    d = 5e-5  # voxel spacing, m
+    alpha = max(k / (r * c) for k, r, c in mats[1:])
+    half = 0.0025 * nx  # cm
+    p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half * ny / nx, zmax=half * nz / nx, mode=1,
+                           precision=precision, pulse_type=1, power=1.0, energy_per_pixel=1e6, total_time=10.0)
+    c = tam.default_config(nmat=3, dt=0.9 / (2 * alpha * 3 / d ** 2))
+    for i, (k, rho, cp) in enumerate(mats):
+        tam.set_material(c, i, 0.3, 10.0, 0.9, 1.4, k, rho, cp)
+    ctx = tam.Context(p, c)
+    grid = np.ones((nx, ny, nz), dtype=np.uint8, order="F")
+    if layered:
+        grid[:, :, :8] = 2
+        grid[5:15, 3:12, 10:16] = 2
+    ctx.upload(tam._abi.TAM_F_MATERIAL, grid)
+    rng = np.random.default_rng(nx)
+    J = np.asfortranarray(rng.uniform(0, 1, (nx, ny, nz)) ** 2 * 5e8)
+    J[nx // 2 - 2:nx // 2 + 2, 10:14, nz - 4:] = 5e10
+    ctx.upload(tam._abi.TAM_F_JMEAN_GLOBAL, J)
+    return ctx
+
+
+@pytest.mark.parametrize("which", ["mixed", "uniform"])
+def test_batch_slab_form_boils_and_ablates_like_fp64(tam, which):
+    # the slab form of the batched step (rows of 45, 37 and 64 voxels: odd
+    # rows leave a half pair at the x+ face) through boiling and ablation,
+    # against each instance's own FP64 steps: the same ablated voxels, 1e-3 K
+    # away from the boiling threshold; "uniform" runs the batch's
+    # one-class kernel, "mixed" the class-table one
+    F = tam._abi
+    shapes = HOT if which == "mixed" else [h for h in HOT if not h[3]]
+    want = []
+    for shp in shapes:
+        with _hot_ctx(tam, *shp, 0) as ctx:
+            T = ctx.heat_steps(300, want=True)
+            want.append((T, ctx.download(F.TAM_F_TISSUE), ctx.download(F.TAM_F_Q), ctx.download(F.TAM_F_MATERIAL)))
+    ctxs = [_hot_ctx(tam, *shp, 1) for shp in shapes]
+    try:
+        ctxs[0].set_tuning("batch.staged", 3)
+        tam.batch_heat_steps(ctxs, 300)
+        for ctx, (T, om, Q, mat) in zip(ctxs, want):
+            assert ctx.device_errors() == 0
+            # the latent-heat branch ran and the hot spot ablated
+            assert (Q > 0).any() and (mat == 0).any()
+            np.testing.assert_array_equal(ctx.download(F.TAM_F_MATERIAL), mat)
+            got = ctx.download(F.TAM_F_TEMP)
+            away = np.abs(T - 373.15) > 0.05  # voxels straddling the threshold enter the clamp a step apart
+            assert np.abs(got - T)[away].max() <= 1e-3
+            assert np.abs(ctx.download(F.TAM_F_TISSUE) - om).max() <= 1e-3 * max(om.max(), 1e-30)
+    finally:
+        for c in ctxs:
+            c.close()

@@ -1,6 +1,6 @@
 """The bit-pattern comparisons and scalings of csrc/ieee_bits.h against the
-compiler's own IEEE double comparisons, multiplies by 0.5 and 2.0 and float
-to double conversion, on the host (the header is plain C++ too).
+compiler's own IEEE double comparisons and multiplies by 0.5 and 2.0, on the
+host (the header is plain C++ too).
 
 The reference-mode kernels use these predicates in place of FP64 compares,
 and must return exactly what the FP64 compare returns, so the check runs
@@ -94,26 +94,6 @@ int main()
         check(lt(from(b), y), from(b) < y, "lt r", from(b), y);
         check(eq(from(b), y), from(b) == y, "eq r", from(b), y);
     }
-    // widen(float) against the conversion: every exponent with mantissas
-    // strided through their range, both signs, the special values
-    for (uint64_t k = 0; k < (1ull << 32); k += 977) {
-        const uint32_t u = (uint32_t)k;
-        float f;
-        std::memcpy(&f, &u, sizeof f);
-        const double w = widen(f), c = (double)f;
-        if (!((w != w && c != c) || bits(w) == bits(c)) && bad++ < 20)
-            std::printf("MISMATCH widen %08x\n", u);
-    }
-    for (uint32_t e = 0; e < 256; ++e)
-        for (uint32_t m : {0u, 1u, 2u, 0x400000u, 0x7ffffeu, 0x7fffffu})
-            for (uint32_t sg : {0u, 0x80000000u}) {
-                const uint32_t u = sg | e << 23 | m;
-                float f;
-                std::memcpy(&f, &u, sizeof f);
-                const double w = widen(f), c = (double)f;
-                if (!((w != w && c != c) || bits(w) == bits(c)) && bad++ < 20)
-                    std::printf("MISMATCH widen %08x\n", u);
-            }
     std::printf("mismatches %ld\n", bad);
     return bad != 0;
 }

@@ -127,32 +127,6 @@ TAM_HD double twice_half(double s, double h)
     return from_bits((hb & SIGN) | ((hb & ~SIGN) << 1));
 }
 
-// FP32 -> FP64 widening, exact like the conversion: for +0 and positive
-// normal numbers by integer operations (the float's exponent field rebiased
-// from 127 to 1023 and its 23 mantissa bits moved to the top of the 52-bit
-// field, i.e. bits(f) << 29 plus 896 << 52), by the conversion for every
-// other input (negative, denormal, infinite, NaN).  The conversion
-// instruction issues on the FP64 pipe; the FP32 transport widens every
-// deposit for its FP64 tally, and deposits are non-negative.
-TAM_HD double widen(float f)
-{
-    uint32_t u;
-#if defined(__CUDA_ARCH__)
-    u = __float_as_uint(f);
-#else
-    std::memcpy(&u, &f, sizeof u);
-#endif
-    if (u == 0u || u - 0x00800000u < 0x7f000000u) {
-        const uint32_t hi = u ? (u >> 3) + 0x38000000u : 0u, lo = u << 29;
-#if defined(__CUDA_ARCH__)
-        return __hiloint2double((int)hi, (int)lo);
-#else
-        return from_bits((uint64_t)hi << 32 | lo);
-#endif
-    }
-    return (double)f;
-}
-
 }  // namespace ieee
 }  // namespace tam
 

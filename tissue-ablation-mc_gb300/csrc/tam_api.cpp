@@ -134,7 +134,8 @@ struct tam_ctx {
     tam::RefIterVals *d_iv = nullptr;
     cudaGraphExec_t rexec[4] = {nullptr, nullptr, nullptr, nullptr};  // by (temperature, rhokap) buffers read first
     std::vector<unsigned char> rkey[4];
-    int batch_staged = 2;            // batched steps: staged voxel pairs (2), staged voxels (1), cached loads (0)
+    int batch_staged = 2;            // batched steps: slab form (3), staged voxel pairs (2), staged voxels (1),
+                                     // cached loads (0)
     int batch_streams = 0;           // 1: batched steps as each instance's own steps on its stream, overlapped
     int batch_transport = 1;         // batched loops: the instances' uniform-medium passes in one launch
     int batch_zchunk = 0;            // batched steps: z planes per work item (0: heat.zchunk, else the default)
@@ -206,18 +207,33 @@ int fail(tam_ctx *c, int code, const std::string &msg)
         if (r_ != TAM_OK) return r_;  \
     } while (0)
 
+// Every context array has DPAD bytes of slack before and after it (the
+// pointer stays 256-byte aligned): the batched heat step copies whole
+// 16-byte-aligned chunks around a row, which may reach up to 16 bytes before
+// an array and a row's length past its end.
+constexpr size_t DPAD = 256;
 int dalloc(tam_ctx *ctx, void **p, size_t bytes)
 {
     if (bytes == 0) bytes = 16;
-    cudaError_t e = cudaMalloc(p, bytes);
+    void *base = nullptr;
+    cudaError_t e = cudaMalloc(&base, bytes + 2 * DPAD);
     if (e != cudaSuccess) {
         *p = nullptr;
         (void)cudaGetLastError();
         return fail(ctx, TAM_E_NOMEM, "cudaMalloc of " + std::to_string(bytes) + " bytes failed: " +
                                            cudaGetErrorString(e));
     }
-    ctx->allocs.push_back(*p);
+    ctx->allocs.push_back(base);
+    *p = (char *)base + DPAD;
     return TAM_OK;
+}
+// Free one array allocated by dalloc before the context ends.
+void dfree(tam_ctx *ctx, void *p)
+{
+    if (!p) return;
+    void *base = (char *)p - DPAD;
+    ctx->allocs.erase(std::remove(ctx->allocs.begin(), ctx->allocs.end(), base), ctx->allocs.end());
+    cudaFree(base);
 }
 
 template <typename T> int dalloc_t(tam_ctx *ctx, T **p, int64_t n)
@@ -626,11 +642,7 @@ int pass_args(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, tam::Tran
         a.bz0 = ctx->nz - bn[2];
         const int64_t cells = (int64_t)bn[0] * bn[1] * bn[2];
         if (cells > ctx->j32_cells) {
-            if (ctx->d_j32) {
-                ctx->allocs.erase(std::remove(ctx->allocs.begin(), ctx->allocs.end(), (void *)ctx->d_j32),
-                                  ctx->allocs.end());
-                cudaFree(ctx->d_j32);
-            }
+            dfree(ctx, ctx->d_j32);
             ctx->d_j32 = nullptr;
             ctx->j32_cells = 0;
             RC(dalloc_t(ctx, &ctx->d_j32, cells));
@@ -837,7 +849,7 @@ int ref_damage_props(tam_ctx *ctx, double ablate_temp)
 // Default z planes per work item of the staged step: long columns for the
 // batched launch (fewer halo planes; the batch's items fill the device) and
 // shorter ones for one context alone (enough items for every SM).
-constexpr int BATCH_ZCHUNK = 32, SINGLE_ZCHUNK = 8;
+constexpr int BATCH_ZCHUNK = 32, SINGLE_ZCHUNK = 8, BATCH_SLAB_ZCHUNK = 6;
 
 // The batched-step description of one context; returns its work items.
 // z planes per item: zforce if positive, else the context's heat.zchunk if
@@ -2202,6 +2214,7 @@ struct DevBatch {
     std::vector<int> prefix;
     std::vector<tam::BatchStep> steps;
     int blocks = 0, kmax = 0, staged = 1;
+    bool uniform = false;  // every instance one material class (the slab form's uniform kernel)
     ~DevBatch()
     {
         cudaFree(d_inst);
@@ -2218,11 +2231,20 @@ int batch_setup(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int kmax)
     tam_ctx *const ctx = ctxs[0];  // CUDA errors are reported on the first instance
     B.inst.resize(n);
     B.prefix.assign(n + 1, 0);
-    for (int32_t i = 0; i < n; ++i) B.prefix[i + 1] = B.prefix[i] + batch_inst(ctxs[i], B.inst[i], BATCH_ZCHUNK, ctx->batch_zchunk);
+    B.staged = ctx->batch_staged;
+    const bool slab = B.staged == 3;
+    B.uniform = true;
+    for (int32_t i = 0; i < n; ++i) {
+        int items = batch_inst(ctxs[i], B.inst[i], slab ? BATCH_SLAB_ZCHUNK : BATCH_ZCHUNK, ctx->batch_zchunk);
+        if (slab && B.inst[i].zchunk > tam::BATCH_SLAB_ZMAX)
+            items = batch_inst(ctxs[i], B.inst[i], BATCH_SLAB_ZCHUNK, tam::BATCH_SLAB_ZMAX);
+        B.prefix[i + 1] = B.prefix[i] + items;
+        if (B.inst[i].L.uniform < 0) B.uniform = false;
+    }
     B.kmax = kmax;
     B.steps.resize((size_t)kmax * n);
-    B.staged = ctx->batch_staged;
-    CK(tam::batch_heat_blocks(&B.blocks, B.staged));
+    if (slab) CK(tam::batch_slab_blocks(&B.blocks, B.uniform));
+    else CK(tam::batch_heat_blocks(&B.blocks, B.staged));
     CK(cudaMalloc(&B.d_inst, sizeof(tam::BatchInst) * n));
     CK(cudaMalloc(&B.d_prefix, sizeof(int) * (n + 1)));
     CK(cudaMalloc(&B.d_steps, sizeof(tam::BatchStep) * B.steps.size()));
@@ -2261,7 +2283,10 @@ int batch_heat_chunk(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int K, const 
         if (ctxs[i]->stream != s) CK(cudaStreamSynchronize(ctxs[i]->stream));
     CK(cudaMemcpyAsync(B.d_inst, B.inst.data(), sizeof(tam::BatchInst) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(B.d_steps, B.steps.data(), sizeof(tam::BatchStep) * (size_t)K * n, cudaMemcpyHostToDevice, s));
-    CK(tam::launch_batch_heat(B.d_inst, n, B.d_prefix, B.d_steps, K, B.d_sync, B.d_err, B.blocks, B.staged, s));
+    if (B.staged == 3)
+        CK(tam::launch_batch_slab(B.d_inst, n, B.d_prefix, B.d_steps, K, B.d_sync, B.d_err, B.blocks, B.uniform, s));
+    else
+        CK(tam::launch_batch_heat(B.d_inst, n, B.d_prefix, B.d_steps, K, B.d_sync, B.d_err, B.blocks, B.staged, s));
     CK(cudaStreamSynchronize(s));
     unsigned bits = 0;
     CK(cudaMemcpy(&bits, B.d_err, sizeof bits, cudaMemcpyDeviceToHost));
@@ -2614,7 +2639,7 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
         if (value < 0 || value > 1 << 20) return fail(ctx, TAM_E_INVALID, "batch.zchunk must be >= 0");
         ctx->batch_zchunk = (int)value;
     } else if (k == "batch.staged") {
-        if (value < 0 || value > 2) return fail(ctx, TAM_E_INVALID, "batch.staged must be 0, 1 or 2");
+        if (value < 0 || value > 3) return fail(ctx, TAM_E_INVALID, "batch.staged must be 0, 1, 2 or 3");
         ctx->batch_staged = (int)value;
     } else if (k == "batch.streams") {
         ctx->batch_streams = value != 0;
@@ -3011,7 +3036,7 @@ int tam_batch_autotune(tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *
     struct Cand {
         int form, z;
     };
-    const Cand cands[] = {{2, 8}, {2, 16}, {2, 32}, {2, 64}, {1, 16}, {1, 32}};
+    const Cand cands[] = {{3, 4}, {3, 6}, {3, 8}, {2, 8}, {2, 16}, {2, 32}, {2, 64}, {1, 16}, {1, 32}};
     // on a failure the settings and every instance's state go back as they were
     auto undo = [&](int code) {
         ctx->batch_staged = form0;

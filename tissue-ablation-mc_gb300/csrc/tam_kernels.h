@@ -336,6 +336,15 @@ cudaError_t batch_heat_blocks(int *blocks, int staged);
 // prefix[n] = total work items; steps is K x n (step-major).
 cudaError_t launch_batch_heat(const BatchInst *insts, int n, const int *prefix, const BatchStep *steps, int K,
                               BatchSync *sync, unsigned *err, int blocks, int staged, cudaStream_t s);
+// The slab form of the batched step (batch.staged 3): z-chunks of at most
+// BATCH_SLAB_ZMAX planes (BatchInst::zchunk), rows of any pitch staged by bulk
+// copies of their 16-byte chunks (the arrays need 256 bytes of slack at both
+// ends), voxels needing rare work handled after each chunk.  uniform: every
+// instance's grid is one material class.
+constexpr int BATCH_SLAB_ZMAX = 8;
+cudaError_t batch_slab_blocks(int *blocks, bool uniform);
+cudaError_t launch_batch_slab(const BatchInst *insts, int n, const int *prefix, const BatchStep *steps, int K,
+                              BatchSync *sync, unsigned *err, int blocks, bool uniform, cudaStream_t s);
 // One step of one instance (inst: device copy of its BatchInst) by the staged
 // voxel-pair kernel, one block per work item (prefix = {0, items}); any row
 // pitch.  fcur selects the buffer pair read by the step.

@@ -1,5 +1,5 @@
 // tma_common.cuh -- TMA plane staging shared by the heat-step kernels:
-// mbarrier and cp.async.bulk.tensor wrappers (inline PTX) and the host-side
+// mbarrier, cp.async.bulk.tensor and cp.async.bulk wrappers (inline PTX) and the host-side
 // tensor-map encoders (cuTensorMapEncodeTiled, fetched from the driver).
 // Every wait is bounded: after WAIT_CYCLES of clock the caller gives up and
 // records DEVERR_SYNC_TIMEOUT instead of spinning forever.
@@ -53,6 +53,15 @@ __device__ __forceinline__ void tma_load_3d(void *dst, const CUtensorMap *map, i
             "r"(su32(dst)),
         "l"(map), "r"(x), "r"(y), "r"(z), "r"(su32(bar))
         : "memory");
+}
+// Non-tensor bulk copy of `bytes` (a multiple of 16) from global to shared
+// memory, both addresses 16-byte aligned, completing on `bar`.
+__device__ __forceinline__ void bulk_load(void *dst, const void *src, uint32_t bytes, uint64_t *bar)
+{
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                     su32(dst)),
+                 "l"(src), "r"(bytes), "r"(su32(bar))
+                 : "memory");
 }
 __device__ __forceinline__ void fence_proxy_async() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
 __device__ __forceinline__ void fence_mbar_init() { asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory"); }

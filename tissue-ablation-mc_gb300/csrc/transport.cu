@@ -44,7 +44,7 @@ __device__ __forceinline__ void deposit(const TransportArgs &a, int cidx, int ix
             return;
         }
     }
-    atomicAdd(a.jmean + cidx, to_tally(dep));
+    atomicAdd(a.jmean + cidx, (double)dep);
 }
 
 // Optical properties of the current cell: extinction and absorption for the

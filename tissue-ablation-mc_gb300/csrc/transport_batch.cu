@@ -151,7 +151,7 @@ __global__ void __launch_bounds__(BTPB, 4)
         auto vstep = [&]() {
             if (mode != M_FLY) return;
             if (++nsteps > s_in[inst].max_steps) {
-                if (dep != 0.f) atomicAdd(s_in[inst].jmean + cidx, to_tally(dep));
+                if (dep != 0.f) atomicAdd(s_in[inst].jmean + cidx, (double)dep);
                 dep = 0.f;
                 atomicAdd(s_in[inst].tally + T_OVERFLOW, 1.0);
                 atomicOr(s_in[inst].err, (unsigned)DEVERR_STEP_CAP);
@@ -177,7 +177,7 @@ __global__ void __launch_bounds__(BTPB, 4)
             const int sg = cx ? sgx : (cy ? sgy : sgz);
             const int j = (cx ? ix : (cy ? iy : iz)) + sg;
             const int N = cx ? NX : (cy ? NY : NZ);
-            atomicAdd(s_in[inst].jmean + cidx, to_tally(dep));
+            atomicAdd(s_in[inst].jmean + cidx, (double)dep);
             dep = 0.f;
             if ((unsigned)j < (unsigned)N) {
                 ix = cx ? j : ix;
@@ -284,7 +284,7 @@ __global__ void __launch_bounds__(BTPB, 4)
                     if (!die) mode = M_FLY;
                 }
                 if (die) {
-                    if (dep != 0.f) atomicAdd(I.jmean + cidx, to_tally(dep));
+                    if (dep != 0.f) atomicAdd(I.jmean + cidx, (double)dep);
                     dep = 0.f;
                     retire();
                 }

@@ -5,7 +5,6 @@
 // set-up and position reconstruction.
 #pragma once
 
-#include "ieee_bits.h"
 #include "tam_device.cuh"
 #include "tam_kernels.h"
 
@@ -156,11 +155,6 @@ template <typename Real> __device__ __forceinline__ Real fresnel(Real n1, Real n
     const Real rp = M<Real>::div(n1 * ct - n2 * cosi, n1 * ct + n2 * cosi);
     return (Real)0.5 * (rs * rs + rp * rp);
 }
-
-// A deposit widened for the FP64 tally (FP32: by integer operations, see
-// ieee::widen).
-__device__ __forceinline__ double to_tally(float d) { return ieee::widen(d); }
-__device__ __forceinline__ double to_tally(double d) { return d; }
 
 template <typename Real> __device__ __forceinline__ Real clamp0h(Real f, Real h)
 {

@@ -166,10 +166,16 @@ def c5(scale=1.0, seed=5, packets=1_000_000_000, steps=100_000):
             d2 = (X - p0[0]) ** 2 + (Y - p0[1]) ** 2 + (z - p0[2]) ** 2
             sl[d2 <= r * r] = 3
     mats = [AIR, DERMIS, BLOOD, INCLUSION]
+    total = 10.0  # s: 10 pulses at 1 Hz
     p = api.default_params(nxg=n, nyg=n, nzg=n, xmax=L / 2, ymax=L / 2, zmax=L / 2, mode=1, precision=1,
                            nphotons=packets, pulse_type=1, power=10.0, energy_per_pixel=10.0 * 50.0,
-                           repetition_rate_1=1.0, pulses_to_do=10, total_time=10.0, loops=1)
-    cfg = _config(mats, retrace_fraction=1e-9, retrace_check=64)
+                           repetition_rate_1=1.0, pulses_to_do=10, total_time=total, loops=1)
+    # `steps` heat steps span the 10 pulses (1e5 steps: dt = 0.1 ms, 500 steps
+    # per 50 ms pulse, well inside the stability limit of the 39 um voxels);
+    # the MC pass is re-run when a pulse starts if the previous one ablated
+    # voxels (the fraction rule never fires at 1.0), checked every 1000 steps
+    # between pulses
+    cfg = _config(mats, retrace_fraction=1.0, retrace_check=1000, dt=total / steps)
     return Workload("C5 vessels and inclusions", p, cfg, grid, packets, steps,
                     {"grid": (n, n, n), "cylinders": len(cyl), "spheres": len(sph)})
 
@@ -197,6 +203,8 @@ def _run_batch(a) -> None:
             print(f"C4 MC ({'batched transport' if on else 'one launch per instance'}): {n} passes of {a.packets} "
                   f"packets in {dt:.3f} s = {n * a.packets / dt:.3e} photons/s", flush=True)
         ctxs[0].set_tuning("batch.transport", 1)
+        if a.staged >= 0:
+            ctxs[0].set_tuning("batch.staged", a.staged)
         if a.autotune:
             print("batch autotune:", api.batch_autotune(ctxs, steps=20), flush=True)
         if a.warm:
@@ -204,7 +212,8 @@ def _run_batch(a) -> None:
         t0 = time.perf_counter()
         api.batch_heat_steps(ctxs, a.steps)
         dt = time.perf_counter() - t0
-        print(f"C4 batch: {len(ctxs)} instances, {nvox} voxels; {a.steps} batched steps after {a.warm}: "
+        print(f"C4 batch (batch.staged {a.staged}): {len(ctxs)} instances, {nvox} voxels; {a.steps} batched steps "
+              f"after {a.warm}: "
               f"{dt * 1e3:.2f} ms = {nvox * a.steps / dt:.3e} voxel updates/s; "
               f"device errors {sum(c.device_errors() for c in ctxs)}", flush=True)
     finally:
@@ -227,6 +236,29 @@ def _run_vessels(a) -> None:
               f"{a.packets} packets in {tr:.2f} ms = {a.packets / (tr * 1e-3):.3e} photons/s, "
               f"{tl['voxel_steps']:.4e} voxel steps = {tl['voxel_steps'] / (tr * 1e-3):.3e} steps/s; "
               f"device errors {ctx.device_errors()}", flush=True)
+
+
+def _run_pulsed(a) -> None:
+    """Configuration 5's whole coupled run at `scale`: the pulsed laser's MC
+    passes (the first, then one at each pulse start after a pulse that
+    ablated voxels) and every heat step, through tam_run; timed on the host
+    clock, with the library's CUDA-event times of the last pass and the last
+    stretch of heat steps."""
+    import time
+
+    w = c5(scale=a.scale, packets=a.packets, steps=a.steps)
+    with w.context() as ctx:
+        n = w.params.nxg
+        t0 = time.perf_counter()
+        its = ctx.run(seed=a.seed)
+        dt = time.perf_counter() - t0
+        st = ctx.state()
+        tr, hm, hl = ctx.timing()
+        T = ctx.download(api._abi.TAM_F_TEMP)
+        print(f"C5 pulsed run on {n}^3: {its} outer iterations of one heat step of {st.delt:.3e} s "
+              f"(simulated {st.time:.4f} s, {st.pulses_done} pulses), {st.mc_passes} MC passes of {a.packets} packets, "
+              f"{st.n_ablated} voxels ablated, max T {T.max():.2f} K; wall {dt:.2f} s; last pass {tr:.1f} ms = "
+              f"{a.packets / (tr * 1e-3):.3e} photons/s; device errors {ctx.device_errors()}", flush=True)
 
 
 def _run_heat(a) -> None:
@@ -260,11 +292,18 @@ def parser():
     b.add_argument("--steps", type=int, default=200, help="timed batched steps")
     b.add_argument("--autotune", action="store_true")
     b.add_argument("--compare-mc", action="store_true", help="also time the passes with one launch per instance")
+    b.add_argument("--staged", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
+                   help="batched step form (batch.staged; -1: the library's default)")
     v = sub.add_parser("vessels", help="configuration 5: MC transport on the vessel grid")
     v.add_argument("--scale", type=float, default=1.0, help="grid edge = 512 * scale")
     v.add_argument("--packets", type=int, default=10_000_000)
     v.add_argument("--warm-packets", type=int, default=1_000_000)
     v.add_argument("--tally32", type=int, default=-1, choices=[-1, 0, 1])
+    r = sub.add_parser("pulsed", help="configuration 5: the whole pulsed coupled run on the vessel grid")
+    r.add_argument("--scale", type=float, default=1.0, help="grid edge = 512 * scale")
+    r.add_argument("--packets", type=int, default=1_000_000_000, help="packets per MC pass")
+    r.add_argument("--steps", type=int, default=100_000, help="heat steps over the 10 pulses")
+    r.add_argument("--seed", type=int, default=1)
     h = sub.add_parser("heat", help="the homogeneous cube's FP32 heat step, one launch per step")
     h.add_argument("--edge", type=int, default=200)
     h.add_argument("--packets", type=int, default=1_000_000)
@@ -275,7 +314,7 @@ def parser():
 
 def main(argv=None) -> None:
     a = parser().parse_args(argv)
-    {"batch": _run_batch, "vessels": _run_vessels, "heat": _run_heat}[a.cmd](a)
+    {"batch": _run_batch, "vessels": _run_vessels, "pulsed": _run_pulsed, "heat": _run_heat}[a.cmd](a)
 
 
 if __name__ == "__main__":
