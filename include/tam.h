@@ -284,15 +284,16 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits),
  * "batch.zchunk" (batched heat steps, read from the first context of the
  * batch: z planes per work item; 0 (default) uses each instance's
- * "heat.zchunk" if set, else 32, or 6 in the slab form, whose items hold at
- * most 8 planes),
+ * "heat.zchunk" if set, else 32; the slab form's items hold at most 32
+ * planes),
  * "batch.staged" (batched heat steps, read from the first context of the
- * batch: 3 is the slab form -- each staged row one bulk copy of the 16-byte
- * chunks that cover it, voxel pairs, boundary faces as ghost neighbours,
- * voxels needing rare work handled after each item's planes; 2 (default)
- * stages each tile's planes in shared memory with 4-byte cp.async copies and
- * updates two x-adjacent voxels per thread, 1 the same with one voxel per
- * thread, 0 reads neighbours with cached global loads),
+ * batch: 3 (default) is the slab form -- each staged row the 16-byte chunks
+ * that cover it, copied by all threads with cp.async, voxel pairs, boundary
+ * faces as ghost neighbours, voxels needing rare work listed and handled
+ * after each item's planes; 2 stages each tile's planes in shared memory with
+ * 4-byte cp.async copies and updates two x-adjacent voxels per thread, 1 the
+ * same with one voxel per thread, 0 reads neighbours with cached global
+ * loads),
  * "batch.streams" (batched heat steps, read from the first context: 1 runs
  * each instance's own single-context steps on its own stream, issued
  * round-robin in chunks of 256 steps so the instances overlap, instead of

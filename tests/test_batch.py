@@ -209,7 +209,7 @@ def test_batch_autotune_restores_state(tam):
         tam.batch_heat_steps(ctxs, 5)
         before = [(c.download(F.TAM_F_TEMP), c.download(F.TAM_F_TISSUE), c.state().time) for c in ctxs]
         chosen = tam.batch_autotune(ctxs, steps=8)
-        assert (chosen["batch.staged"], chosen["batch.zchunk"]) in [(3, 4), (3, 6), (3, 8), (2, 8), (2, 16), (2, 32),
+        assert (chosen["batch.staged"], chosen["batch.zchunk"]) in [(3, 8), (3, 16), (3, 32), (2, 8), (2, 16), (2, 32),
                                                                     (2, 64), (1, 16), (1, 32)]
         assert chosen["batch.streams"] in (0, 1)
         for c, (T, om, t) in zip(ctxs, before):

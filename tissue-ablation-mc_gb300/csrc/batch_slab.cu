@@ -2,19 +2,22 @@
 //
 // All instances of a batch advance K steps in one cooperative launch, as in
 // batch.cu: per step the resident blocks share out the work items (instance,
-// 32 x 8 tile, z-chunk of at most BZMAX planes) of every instance, and a
+// 32 x 8 tile, z-chunk) of every instance, and a
 // bounded software grid barrier separates the steps.  Each item is updated
 // with the scheme of the single-instance slab kernel (heat_slab.cu): two
 // x-adjacent voxels per thread, z neighbours in registers, the ghost
 // neighbour of a boundary face written into the thread's own halo cell,
 // voxels needing rare work (boiling, damage window, ablation, negative or NaN)
-// listed and handled after the item's planes.
+// listed and handled after the item's planes.  The list holds every voxel of
+// an item of up to BATCH_SLAB_ZMAX planes, so that an item's z-chunk can be
+// long and the ring's start-up latency is paid once per long item.
 //
 // The instances' grid edges are arbitrary, so their rows are generally not
-// 16-byte aligned and TMA tensor copies cannot stage them.  Each staged row
-// is instead one non-tensor bulk copy (cp.async.bulk) of the 16-byte chunks
-// that cover it, issued by one lane of the block's first warp and completing
-// on the stage's mbarrier; where the row starts inside its first chunk,
+// 16-byte aligned and TMA tensor copies cannot stage them.  A staged row is
+// instead the run of 16-byte chunks that covers it, copied chunk by chunk
+// with 16-byte cp.async by all threads of the block (each thread then
+// arrives on the stage's mbarrier, which completes once every thread's
+// copies have landed); where the row starts inside its first chunk,
 // (index & 3), is applied when it is read.  The context arrays carry 256
 // bytes of slack at both ends, so a chunk never leaves its allocation.  Rows
 // and planes outside the grid are not copied; their cells are read only
@@ -42,7 +45,7 @@ template <bool UNIFORM> struct BLay {
     static constexpr int T_OFF = 0, E_OFF = (BR + 2) * RT * 4, J_OFF = 2 * (BR + 2) * RT * 4;
     static constexpr int C_OFF = J_OFF + BR * RJ * 4;
     static constexpr int STAGE = ((C_OFF + (UNIFORM ? 0 : (BR + 2) * RC) + 127) / 128) * 128;
-    static constexpr int LIST = BW * BR * BATCH_SLAB_ZMAX;
+    static constexpr int LIST = BW * BR * BATCH_SLAB_ZMAX;   // u16 local indices: every voxel of an item
     static constexpr int SMEM = BS * STAGE + BS * 8 + LIST * 2 + 16 + 128;
     static_assert(E_OFF % 16 == 0 && J_OFF % 16 == 0 && C_OFF % 16 == 0, "16-byte aligned copy targets");
 };
@@ -61,6 +64,54 @@ struct __align__(16) BItem {
     int inst, x0, y0, z0, z1, cpitch;
 };
 
+// The listed voxels of an item whose tile starts at (bxW, byR, zb) (the
+// block's own plane stores come first), as in the single-instance slab
+// kernel: the damage-window voxels' pairs and damage integrals loaded four
+// entries at a time, the others through slab_fix; returns error bits.  The
+// whole block shares the list out, so a hot region's many entries do not
+// wait on the few threads that own them.
+template <bool UNIFORM>
+__device__ __noinline__ unsigned list_pass(const FusedArgs &A, const ClassLut &L, const unsigned short *list, int cnt,
+                                           int bxW, int byR, int zb, const float *Ti, const float *Tw, const float *Ew,
+                                           const uint8_t *cls, int cpitch, float Pdt, double t_new)
+{
+    unsigned errbits = 0;
+    const int nx = A.nx, sz = A.nx * A.ny;
+    const int64_t ni = (int64_t)sz * A.nz;
+    constexpr int NT = BP * BR, B = 4;
+    for (int q = (int)threadIdx.x; q < cnt; q += B * NT) {
+        int vv[B], xx[B], yy[B], zz[B];
+        float tt[B], ee[B], tcv[B];
+        double oo[B];
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            const int qq = q + j * NT;
+            vv[j] = -1;
+            if (qq < cnt) {
+                const int l = list[qq];
+                xx[j] = bxW + l % BW;
+                yy[j] = byR + (l / BW) % BR;
+                zz[j] = zb + l / (BW * BR);
+                vv[j] = xx[j] + nx * yy[j] + sz * zz[j];
+                tt[j] = Tw[vv[j]];
+                ee[j] = Ew[vv[j]];
+                tcv[j] = Ti[vv[j]];
+                oo[j] = A.omega[vv[j]];
+            }
+        }
+#pragma unroll
+        for (int j = 0; j < B; ++j) {
+            if (vv[j] < 0) continue;
+            const float Ts = tt[j] - ee[j];
+            const bool general = (A.boil && tcv[j] >= A.fc[FC_TBOIL]) || !(Ts >= 0.f) ||
+                                 ge_ff(tt[j], ee[j], A.fc[FC_TABL], A.fc[FC_TABL_LO]);
+            if (general) slab_fix<UNIFORM>(A, L, cls, cpitch, xx[j], yy[j], zz[j], Pdt, t_new, errbits);
+            else if (Ts >= A.fc[FC_SCREEN]) rare_update_f32(A, vv[j], ni, tt[j], ee[j], t_new, true, oo[j]);
+        }
+    }
+    return errbits;
+}
+
 template <bool UNIFORM>
 __global__ void __launch_bounds__(BP *BR, bslab_minb(UNIFORM))
     batch_slab_kernel(const BatchInst *__restrict__ insts, int n, const int *__restrict__ prefix,
@@ -77,12 +128,12 @@ __global__ void __launch_bounds__(BP *BR, bslab_minb(UNIFORM))
     uint64_t *bar = reinterpret_cast<uint64_t *>(sm + BS * Lay::STAGE);
     unsigned short *list = reinterpret_cast<unsigned short *>(sm + BS * Lay::STAGE + BS * 8);
     int *s_cnt = reinterpret_cast<int *>(sm + BS * Lay::STAGE + BS * 8 + Lay::LIST * 2);
-    const int tid = threadIdx.x, r = tid / BP, p = tid % BP, warp = tid >> 5, lane = tid & 31;
+    const int tid = threadIdx.x, r = tid / BP, p = tid % BP;
     constexpr int ARGS_W = (int)(sizeof(FusedArgs) / 4), LUT_W = (int)(sizeof(ClassLut) / 4);
     static_assert(sizeof(FusedArgs) % 4 == 0 && sizeof(ClassLut) % 4 == 0, "word copies");
 
     if (tid == 0) {
-        for (int s = 0; s < BS; ++s) mbar_init(bar + s, 1);
+        for (int s = 0; s < BS; ++s) mbar_init(bar + s, BP * BR);  // every thread arrives on each phase
         fence_mbar_init();
     }
     __syncthreads();
@@ -153,47 +204,51 @@ __global__ void __launch_bounds__(BP *BR, bslab_minb(UNIFORM))
             const float lo_t = 0.5f * rare_thr;  // new temperatures outside (0, rare_thr) are listed
 
             // planes idx = 0 .. last (z = z0 - 1 .. z1): rows y0 - 1 .. y0 + 8 of T and
-            // the Kahan term, rows y0 .. y0 + 7 of J for the item's own planes,
-            // and the class rows; issued by the first warp, one row per lane
-            // (the issuing warp reads the item from shared memory, so that none of
-            // it stays in registers through the plane loop)
+            // the Kahan term (11 chunks each), rows y0 .. y0 + 7 of J for the item's
+            // own planes (9 chunks each) and the class rows (4 chunks each).  Every
+            // thread copies one or two units of 16 bytes per array with cp.async
+            // and then arrives on the stage's barrier, which completes once every
+            // thread's copies have landed.  Units 0..109: T and Kahan-term chunk
+            // (row u / 11, chunk u % 11); 110..181: J (row (u - 110) / 9);
+            // 182..221: class rows (row (u - 182) / 4).  Thread t takes units t and
+            // t + 128.  Per unit: its row's first index plus 4 x chunk (the plane's
+            // offset is added, then the sum rounded down to a chunk), its shared
+            // offset, and its kind (0: none, the row is outside the grid).
+            int rbA = 0, rbB = 0, dA = 0, dB = 0, kA = 0, kB = 0;
+            {
+                auto unit = [&](int u, int &rb, int &dst, int &kind) {
+                    if (u < 110) {
+                        const int q = u / 11, c = u % 11, yy = byR - 1 + q;
+                        if (yy >= 0 && yy < ny) kind = 1, rb = bxW - 4 + nx * yy + 4 * c, dst = Lay::T_OFF + q * RT * 4 + 16 * c;
+                    } else if (u < 182) {
+                        const int q = (u - 110) / 9, c = (u - 110) % 9, yy = byR + q;
+                        if (yy < ny) kind = 2, rb = bxW + nx * yy + 4 * c, dst = Lay::J_OFF + q * RJ * 4 + 16 * c;
+                    } else if (!UNIFORM && u < 222) {
+                        const int q = (u - 182) / 4, c = (u - 182) % 4, yy = byR - 1 + q;
+                        if (yy >= 0 && yy < ny) kind = 3, rb = d.cpitch * yy + bxW - 16 + 16 * c, dst = Lay::C_OFF + q * RC + 16 * c;
+                    }
+                };
+                unit(tid, rbA, dA, kA);
+                unit(tid + BP * BR, rbB, dB, kB);
+            }
             auto issue = [&](int idx) {
                 const uint32_t g = G + (uint32_t)idx;
                 unsigned char *b = sm + (g % BS) * Lay::STAGE;
-                uint64_t *br = bar + g % BS;
-                const int nx = A.nx, ny = A.ny, nz = A.nz, sz = nx * ny, bxW = d.x0, byR = d.y0;
-                const int ylo = max(byR - 1, 0), yhi = min(byR + BR, ny - 1), jhi = min(byR + BR - 1, ny - 1);
-                const int zz = d.z0 - 1 + idx;
-                const bool pl = zz >= 0 && zz < nz;
-                const bool own = idx >= 1 && idx <= d.z1 - d.z0;
-                const uint32_t bytes =
-                    pl ? (uint32_t)(yhi - ylo + 1) * (2u * RT * 4u + (UNIFORM ? 0u : (uint32_t)RC)) +
-                             (own ? (uint32_t)(jhi - byR + 1) * (RJ * 4u) : 0u)
-                       : 0u;
-                if (lane == 0) {
-                    fence_proxy_async();
-                    mbar_expect_tx(br, bytes);
-                }
-                __syncwarp();
-                if (!pl) return;
-                fence_proxy_async();
-                if (lane < 20) {
-                    const int q = lane < 10 ? lane : lane - 10, yy = byR - 1 + q;
-                    if (yy >= 0 && yy < ny) {
-                        const int s = (bxW - 4 + nx * yy + sz * zz) & ~3;  // >= -4: inside the slack
-                        bulk_load(b + (lane < 10 ? Lay::T_OFF : Lay::E_OFF) + q * RT * 4, (lane < 10 ? d.T : d.E) + s,
-                                  RT * 4, br);
+                const int zz = z0 - 1 + idx;
+                if (zz >= 0 && zz < nz) {
+                    const bool own = idx >= 1 && idx <= np;
+                    const int pz = sz * zz;
+                    if (kA == 1) {
+                        const int q = (rbA + pz) & ~3;  // >= -4: inside the slack before the array
+                        cp_async16(b + dA, d.T + q);
+                        cp_async16(b + dA + (Lay::E_OFF - Lay::T_OFF), d.E + q);
+                    } else if (kA == 2 && own) {
+                        cp_async16(b + dA, d.J + ((rbA + pz) & ~3));
                     }
-                } else if (lane < 20 + BR) {
-                    const int q = lane - 20, yy = byR + q;
-                    if (own && yy < ny) bulk_load(b + Lay::J_OFF + q * RJ * 4, d.J + ((bxW + nx * yy + sz * zz) & ~3),
-                                                  RJ * 4, br);
+                    if (kB == 2 && own) cp_async16(b + dB, d.J + ((rbB + pz) & ~3));
+                    else if (!UNIFORM && kB == 3) cp_async16(b + dB, d.C + (d.cpitch * ny * zz + rbB));
                 }
-                if (!UNIFORM && lane < BR + 2) {
-                    const int yy = byR - 1 + lane;
-                    if (yy >= 0 && yy < ny)
-                        bulk_load(b + Lay::C_OFF + lane * RC, d.C + (d.cpitch * (ny * zz + yy) + bxW - 16), RC, br);
-                }
+                cp_async_arrive(bar + g % BS);
             };
             auto stage = [&](int idx) { return sm + ((G + (uint32_t)idx) % BS) * Lay::STAGE; };
             auto wait = [&](int idx) {
@@ -201,8 +256,7 @@ __global__ void __launch_bounds__(BP *BR, bslab_minb(UNIFORM))
                 return mbar_wait(bar + g % BS, (g / BS) & 1u);
             };
 
-            if (warp == 0)
-                for (int idx = 0; idx < BS && idx <= last; ++idx) issue(idx);
+            for (int idx = 0; idx < BS && idx <= last; ++idx) issue(idx);
             int issued = BS < last + 1 ? BS : last + 1;
             bool ok = wait(0) && wait(1);
             // where a row starts inside its first chunk: (index of x0 - 4) & 3,
@@ -240,7 +294,7 @@ __global__ void __launch_bounds__(BP *BR, bslab_minb(UNIFORM))
                 ok = __syncthreads_and(ok) != 0;
                 if (!ok) break;
                 if (i + BS <= last) {
-                    if (warp == 0) issue(i + BS);
+                    issue(i + BS);
                     issued = i + BS + 1;
                 }
                 ok = wait(i + 2);
@@ -389,7 +443,6 @@ __global__ void __launch_bounds__(BP *BR, bslab_minb(UNIFORM))
             }
             // the last plane's wait may have failed in some threads only: agree first
             ok = __syncthreads_and(ok) != 0;
-            unsigned errbits = 0;
             if (!ok) {
                 // wait (bounded) for this block's copies in flight, then leave;
                 // the other blocks leave at their next grid barrier
@@ -401,43 +454,9 @@ __global__ void __launch_bounds__(BP *BR, bslab_minb(UNIFORM))
                 }
                 return;
             }
-            // the listed voxels (the block's own plane stores come first), as in
-            // the single-instance slab kernel
-            const int cnt = *s_cnt;
-            const double t_new = d.t_new;
-            const int64_t ni = (int64_t)sz * nz;
-            const float *Ti = d.T, *Tw = d.To, *Ew = d.Eo;
-            constexpr int NT = BP * BR, B = 4;
-            for (int q = tid; q < cnt; q += B * NT) {
-                int vv[B], xx[B], yy[B], zz[B];
-                float tt[B], ee[B], tcv[B];
-                double oo[B];
-#pragma unroll
-                for (int j = 0; j < B; ++j) {
-                    const int qq = q + j * NT;
-                    vv[j] = -1;
-                    if (qq < cnt) {
-                        const int l = list[qq];
-                        xx[j] = bxW + l % BW;
-                        yy[j] = byR + (l / BW) % BR;
-                        zz[j] = z0 + l / (BW * BR);
-                        vv[j] = xx[j] + nx * yy[j] + sz * zz[j];
-                        tt[j] = Tw[vv[j]];
-                        ee[j] = Ew[vv[j]];
-                        tcv[j] = Ti[vv[j]];
-                        oo[j] = A.omega[vv[j]];
-                    }
-                }
-#pragma unroll
-                for (int j = 0; j < B; ++j) {
-                    if (vv[j] < 0) continue;
-                    const float Ts = tt[j] - ee[j];
-                    const bool general = (A.boil && tcv[j] >= A.fc[FC_TBOIL]) || !(Ts >= 0.f) ||
-                                         ge_ff(tt[j], ee[j], A.fc[FC_TABL], A.fc[FC_TABL_LO]);
-                    if (general) slab_fix<UNIFORM>(A, L, d.C, d.cpitch, xx[j], yy[j], zz[j], Pdt, t_new, errbits);
-                    else if (Ts >= A.fc[FC_SCREEN]) rare_update_f32(A, vv[j], ni, tt[j], ee[j], t_new, true, oo[j]);
-                }
-            }
+            // (the barrier above also made the block's plane stores and list visible)
+            const unsigned errbits =
+                list_pass<UNIFORM>(A, L, list, *s_cnt, bxW, byR, z0, d.T, d.To, d.Eo, d.C, d.cpitch, Pdt, d.t_new);
             if (errbits) atomicOr(A.err, errbits);
             G += (uint32_t)issued;
             __syncthreads();  // the next item rewrites the stages, the list and the instance's tables

@@ -134,7 +134,7 @@ struct tam_ctx {
     tam::RefIterVals *d_iv = nullptr;
     cudaGraphExec_t rexec[4] = {nullptr, nullptr, nullptr, nullptr};  // by (temperature, rhokap) buffers read first
     std::vector<unsigned char> rkey[4];
-    int batch_staged = 2;            // batched steps: slab form (3), staged voxel pairs (2), staged voxels (1),
+    int batch_staged = 3;            // batched steps: slab form (3), staged voxel pairs (2), staged voxels (1),
                                      // cached loads (0)
     int batch_streams = 0;           // 1: batched steps as each instance's own steps on its stream, overlapped
     int batch_transport = 1;         // batched loops: the instances' uniform-medium passes in one launch
@@ -849,7 +849,7 @@ int ref_damage_props(tam_ctx *ctx, double ablate_temp)
 // Default z planes per work item of the staged step: long columns for the
 // batched launch (fewer halo planes; the batch's items fill the device) and
 // shorter ones for one context alone (enough items for every SM).
-constexpr int BATCH_ZCHUNK = 32, SINGLE_ZCHUNK = 8, BATCH_SLAB_ZCHUNK = 6;
+constexpr int BATCH_ZCHUNK = 32, SINGLE_ZCHUNK = 8, BATCH_SLAB_ZCHUNK = 32;
 
 // The batched-step description of one context; returns its work items.
 // z planes per item: zforce if positive, else the context's heat.zchunk if
@@ -3036,7 +3036,7 @@ int tam_batch_autotune(tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *
     struct Cand {
         int form, z;
     };
-    const Cand cands[] = {{3, 4}, {3, 6}, {3, 8}, {2, 8}, {2, 16}, {2, 32}, {2, 64}, {1, 16}, {1, 32}};
+    const Cand cands[] = {{3, 8}, {3, 16}, {3, 32}, {2, 8}, {2, 16}, {2, 32}, {2, 64}, {1, 16}, {1, 32}};
     // on a failure the settings and every instance's state go back as they were
     auto undo = [&](int code) {
         ctx->batch_staged = form0;

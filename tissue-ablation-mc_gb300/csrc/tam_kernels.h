@@ -337,11 +337,11 @@ cudaError_t batch_heat_blocks(int *blocks, int staged);
 cudaError_t launch_batch_heat(const BatchInst *insts, int n, const int *prefix, const BatchStep *steps, int K,
                               BatchSync *sync, unsigned *err, int blocks, int staged, cudaStream_t s);
 // The slab form of the batched step (batch.staged 3): z-chunks of at most
-// BATCH_SLAB_ZMAX planes (BatchInst::zchunk), rows of any pitch staged by bulk
-// copies of their 16-byte chunks (the arrays need 256 bytes of slack at both
-// ends), voxels needing rare work handled after each chunk.  uniform: every
-// instance's grid is one material class.
-constexpr int BATCH_SLAB_ZMAX = 8;
+// BATCH_SLAB_ZMAX planes (BatchInst::zchunk), rows of any pitch staged by
+// 16-byte copies of the aligned chunks that cover them (the arrays need 256
+// bytes of slack at both ends), voxels needing rare work handled after each
+// item.  uniform: every instance's grid is one material class.
+constexpr int BATCH_SLAB_ZMAX = 32;
 cudaError_t batch_slab_blocks(int *blocks, bool uniform);
 cudaError_t launch_batch_slab(const BatchInst *insts, int n, const int *prefix, const BatchStep *steps, int K,
                               BatchSync *sync, unsigned *err, int blocks, bool uniform, cudaStream_t s);

@@ -205,6 +205,8 @@ def _run_batch(a) -> None:
         ctxs[0].set_tuning("batch.transport", 1)
         if a.staged >= 0:
             ctxs[0].set_tuning("batch.staged", a.staged)
+        if a.zchunk > 0:
+            ctxs[0].set_tuning("batch.zchunk", a.zchunk)
         if a.autotune:
             print("batch autotune:", api.batch_autotune(ctxs, steps=20), flush=True)
         if a.warm:
@@ -212,7 +214,8 @@ def _run_batch(a) -> None:
         t0 = time.perf_counter()
         api.batch_heat_steps(ctxs, a.steps)
         dt = time.perf_counter() - t0
-        print(f"C4 batch (batch.staged {a.staged}): {len(ctxs)} instances, {nvox} voxels; {a.steps} batched steps "
+        print(f"C4 batch (batch.staged {a.staged}, batch.zchunk {a.zchunk}): {len(ctxs)} instances, {nvox} voxels; "
+              f"{a.steps} batched steps "
               f"after {a.warm}: "
               f"{dt * 1e3:.2f} ms = {nvox * a.steps / dt:.3e} voxel updates/s; "
               f"device errors {sum(c.device_errors() for c in ctxs)}", flush=True)
@@ -294,6 +297,7 @@ def parser():
     b.add_argument("--compare-mc", action="store_true", help="also time the passes with one launch per instance")
     b.add_argument("--staged", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
                    help="batched step form (batch.staged; -1: the library's default)")
+    b.add_argument("--zchunk", type=int, default=0, help="z planes per work item (batch.zchunk; 0: default)")
     v = sub.add_parser("vessels", help="configuration 5: MC transport on the vessel grid")
     v.add_argument("--scale", type=float, default=1.0, help="grid edge = 512 * scale")
     v.add_argument("--packets", type=int, default=10_000_000)
