@@ -248,9 +248,11 @@ int tam_get_tallies_ex(struct tam_ctx *ctx, double *out, int32_t n);
 int tam_get_state(struct tam_ctx *ctx, tam_state *st);
 
 /* Device time of the last hot calls, from CUDA events recorded on the
- * context's stream: the transport kernel of the last tam_mc_pass, and the
- * span of the last tam_heat_steps from its first to its last kernel, with the
- * number of heat kernels it launched. */
+ * context's stream: the transport kernel of the last MC pass (for a batched
+ * pass, the batched launch that carried it), and the span of the last run of
+ * heat steps from its first to its last kernel, with the number of heat
+ * kernels it launched (graph replays count their kernels).  In the coupled
+ * loops these are the last iteration's pass and steps. */
 int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, int64_t *heat_launches);
 /* Kernel tuning knobs (no reference counterpart; defaults are tuned for
  * GB300).  Keys: "transport.scat_min" (lanes of a warp that wait at an

@@ -327,12 +327,9 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
         }
         };
         for (;;) {
-            // two voxel steps per vote: the votes are a sizeable share of a
-            // step, and a lane that stops after the first step only idles
-            // for the second (its packet's walk does not depend on when the
-            // event batch runs)
-            vstep();
-            vstep();
+            // TAM_VSTEPS voxel steps per vote (transport_common.cuh)
+#pragma unroll
+            for (int q = 0; q < TAM_VSTEPS; ++q) vstep();
             sc = __ballot_sync(FULL, mode >= M_SCAT);
             fl = __ballot_sync(FULL, mode == M_FLY);
             if (fl == 0 || __popc(sc) >= scat_min || (!exhausted && (sc | fl) != FULL)) break;

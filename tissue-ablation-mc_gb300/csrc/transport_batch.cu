@@ -56,11 +56,14 @@ __global__ void __launch_bounds__(BTPB, 4)
     float cpv = 1, spv = 0;
     float tdx = 0, tdy = 0, tdz = 0, tmx = 0, tmy = 0, tmz = 0, t = 0;
     float w = 0, tau = 0, dep = 0;
-    uint32_t ev = 0, plo = 0, phi32 = 0, nsteps = 0, nscat = 0;
+    double *jm = nullptr;  // the lane's instance's tally
+    // voxel steps the packet may still take (its instance's cap counts down,
+    // so the per-step test needs no table lookup; steps taken = cap - left)
+    uint32_t ev = 0, plo = 0, phi32 = 0, left = 0, nscat = 0;
 
     // the packet's end: its counts go to its instance
     auto retire = [&]() {
-        atomicAdd(&s_cnt[inst][0], (unsigned long long)nsteps);
+        atomicAdd(&s_cnt[inst][0], (unsigned long long)(uint32_t)(s_in[inst].max_steps - left));
         atomicAdd(&s_cnt[inst][1], (unsigned long long)nscat);
         mode = M_DEAD;
     };
@@ -109,7 +112,8 @@ __global__ void __launch_bounds__(BTPB, 4)
                     cpv = cp;
                     spv = sp;
                     sint = 0.f;
-                    nsteps = 0;
+                    left = I.max_steps;
+                    jm = I.jmean;
                     nscat = 0;
                     if (!(X >= 0.f && X < I.w2x && Y >= 0.f && Y < I.w2y)) {
                         atomicAdd(I.tally + T_MISSED, 1.0);
@@ -150,8 +154,9 @@ __global__ void __launch_bounds__(BTPB, 4)
         unsigned sc, fl;
         auto vstep = [&]() {
             if (mode != M_FLY) return;
-            if (++nsteps > s_in[inst].max_steps) {
-                if (dep != 0.f) atomicAdd(s_in[inst].jmean + cidx, (double)dep);
+            if (left-- == 0u) {
+                // past the cap (left wraps: cap - left = cap + 1 steps, as the single pass counts)
+                if (dep != 0.f) atomicAdd(jm + cidx, (double)dep);
                 dep = 0.f;
                 atomicAdd(s_in[inst].tally + T_OVERFLOW, 1.0);
                 atomicOr(s_in[inst].err, (unsigned)DEVERR_STEP_CAP);
@@ -177,7 +182,7 @@ __global__ void __launch_bounds__(BTPB, 4)
             const int sg = cx ? sgx : (cy ? sgy : sgz);
             const int j = (cx ? ix : (cy ? iy : iz)) + sg;
             const int N = cx ? NX : (cy ? NY : NZ);
-            atomicAdd(s_in[inst].jmean + cidx, (double)dep);
+            atomicAdd(jm + cidx, (double)dep);
             dep = 0.f;
             if ((unsigned)j < (unsigned)N) {
                 ix = cx ? j : ix;
@@ -196,8 +201,8 @@ __global__ void __launch_bounds__(BTPB, 4)
             }
         };
         for (;;) {
-            vstep();
-            vstep();
+#pragma unroll
+            for (int q = 0; q < TAM_VSTEPS; ++q) vstep();
             sc = __ballot_sync(FULL, mode >= M_SCAT);
             fl = __ballot_sync(FULL, mode == M_FLY);
             if (fl == 0 || __popc(sc) >= scat_min || (!exhausted && (sc | fl) != FULL)) break;
@@ -284,7 +289,7 @@ __global__ void __launch_bounds__(BTPB, 4)
                     if (!die) mode = M_FLY;
                 }
                 if (die) {
-                    if (dep != 0.f) atomicAdd(I.jmean + cidx, (double)dep);
+                    if (dep != 0.f) atomicAdd(jm + cidx, (double)dep);
                     dep = 0.f;
                     retire();
                 }

@@ -161,6 +161,14 @@ template <typename Real> __device__ __forceinline__ Real clamp0h(Real f, Real h)
     return f < (Real)0 ? (Real)0 : (f > h ? h : f);
 }
 
+// Voxel steps per warp vote of the flight phase: the votes are a sizeable
+// share of a step, and a lane that stops early only idles for the rest (its
+// packet's walk does not depend on when the event batch runs).  Measured on
+// the 200^3 bench pass: 2 -> 190.5, 4 -> 193.5, 6 -> 189.9 Mphotons/s.
+#ifndef TAM_VSTEPS
+#define TAM_VSTEPS 4
+#endif
+
 enum : int { M_DEAD = 0, M_FLY = 1, M_SCAT = 2, M_FACE = 3 };  // M_SCAT, M_FACE: waiting for the event batch
 
 // Per-flight DDA set-up from the in-cell position f and direction n of one

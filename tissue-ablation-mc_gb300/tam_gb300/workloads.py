@@ -264,6 +264,24 @@ def _run_pulsed(a) -> None:
               f"{a.packets / (tr * 1e-3):.3e} photons/s; device errors {ctx.device_errors()}", flush=True)
 
 
+def _run_layers(a) -> None:
+    """Configuration 3's coupled loop at `scale`: `steps` outer iterations of
+    one heat step each, with the MC passes the re-trace rule asks for, timed
+    on the host clock (the call returns after the device has finished)."""
+    import time
+
+    w = c3(scale=a.scale, packets=a.packets, steps=a.steps)
+    with w.context() as ctx:
+        t0 = time.perf_counter()
+        ctx.step_coupled(a.steps, seed=a.seed)
+        dt = time.perf_counter() - t0
+        st = ctx.state()
+        T = ctx.download(api._abi.TAM_F_TEMP)
+        print(f"C3 three-layer slab {w.info['grid']}: {a.steps} heat steps of {st.delt:.3e} s (simulated "
+              f"{st.time:.2f} s), {st.mc_passes} MC passes of {a.packets} packets, {st.n_ablated} voxels ablated, "
+              f"max T {T.max():.1f} K; wall {dt:.2f} s; device errors {ctx.device_errors()}", flush=True)
+
+
 def _run_heat(a) -> None:
     """The heat step of the homogeneous cube (configuration 2 at edge 200):
     one MC pass for the absorbed-power field, then `steps` steps of each
@@ -303,6 +321,11 @@ def parser():
     v.add_argument("--packets", type=int, default=10_000_000)
     v.add_argument("--warm-packets", type=int, default=1_000_000)
     v.add_argument("--tally32", type=int, default=-1, choices=[-1, 0, 1])
+    q = sub.add_parser("layers", help="configuration 3: the coupled loop on the three-layer skin slab")
+    q.add_argument("--scale", type=float, default=1.0, help="grid 256 x 256 x 128 times scale")
+    q.add_argument("--packets", type=int, default=100_000_000, help="packets per MC pass")
+    q.add_argument("--steps", type=int, default=20_000, help="outer iterations (one heat step each)")
+    q.add_argument("--seed", type=int, default=1)
     r = sub.add_parser("pulsed", help="configuration 5: the whole pulsed coupled run on the vessel grid")
     r.add_argument("--scale", type=float, default=1.0, help="grid edge = 512 * scale")
     r.add_argument("--packets", type=int, default=1_000_000_000, help="packets per MC pass")
@@ -318,7 +341,8 @@ def parser():
 
 def main(argv=None) -> None:
     a = parser().parse_args(argv)
-    {"batch": _run_batch, "vessels": _run_vessels, "pulsed": _run_pulsed, "heat": _run_heat}[a.cmd](a)
+    {"batch": _run_batch, "vessels": _run_vessels, "layers": _run_layers, "pulsed": _run_pulsed,
+     "heat": _run_heat}[a.cmd](a)
 
 
 if __name__ == "__main__":
