@@ -224,5 +224,21 @@ module tam_gpu
             integer(c_int32_t), value :: n, steps, nchosen
             integer(c_int64_t), intent(out) :: chosen(*)
         end function
+        ! one MC pass of every instance; nphotons and streams may be c_null_ptr
+        ! (each context's nphotons x numproc, its count of passes)
+        integer(c_int) function tam_batch_mc_pass(ctxs, n, nphotons, seeds, streams) bind(C)
+            import
+            type(c_ptr), intent(in) :: ctxs(*)
+            integer(c_int32_t), value :: n
+            type(c_ptr), value :: nphotons
+            integer(c_int64_t), intent(in) :: seeds(*)
+            type(c_ptr), value :: streams
+        end function
+        integer(c_int) function tam_measure_tally_atomics(cells, fp32, per_second) bind(C)
+            import
+            integer(c_int64_t), value :: cells
+            integer(c_int32_t), value :: fp32
+            real(c_double), intent(out) :: per_second
+        end function
     end interface
 end module tam_gpu
