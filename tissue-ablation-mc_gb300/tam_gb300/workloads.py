@@ -100,9 +100,11 @@ def c3(scale=1.0, packets=100_000_000, steps=20_000):
     grid[:, :, nz - 1] = 1
     mats = [AIR, EPIDERMIS, DERMIS, SUBCUTIS]
     dt_steps = steps
+    # the laser stays on for the whole run: 2e4 steps of ~2.45 ms are ~49 s
+    # (a 60 s top-hat pulse at 5 W)
     p = api.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=0.5, ymax=0.5, zmax=0.25, mode=1, precision=1,
-                           nphotons=packets, pulse_type=1, power=5.0, energy_per_pixel=5.0 * 1e3, total_time=1.0,
-                           loops=1)
+                           nphotons=packets, pulse_type=1, power=5.0, energy_per_pixel=5.0 * 60.0 * 1e3,
+                           total_time=60.0, loops=1)
     c = _config(mats, retrace_fraction=1e-3, retrace_check=50)
     return Workload("C3 three-layer skin slab", p, c, grid, packets, dt_steps,
                     {"grid": (nx, ny, nz), "layers_cm": (0.01, 0.2, 0.29)})
