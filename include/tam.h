@@ -286,16 +286,18 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * ln A - Ea/RT in FP64, 0 (default) in float-float arithmetic, ~44 bits),
  * "batch.zchunk" (batched heat steps, read from the first context of the
  * batch: z planes per work item; 0 (default) uses each instance's
- * "heat.zchunk" if set, else 32; the slab form's items hold at most 32
- * planes),
+ * "heat.zchunk" if set, else 32; the slab form's items hold at most 128
+ * planes (batch.staged 4) or 32 (3)),
  * "batch.staged" (batched heat steps, read from the first context of the
- * batch: 3 (default) is the slab form -- each staged row the 16-byte chunks
- * that cover it, copied by all threads with cp.async, voxel pairs, boundary
- * faces as ghost neighbours, voxels needing rare work listed and handled
- * after each item's planes; 2 stages each tile's planes in shared memory with
- * 4-byte cp.async copies and updates two x-adjacent voxels per thread, 1 the
- * same with one voxel per thread, 0 reads neighbours with cached global
- * loads),
+ * batch: 4 (default) and 3 are the slab form -- each staged row the 16-byte
+ * chunks that cover it, copied by all threads with cp.async, voxel pairs,
+ * boundary faces as ghost neighbours; 4 launches one block per work item and
+ * step and handles the voxels needing rare work (boiling, damage window,
+ * ablation) in a second kernel over the step's list of them, 3 runs a chunk
+ * of steps in one cooperative launch and handles them after each item's
+ * planes; 2 stages each tile's planes in shared memory with 4-byte cp.async
+ * copies and updates two x-adjacent voxels per thread, 1 the same with one
+ * voxel per thread, 0 reads neighbours with cached global loads),
  * "batch.streams" (batched heat steps, read from the first context: 1 runs
  * each instance's own single-context steps on its own stream, issued
  * round-robin in chunks of 256 steps so the instances overlap, instead of
@@ -360,8 +362,8 @@ int tam_load_state(struct tam_ctx *ctx, const char *path);
 int tam_autotune(struct tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, int32_t nchosen);
 /* Autotuner of the batched heat step: times `steps` batched steps of the n
  * contexts (as tam_batch_heat_steps requires them) for each candidate form
- * and z-chunk length ("batch.staged" 3 with "batch.zchunk" 4..8, 2 or 1 with
- * 8..64), keeps the
+ * and z-chunk length ("batch.staged" 4 with "batch.zchunk" 16..64, 3 with
+ * 8..32, 2 or 1 with 8..64), keeps the
  * fastest on ctxs[0] (whose settings the batch reads) and puts every
  * instance's state back.  The candidates include the streams form
  * ("batch.streams" 1).  chosen (nullable): staged form, z-chunk, streams. */

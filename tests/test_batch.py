@@ -85,12 +85,13 @@ def _fp32_instance(tam, nx, ny, nz, layered, power):
 SHAPES = [(37, 29, 23, True, 1.0), (48, 40, 36, False, 2.0), (64, 20, 18, True, 3.0)]
 
 
-@pytest.mark.parametrize("streams,staged", [(0, 2), (1, 2), (0, 3)])
+@pytest.mark.parametrize("streams,staged", [(0, 2), (1, 2), (0, 3), (0, 4)])
 def test_batch_heat_steps_matches_single_contexts(tam, streams, staged):
-    # streams 0: the batched cooperative kernel (staged 2: 4-byte cp.async
-    # copies; 3: the slab form); 1: each instance's own single-context steps
-    # on its stream, issued round-robin (bit-identical to the single runs, so
-    # held to the same bound here)
+    # streams 0: the batched kernels (staged 2: 4-byte cp.async copies; 3:
+    # the slab form in one cooperative launch; 4: the slab form one launch per
+    # step with the rare voxels in a kernel of their own); 1: each instance's
+    # own single-context steps on its stream, issued round-robin
+    # (bit-identical to the single runs, so held to the same bound here)
     F = tam._abi
     want = []
     for shp in SHAPES:
@@ -180,7 +181,7 @@ def test_batch_staged_matches_cached_loads(tam, zchunk):
     # default
     F = tam._abi
     res = []
-    for staged in (0, 1, 2, 3):
+    for staged in (0, 1, 2, 3, 4):
         ctxs = [_fp32_instance(tam, *shp) for shp in SHAPES]
         try:
             for c in ctxs:
@@ -209,8 +210,8 @@ def test_batch_autotune_restores_state(tam):
         tam.batch_heat_steps(ctxs, 5)
         before = [(c.download(F.TAM_F_TEMP), c.download(F.TAM_F_TISSUE), c.state().time) for c in ctxs]
         chosen = tam.batch_autotune(ctxs, steps=8)
-        assert (chosen["batch.staged"], chosen["batch.zchunk"]) in [(3, 8), (3, 16), (3, 32), (2, 8), (2, 16), (2, 32),
-                                                                    (2, 64), (1, 16), (1, 32)]
+        assert (chosen["batch.staged"], chosen["batch.zchunk"]) in [(4, 16), (4, 32), (4, 64), (3, 8), (3, 16), (3, 32),
+                                                                    (2, 8), (2, 16), (2, 32), (2, 64), (1, 16), (1, 32)]
         assert chosen["batch.streams"] in (0, 1)
         for c, (T, om, t) in zip(ctxs, before):
             np.testing.assert_array_equal(c.download(F.TAM_F_TEMP), T)
@@ -400,8 +401,9 @@ def _hot_ctx(tam, nx, ny, nz, layered, precision):
     return ctx
 
 
+@pytest.mark.parametrize("staged", [3, 4])
 @pytest.mark.parametrize("which", ["mixed", "uniform"])
-def test_batch_slab_form_boils_and_ablates_like_fp64(tam, which):
+def test_batch_slab_form_boils_and_ablates_like_fp64(tam, which, staged):
     # the slab form of the batched step (rows of 45, 37 and 64 voxels: odd
     # rows leave a half pair at the x+ face) through boiling and ablation,
     # against each instance's own FP64 steps: the same ablated voxels, 1e-3 K
@@ -416,7 +418,7 @@ def test_batch_slab_form_boils_and_ablates_like_fp64(tam, which):
             want.append((T, ctx.download(F.TAM_F_TISSUE), ctx.download(F.TAM_F_Q), ctx.download(F.TAM_F_MATERIAL)))
     ctxs = [_hot_ctx(tam, *shp, 1) for shp in shapes]
     try:
-        ctxs[0].set_tuning("batch.staged", 3)
+        ctxs[0].set_tuning("batch.staged", staged)
         tam.batch_heat_steps(ctxs, 300)
         for ctx, (T, om, Q, mat) in zip(ctxs, want):
             assert ctx.device_errors() == 0

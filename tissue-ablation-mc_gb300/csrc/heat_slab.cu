@@ -348,7 +348,9 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
                 const float Ts = tt[j] - ee[j];
                 const bool general = (a.boil && tcv[j] >= a.fc[FC_TBOIL]) || !(Ts >= 0.f) ||
                                      ge_ff(tt[j], ee[j], a.fc[FC_TABL], a.fc[FC_TABL_LO]);
-                if (general) slab_fix<UNIFORM>(a, L, cls, cpitch, xx[j], yy[j], zz[j], Pdt, t_new, errbits);
+                if (general)
+                    slab_fix<UNIFORM>(a, L, cls, cpitch, xx[j], yy[j], zz[j], Pdt, t_new, errbits, (const float *)a.T_in,
+                                      a.Tc_in, (float *)a.T_out, a.Tc_out);
                 else if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, vv[j], ni, tt[j], ee[j], t_new, true, oo[j]);
             }
         }

@@ -12,14 +12,14 @@ namespace {
 // One listed voxel: the latent-heat clamp (src/3dFD.f90:169-175 in the
 // config-mode form; the stencil redone from global memory with its ghost
 // faces), the error word, then damage and ablation of the new temperature.
+// Ti / Ei: the step's input temperature and Kahan term; To / Eo: its output.
 template <bool UNIFORM>
 __device__ __noinline__ void slab_fix(const FusedArgs &a, const ClassLut &L, const uint8_t *cls, int cpitch, int x,
-                                      int y, int z, float Pdt, double t_new, unsigned &errbits)
+                                      int y, int z, float Pdt, double t_new, unsigned &errbits, const float *Ti,
+                                      const float *Ei, float *To, float *Eo)
 {
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const int64_t sy = nx, sz = (int64_t)nx * ny, ni = sz * nz, v = x + sy * y + sz * z;
-    const float *Ti = (const float *)a.T_in, *Ei = a.Tc_in;
-    float *To = (float *)a.T_out, *Eo = a.Tc_out;
     const float tc = Ti[v], e0 = Ei[v];
     float t = To[v], e = Eo[v];
     const int64_t cs = (int64_t)cpitch * ny;

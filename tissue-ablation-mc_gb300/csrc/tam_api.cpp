@@ -134,8 +134,8 @@ struct tam_ctx {
     tam::RefIterVals *d_iv = nullptr;
     cudaGraphExec_t rexec[4] = {nullptr, nullptr, nullptr, nullptr};  // by (temperature, rhokap) buffers read first
     std::vector<unsigned char> rkey[4];
-    int batch_staged = 3;            // batched steps: slab form (3), staged voxel pairs (2), staged voxels (1),
-                                     // cached loads (0)
+    int batch_staged = 4;            // batched steps: slab form one launch per step (4) or persistent (3),
+                                     // staged voxel pairs (2), staged voxels (1), cached loads (0)
     int batch_streams = 0;           // 1: batched steps as each instance's own steps on its stream, overlapped
     int batch_transport = 1;         // batched loops: the instances' uniform-medium passes in one launch
     int batch_zchunk = 0;            // batched steps: z planes per work item (0: heat.zchunk, else the default)
@@ -2210,10 +2210,12 @@ struct DevBatch {
     tam::BatchSync *d_sync = nullptr;
     unsigned *d_err = nullptr;
     TrTable tr;  // the batched transport's instance table
+    int *d_vox0 = nullptr;     // slab form, one launch per step: first voxel of each instance in the batch
+    unsigned *d_rare = nullptr, *d_rcnt = nullptr;  // ... its list of rare voxels and the list's length
     std::vector<tam::BatchInst> inst;
     std::vector<int> prefix;
     std::vector<tam::BatchStep> steps;
-    int blocks = 0, kmax = 0, staged = 1;
+    int blocks = 0, kmax = 0, staged = 1, zmax = 1;
     bool uniform = false;  // every instance one material class (the slab form's uniform kernel)
     ~DevBatch()
     {
@@ -2222,6 +2224,9 @@ struct DevBatch {
         cudaFree(d_steps);
         cudaFree(d_sync);
         cudaFree(d_err);
+        cudaFree(d_vox0);
+        cudaFree(d_rare);
+        cudaFree(d_rcnt);
     }
 };
 
@@ -2232,19 +2237,37 @@ int batch_setup(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int kmax)
     B.inst.resize(n);
     B.prefix.assign(n + 1, 0);
     B.staged = ctx->batch_staged;
-    const bool slab = B.staged == 3;
+    const bool slab = B.staged == 3 || B.staged == 4;
     B.uniform = true;
     for (int32_t i = 0; i < n; ++i) {
         int items = batch_inst(ctxs[i], B.inst[i], slab ? BATCH_SLAB_ZCHUNK : BATCH_ZCHUNK, ctx->batch_zchunk);
-        if (slab && B.inst[i].zchunk > tam::BATCH_SLAB_ZMAX)
-            items = batch_inst(ctxs[i], B.inst[i], BATCH_SLAB_ZCHUNK, tam::BATCH_SLAB_ZMAX);
+        const int zcap = B.staged == 4 ? tam::BATCH_STEP_ZMAX : tam::BATCH_SLAB_ZMAX;
+        if (slab && B.inst[i].zchunk > zcap) items = batch_inst(ctxs[i], B.inst[i], BATCH_SLAB_ZCHUNK, zcap);
         B.prefix[i + 1] = B.prefix[i] + items;
+        B.zmax = std::max(B.zmax, B.inst[i].zchunk);
         if (B.inst[i].L.uniform < 0) B.uniform = false;
     }
     B.kmax = kmax;
     B.steps.resize((size_t)kmax * n);
-    if (slab) CK(tam::batch_slab_blocks(&B.blocks, B.uniform));
-    else CK(tam::batch_heat_blocks(&B.blocks, B.staged));
+    if (B.staged == 4) {
+        // every voxel of the batch indexed from 0 (each voxel joins a step's list at most once)
+        std::vector<int> vox0(n + 1, 0);
+        int64_t tot = 0;
+        for (int32_t i = 0; i < n; ++i) {
+            vox0[i] = (int)tot;
+            tot += ctxs[i]->ni;
+            if (tot >= ((int64_t)1 << 31)) return fail(ctx, TAM_E_INVALID, "batch too large for batch.staged 4");
+        }
+        vox0[n] = (int)tot;
+        CK(cudaMalloc(&B.d_vox0, sizeof(int) * (n + 1)));
+        CK(cudaMalloc(&B.d_rare, sizeof(unsigned) * (size_t)std::max<int64_t>(tot, 1)));
+        CK(cudaMalloc(&B.d_rcnt, sizeof(unsigned)));
+        CK(cudaMemcpy(B.d_vox0, vox0.data(), sizeof(int) * (n + 1), cudaMemcpyHostToDevice));
+    } else if (slab) {
+        CK(tam::batch_slab_blocks(&B.blocks, B.uniform));
+    } else {
+        CK(tam::batch_heat_blocks(&B.blocks, B.staged));
+    }
     CK(cudaMalloc(&B.d_inst, sizeof(tam::BatchInst) * n));
     CK(cudaMalloc(&B.d_prefix, sizeof(int) * (n + 1)));
     CK(cudaMalloc(&B.d_steps, sizeof(tam::BatchStep) * B.steps.size()));
@@ -2283,7 +2306,10 @@ int batch_heat_chunk(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int K, const 
         if (ctxs[i]->stream != s) CK(cudaStreamSynchronize(ctxs[i]->stream));
     CK(cudaMemcpyAsync(B.d_inst, B.inst.data(), sizeof(tam::BatchInst) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(B.d_steps, B.steps.data(), sizeof(tam::BatchStep) * (size_t)K * n, cudaMemcpyHostToDevice, s));
-    if (B.staged == 3)
+    if (B.staged == 4)
+        CK(tam::launch_batch_slab_steps(B.d_inst, n, B.d_prefix, B.prefix[n], B.zmax, B.d_vox0, B.d_steps, K,
+                                        B.d_rare, B.d_rcnt, B.d_err, B.uniform, ctx->sm_count, s));
+    else if (B.staged == 3)
         CK(tam::launch_batch_slab(B.d_inst, n, B.d_prefix, B.d_steps, K, B.d_sync, B.d_err, B.blocks, B.uniform, s));
     else
         CK(tam::launch_batch_heat(B.d_inst, n, B.d_prefix, B.d_steps, K, B.d_sync, B.d_err, B.blocks, B.staged, s));
@@ -2639,7 +2665,7 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
         if (value < 0 || value > 1 << 20) return fail(ctx, TAM_E_INVALID, "batch.zchunk must be >= 0");
         ctx->batch_zchunk = (int)value;
     } else if (k == "batch.staged") {
-        if (value < 0 || value > 3) return fail(ctx, TAM_E_INVALID, "batch.staged must be 0, 1, 2 or 3");
+        if (value < 0 || value > 4) return fail(ctx, TAM_E_INVALID, "batch.staged must be in 0..4");
         ctx->batch_staged = (int)value;
     } else if (k == "batch.streams") {
         ctx->batch_streams = value != 0;
@@ -3036,7 +3062,7 @@ int tam_batch_autotune(tam_ctx *const *ctxs, int32_t n, int32_t steps, int64_t *
     struct Cand {
         int form, z;
     };
-    const Cand cands[] = {{3, 8}, {3, 16}, {3, 32}, {2, 8}, {2, 16}, {2, 32}, {2, 64}, {1, 16}, {1, 32}};
+    const Cand cands[] = {{4, 16}, {4, 32}, {4, 64}, {3, 8}, {3, 16}, {3, 32}, {2, 8}, {2, 16}, {2, 32}, {2, 64}, {1, 16}, {1, 32}};
     // on a failure the settings and every instance's state go back as they were
     auto undo = [&](int code) {
         ctx->batch_staged = form0;

@@ -345,6 +345,15 @@ constexpr int BATCH_SLAB_ZMAX = 32;
 cudaError_t batch_slab_blocks(int *blocks, bool uniform);
 cudaError_t launch_batch_slab(const BatchInst *insts, int n, const int *prefix, const BatchStep *steps, int K,
                               BatchSync *sync, unsigned *err, int blocks, bool uniform, cudaStream_t s);
+// The same step with one launch per step (batch.staged 4): a block per work
+// item (items = prefix[n]; zmax: the longest item's planes, at most
+// BATCH_STEP_ZMAX), then a kernel over the step's list of rare voxels (rare:
+// room for every voxel of the batch, as indices from vox0[i], the first voxel
+// of instance i; rare_cnt: the list's length, zeroed before each step).
+constexpr int BATCH_STEP_ZMAX = 128;
+cudaError_t launch_batch_slab_steps(const BatchInst *insts, int n, const int *prefix, int items, int zmax,
+                                    const int *vox0, const BatchStep *steps, int K, unsigned *rare,
+                                    unsigned *rare_cnt, unsigned *err, bool uniform, int sm_count, cudaStream_t s);
 // One step of one instance (inst: device copy of its BatchInst) by the staged
 // voxel-pair kernel, one block per work item (prefix = {0, items}); any row
 // pitch.  fcur selects the buffer pair read by the step.

@@ -315,7 +315,7 @@ def parser():
     b.add_argument("--steps", type=int, default=200, help="timed batched steps")
     b.add_argument("--autotune", action="store_true")
     b.add_argument("--compare-mc", action="store_true", help="also time the passes with one launch per instance")
-    b.add_argument("--staged", type=int, default=-1, choices=[-1, 0, 1, 2, 3],
+    b.add_argument("--staged", type=int, default=-1, choices=[-1, 0, 1, 2, 3, 4],
                    help="batched step form (batch.staged; -1: the library's default)")
     b.add_argument("--zchunk", type=int, default=0, help="z planes per work item (batch.zchunk; 0: default)")
     v = sub.add_parser("vessels", help="configuration 5: MC transport on the vessel grid")
