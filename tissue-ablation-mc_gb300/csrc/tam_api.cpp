@@ -2212,6 +2212,10 @@ struct DevBatch {
     TrTable tr;  // the batched transport's instance table
     int *d_vox0 = nullptr;     // slab form, one launch per step: first voxel of each instance in the batch
     unsigned *d_rare = nullptr, *d_rcnt = nullptr;  // ... its list of rare voxels and the list's length
+    // ... and a chunk's launches as a CUDA graph per chunk length, captured on
+    // a private stream (the context's stream may be the legacy default one)
+    cudaStream_t cap = nullptr;
+    std::vector<std::pair<int, cudaGraphExec_t>> graphs;
     std::vector<tam::BatchInst> inst;
     std::vector<int> prefix;
     std::vector<tam::BatchStep> steps;
@@ -2227,8 +2231,43 @@ struct DevBatch {
         cudaFree(d_vox0);
         cudaFree(d_rare);
         cudaFree(d_rcnt);
+        for (auto &g : graphs) cudaGraphExecDestroy(g.second);
+        if (cap) cudaStreamDestroy(cap);
     }
 };
+
+// The launches of a chunk of K steps of the per-step slab form, replayed from
+// a CUDA graph captured once per chunk length: the kernels read the chunk's
+// instance table and steps from device buffers refreshed before each chunk,
+// so the captured nodes never change.
+int batch_slab_graph(DevBatch &B, tam_ctx *ctx, int32_t n, int K, cudaStream_t s)
+{
+    for (auto &g : B.graphs)
+        if (g.first == K) {
+            CK(cudaGraphLaunch(g.second, s));
+            tam::count_launch(2 * K);
+            return TAM_OK;
+        }
+    if (!B.cap) CK(cudaStreamCreateWithFlags(&B.cap, cudaStreamNonBlocking));
+    CK(cudaStreamBeginCapture(B.cap, cudaStreamCaptureModeThreadLocal));
+    const int64_t l0 = tam::launch_count();
+    const cudaError_t e = tam::launch_batch_slab_steps(B.d_inst, n, B.d_prefix, B.prefix[n], B.zmax, B.d_vox0,
+                                                       B.d_steps, K, B.d_rare, B.d_rcnt, B.d_err, B.uniform,
+                                                       ctx->sm_count, B.cap);
+    cudaGraph_t g = nullptr;
+    const cudaError_t e2 = cudaStreamEndCapture(B.cap, &g);
+    tam::count_launch(-(int)(tam::launch_count() - l0));  // counted when replayed
+    CK(e);
+    CK(e2);
+    cudaGraphExec_t x = nullptr;
+    const cudaError_t e3 = cudaGraphInstantiate(&x, g, 0);
+    cudaGraphDestroy(g);
+    CK(e3);
+    B.graphs.emplace_back(K, x);
+    CK(cudaGraphLaunch(x, s));
+    tam::count_launch(2 * K);
+    return TAM_OK;
+}
 
 
 int batch_setup(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int kmax)
@@ -2307,8 +2346,7 @@ int batch_heat_chunk(DevBatch &B, tam_ctx *const *ctxs, int32_t n, int K, const 
     CK(cudaMemcpyAsync(B.d_inst, B.inst.data(), sizeof(tam::BatchInst) * n, cudaMemcpyHostToDevice, s));
     CK(cudaMemcpyAsync(B.d_steps, B.steps.data(), sizeof(tam::BatchStep) * (size_t)K * n, cudaMemcpyHostToDevice, s));
     if (B.staged == 4)
-        CK(tam::launch_batch_slab_steps(B.d_inst, n, B.d_prefix, B.prefix[n], B.zmax, B.d_vox0, B.d_steps, K,
-                                        B.d_rare, B.d_rcnt, B.d_err, B.uniform, ctx->sm_count, s));
+        RC(batch_slab_graph(B, ctx, n, K, s));
     else if (B.staged == 3)
         CK(tam::launch_batch_slab(B.d_inst, n, B.d_prefix, B.d_steps, K, B.d_sync, B.d_err, B.blocks, B.uniform, s));
     else
