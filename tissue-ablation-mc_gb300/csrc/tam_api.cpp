@@ -127,6 +127,7 @@ struct tam_ctx {
     cudaStream_t cap_stream = nullptr;       // capture stream (replays run on `stream`)
     tam::StepVals *d_sv = nullptr;           // the table
     cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // by the buffer pair the chunk reads first
+    int glaunches[2] = {0, 0};                       // kernels in each graph
     std::vector<unsigned char> gkey[2];      // what the graphs were captured with
     // reference-mode outer iterations replayed from CUDA graphs: chunks of
     // REF_GRAPH_ITERS iterations whose changing values come from a device table
@@ -985,12 +986,14 @@ bool graph_capture(tam_ctx *ctx, const tam::FusedArgs &a0, HeatForm form, int wh
         return false;
     }
     bool ok = true;
+    const int64_t l0 = tam::launch_count();
     for (int j = 0; j < GRAPH_STEPS && ok; ++j) {
         tam::FusedArgs a = a0;
         a.sv = ctx->d_sv + j;
         ok = launch_heat(ctx, a, form, (which + j) & 1, ctx->cap_stream) == TAM_OK;
     }
-    tam::count_launch(-GRAPH_STEPS);  // captured, not launched
+    ctx->glaunches[which] = (int)(tam::launch_count() - l0);
+    tam::count_launch(-ctx->glaunches[which]);  // captured, not launched; counted when replayed
     cudaGraph_t g = nullptr;
     const cudaError_t e = cudaStreamEndCapture(ctx->cap_stream, &g);
     ok = ok && e == cudaSuccess && g;
@@ -1064,7 +1067,7 @@ int cfg_heat(tam_ctx *ctx, int32_t nsteps, int32_t *done = nullptr, bool stop_on
             if (fits) {
                 CK(cudaMemcpyAsync(ctx->d_sv, tab, sizeof tab, cudaMemcpyHostToDevice, ctx->stream));  // pageable: copied now
                 CK(cudaGraphLaunch(ctx->gexec[which], ctx->stream));
-                tam::count_launch(GRAPH_STEPS);
+                tam::count_launch(ctx->glaunches[which]);
                 ctx->fcur = (ctx->fcur + GRAPH_STEPS) & 1;
                 it += GRAPH_STEPS;
                 if (due) RC(retrace_check(on));
