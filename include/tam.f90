@@ -58,6 +58,10 @@ module tam_gpu
             import
             type(tam_params), intent(out) :: p
         end function
+        ! config-mode extension file; cfg is c_loc of a tam_config buffer (the C struct)
+        integer(c_int) function tam_read_config(path, cfg) bind(C)
+            import; character(kind=c_char), intent(in) :: path(*); type(c_ptr), value :: cfg
+        end function
         integer(c_int) function tam_read_input_params(path, p) bind(C)
             import
             character(kind=c_char), intent(in) :: path(*)

@@ -179,6 +179,27 @@ int tam_config_default(tam_config *c);
  * Fields not in the file (grid, mode, ...) are left untouched.
  */
 int tam_read_input_params(const char *path, tam_params *p);
+/*
+ * Parse a config-mode extension file (the parameters input.params has no slot
+ * for; e.g. res/tissue.params beside it) into *c, which holds the values the
+ * file leaves out (start from tam_config_default).  One setting per line,
+ * '#' starts a comment:
+ *   nmat N
+ *   material I mua mus g n k rho c   (/cm, /cm, -, -, W/m/K, kg/m^3, J/kg/K;
+ *                                      raises nmat to I + 1 when needed)
+ *   source gaussian|disk   source_radius R   n_ambient N
+ *   fresnel 0|1   roulette 0|1   roulette_w W   roulette_m M   max_steps S
+ *   bc FACE dirichlet T=K   |   bc FACE robin h=H Tamb=K
+ *                                     (FACE: x- x+ y- y+ z- z+; z+ is the beam side)
+ *   T0 K   dt_factor F   dt S   opscale F   boil 0|1   T_boil K   lw J/kg
+ *   T_abl K   arrhenius 0|1   A 1/s   Ea J/mol   Rgas J/mol/K   T_lo K
+ *   T_hi K   thr O1 O2 O3   retrace_fraction F   retrace_check N
+ *   isolation 0|1
+ * TAM_E_IO if the file cannot be opened; TAM_E_PARSE (with "path:line: ..."
+ * from tam_last_error(NULL)) for an unknown key or a malformed value, in
+ * which case *c is left unchanged.
+ */
+int tam_read_config(const char *path, tam_config *c);
 
 /*
  * Create a context: allocates the device state and runs the initialisation

@@ -1260,6 +1260,126 @@ int tam_config_default(tam_config *c)
     return TAM_OK;
 }
 
+int tam_read_config(const char *path, tam_config *c)
+{
+    if (!path || !c) return fail(nullptr, TAM_E_INVALID, "null argument");
+    std::ifstream in(path);
+    if (!in) return fail(nullptr, TAM_E_IO, std::string("cannot open ") + path);
+    tam_config q = *c;
+    std::string line;
+    int lineno = 0;
+    auto bad = [&](const std::string &what) {
+        return fail(nullptr, TAM_E_PARSE, std::string(path) + ":" + std::to_string(lineno) + ": " + what);
+    };
+    auto num = [](const std::string &t, double &v) -> bool {
+        char *end = nullptr;
+        const double x = std::strtod(t.c_str(), &end);
+        if (t.empty() || *end != '\0') return false;
+        v = x;
+        return true;
+    };
+    auto inum = [](const std::string &t, long long &v) -> bool {
+        char *end = nullptr;
+        const long long x = std::strtoll(t.c_str(), &end, 10);
+        if (t.empty() || *end != '\0') return false;
+        v = x;
+        return true;
+    };
+    while (std::getline(in, line)) {
+        ++lineno;
+        const size_t hash = line.find('#');
+        if (hash != std::string::npos) line.resize(hash);
+        std::istringstream ls(line);
+        std::vector<std::string> w;
+        for (std::string t; ls >> t;) w.push_back(t);
+        if (w.empty()) continue;
+        const std::string &k = w[0];
+        const size_t na = w.size() - 1;
+        // scalar settings: key, destination, and whether it is an integer flag / count
+        struct D {
+            const char *key;
+            double *d;
+            int32_t *i;
+        };
+        const D scalars[] = {{"n_ambient", &q.n_ambient, nullptr}, {"source_radius", &q.source_radius, nullptr},
+                             {"fresnel", nullptr, &q.fresnel},      {"roulette", nullptr, &q.roulette},
+                             {"roulette_w", &q.roulette_w, nullptr}, {"roulette_m", &q.roulette_m, nullptr},
+                             {"T0", &q.T0, nullptr},                {"dt_factor", &q.dt_factor, nullptr},
+                             {"dt", &q.dt, nullptr},                {"opscale", &q.opscale, nullptr},
+                             {"boil", nullptr, &q.boil},            {"T_boil", &q.T_boil, nullptr},
+                             {"lw", &q.lw, nullptr},                {"T_abl", &q.T_abl, nullptr},
+                             {"arrhenius", nullptr, &q.arrhenius},  {"A", &q.A, nullptr},
+                             {"Ea", &q.Ea, nullptr},                {"Rgas", &q.Rgas, nullptr},
+                             {"T_lo", &q.T_lo, nullptr},            {"T_hi", &q.T_hi, nullptr},
+                             {"retrace_fraction", &q.retrace_fraction, nullptr},
+                             {"retrace_check", nullptr, &q.retrace_check},
+                             {"isolation", nullptr, &q.isolation}};
+        bool done = false;
+        for (const D &d : scalars) {
+            if (k != d.key) continue;
+            if (na != 1) return bad(k + " takes one value");
+            if (d.d) {
+                if (!num(w[1], *d.d)) return bad("malformed value for " + k);
+            } else {
+                long long v = 0;
+                if (!inum(w[1], v) || v < INT32_MIN || v > INT32_MAX) return bad("malformed integer for " + k);
+                *d.i = (int32_t)v;
+            }
+            done = true;
+            break;
+        }
+        if (done) continue;
+        if (k == "nmat") {
+            long long v = 0;
+            if (na != 1 || !inum(w[1], v) || v < 1 || v > TAM_MAX_MATERIALS)
+                return bad("nmat takes one count in 1.." + std::to_string(TAM_MAX_MATERIALS));
+            q.nmat = (int32_t)v;
+        } else if (k == "material") {
+            long long id = 0;
+            double v[7];
+            if (na != 8 || !inum(w[1], id) || id < 0 || id >= TAM_MAX_MATERIALS)
+                return bad("material takes an id in 0.." + std::to_string(TAM_MAX_MATERIALS - 1) +
+                           " and mua mus g n k rho c");
+            for (int j = 0; j < 7; ++j)
+                if (!num(w[2 + j], v[j])) return bad("malformed material value '" + w[2 + j] + "'");
+            q.mat[id] = tam_material{v[0], v[1], v[2], v[3], v[4], v[5], v[6]};
+            if (q.nmat < id + 1) q.nmat = (int32_t)(id + 1);
+        } else if (k == "source") {
+            if (na != 1 || (w[1] != "gaussian" && w[1] != "disk")) return bad("source is gaussian or disk");
+            q.source = w[1] == "gaussian" ? TAM_SRC_GAUSSIAN : TAM_SRC_DISK;
+        } else if (k == "max_steps") {
+            long long v = 0;
+            if (na != 1 || !inum(w[1], v) || v < 1) return bad("max_steps takes a positive count");
+            q.max_steps = v;
+        } else if (k == "thr") {
+            if (na != 3 || !num(w[1], q.thr[0]) || !num(w[2], q.thr[1]) || !num(w[3], q.thr[2]))
+                return bad("thr takes three damage thresholds");
+        } else if (k == "bc") {
+            static const char *faces[6] = {"x-", "x+", "y-", "y+", "z-", "z+"};
+            int f = -1;
+            for (int j = 0; j < 6 && na >= 2; ++j)
+                if (w[1] == faces[j]) f = j;
+            if (f < 0 || (w[2] != "dirichlet" && w[2] != "robin"))
+                return bad("bc takes a face (x- x+ y- y+ z- z+) and dirichlet or robin");
+            q.bc_type[f] = w[2] == "robin" ? TAM_BC_ROBIN : TAM_BC_DIRICHLET;
+            for (size_t j = 3; j < w.size(); ++j) {
+                const size_t eq = w[j].find('=');
+                const std::string key = eq == std::string::npos ? w[j] : w[j].substr(0, eq);
+                double v = 0.0;
+                if (eq == std::string::npos || !num(w[j].substr(eq + 1), v)) return bad("bc value '" + w[j] + "'");
+                if (key == "T") q.bc_T[f] = v;
+                else if (key == "h") q.bc_h[f] = v;
+                else if (key == "Tamb") q.bc_Tamb[f] = v;
+                else return bad("bc value '" + key + "' (T, h or Tamb)");
+            }
+        } else {
+            return bad("unknown setting '" + k + "'");
+        }
+    }
+    *c = q;
+    return TAM_OK;
+}
+
 int tam_read_input_params(const char *path, tam_params *p)
 {
     if (!path || !p) return fail(nullptr, TAM_E_INVALID, "null argument");

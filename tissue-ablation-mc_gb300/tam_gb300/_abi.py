@@ -106,6 +106,7 @@ SIGNATURES = [
     ("tam_params_default", C.c_int, [C.POINTER(Params)]),
     ("tam_config_default", C.c_int, [C.POINTER(Config)]),
     ("tam_read_input_params", C.c_int, [C.c_char_p, C.POINTER(Params)]),
+    ("tam_read_config", C.c_int, [C.c_char_p, C.POINTER(Config)]),
     ("tam_create", C.c_int, [C.POINTER(Params), C.POINTER(Config), C.POINTER(_P)]),
     ("tam_destroy", C.c_int, [_P]),
     ("tam_last_error", C.c_char_p, [_P]),

@@ -62,6 +62,14 @@ def read_input_params(path: str, base: Params | None = None) -> Params:
     return p
 
 
+def read_config(path: str, base: Config | None = None) -> Config:
+    """A config-mode extension file (tam_read_config) over `base` (default:
+    the library's defaults)."""
+    c = base if base is not None else default_config()
+    check(lib().tam_read_config(path.encode(), C.byref(c)))
+    return c
+
+
 def _dptr(a: np.ndarray):
     return a.ctypes.data_as(C.POINTER(C.c_double))
 
