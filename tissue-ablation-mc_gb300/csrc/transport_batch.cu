@@ -71,7 +71,7 @@ __global__ void __launch_bounds__(BTPB, 4)
     for (;;) {
         // ---------------------------------------------- refill dead lanes --
         const unsigned need = exhausted ? 0u : __ballot_sync(FULL, mode == M_DEAD);
-        if (need) {
+        if (need && (__popc(need) >= TAM_REFILL_MIN || need == FULL)) {
             const int leader = __ffs(need) - 1;
             unsigned long long base = 0;
             if ((int)lane == leader) base = atomicAdd(work, (unsigned long long)__popc(need));
@@ -205,7 +205,7 @@ __global__ void __launch_bounds__(BTPB, 4)
             for (int q = 0; q < TAM_VSTEPS; ++q) vstep();
             sc = __ballot_sync(FULL, mode >= M_SCAT);
             fl = __ballot_sync(FULL, mode == M_FLY);
-            if (fl == 0 || __popc(sc) >= scat_min || (!exhausted && (sc | fl) != FULL)) break;
+            if (fl == 0 || __popc(sc) >= scat_min || (!exhausted && __popc(~(sc | fl)) >= TAM_REFILL_MIN)) break;
         }
         if ((sc | fl) == 0) {
             if (exhausted) break;

@@ -169,6 +169,15 @@ template <typename Real> __device__ __forceinline__ Real clamp0h(Real f, Real h)
 #define TAM_VSTEPS 4
 #endif
 
+// Dead lanes of a warp that make it draw new packets: the launch code runs
+// for the dead lanes only, so refilling them together spends fewer of its
+// warp instructions per packet, while they idle in the flight phase meanwhile.
+// On the 200^3 bench pass: 1 -> 516.2, 2 -> 513.4, 4 -> 526.3, 8 -> 573.2 ms
+// per 1e8 packets.
+#ifndef TAM_REFILL_MIN
+#define TAM_REFILL_MIN 2
+#endif
+
 enum : int { M_DEAD = 0, M_FLY = 1, M_SCAT = 2, M_FACE = 3 };  // M_SCAT, M_FACE: waiting for the event batch
 
 // Per-flight DDA set-up from the in-cell position f and direction n of one
