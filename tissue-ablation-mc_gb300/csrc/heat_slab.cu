@@ -54,7 +54,12 @@ namespace {
 constexpr int SP = 16;          // voxel pairs per tile row
 constexpr int SW = 2 * SP;      // voxels per tile row
 constexpr int SR = 8;           // voxel rows per tile
-constexpr int SLAB_STAGES = 6;  // ring stages (prefetch depth SLAB_STAGES - 2 planes)
+// (5 or 4 stages with 8 blocks per SM, and 5 stages with 7, measured within
+// 1 % of 6 stages with 7 blocks on the 200^3 step)
+#ifndef TAM_SLAB_STAGES
+#define TAM_SLAB_STAGES 6
+#endif
+constexpr int SLAB_STAGES = TAM_SLAB_STAGES;  // ring stages (prefetch depth SLAB_STAGES - 2 planes)
 constexpr int SLAB_ZMAX = 8;    // planes per block at most (the list holds every voxel of a slab)
 
 template <bool UNIFORM> struct SlabLayout {
@@ -72,7 +77,10 @@ template <bool UNIFORM> struct SlabLayout {
     static_assert(LIST <= 65536, "local indices fit 16 bits");
 };
 
-constexpr int slab_minb(bool uniform) { return uniform ? 7 : 6; }
+#ifndef TAM_SLAB_MINB
+#define TAM_SLAB_MINB 7
+#endif
+constexpr int slab_minb(bool uniform) { return uniform ? TAM_SLAB_MINB : 6; }
 
 struct SlabMaps {
     CUtensorMap T, E, J, cls;
