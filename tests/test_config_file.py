@@ -4,6 +4,7 @@ boundaries, Arrhenius constants -- read from a file beside it.  Host-side
 parsing only: no GPU needed."""
 import math
 
+import numpy as np
 import pytest
 
 SKIN = """
@@ -102,3 +103,32 @@ def test_config_file_missing(tam, tmp_path):
     with pytest.raises(tam.TamError) as e:
         tam.read_config(str(tmp_path / "absent.params"))
     assert e.value.code == tam._abi.TAM_E_IO
+
+
+@pytest.mark.gpu
+def test_config_file_drives_a_run_like_the_same_struct(tam, tmp_path):
+    # a context built from the file runs exactly as one built from the same
+    # settings made in code (same Philox streams, same kernels)
+    F = tam._abi
+    text = ("nmat 3\nmaterial 1 1.0 200 0.8 1.4 0.21 1200 3590\nmaterial 2 0.3 120 0.9 1.4 0.37 1200 3300\n"
+            "source_radius 0.03\nbc z+ robin h=20 Tamb=295\nretrace_fraction 0\n")
+    c_file = tam.read_config(_write(tmp_path, text))
+    c_code = tam.default_config(nmat=3, source_radius=0.03, retrace_fraction=0.0)
+    tam.set_material(c_code, 1, 1.0, 200.0, 0.8, 1.4, 0.21, 1200.0, 3590.0)
+    tam.set_material(c_code, 2, 0.3, 120.0, 0.9, 1.4, 0.37, 1200.0, 3300.0)
+    c_code.bc_h[5], c_code.bc_Tamb[5] = 20.0, 295.0
+    assert bytes(c_file) == bytes(c_code)
+    out = []
+    for c in (c_file, c_code):
+        p = tam.default_params(nxg=24, nyg=24, nzg=16, xmax=0.06, ymax=0.06, zmax=0.04, mode=1, precision=0,
+                               nphotons=5000, pulse_type=1, power=2.0, energy_per_pixel=2e3, total_time=1.0, loops=1)
+        with tam.Context(p, c) as ctx:
+            grid = np.ones((24, 24, 16), dtype=np.uint8, order="F")
+            grid[:, :, 12:] = 2
+            ctx.upload(F.TAM_F_MATERIAL, grid)
+            ctx.step_coupled(20, seed=3)
+            out.append((ctx.download(F.TAM_F_TEMP), ctx.download(F.TAM_F_JMEAN), ctx.device_errors()))
+    (Ta, Ja, ea), (Tb, Jb, eb) = out
+    assert ea == eb == 0 and Ja.max() > 0
+    np.testing.assert_allclose(Ja, Jb, rtol=1e-9, atol=1e-9 * Jb.max())
+    np.testing.assert_allclose(Ta, Tb, rtol=1e-12)
