@@ -52,6 +52,30 @@ __host__ __device__ __forceinline__ U4 philox4x32_10(uint32_t c0, uint32_t c1, u
     return U4{c0, c1, c2, c3};
 }
 
+// The same generator with the ten round keys given (rk[2r], rk[2r + 1]: the
+// key of round r, i.e. the key plus r times the Weyl increments): from a
+// kernel parameter block they are constant-bank operands of the rounds'
+// XORs, and no round adds to the key.
+__device__ __forceinline__ U4 philox4x32_10_rk(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, const uint32_t *rk)
+{
+#pragma unroll
+    for (int r = 0; r < 10; ++r) {
+        const uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+        const uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+        const uint32_t n0 = hi1 ^ c1 ^ rk[2 * r], n2 = hi0 ^ c3 ^ rk[2 * r + 1];
+        c0 = n0; c1 = lo1; c2 = n2; c3 = lo0;
+    }
+    return U4{c0, c1, c2, c3};
+}
+__host__ __device__ inline void philox_round_keys(uint64_t seed, uint32_t *rk)
+{
+    uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+    for (int r = 0; r < 10; ++r, k0 += 0x9E3779B9u, k1 += 0xBB67AE85u) {
+        rk[2 * r] = k0;
+        rk[2 * r + 1] = k1;
+    }
+}
+
 template <typename Real> struct Uniform;
 // FP64: u = (x + 0.5) 2^-32, exact in (0,1).
 template <> struct Uniform<double> {

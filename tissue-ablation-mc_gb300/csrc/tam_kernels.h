@@ -87,6 +87,7 @@ struct TransportArgs {
     unsigned *err;                    // device error word
     TrConst<double> cd;               // filled by launch_transport
     TrConst<float> cf;
+    uint32_t rk[20];                  // Philox round keys of `seed`, filled by launch_transport
 };
 
 // One instance of a batched FP32 transport pass (config mode, a uniform

@@ -94,7 +94,7 @@ template <typename Real> __device__ __forceinline__ const TrConst<Real> &consts(
 }
 
 template <typename Real, int MED, bool T32>
-__global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) transport_kernel(const TransportArgs a, int scat_min)
+__global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) transport_kernel(const __grid_constant__ TransportArgs a, int scat_min)
 {
     __shared__ MatR<Real> lut[MAX_MAT];
     for (int t = threadIdx.x; t < MAX_MAT; t += blockDim.x) {
@@ -125,7 +125,6 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
     // after a crossing the next face along the crossed axis is (h - nudge)
     // away along the axis: tm advances by td * (1 - nudge / h)
     const Real knx = K.knx, kny = K.kny, knz = K.knz;
-    const uint32_t k0 = (uint32_t)a.seed, k1 = (uint32_t)(a.seed >> 32);
     const uint32_t strm = a.stream_dev ? *a.stream_dev : a.stream;
     const unsigned lane = threadIdx.x & 31u;
     const Real wmin = K.wmin, rm = K.rm, inv_rm = K.inv_rm;
@@ -180,7 +179,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                     const uint64_t pid = (uint64_t)a.p0 + my;
                     plo = (uint32_t)pid;
                     phi32 = (uint32_t)(pid >> 32);
-                    const U4 r = philox4x32_10(0u, plo, phi32, strm, k0, k1);
+                    const U4 r = philox4x32_10_rk(0u, plo, phi32, strm, a.rk);
                     ev = 1;
                     const Real u0 = Uniform<Real>::from(r.x), u1 = Uniform<Real>::from(r.y);
                     const Real u2 = Uniform<Real>::from(r.z), u3 = Uniform<Real>::from(r.w);
@@ -349,7 +348,7 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
                 if (!face) w *= MED == MED_RHOKAP ? (Real)0 : lut[mid].alb;
                 bool die = !face && !(w > (Real)0);
                 U4 r{0u, 0u, 0u, 0u};
-                if (!die) r = philox4x32_10(ev++, plo, phi32, strm, k0, k1);
+                if (!die) r = philox4x32_10_rk(ev++, plo, phi32, strm, a.rk);
                 if (face) {
                     const bool cx = fax == 0, cy = fax == 1;
                     const Real nc = cx ? nx : (cy ? ny : nz);
@@ -621,6 +620,7 @@ cudaError_t launch_transport(const TransportArgs &args, bool fp64, int sm_count,
     if (args.n <= 0) return cudaSuccess;
     TransportArgs a = args;
     fill_consts(a);
+    philox_round_keys(a.seed, a.rk);
     cudaError_t e = cudaMemsetAsync(a.work, 0, sizeof(unsigned long long), s);
     if (e != cudaSuccess) return e;
     if (fp64) {
