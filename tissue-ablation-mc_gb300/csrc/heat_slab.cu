@@ -9,7 +9,7 @@
 //  * a block owns a tile of 32 x 8 voxels and marches it through a slab of
 //    z planes; every thread updates two x-adjacent voxels (64-bit shared
 //    loads and global stores), and the z neighbours travel in registers;
-//  * one elected thread streams each plane into a ring of SLAB_STAGES
+//  * one elected thread streams each plane into a ring of 5-6
 //    shared-memory stages with cp.async.bulk.tensor (TMA): T and the Kahan
 //    term with a one-voxel x / y halo, J of the tile's own voxels, and for
 //    heterogeneous grids the u8 class ids with halo.  One block barrier and
@@ -59,10 +59,17 @@ constexpr int SR = 8;           // voxel rows per tile
 #ifndef TAM_SLAB_STAGES
 #define TAM_SLAB_STAGES 6
 #endif
-constexpr int SLAB_STAGES = TAM_SLAB_STAGES;  // ring stages (prefetch depth SLAB_STAGES - 2 planes)
+constexpr int SLAB_STAGES = TAM_SLAB_STAGES;  // ring stages of the one-class kernel (prefetch depth stages - 2 planes)
 constexpr int SLAB_ZMAX = 8;    // planes per block at most (the list holds every voxel of a slab)
 
+// The class-grid kernel (80 registers at 6 blocks per SM, its stages 640 B
+// larger) runs 5 stages at 7 blocks per SM: 679 against 710 us per step on
+// the 512^3 vessel grid, 4.0 % less at 256^3; 4 stages at 8 blocks, 682 us.
+#ifndef TAM_SLAB_STAGES_CLS
+#define TAM_SLAB_STAGES_CLS 5
+#endif
 template <bool UNIFORM> struct SlabLayout {
+    static constexpr int NST = UNIFORM ? SLAB_STAGES : TAM_SLAB_STAGES_CLS;  // ring stages
     static constexpr int TP = SW + 8;                        // staged T / Kahan row: x from the tile origin - 4
     static constexpr int CP = 64;                            // staged class row (u8) from the tile origin - 16
     static constexpr int H_BYTES = (((SR + 2) * TP * 4 + 127) / 128) * 128;  // T or Kahan term with halo
@@ -72,7 +79,7 @@ template <bool UNIFORM> struct SlabLayout {
     static constexpr int STAGE = ((C_OFF + (UNIFORM ? 0 : C_BYTES) + 127) / 128) * 128;
     static constexpr uint32_t TX_H = 2 * (SR + 2) * TP * 4, TX_J = J_BYTES, TX_C = (SR + 2) * CP;
     static constexpr int LIST = SW * SR * SLAB_ZMAX;         // list entries (u16 local indices)
-    static constexpr int SMEM = SLAB_STAGES * STAGE + SLAB_STAGES * 8 + LIST * 2 + 16 + 128;
+    static constexpr int SMEM = NST * STAGE + NST * 8 + LIST * 2 + 16 + 128;
     static_assert(J_BYTES % 128 == 0, "own-voxel array keeps 128-byte stage alignment");
     static_assert(LIST <= 65536, "local indices fit 16 bits");
 };
@@ -80,7 +87,10 @@ template <bool UNIFORM> struct SlabLayout {
 #ifndef TAM_SLAB_MINB
 #define TAM_SLAB_MINB 7
 #endif
-constexpr int slab_minb(bool uniform) { return uniform ? TAM_SLAB_MINB : 6; }
+#ifndef TAM_SLAB_MINB_CLS
+#define TAM_SLAB_MINB_CLS 7
+#endif
+constexpr int slab_minb(bool uniform) { return uniform ? TAM_SLAB_MINB : TAM_SLAB_MINB_CLS; }
 
 struct SlabMaps {
     CUtensorMap T, E, J, cls;
@@ -94,13 +104,13 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
                      const __grid_constant__ ClassLut L, const uint8_t *cls, int cpitch, int zchunk, float rare_thr)
 {
     using Lay = SlabLayout<UNIFORM>;
-    constexpr int TP = Lay::TP, CP = Lay::CP;
+    constexpr int TP = Lay::TP, CP = Lay::CP, NST = Lay::NST;
     extern __shared__ unsigned char smem_raw[];
     __shared__ float s_fa[UNIFORM ? 1 : MAX_MAT * MAX_MAT];
     unsigned char *sm = smem_raw + ((128 - (su32(smem_raw) & 127)) & 127);
-    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + SLAB_STAGES * Lay::STAGE);
-    unsigned short *list = reinterpret_cast<unsigned short *>(sm + SLAB_STAGES * Lay::STAGE + SLAB_STAGES * 8);
-    int *s_cnt = reinterpret_cast<int *>(sm + SLAB_STAGES * Lay::STAGE + SLAB_STAGES * 8 + Lay::LIST * 2);
+    uint64_t *bar = reinterpret_cast<uint64_t *>(sm + NST * Lay::STAGE);
+    unsigned short *list = reinterpret_cast<unsigned short *>(sm + NST * Lay::STAGE + NST * 8);
+    int *s_cnt = reinterpret_cast<int *>(sm + NST * Lay::STAGE + NST * 8 + Lay::LIST * 2);
     const int tid = threadIdx.x;
     const int r = tid / SP, p = tid % SP;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
@@ -131,8 +141,8 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
         for (int t = tid; t < MAX_MAT * MAX_MAT; t += SP * SR) s_fa[t] = L.fa[t];
 
     auto issue = [&](int idx) {
-        unsigned char *b = sm + (idx % SLAB_STAGES) * Lay::STAGE;
-        uint64_t *br = bar + (idx % SLAB_STAGES);
+        unsigned char *b = sm + (idx % NST) * Lay::STAGE;
+        uint64_t *br = bar + (idx % NST);
         const int zz = z0 - 1 + idx;
         const bool own = idx >= 1 && idx <= nplanes;  // the halo planes need no J
         fence_proxy_async();
@@ -144,15 +154,15 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     };
 
     if (leader) {
-        for (int s = 0; s < SLAB_STAGES; ++s) mbar_init(bar + s, 1);
+        for (int s = 0; s < NST; ++s) mbar_init(bar + s, 1);
         *s_cnt = 0;
         fence_mbar_init();
         fence_proxy_async();
     }
     __syncthreads();
     if (leader)
-        for (int idx = 0; idx < SLAB_STAGES && idx <= last; ++idx) issue(idx);
-    int issued = SLAB_STAGES < last + 1 ? SLAB_STAGES : last + 1;
+        for (int idx = 0; idx < NST && idx <= last; ++idx) issue(idx);
+    int issued = NST < last + 1 ? NST : last + 1;
     bool ok = mbar_wait(bar, 0) && mbar_wait(bar + 1, 0);
     const int qT = (r + 1) * TP + 4 + 2 * p;   // the pair in the staged T / Kahan rows (even: 8-byte aligned)
     const int qO = r * SW + 2 * p;             // ... in the own-voxel J
@@ -181,14 +191,14 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
         // every thread is done with the stages of plane i - 1: stage i is free
         ok = __syncthreads_and(ok) != 0;
         if (!ok) break;
-        if (i + SLAB_STAGES <= last) {
-            if (leader) issue(i + SLAB_STAGES);
-            issued = i + SLAB_STAGES + 1;
+        if (i + NST <= last) {
+            if (leader) issue(i + NST);
+            issued = i + NST + 1;
         }
         ok = mbar_wait(bar + s2, ph2);
         const unsigned char *S = sm + s1 * Lay::STAGE, *N = sm + s2 * Lay::STAGE;
         s1 = s2;
-        if (++s2 == SLAB_STAGES) {
+        if (++s2 == NST) {
             s2 = 0;
             ph2 ^= 1u;
         }
@@ -315,8 +325,8 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     unsigned errbits = 0;
     if (!ok) {
         errbits |= DEVERR_SYNC_TIMEOUT;
-        for (int idx = issued > SLAB_STAGES ? issued - SLAB_STAGES : 0; idx < issued; ++idx)
-            (void)mbar_wait(bar + (idx % SLAB_STAGES), (uint32_t)((idx / SLAB_STAGES) & 1));
+        for (int idx = issued > NST ? issued - NST : 0; idx < issued; ++idx)
+            (void)mbar_wait(bar + (idx % NST), (uint32_t)((idx / NST) & 1));
     } else {
         // the listed voxels; this block's own plane stores come first.  Most
         // of them are in the damage window only: their pairs and damage

@@ -285,11 +285,15 @@ def _run_layers(a) -> None:
 
 
 def _run_heat(a) -> None:
-    """The heat step of the homogeneous cube (configuration 2 at edge 200):
-    one MC pass for the absorbed-power field, then `steps` steps of each
-    requested form launched one by one (no graph replay), timed with the
+    """The heat step of the homogeneous cube (configuration 2 at edge 200), or
+    of configuration 5's vessel grid (edge 512 at scale 1: the class-table
+    kernel): one MC pass for the absorbed-power field, then `steps` steps of
+    each requested form launched one by one (no graph replay), timed with the
     library's CUDA events; the form used by profiles of the heat kernels."""
-    w = homogeneous(a.edge, a.packets, 2.0, 2.0, precision=1)
+    if a.geometry == "vessels":
+        w = c5(scale=a.edge / 512.0, packets=a.packets)
+    else:
+        w = homogeneous(a.edge, a.packets, 2.0, 2.0, precision=1)
     with w.context() as ctx:
         ctx.mc_pass(a.packets, seed=1)
         ctx.set_tuning("heat.graph", 0)
@@ -333,11 +337,13 @@ def parser():
     r.add_argument("--packets", type=int, default=1_000_000_000, help="packets per MC pass")
     r.add_argument("--steps", type=int, default=100_000, help="heat steps over the 10 pulses")
     r.add_argument("--seed", type=int, default=1)
-    h = sub.add_parser("heat", help="the homogeneous cube's FP32 heat step, one launch per step")
+    h = sub.add_parser("heat", help="the FP32 heat step (cube or vessel grid), one launch per step")
     h.add_argument("--edge", type=int, default=200)
     h.add_argument("--packets", type=int, default=1_000_000)
     h.add_argument("--steps", type=int, default=4)
     h.add_argument("--forms", default="slab,pair", help="comma list of slab / pair")
+    h.add_argument("--geometry", default="cube", choices=["cube", "vessels"],
+                   help="the homogeneous cube, or configuration 5's vessels and inclusions at this edge")
     return ap
 
 
