@@ -18,7 +18,9 @@ e2e     : the same through the C ABI with pinned host buffers: every step
           temperature, damage and the absorbed-power field.
 roofline: the dominant kernel (transport): 12 B per voxel step (rhokap /
           material read + FP64 tally read-modify-write) against the measured
-          HBM copy bandwidth; the stencil's 36 B per voxel update likewise.
+          HBM copy bandwidth; the stencil's 20 B moved per voxel update
+          likewise (and the fixed 36 B definition), on the 200^3 step and on
+          a 512^3 cube (roofline_stencil_512, 64 steps; --no-scale skips it).
 
 --impl reference runs the CPU oracle (the C restatement of the reference,
 OpenMP on all host cores) on bounded samples of the same workload, scaled to
@@ -320,6 +322,35 @@ def run_gpu(args):
                 sec = ev0.elapsed_time(ev1) * 1e-3
                 c1[name] = {"seconds": sec, "photons_per_s": w.packets / sec, "heat_steps": w.heat_steps}
 
+    # ---- the same stencil kernel at scale: a 512^3 cube (134 M voxels, 2.7 GB moved per step) ----
+    big = None
+    if rank == 0 and not args.no_scale:
+        from tam_gb300 import workloads
+
+        edge, nbig = 512, 64
+        w = workloads.homogeneous(edge, 1_000_000, 2.0, 2.0, precision=tam._abi.TAM_FP32)
+        w.params.device = local
+        with w.context() as cb:
+            cb.set_stream(stream.cuda_stream)
+            cb.mc_pass(w.packets, seed=SEED, stream=3)
+            cb.heat_steps(32)    # warm-up: the chunk graphs are captured here
+            cb.heat_steps(nbig)  # replayed from CUDA graphs, timed with the library's CUDA events
+            _, hb, _ = cb.timing()
+            errs = cb.device_errors()
+        vb = edge ** 3
+        big = {
+            "workload": f"{edge}^3 homogeneous cube (2 W beam, 1e6-packet source), {nbig} heat steps after 32",
+            "kernel": "slab_step_kernel<uniform>",
+            "us_per_step": hb * 1e3 / nbig,
+            "voxel_updates_per_s": vb * nbig / (hb * 1e-3),
+            "achieved": B_STENCIL_CLS * vb * nbig / (hb * 1e-3) / 1e9,
+            "peak": hbm,
+            "unit": "GB/s",
+            "frac": B_STENCIL_CLS * vb * nbig / (hb * 1e-3) / 1e9 / hbm,
+            "bytes_per_unit": f"{B_STENCIL_CLS:g} B per voxel update moved",
+            "device_errors": errs,
+        }
+
     # ---- CPU baseline (oracle port, all host cores, in a fresh process) ----
     cpu = None
     if rank == 0 and not args.no_cpu:
@@ -400,6 +431,7 @@ def run_gpu(args):
             },
             "peak_kind": peak_kind,
         },
+        "roofline_stencil_512": big,
         "e2e": {"value": e2e_val, "unit": "photons/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": launches,
         "clocks": clk_s,
@@ -631,6 +663,7 @@ def main():
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-c1", action="store_true", help="skip the full run of configuration 1")
+    ap.add_argument("--no-scale", action="store_true", help="skip the 512^3 stencil measurement")
     ap.add_argument("--cpu-leg", action="store_true", help=argparse.SUPPRESS)
     ap.add_argument("--cpu-c1", action="store_true", help=argparse.SUPPRESS)
     args = ap.parse_args()
