@@ -79,6 +79,8 @@ def test_config_file_keeps_what_it_leaves_out(tam, tmp_path):
 @pytest.mark.parametrize("text,what", [
     ("colour blue\n", "unknown setting 'colour'"),
     ("T0 hot\n", "malformed value for T0"),
+    ("T0 nan\n", "malformed value for T0"),
+    ("material 2 0.3 inf 0.9 1.4 0.37 1200 3300\n", "malformed material value 'inf'"),
     ("material 16 0 0 0 1 1 1 1\n", "material takes an id"),
     ("material 2 0.3 100\n", "material takes an id"),
     ("bc top robin h=10\n", "bc takes a face"),
@@ -97,6 +99,14 @@ def test_config_file_errors_name_the_line(tam, tmp_path, text, what):
     assert e.value.code == F.TAM_E_PARSE
     assert f"{path}:3: {what}" in str(e.value)
     assert bytes(base) == before  # left unchanged
+
+
+def test_config_file_crlf_tabs_and_comments(tam, tmp_path):
+    # a file saved on Windows with tabs between fields reads like the plain one
+    plain = tam.read_config(_write(tmp_path, SKIN))
+    dos = SKIN.replace(" ", "\t").replace("\n", "\r\n")
+    c = tam.read_config(_write(tmp_path, "   # leading comment\r\n" + dos, "dos.params"))
+    assert bytes(c) == bytes(plain)
 
 
 def test_config_file_missing(tam, tmp_path):

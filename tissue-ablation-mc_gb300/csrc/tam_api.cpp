@@ -1274,7 +1274,7 @@ int tam_read_config(const char *path, tam_config *c)
     auto num = [](const std::string &t, double &v) -> bool {
         char *end = nullptr;
         const double x = std::strtod(t.c_str(), &end);
-        if (t.empty() || *end != '\0') return false;
+        if (t.empty() || *end != '\0' || !std::isfinite(x)) return false;
         v = x;
         return true;
     };
