@@ -657,6 +657,55 @@ def test_slab_step_matches_pair_step_and_fp64(tam, nx, layered):
     assert np.abs(out["slab"][1] - om).max() <= 1e-3 * max(om.max(), 1e-30)
 
 
+def test_slab_one_class_blocks_follow_material_changes(tam, tmp_path):
+    # blocks whose tile, rim and planes hold one class take the one-class
+    # update, decided from per-(tile, plane) flags of the class grid: after a
+    # new material grid is uploaded, and after a state file with another grid
+    # is loaded, the flags must describe the new grid.  The slab form (flags)
+    # against the voxel-pair form (no flags) on the same steps, 1e-4 K; a
+    # stale flag would apply one class's coefficients across an interface.
+    nx, ny, nz = 64, 40, 36
+    mats = [(0.026, 1.2, 1005.0), (0.56, 1070.0, 3400.0), (0.21, 911.0, 2348.0), (0.47, 1090.0, 3421.0)]
+    ga = np.ones((nx, ny, nz), dtype=np.uint8, order="F")
+    ga[:, :, 12:24] = 2
+    gb = np.ones((nx, ny, nz), dtype=np.uint8, order="F")
+    gb[:, 20:, :] = 3
+    gb[40:50, :12, 5:30] = 2
+    rng = np.random.default_rng(5)
+    J = np.asfortranarray(rng.uniform(0, 1, (nx, ny, nz)) ** 2 * 2e9)
+    d = 5e-5
+    alpha = max(k / (r * c) for k, r, c in mats[1:])
+    dt = 0.9 / (2 * alpha * 3 / d ** 2)
+    ckpt = str(tmp_path / "a.state")
+    out = {}
+    for name, slab, rows in (("slab", 1, 0), ("pair", 0, 0)):
+        ctx = _layered_heat_ctx(tam, nx, ny, nz, 1, 1, dt, J, ga, mats, rows, 1, slab)
+        ctx.heat_steps(40)
+        if name == "slab":
+            ctx.save_state(ckpt)          # grid A
+        ctx.upload(F.TAM_F_MATERIAL, gb)  # grid B: other interfaces
+        ctx.upload(F.TAM_F_JMEAN_GLOBAL, J)
+        tb = ctx.heat_steps(40, want=True)
+        out[name] = (tb, ctx.device_errors())
+        ctx.close()
+    assert out["slab"][1] == 0 and out["pair"][1] == 0
+    assert np.abs(out["slab"][0] - out["pair"][0]).max() <= 1e-4
+    # a context holding grid B loads the state of grid A: its steps must equal
+    # those of a context that never left grid A
+    res = []
+    for src in ("loaded", "straight"):
+        ctx = _layered_heat_ctx(tam, nx, ny, nz, 1, 1, dt, J, gb if src == "loaded" else ga, mats, 0, 1, 1)
+        if src == "loaded":
+            ctx.heat_steps(3)
+            ctx.load_state(ckpt)
+        else:
+            ctx.heat_steps(40)
+        res.append((ctx.heat_steps(40, want=True), ctx.device_errors()))
+        ctx.close()
+    assert res[0][1] == 0 and res[1][1] == 0
+    np.testing.assert_array_equal(res[0][0], res[1][0])
+
+
 def test_fused_class_table_off_after_per_voxel_properties(tam):
     # uploading k per voxel switches the FP32 step to the coefficient arrays
     nx, ny, nz = 32, 24, 20

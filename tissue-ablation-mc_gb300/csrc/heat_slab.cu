@@ -35,7 +35,9 @@
 //  * the slabs are launched from the top face down: the beam enters there,
 //    so the blocks with the longest lists start first instead of forming the
 //    launch's tail.
+#include <algorithm>
 #include <atomic>
+#include <type_traits>
 
 #include "heat_common.cuh"
 #include "slab_common.cuh"
@@ -47,6 +49,8 @@ struct FusedSlab {
     CUtensorMap T[2], E[2], J, cls;
     const uint8_t *cls_grid;  // the class grid (rows of cls_pitch bytes) for the fix-up pass
     int cls_pitch;
+    int nx, ny, nz;
+    uint8_t *tflag;           // per (tile, plane): the one class of the tile and its x / y rim, or 0xFF
 };
 
 namespace {
@@ -101,7 +105,8 @@ __device__ __forceinline__ float2 lds2(const float *p) { return *reinterpret_cas
 template <bool UNIFORM>
 __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     slab_step_kernel(const __grid_constant__ FusedArgs a, const __grid_constant__ SlabMaps m,
-                     const __grid_constant__ ClassLut L, const uint8_t *cls, int cpitch, int zchunk, float rare_thr)
+                     const __grid_constant__ ClassLut L, const uint8_t *cls, int cpitch, int zchunk, float rare_thr,
+                     const uint8_t *tflag)
 {
     using Lay = SlabLayout<UNIFORM>;
     constexpr int TP = Lay::TP, CP = Lay::CP, NST = Lay::NST;
@@ -129,9 +134,6 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     // face coefficients with dt folded in
     const float cxd = a.fc[FC_DT] * a.fc[FC_CX], cyd = a.fc[FC_DT] * a.fc[FC_CY], czd = a.fc[FC_DT] * a.fc[FC_CZ];
     const int uc = L.uniform >= 0 ? L.uniform : 0;
-    const float au = L.fa[uc * MAX_MAT + uc];
-    const float Cx = cxd * au, Cy = cyd * au, Cz = czd * au, C6 = 2.f * ((Cx + Cy) + Cz);
-    const float Ku = Pdt * L.irc[uc];
     // boundary faces of the pair in x / y: x- of the first voxel, x+ of the
     // second, y- and y+ of both
     const unsigned exy = (unsigned)(x == 0) | (unsigned)(x + 1 == nx - 1) << 1 | (unsigned)(y == 0) << 2 |
@@ -163,25 +165,44 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     if (leader)
         for (int idx = 0; idx < NST && idx <= last; ++idx) issue(idx);
     int issued = NST < last + 1 ? NST : last + 1;
+    // heterogeneous grids: a block whose tile, x / y rim and planes z0 - 1 ..
+    // z1 all hold one class (the tile flags) takes the one-class update with
+    // that class's coefficients, without class lookups
+    int blk = -1;
+    if (!UNIFORM && tflag) {
+        const uint8_t *tf = tflag + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * nz;
+        const int za = max(z0 - 1, 0), zb = min(z1, nz - 1);
+        blk = __ldg(tf + za);
+        for (int zz = za + 1; zz <= zb; ++zz)
+            if (__ldg(tf + zz) != blk) blk = 0xFF;
+        if (blk == 0xFF) blk = -1;
+    }
+    const int kb = blk >= 0 ? blk : uc;  // the class of a one-class block
+    const float au = L.fa[kb * MAX_MAT + kb];
+    const float Cx = cxd * au, Cy = cyd * au, Cz = czd * au, C6 = 2.f * ((Cx + Cy) + Cz);
+    const float Ku = Pdt * L.irc[kb];
     bool ok = mbar_wait(bar, 0) && mbar_wait(bar + 1, 0);
     const int qT = (r + 1) * TP + 4 + 2 * p;   // the pair in the staged T / Kahan rows (even: 8-byte aligned)
     const int qO = r * SW + 2 * p;             // ... in the own-voxel J
     const int qC = (r + 1) * CP + 16 + 2 * p;  // ... in the class rows (even)
-    float2 Tp = {0.f, 0.f}, Tc = {0.f, 0.f}, Ep = {0.f, 0.f}, Ec = {0.f, 0.f};
-    int kp0 = uc, kp1 = uc, kc0 = uc, kc1 = uc;
     auto cls2 = [&](const unsigned char *b, int i, int &k0, int &k1) {
         const unsigned short w = *reinterpret_cast<const unsigned short *>(b + Lay::C_OFF + i);
         k0 = w & (MAX_MAT - 1);
         k1 = (w >> 8) & (MAX_MAT - 1);
     };
+    // the plane loop, for the class lookups (U false) or one class (U true)
+    auto run = [&](auto one_class) {
+    constexpr bool U = decltype(one_class)::value;
+    float2 Tp = {0.f, 0.f}, Tc = {0.f, 0.f}, Ep = {0.f, 0.f}, Ec = {0.f, 0.f};
+    int kp0 = kb, kp1 = kb, kc0 = kb, kc1 = kb;
     if (ok && act) {
         Tc = lds2((const float *)(sm + Lay::STAGE + Lay::T_OFF) + qT);
         Ec = lds2((const float *)(sm + Lay::STAGE + Lay::E_OFF) + qT);
-        if (!UNIFORM) cls2(sm + Lay::STAGE, qC, kc0, kc1);
+        if (!U) cls2(sm + Lay::STAGE, qC, kc0, kc1);
         if (z0 > 0) {
             Tp = lds2((const float *)(sm + Lay::T_OFF) + qT);
             Ep = lds2((const float *)(sm + Lay::E_OFF) + qT);
-            if (!UNIFORM) cls2(sm, qC, kp0, kp1);
+            if (!U) cls2(sm, qC, kp0, kp1);
         }
     }
     float *To = (float *)a.T_out + (x + nx * y + sz * z0), *Eo = a.Tc_out + (x + nx * y + sz * z0);
@@ -213,20 +234,20 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
                 const float2 g = ghost_pair(a, 0, Tc.x, Ec.x, L.k[kc0]);
                 WT[qT - 1] = g.x;
                 WE[qT - 1] = g.y;
-                if (!UNIFORM) WC[qC - 1] = (unsigned char)kc0;
+                if (!U) WC[qC - 1] = (unsigned char)kc0;
             }
             if (exy & 2u) {
                 const float2 g = ghost_pair(a, 1, Tc.y, Ec.y, L.k[kc1]);
                 WT[qT + 2] = g.x;
                 WE[qT + 2] = g.y;
-                if (!UNIFORM) WC[qC + 2] = (unsigned char)kc1;
+                if (!U) WC[qC + 2] = (unsigned char)kc1;
             }
             if (exy & 12u) {
                 const int f = (exy & 4u) ? 2 : 3, o = (exy & 4u) ? -TP : TP, oc = (exy & 4u) ? -CP : CP;
                 const float2 g0 = ghost_pair(a, f, Tc.x, Ec.x, L.k[kc0]), g1 = ghost_pair(a, f, Tc.y, Ec.y, L.k[kc1]);
                 *reinterpret_cast<float2 *>(WT + qT + o) = make_float2(g0.x, g1.x);
                 *reinterpret_cast<float2 *>(WE + qT + o) = make_float2(g0.y, g1.y);
-                if (!UNIFORM) {
+                if (!U) {
                     WC[qC + oc] = (unsigned char)kc0;
                     WC[qC + 1 + oc] = (unsigned char)kc1;
                 }
@@ -238,8 +259,8 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
         const float2 eym = lds2(SE + qT - TP), eyp = lds2(SE + qT + TP);
         const float txl = ST[qT - 1], txr = ST[qT + 2], exl = SE[qT - 1], exr = SE[qT + 2];
         const float2 j2 = lds2((const float *)(S + Lay::J_OFF) + qO);
-        int kn0 = uc, kn1 = uc;
-        if (!UNIFORM) cls2(N, qC, kn0, kn1);
+        int kn0 = kb, kn1 = kb;
+        if (!U) cls2(N, qC, kn0, kn1);
         // ghost neighbours of the z boundary planes (registers only)
         float2 Tpz = Tp, Epz = Ep;
         int kpz0 = kp0, kpz1 = kp1;
@@ -269,7 +290,7 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
             const float eyM = h ? eym.y : eym.x, eyP = h ? eyp.y : eyp.x;
             const float tzM = h ? Tpz.y : Tpz.x, tzP = h ? Tnz.y : Tnz.x, ezM = h ? Epz.y : Epz.x, ezP = h ? Enz.y : Enz.x;
             float dT;
-            if (UNIFORM) {
+            if (U) {
                 // sum over the faces of C_f [(T_f - T_c) - (e_f - e_c)]
                 const float sx = ((txm - tc) + (txp - tc)) - (exm + exp_);
                 const float sy = ((tyM - tc) + (tyP - tc)) - (eyM + eyP);
@@ -289,7 +310,7 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
                       (aym * ((tyM - tc) - (eyM - e0)) + ayp * ((tyP - tc) - (eyP - e0)))) +
                      (axm * ((txm - tc) - (exm - e0)) + axp * ((txp - tc) - (exp_ - e0)));
             }
-            const float Kk = UNIFORM ? Ku : Pdt * L.irc[h ? kc1 : kc0];
+            const float Kk = U ? Ku : Pdt * L.irc[h ? kc1 : kc0];
             const float inc = __fmaf_rn(Kk, h ? j2.y : j2.x, dT);
             const float yk = inc - e0;
             const float t = tc + yk;
@@ -313,12 +334,19 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
         Tc = Tn;
         Ep = Ec;
         Ec = En;
-        if (!UNIFORM) {
+        if (!U) {
             kp0 = kc0;
             kp1 = kc1;
             kc0 = kn0;
             kc1 = kn1;
         }
+    }
+    };
+    if constexpr (UNIFORM) {
+        run(std::true_type{});
+    } else {
+        if (blk >= 0) run(std::true_type{});
+        else run(std::false_type{});
     }
     // the last plane's wait may have failed in some threads only: agree first
     ok = __syncthreads_and(ok) != 0;
@@ -378,7 +406,7 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
 
 template <bool UNIFORM>
 cudaError_t launch_slab_t(const FusedArgs &a, const SlabMaps &m, const ClassLut &L, const uint8_t *cls, int cpitch,
-                          float rare_thr, cudaStream_t s)
+                          float rare_thr, const uint8_t *tflag, cudaStream_t s)
 {
     const int bx = (a.nx + SW - 1) / SW, by = (a.ny + SR - 1) / SR;
     int zchunk = a.zchunk > 0 ? a.zchunk : 6;  // measured fastest at 200^3 (37.7 us against 38.4 at 5, 40.6 at 8)
@@ -397,11 +425,54 @@ cudaError_t launch_slab_t(const FusedArgs &a, const SlabMaps &m, const ClassLut 
         attr_set.fetch_or(bit);
     }
     count_launch();
-    slab_step_kernel<UNIFORM><<<dim3(bx, by, chunks), SP * SR, smem, s>>>(a, m, L, cls, cpitch, zchunk, rare_thr);
+    slab_step_kernel<UNIFORM><<<dim3(bx, by, chunks), SP * SR, smem, s>>>(a, m, L, cls, cpitch, zchunk, rare_thr, tflag);
     return cudaGetLastError();
 }
 
+// The slab kernel's tile flags: for every (tile, plane), the class that all
+// voxels of the 32 x 8 tile and of its one-voxel x / y rim (inside the grid)
+// hold, or 0xFF when they differ.  One warp per (tile, plane): each lane
+// takes one x column of the rim rows and of the tile rows, lanes 0 and 1 the
+// rim columns, and the warp compares its lanes' smallest and largest class.
+__global__ void slab_tile_flags_kernel(const uint8_t *cls, int pitch, int nx, int ny, int nz, uint8_t *flags)
+{
+    const int tx = (nx + SW - 1) / SW, ty = (ny + SR - 1) / SR;
+    const int64_t items = (int64_t)tx * ty * nz;
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t it = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; it < items; it += nw) {
+        // it = (z * ty + tile row) * tx + tile column: neighbouring warps read neighbouring tiles
+        const int txi = (int)(it % tx);
+        const int64_t rest = it / tx;
+        const int tyi = (int)(rest % ty), z = (int)(rest / ty);
+        const int bx = txi * SW, by = tyi * SR;
+        const uint8_t *pl = cls + (int64_t)pitch * ny * z;
+        int cmin = 255, cmax = -1;
+        auto take = [&](int xx, int yy) {
+            if (xx < 0 || xx >= nx || yy < 0 || yy >= ny) return;
+            const int c = pl[(int64_t)pitch * yy + xx] & (MAX_MAT - 1);
+            cmin = min(cmin, c);
+            cmax = max(cmax, c);
+        };
+        for (int yy = by - 1; yy <= by + SR; ++yy) take(bx + lane, yy);
+        if (lane < 2)
+            for (int yy = by; yy < by + SR; ++yy) take(lane ? bx + SW : bx - 1, yy);
+        cmin = __reduce_min_sync(0xffffffffu, cmin);
+        cmax = __reduce_max_sync(0xffffffffu, cmax);
+        if (lane == 0) flags[((int64_t)tyi * tx + txi) * nz + z] = (uint8_t)(cmin == cmax ? cmin : 0xFF);
+    }
+}
+
 }  // namespace
+
+cudaError_t fused_slab_tile_flags(const FusedSlab *m, cudaStream_t s)
+{
+    const int64_t items = (int64_t)((m->nx + SW - 1) / SW) * ((m->ny + SR - 1) / SR) * m->nz;
+    const int64_t blocks = std::min<int64_t>((items + 7) / 8, 152 * 32);
+    count_launch();
+    slab_tile_flags_kernel<<<(unsigned)blocks, 256, 0, s>>>(m->cls_grid, m->cls_pitch, m->nx, m->ny, m->nz, m->tflag);
+    return cudaGetLastError();
+}
 
 bool fused_slab_supported(int nx, int ny, int nz)
 {
@@ -418,13 +489,22 @@ cudaError_t fused_slab_create(FusedSlab **out, int nx, int ny, int nz, float *co
     FusedSlab *m = new FusedSlab();
     m->cls_grid = cls;
     m->cls_pitch = pitch;
+    m->nx = nx;
+    m->ny = ny;
+    m->nz = nz;
+    m->tflag = nullptr;
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
         e = encode(&m->T[b], T[b], nx, ny, nz, SW + 8, SR + 2);
         if (e == cudaSuccess) e = encode(&m->E[b], Tc[b], nx, ny, nz, SW + 8, SR + 2);
     }
     if (e == cudaSuccess) e = encode(&m->J, J, nx, ny, nz, SW, SR);
     if (e == cudaSuccess) e = encode_u8(&m->cls, cls, pitch, ny, nz, SlabLayout<false>::CP, SR + 2);
+    // tile flags: none one-class until fused_slab_tile_flags has run on the class grid
+    const size_t nflag = (size_t)((nx + SW - 1) / SW) * ((ny + SR - 1) / SR) * nz;
+    if (e == cudaSuccess) e = cudaMalloc(&m->tflag, nflag);
+    if (e == cudaSuccess) e = cudaMemset(m->tflag, 0xFF, nflag);
     if (e != cudaSuccess) {
+        if (m->tflag) cudaFree(m->tflag);
         delete m;
         return e;
     }
@@ -432,7 +512,11 @@ cudaError_t fused_slab_create(FusedSlab **out, int nx, int ny, int nz, float *co
     return cudaSuccess;
 }
 
-void fused_slab_destroy(FusedSlab *m) { delete m; }
+void fused_slab_destroy(FusedSlab *m)
+{
+    if (m && m->tflag) cudaFree(m->tflag);
+    delete m;
+}
 
 cudaError_t launch_fused_slab(const FusedArgs &a0, const FusedSlab *sm, int which, const ClassLut &L, cudaStream_t s)
 {
@@ -446,8 +530,8 @@ cudaError_t launch_fused_slab(const FusedArgs &a0, const FusedSlab *sm, int whic
     // one screen for the listed rare work: damage / ablation, and boiling
     float rare_thr = a.fc[FC_SCREEN];
     if (a.boil && a.fc[FC_TBOIL] < rare_thr) rare_thr = a.fc[FC_TBOIL];
-    return L.uniform >= 0 ? launch_slab_t<true>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, s)
-                          : launch_slab_t<false>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, s);
+    return L.uniform >= 0 ? launch_slab_t<true>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, nullptr, s)
+                          : launch_slab_t<false>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, sm->tflag, s);
 }
 
 }  // namespace tam

@@ -438,6 +438,7 @@ int set_thermal_classes(tam_ctx *ctx, int u)
     ctx->thermal_by_class = true;
     if (ctx->d_cls)
         CK(tam::launch_cls_from_mat(ctx->d_mat, nm, ctx->d_cls, ctx->nx, ctx->ny, ctx->nz, ctx->cls_pitch, ctx->stream));
+    if (ctx->d_cls && ctx->fslab) CK(tam::fused_slab_tile_flags(ctx->fslab, ctx->stream));
     return TAM_OK;
 }
 
@@ -3023,6 +3024,8 @@ int tam_load_state(tam_ctx *ctx, const char *path)
         if (!f) return fail(ctx, TAM_E_PARSE, "state file truncated");
         CK(cudaMemcpy(b.first, host.data(), n, cudaMemcpyHostToDevice));
     }
+    // the slab form's tile flags follow the class grid just loaded
+    if (ctx->config && ctx->d_cls && ctx->fslab) CK(tam::fused_slab_tile_flags(ctx->fslab, ctx->stream));
     set_scalars(ctx, S);
     std::memcpy(ctx->tally, tally, sizeof tally);
     ctx->tally_stale = false;

@@ -307,6 +307,10 @@ bool fused_slab_supported(int nx, int ny, int nz);
 cudaError_t fused_slab_create(FusedSlab **out, int nx, int ny, int nz, float *const T[2], float *const Tc[2],
                               const float *J, const uint8_t *cls, int pitch);
 void fused_slab_destroy(FusedSlab *m);
+// Recompute the slab form's per-(tile, plane) one-class flags from the class
+// grid given at creation (after every change of that grid); until the first
+// call no tile counts as one-class.
+cudaError_t fused_slab_tile_flags(const FusedSlab *m, cudaStream_t s);
 cudaError_t launch_fused_slab(const FusedArgs &a, const FusedSlab *m, int which, const ClassLut &L, cudaStream_t s);
 
 // Batched FP32 heat step of many instances in one persistent cooperative
