@@ -285,7 +285,11 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * = 96 MB: larger grids get a box of that many cells centred on the beam axis
  * and reaching down from the top face, whose deposits are tallied in FP32;
  * deposits outside it go to the FP64 jmean directly; FP64 contexts use the
- * FP32 tally only with "transport.tally32" 1), "heat.zchunk" (z planes per
+ * FP32 tally only with "transport.tally32" 1), "transport.bricks" (config-mode
+ * transport on a heterogeneous grid: -1 (default) looks the cells' materials
+ * up through a table of 8 x 8 x 8 bricks -- the one material of a brick, or
+ * the grid itself inside mixed bricks -- for grids of 2^25 voxels or more, 0
+ * never, 1 always; same walks either way), "heat.zchunk" (z planes per
  * thread column of the fused step, 0 = automatic), "heat.tma" (1: stage the
  * FP32 fused step's planes with TMA where the row pitch allows, 0: cp.async),
  * "heat.cls" (1: while the thermal properties are those of the material

@@ -809,6 +809,74 @@ def test_fp32_tally_flushed_matches_fp64_tally(tam, layered, box):
         assert Ja[~inside].sum() > 0.1 * Ja.sum() and Ja[inside].sum() > 0.1 * Ja.sum()
 
 
+def _brick_grid(nx, ny, nz):
+    # one-material bricks (background, a layer), mixed bricks (a tilted
+    # cylinder, layer edges off the brick boundaries), partial bricks at the
+    # grid's far faces (edges not multiples of 8)
+    g = np.full((nx, ny, nz), 3, dtype=np.uint8, order="F")
+    g[:, :, nz - 5:] = 1
+    g[:, :, 9:nz - 5] = 2
+    X, Y, Z = np.meshgrid(np.arange(nx), np.arange(ny), np.arange(nz), indexing="ij")
+    g[((X - 0.6 * Z - 6) ** 2 + (Y - ny / 2) ** 2) < 9.0] = 1
+    return g
+
+
+def test_brick_table_fp64_transport_matches_oracle(tam, orc):
+    # the transport's material lookups through the 8^3 brick table (forced on
+    # for a small grid) against the oracle, which reads the grid cell by cell,
+    # on the same Philox streams: identical walks
+    mats = [(0.0, 0.0, 0.0, 1.0), (1.0, 200.0, 0.8, 1.4), (0.3, 120.0, 0.9, 1.4), (0.1, 80.0, 0.9, 1.4)]
+    nx, ny, nz = 36, 30, 28
+    ctx, d = cfg_pair(tam, orc, nx, ny, nz, 0.2, mats=mats, radius=0.06)
+    grid = _brick_grid(nx, ny, nz)
+    ctx.upload(F.TAM_F_MATERIAL, grid)
+    ctx.set_tuning("transport.bricks", 1)
+    npk = 20000
+    ctx.mc_pass(npk, seed=9, stream=4)
+    J = ctx.download(F.TAM_F_JMEAN)
+    t = ctx.tallies()
+    Jo, to = orc.mc_transport(d, grid, npk, seed=9, stream=4, nthreads=0)
+    assert ctx.device_errors() == 0
+    assert t["scatters"] == to["scatters"] and t["voxel_steps"] == to["voxel_steps"]
+    assert np.abs(J - Jo).sum() / np.abs(Jo).sum() < 1e-9
+    ctx.close()
+
+
+def test_brick_table_follows_material_changes(tam):
+    # FP32 transport with the brick table on and off, same streams: the same
+    # walks (step and scatter counts equal, tallies to the order of the FP64
+    # atomic sums), on a grid with ids beyond the material table (read as 0,
+    # a whole brick of id 255 included), then again after the grid changed
+    # (the table is rebuilt for every pass)
+    nx, ny, nz = 44, 40, 34
+    half = 0.0025 * nx
+    p = tam.default_params(nxg=nx, nyg=ny, nzg=nz, xmax=half, ymax=half * ny / nx, zmax=half * nz / nx, mode=1,
+                           precision=1, nphotons=50000)
+    c = tam.default_config(source_radius=0.03, nmat=4)
+    tam.set_material(c, 1, 1.0, 200.0, 0.8, 1.4, 0.56, 1070.0, 3400.0)
+    tam.set_material(c, 2, 0.3, 120.0, 0.9, 1.4, 0.56, 1070.0, 3400.0)
+    tam.set_material(c, 3, 0.1, 80.0, 0.9, 1.4, 0.56, 1070.0, 3400.0)
+    g1 = _brick_grid(nx, ny, nz)
+    g1[16:24, 8:16, 8:16] = 255
+    g1[3, 30, 20] = 200
+    g2 = g1.copy()
+    g2[10:30, 5:35, nz - 8:] = 0  # a crater at the top, as ablation leaves it
+    out = []
+    for bricks in (0, 1):
+        with tam.Context(p, c) as ctx:
+            ctx.set_tuning("transport.bricks", bricks)
+            res = []
+            for g, seed in ((g1, 3), (g2, 4)):
+                ctx.upload(F.TAM_F_MATERIAL, g)
+                J = ctx.mc_pass(50000, seed=seed, stream=1, want=True)
+                res.append((J, ctx.tallies(), ctx.device_errors()))
+            out.append(res)
+    for (Ja, ta, ea), (Jb, tb, eb) in zip(*out):
+        assert ea == eb == 0
+        assert ta["voxel_steps"] == tb["voxel_steps"] and ta["scatters"] == tb["scatters"]
+        assert np.abs(Ja - Jb).sum() / np.abs(Ja).sum() < 1e-9
+
+
 def test_box_tally_fp64_transport_matches_oracle(tam, orc):
     # the FP32 box tally on the FP64 transport (a 16 x 16 x 12 box under the
     # beam of a 32^3 layered grid) against the oracle on the same Philox

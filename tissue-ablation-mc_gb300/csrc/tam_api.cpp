@@ -105,10 +105,13 @@ struct tam_ctx {
     // tuning knobs
     int scat_min = 20;
     int tally32 = -1;                // FP32 transport: -1 auto (FP32 tally when the FP64 one exceeds 256 MB), 0 off, 1 on
+    int bricks = -1;                 // material lookups through the brick table: -1 auto (grids of 2^25 voxels
+                                     // and more), 0 off, 1 on
     int64_t tally32_chunk = (int64_t)1 << 24;  // packets per flush of the FP32 tally (each launch ends in a tail)
     int64_t tally32_box = (int64_t)24 << 20;   // cells of the FP32 box tally at most (96 MB: L2-resident)
     int64_t j32_cells = 0;                     // cells allocated for the FP32 box tally
     float *d_j32 = nullptr;
+    uint8_t *d_btab = nullptr;       // brick table of the material grid (transport on large grids)
     int zchunk = 0;
     bool use_tma = true;
     tam::FusedTma *tma = nullptr;  // tensor maps of the FP32 fused step
@@ -610,6 +613,17 @@ int pass_args(tam_ctx *ctx, int64_t n, uint64_t seed, uint32_t stream, tam::Tran
         CK(cudaStreamSynchronize(s));
         if ((long long)nab != ctx->nabl_at_uniform) ctx->uniform_id = -1;
         a.uniform_id = ctx->uniform_id;
+    }
+    // a heterogeneous grid too large for L2 next to its tally: the cells'
+    // material ids come from the brick table where a brick holds one material
+    // (rebuilt here, since heat steps may have ablated voxels since the last pass)
+    if (ctx->config && a.uniform_id < 0 &&
+        (ctx->bricks > 0 || (ctx->bricks < 0 && ctx->ni >= ((int64_t)1 << 25)))) {
+        if (!ctx->d_btab) RC(dalloc_t(ctx, &ctx->d_btab, tam::brick_table_size(ctx->nx, ctx->ny, ctx->nz)));
+        CK(tam::launch_brick_table(ctx->d_mat, ctx->nx, ctx->ny, ctx->nz, ctx->d_btab, s));
+        a.btab = ctx->d_btab;
+        a.bbx = (ctx->nx + 7) / 8;
+        a.bby = (ctx->ny + 7) / 8;
     }
     a.seed = seed;
     a.stream = stream;
@@ -2804,6 +2818,9 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
     } else if (k == "transport.tally32") {
         if (value < -1 || value > 1) return fail(ctx, TAM_E_INVALID, "transport.tally32 must be -1 (auto), 0 or 1");
         ctx->tally32 = (int)value;
+    } else if (k == "transport.bricks") {
+        if (value < -1 || value > 1) return fail(ctx, TAM_E_INVALID, "transport.bricks must be -1 (auto), 0 or 1");
+        ctx->bricks = (int)value;
     } else if (k == "transport.tally32_box") {
         if (value < 1) return fail(ctx, TAM_E_INVALID, "transport.tally32_box must be positive");
         ctx->tally32_box = value;

@@ -61,6 +61,8 @@ struct TransportArgs {
     int32_t medium;                   // Medium
     const double *rhokap;             // halo (nx+2)(ny+2)(nz+2), MED_RHOKAP
     const uint8_t *mat;               // interior nx*ny*nz, MED_MATERIAL
+    const uint8_t *btab;              // MED_MATERIAL, nullable: per 8^3 brick its one material id, or 0xFF
+    int32_t bbx, bby;                 // bricks along x and y
     int32_t nmat;
     OptMat lut[MAX_MAT];
     double rhokap_n;                  // refractive index of the rhokap medium
@@ -120,6 +122,11 @@ cudaError_t launch_batch_transport(const BatchTrInst *insts, int n, int64_t tota
 
 // Launch the transport kernel in FP32 (fp64 == false) or FP64.
 cudaError_t launch_transport(const TransportArgs &a, bool fp64, int sm_count, cudaStream_t s);
+// Brick table of a material grid for the transport's cell lookups: for every
+// 8 x 8 x 8 brick (bricks ceil(n / 8) per axis, x fastest) the material id all
+// its voxels inside the grid hold, or 0xFF.
+int64_t brick_table_size(int nx, int ny, int nz);
+cudaError_t launch_brick_table(const uint8_t *mat, int nx, int ny, int nz, uint8_t *btab, cudaStream_t s);
 
 // acc[cell of q] += (double)part[q], part[q] = 0 for the bnx x bny x bnz box
 // of cells starting at (bx0, by0, bz0) in an nx x ny grid (flush of the

@@ -14,6 +14,8 @@
 // Philox4x32-10 with counter {event, packet_lo, packet_hi, stream}.
 #include <curand_philox4x32_x.h>
 
+#include <algorithm>
+
 #include "tam_device.cuh"
 #include "tam_kernels.h"
 #include "transport_common.cuh"
@@ -61,7 +63,16 @@ __device__ __forceinline__ void fetch(const TransportArgs &a, const MatR<Real> *
         mua = v;
         mid = 0;
     } else if (MED == MED_MATERIAL) {
-        int id = __ldg(a.mat + cidx);
+        // large grids: most cells lie in bricks of one material, whose id the
+        // small (L2- and mostly L1-resident) brick table holds; the material
+        // grid itself is read only inside mixed bricks
+        int id;
+        if (a.btab) {
+            id = __ldg(a.btab + ((ix >> 3) + a.bbx * ((iy >> 3) + a.bby * (iz >> 3))));
+            if (id == 0xFF) id = __ldg(a.mat + cidx);
+        } else {
+            id = __ldg(a.mat + cidx);
+        }
         id = id < a.nmat ? id : 0;
         mid = id;
         mut = lut[id].mut;
@@ -470,6 +481,34 @@ __global__ void __launch_bounds__(TPB, sizeof(Real) == 4 ? TAM_TR_MINB : 2) tran
     }
 }
 
+// One warp per 8^3 brick: lane l takes the brick's x-rows l and l + 32 (of
+// 64: y fastest, then z), the warp compares its smallest and largest id.
+__global__ void brick_table_kernel(const uint8_t *mat, int nx, int ny, int nz, int bbx, int bby, int64_t nb,
+                                   uint8_t *btab)
+{
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t b = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; b < nb; b += nw) {
+        const int bx = (int)(b % bbx);
+        const int64_t rest = b / bbx;
+        const int by = (int)(rest % bby), bz = (int)(rest / bby);
+        int lo = 256, hi = -1;
+        for (int row = lane; row < 64; row += 32) {
+            const int y = by * 8 + (row & 7), z = bz * 8 + (row >> 3);
+            if (y >= ny || z >= nz) continue;
+            const uint8_t *p = mat + (int64_t)nx * (y + (int64_t)ny * z);
+            for (int x = bx * 8; x < bx * 8 + 8 && x < nx; ++x) {
+                const int v = p[x];
+                lo = min(lo, v);
+                hi = max(hi, v);
+            }
+        }
+        lo = __reduce_min_sync(0xffffffffu, lo);
+        hi = __reduce_max_sync(0xffffffffu, hi);
+        if (lane == 0) btab[b] = (uint8_t)(lo == hi ? lo : 0xFF);
+    }
+}
+
 // out = in * f (normalisation of the tally), and with `sum` the total of
 // `in` added to *sum: one FP64 atomic per block, so the grid is kept to a few
 // thousand blocks
@@ -658,6 +697,20 @@ cudaError_t launch_scale_f64(double *out, double *in, double f, int64_t n, bool 
     if (n <= 0) return cudaSuccess;
     count_launch();
     scale_kernel<double><<<scale_grid(n), 256, 0, s>>>(out, in, f, n, zero_in ? 1 : 0, sum, f_dev);
+    return cudaGetLastError();
+}
+
+int64_t brick_table_size(int nx, int ny, int nz)
+{
+    return (int64_t)((nx + 7) / 8) * ((ny + 7) / 8) * ((nz + 7) / 8);
+}
+
+cudaError_t launch_brick_table(const uint8_t *mat, int nx, int ny, int nz, uint8_t *btab, cudaStream_t s)
+{
+    const int64_t nb = brick_table_size(nx, ny, nz);
+    const int64_t blocks = std::min<int64_t>((nb + 7) / 8, 152 * 32);
+    count_launch();
+    brick_table_kernel<<<(unsigned)blocks, 256, 0, s>>>(mat, nx, ny, nz, (nx + 7) / 8, (ny + 7) / 8, nb, btab);
     return cudaGetLastError();
 }
 

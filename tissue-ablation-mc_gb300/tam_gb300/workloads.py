@@ -232,12 +232,14 @@ def _run_vessels(a) -> None:
     w = c5(scale=a.scale, packets=a.packets)
     with w.context() as ctx:
         ctx.set_tuning("transport.tally32", a.tally32)
+        ctx.set_tuning("transport.bricks", a.bricks)
         ctx.mc_pass(a.warm_packets, seed=1)
         ctx.mc_pass(a.packets, seed=2)
         tr, _, _ = ctx.timing()
         tl = ctx.tallies()
         n = w.params.nxg
-        print(f"C5 grid {n}^3 (FP64 tally {n ** 3 * 8 / 1e6:.0f} MB), transport.tally32={a.tally32}: "
+        print(f"C5 grid {n}^3 (FP64 tally {n ** 3 * 8 / 1e6:.0f} MB), transport.tally32={a.tally32}, "
+              f"transport.bricks={a.bricks}: "
               f"{a.packets} packets in {tr:.2f} ms = {a.packets / (tr * 1e-3):.3e} photons/s, "
               f"{tl['voxel_steps']:.4e} voxel steps = {tl['voxel_steps'] / (tr * 1e-3):.3e} steps/s; "
               f"device errors {ctx.device_errors()}", flush=True)
@@ -327,6 +329,8 @@ def parser():
     v.add_argument("--packets", type=int, default=10_000_000)
     v.add_argument("--warm-packets", type=int, default=1_000_000)
     v.add_argument("--tally32", type=int, default=-1, choices=[-1, 0, 1])
+    v.add_argument("--bricks", type=int, default=-1, choices=[-1, 0, 1],
+                   help="material lookups through the brick table (transport.bricks)")
     q = sub.add_parser("layers", help="configuration 3: the coupled loop on the three-layer skin slab")
     q.add_argument("--scale", type=float, default=1.0, help="grid 256 x 256 x 128 times scale")
     q.add_argument("--packets", type=int, default=100_000_000, help="packets per MC pass")
