@@ -37,7 +37,7 @@
 //    launch's tail.
 #include <algorithm>
 #include <atomic>
-#include <type_traits>
+#include <vector>
 
 #include "heat_common.cuh"
 #include "slab_common.cuh"
@@ -50,7 +50,14 @@ struct FusedSlab {
     const uint8_t *cls_grid;  // the class grid (rows of cls_pitch bytes) for the fix-up pass
     int cls_pitch;
     int nx, ny, nz;
-    uint8_t *tflag;           // per (tile, plane): the one class of the tile and its x / y rim, or 0xFF
+    // heterogeneous grids: per (tile, plane) the one class of the tile and its
+    // x / y rim, or 0xFF; per block of the launch at z-chunk list_zc its class
+    // (or 0xFF); the blocks of one class (item | class << 24) and the others
+    uint8_t *tflag, *bclass;
+    unsigned *one_items, *mixed_items;
+    int n_one, n_mixed, list_zc;
+    bool mixed_first;         // mixed blocks make up a quarter or more of the top three z-chunks
+    unsigned gen;             // lists rebuilt so many times
 };
 
 namespace {
@@ -106,9 +113,12 @@ template <bool UNIFORM>
 __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     slab_step_kernel(const __grid_constant__ FusedArgs a, const __grid_constant__ SlabMaps m,
                      const __grid_constant__ ClassLut L, const uint8_t *cls, int cpitch, int zchunk, float rare_thr,
-                     const uint8_t *tflag)
+                     const unsigned *items, int early)
 {
     using Lay = SlabLayout<UNIFORM>;
+    // early: the launch behind this one (the other list's blocks, which
+    // touch other voxels) may start as soon as this one's blocks are placed
+    if (early) asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
     constexpr int TP = Lay::TP, CP = Lay::CP, NST = Lay::NST;
     extern __shared__ unsigned char smem_raw[];
     __shared__ float s_fa[UNIFORM ? 1 : MAX_MAT * MAX_MAT];
@@ -119,10 +129,25 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     const int tid = threadIdx.x;
     const int r = tid / SP, p = tid % SP;
     const int nx = a.nx, ny = a.ny, nz = a.nz;
-    const int bxW = (int)blockIdx.x * SW, byR = (int)blockIdx.y * SR;
+    // the block's tile and z-chunk: its place in the launch, or on a
+    // heterogeneous grid the item of a list (one list per kernel: the
+    // one-class kernel takes the blocks whose tile, rim and planes hold one
+    // class, with that class in the item's top byte; the class kernel the rest)
+    int bx = (int)blockIdx.x, by = (int)blockIdx.y, bz = (int)blockIdx.z, nzc = (int)gridDim.z;
+    unsigned item_cls = 0xFFu;
+    if (items) {
+        const unsigned it = items[blockIdx.x], u = it & 0xFFFFFFu;
+        const unsigned gx = (unsigned)(nx + SW - 1) / SW, gy = (unsigned)(ny + SR - 1) / SR;
+        item_cls = it >> 24;
+        bx = (int)(u % gx);
+        by = (int)((u / gx) % gy);
+        bz = (int)(u / (gx * gy));
+        nzc = (nz + zchunk - 1) / zchunk;
+    }
+    const int bxW = bx * SW, byR = by * SR;
     const int x = bxW + 2 * p, y = byR + r;
     // slabs from the top face down (see the file comment)
-    const int z0 = ((int)gridDim.z - 1 - (int)blockIdx.z) * zchunk;
+    const int z0 = (nzc - 1 - bz) * zchunk;
     const int z1 = min(nz, z0 + zchunk);
     const int nplanes = z1 - z0, last = nplanes + 1;
     const bool act = x < nx && y < ny;  // nx is even: the pair's second voxel is inside too
@@ -133,7 +158,10 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     const float Pdt = step_pdt<float>(a);
     // face coefficients with dt folded in
     const float cxd = a.fc[FC_DT] * a.fc[FC_CX], cyd = a.fc[FC_DT] * a.fc[FC_CY], czd = a.fc[FC_DT] * a.fc[FC_CZ];
-    const int uc = L.uniform >= 0 ? L.uniform : 0;
+    const int uc = UNIFORM && item_cls != 0xFFu ? (int)item_cls : (L.uniform >= 0 ? L.uniform : 0);
+    const float au = L.fa[uc * MAX_MAT + uc];
+    const float Cx = cxd * au, Cy = cyd * au, Cz = czd * au, C6 = 2.f * ((Cx + Cy) + Cz);
+    const float Ku = Pdt * L.irc[uc];
     // boundary faces of the pair in x / y: x- of the first voxel, x+ of the
     // second, y- and y+ of both
     const unsigned exy = (unsigned)(x == 0) | (unsigned)(x + 1 == nx - 1) << 1 | (unsigned)(y == 0) << 2 |
@@ -165,44 +193,25 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     if (leader)
         for (int idx = 0; idx < NST && idx <= last; ++idx) issue(idx);
     int issued = NST < last + 1 ? NST : last + 1;
-    // heterogeneous grids: a block whose tile, x / y rim and planes z0 - 1 ..
-    // z1 all hold one class (the tile flags) takes the one-class update with
-    // that class's coefficients, without class lookups
-    int blk = -1;
-    if (!UNIFORM && tflag) {
-        const uint8_t *tf = tflag + ((int64_t)blockIdx.y * gridDim.x + blockIdx.x) * nz;
-        const int za = max(z0 - 1, 0), zb = min(z1, nz - 1);
-        blk = __ldg(tf + za);
-        for (int zz = za + 1; zz <= zb; ++zz)
-            if (__ldg(tf + zz) != blk) blk = 0xFF;
-        if (blk == 0xFF) blk = -1;
-    }
-    const int kb = blk >= 0 ? blk : uc;  // the class of a one-class block
-    const float au = L.fa[kb * MAX_MAT + kb];
-    const float Cx = cxd * au, Cy = cyd * au, Cz = czd * au, C6 = 2.f * ((Cx + Cy) + Cz);
-    const float Ku = Pdt * L.irc[kb];
     bool ok = mbar_wait(bar, 0) && mbar_wait(bar + 1, 0);
     const int qT = (r + 1) * TP + 4 + 2 * p;   // the pair in the staged T / Kahan rows (even: 8-byte aligned)
     const int qO = r * SW + 2 * p;             // ... in the own-voxel J
     const int qC = (r + 1) * CP + 16 + 2 * p;  // ... in the class rows (even)
+    float2 Tp = {0.f, 0.f}, Tc = {0.f, 0.f}, Ep = {0.f, 0.f}, Ec = {0.f, 0.f};
+    int kp0 = uc, kp1 = uc, kc0 = uc, kc1 = uc;
     auto cls2 = [&](const unsigned char *b, int i, int &k0, int &k1) {
         const unsigned short w = *reinterpret_cast<const unsigned short *>(b + Lay::C_OFF + i);
         k0 = w & (MAX_MAT - 1);
         k1 = (w >> 8) & (MAX_MAT - 1);
     };
-    // the plane loop, for the class lookups (U false) or one class (U true)
-    auto run = [&](auto one_class) {
-    constexpr bool U = decltype(one_class)::value;
-    float2 Tp = {0.f, 0.f}, Tc = {0.f, 0.f}, Ep = {0.f, 0.f}, Ec = {0.f, 0.f};
-    int kp0 = kb, kp1 = kb, kc0 = kb, kc1 = kb;
     if (ok && act) {
         Tc = lds2((const float *)(sm + Lay::STAGE + Lay::T_OFF) + qT);
         Ec = lds2((const float *)(sm + Lay::STAGE + Lay::E_OFF) + qT);
-        if (!U) cls2(sm + Lay::STAGE, qC, kc0, kc1);
+        if (!UNIFORM) cls2(sm + Lay::STAGE, qC, kc0, kc1);
         if (z0 > 0) {
             Tp = lds2((const float *)(sm + Lay::T_OFF) + qT);
             Ep = lds2((const float *)(sm + Lay::E_OFF) + qT);
-            if (!U) cls2(sm, qC, kp0, kp1);
+            if (!UNIFORM) cls2(sm, qC, kp0, kp1);
         }
     }
     float *To = (float *)a.T_out + (x + nx * y + sz * z0), *Eo = a.Tc_out + (x + nx * y + sz * z0);
@@ -234,20 +243,20 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
                 const float2 g = ghost_pair(a, 0, Tc.x, Ec.x, L.k[kc0]);
                 WT[qT - 1] = g.x;
                 WE[qT - 1] = g.y;
-                if (!U) WC[qC - 1] = (unsigned char)kc0;
+                if (!UNIFORM) WC[qC - 1] = (unsigned char)kc0;
             }
             if (exy & 2u) {
                 const float2 g = ghost_pair(a, 1, Tc.y, Ec.y, L.k[kc1]);
                 WT[qT + 2] = g.x;
                 WE[qT + 2] = g.y;
-                if (!U) WC[qC + 2] = (unsigned char)kc1;
+                if (!UNIFORM) WC[qC + 2] = (unsigned char)kc1;
             }
             if (exy & 12u) {
                 const int f = (exy & 4u) ? 2 : 3, o = (exy & 4u) ? -TP : TP, oc = (exy & 4u) ? -CP : CP;
                 const float2 g0 = ghost_pair(a, f, Tc.x, Ec.x, L.k[kc0]), g1 = ghost_pair(a, f, Tc.y, Ec.y, L.k[kc1]);
                 *reinterpret_cast<float2 *>(WT + qT + o) = make_float2(g0.x, g1.x);
                 *reinterpret_cast<float2 *>(WE + qT + o) = make_float2(g0.y, g1.y);
-                if (!U) {
+                if (!UNIFORM) {
                     WC[qC + oc] = (unsigned char)kc0;
                     WC[qC + 1 + oc] = (unsigned char)kc1;
                 }
@@ -259,8 +268,8 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
         const float2 eym = lds2(SE + qT - TP), eyp = lds2(SE + qT + TP);
         const float txl = ST[qT - 1], txr = ST[qT + 2], exl = SE[qT - 1], exr = SE[qT + 2];
         const float2 j2 = lds2((const float *)(S + Lay::J_OFF) + qO);
-        int kn0 = kb, kn1 = kb;
-        if (!U) cls2(N, qC, kn0, kn1);
+        int kn0 = uc, kn1 = uc;
+        if (!UNIFORM) cls2(N, qC, kn0, kn1);
         // ghost neighbours of the z boundary planes (registers only)
         float2 Tpz = Tp, Epz = Ep;
         int kpz0 = kp0, kpz1 = kp1;
@@ -290,7 +299,7 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
             const float eyM = h ? eym.y : eym.x, eyP = h ? eyp.y : eyp.x;
             const float tzM = h ? Tpz.y : Tpz.x, tzP = h ? Tnz.y : Tnz.x, ezM = h ? Epz.y : Epz.x, ezP = h ? Enz.y : Enz.x;
             float dT;
-            if (U) {
+            if (UNIFORM) {
                 // sum over the faces of C_f [(T_f - T_c) - (e_f - e_c)]
                 const float sx = ((txm - tc) + (txp - tc)) - (exm + exp_);
                 const float sy = ((tyM - tc) + (tyP - tc)) - (eyM + eyP);
@@ -310,7 +319,7 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
                       (aym * ((tyM - tc) - (eyM - e0)) + ayp * ((tyP - tc) - (eyP - e0)))) +
                      (axm * ((txm - tc) - (exm - e0)) + axp * ((txp - tc) - (exp_ - e0)));
             }
-            const float Kk = U ? Ku : Pdt * L.irc[h ? kc1 : kc0];
+            const float Kk = UNIFORM ? Ku : Pdt * L.irc[h ? kc1 : kc0];
             const float inc = __fmaf_rn(Kk, h ? j2.y : j2.x, dT);
             const float yk = inc - e0;
             const float t = tc + yk;
@@ -334,19 +343,12 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
         Tc = Tn;
         Ep = Ec;
         Ec = En;
-        if (!U) {
+        if (!UNIFORM) {
             kp0 = kc0;
             kp1 = kc1;
             kc0 = kn0;
             kc1 = kn1;
         }
-    }
-    };
-    if constexpr (UNIFORM) {
-        run(std::true_type{});
-    } else {
-        if (blk >= 0) run(std::true_type{});
-        else run(std::false_type{});
     }
     // the last plane's wait may have failed in some threads only: agree first
     ok = __syncthreads_and(ok) != 0;
@@ -396,7 +398,7 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
                                      ge_ff(tt[j], ee[j], a.fc[FC_TABL], a.fc[FC_TABL_LO]);
                 if (general)
                     slab_fix<UNIFORM>(a, L, cls, cpitch, xx[j], yy[j], zz[j], Pdt, t_new, errbits, (const float *)a.T_in,
-                                      a.Tc_in, (float *)a.T_out, a.Tc_out);
+                                      a.Tc_in, (float *)a.T_out, a.Tc_out, uc);
                 else if (Ts >= a.fc[FC_SCREEN]) rare_update_f32(a, vv[j], ni, tt[j], ee[j], t_new, true, oo[j]);
             }
         }
@@ -404,14 +406,23 @@ __global__ void __launch_bounds__(SP *SR, slab_minb(UNIFORM))
     if (errbits) atomicOr(a.err, errbits);
 }
 
+// The z-chunk of a launch: measured fastest at 200^3 (37.7 us against 38.4
+// at 5, 40.6 at 8).
+int eff_zchunk(int requested, int nz)
+{
+    int zchunk = requested > 0 ? requested : 6;
+    if (zchunk > SLAB_ZMAX) zchunk = SLAB_ZMAX;
+    if (zchunk > nz) zchunk = nz;
+    return zchunk;
+}
+
+// items == nullptr: every block of the grid; else `n` listed blocks
 template <bool UNIFORM>
 cudaError_t launch_slab_t(const FusedArgs &a, const SlabMaps &m, const ClassLut &L, const uint8_t *cls, int cpitch,
-                          float rare_thr, const uint8_t *tflag, cudaStream_t s)
+                          float rare_thr, const unsigned *items, int n, int early, bool overlap, cudaStream_t s)
 {
     const int bx = (a.nx + SW - 1) / SW, by = (a.ny + SR - 1) / SR;
-    int zchunk = a.zchunk > 0 ? a.zchunk : 6;  // measured fastest at 200^3 (37.7 us against 38.4 at 5, 40.6 at 8)
-    if (zchunk > SLAB_ZMAX) zchunk = SLAB_ZMAX;
-    if (zchunk > a.nz) zchunk = a.nz;
+    const int zchunk = eff_zchunk(a.zchunk, a.nz);
     const int chunks = (a.nz + zchunk - 1) / zchunk;
     const int smem = SlabLayout<UNIFORM>::SMEM;
     static std::atomic<unsigned long long> attr_set{0};
@@ -425,8 +436,24 @@ cudaError_t launch_slab_t(const FusedArgs &a, const SlabMaps &m, const ClassLut 
         attr_set.fetch_or(bit);
     }
     count_launch();
-    slab_step_kernel<UNIFORM><<<dim3(bx, by, chunks), SP * SR, smem, s>>>(a, m, L, cls, cpitch, zchunk, rare_thr, tflag);
-    return cudaGetLastError();
+    const dim3 grid = items ? dim3((unsigned)n, 1, 1) : dim3(bx, by, chunks);
+    if (!overlap) {
+        slab_step_kernel<UNIFORM><<<grid, SP * SR, smem, s>>>(a, m, L, cls, cpitch, zchunk, rare_thr, items, early);
+        return cudaGetLastError();
+    }
+    // programmatic dependent launch: may begin while the launch before it
+    // (which signals early) is still running
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = dim3(SP * SR);
+    cfg.dynamicSmemBytes = (size_t)smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, slab_step_kernel<UNIFORM>, a, m, L, cls, cpitch, zchunk, rare_thr, items, 0);
 }
 
 // The slab kernel's tile flags: for every (tile, plane), the class that all
@@ -463,16 +490,68 @@ __global__ void slab_tile_flags_kernel(const uint8_t *cls, int pitch, int nx, in
     }
 }
 
+// Per block of the slab launch at z-chunk zc (launch order: x tiles fastest,
+// then y tiles, then z-chunks from the top face down): the class that the
+// tile flags of all its planes z0 - 1 .. z1 (inside the grid) agree on, or 0xFF.
+__global__ void slab_block_class_kernel(const uint8_t *flags, int tx, int ty, int nz, int zc, uint8_t *bclass)
+{
+    const int nzc = (nz + zc - 1) / zc;
+    const int64_t items = (int64_t)tx * ty * nzc;
+    for (int64_t u = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; u < items; u += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t tile = u % ((int64_t)tx * ty);
+        const int bz = (int)(u / ((int64_t)tx * ty));
+        const int z0 = (nzc - 1 - bz) * zc, z1 = min(nz, z0 + zc);
+        const int za = max(z0 - 1, 0), zb = min(z1, nz - 1);
+        const uint8_t *f = flags + tile * nz;
+        int c = f[za];
+        for (int z = za + 1; z <= zb && c != 0xFF; ++z)
+            if (f[z] != c) c = 0xFF;
+        bclass[u] = (uint8_t)c;
+    }
+}
+
 }  // namespace
 
-cudaError_t fused_slab_tile_flags(const FusedSlab *m, cudaStream_t s)
+cudaError_t fused_slab_tile_flags(FusedSlab *m, int zchunk, cudaStream_t s)
 {
-    const int64_t items = (int64_t)((m->nx + SW - 1) / SW) * ((m->ny + SR - 1) / SR) * m->nz;
-    const int64_t blocks = std::min<int64_t>((items + 7) / 8, 152 * 32);
-    count_launch();
-    slab_tile_flags_kernel<<<(unsigned)blocks, 256, 0, s>>>(m->cls_grid, m->cls_pitch, m->nx, m->ny, m->nz, m->tflag);
-    return cudaGetLastError();
+    const int tx = (m->nx + SW - 1) / SW, ty = (m->ny + SR - 1) / SR;
+    const int zc = eff_zchunk(zchunk, m->nz), nzc = (m->nz + zc - 1) / zc;
+    const int64_t tiles = (int64_t)tx * ty * m->nz, items = (int64_t)tx * ty * nzc;
+    count_launch(2);
+    slab_tile_flags_kernel<<<(unsigned)std::min<int64_t>((tiles + 7) / 8, 152 * 32), 256, 0, s>>>(
+        m->cls_grid, m->cls_pitch, m->nx, m->ny, m->nz, m->tflag);
+    slab_block_class_kernel<<<(unsigned)std::min<int64_t>((items + 255) / 256, 152 * 16), 256, 0, s>>>(
+        m->tflag, tx, ty, m->nz, zc, m->bclass);
+    // the two lists, in launch order, built on the host (a rare call: after a
+    // change of the class grid or of the z-chunk)
+    std::vector<uint8_t> bc((size_t)items);
+    cudaError_t e = cudaMemcpyAsync(bc.data(), m->bclass, (size_t)items, cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    std::vector<unsigned> one, mixed;
+    int64_t top_mixed = 0;
+    for (int64_t u = 0; u < items; ++u) {
+        if (bc[u] < MAX_MAT) {
+            one.push_back((unsigned)u | (unsigned)bc[u] << 24);
+        } else {
+            mixed.push_back((unsigned)u);
+            if (u < 3 * (int64_t)tx * ty) ++top_mixed;  // the top z-chunks come first in launch order
+        }
+    }
+    if (!one.empty()) e = cudaMemcpyAsync(m->one_items, one.data(), one.size() * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess && !mixed.empty())
+        e = cudaMemcpyAsync(m->mixed_items, mixed.data(), mixed.size() * 4, cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+    m->n_one = (int)one.size();
+    m->n_mixed = (int)mixed.size();
+    m->mixed_first = 4 * top_mixed >= std::min<int64_t>(items, 3 * (int64_t)tx * ty);
+    m->list_zc = zc;
+    ++m->gen;
+    return cudaSuccess;
 }
+
+unsigned fused_slab_generation(const FusedSlab *m) { return m ? m->gen : 0u; }
 
 bool fused_slab_supported(int nx, int ny, int nz)
 {
@@ -492,20 +571,26 @@ cudaError_t fused_slab_create(FusedSlab **out, int nx, int ny, int nz, float *co
     m->nx = nx;
     m->ny = ny;
     m->nz = nz;
-    m->tflag = nullptr;
+    m->tflag = m->bclass = nullptr;
+    m->one_items = m->mixed_items = nullptr;
+    m->n_one = m->n_mixed = 0;
+    m->list_zc = 0;  // no lists: the class kernel takes every block
+    m->mixed_first = false;
+    m->gen = 0;
     for (int b = 0; b < 2 && e == cudaSuccess; ++b) {
         e = encode(&m->T[b], T[b], nx, ny, nz, SW + 8, SR + 2);
         if (e == cudaSuccess) e = encode(&m->E[b], Tc[b], nx, ny, nz, SW + 8, SR + 2);
     }
     if (e == cudaSuccess) e = encode(&m->J, J, nx, ny, nz, SW, SR);
     if (e == cudaSuccess) e = encode_u8(&m->cls, cls, pitch, ny, nz, SlabLayout<false>::CP, SR + 2);
-    // tile flags: none one-class until fused_slab_tile_flags has run on the class grid
-    const size_t nflag = (size_t)((nx + SW - 1) / SW) * ((ny + SR - 1) / SR) * nz;
-    if (e == cudaSuccess) e = cudaMalloc(&m->tflag, nflag);
-    if (e == cudaSuccess) e = cudaMemset(m->tflag, 0xFF, nflag);
+    // tile flags and lists, sized for the smallest z-chunk (the most blocks)
+    const int64_t tiles = (int64_t)((nx + SW - 1) / SW) * ((ny + SR - 1) / SR);
+    if (e == cudaSuccess) e = cudaMalloc(&m->tflag, (size_t)(tiles * nz));
+    if (e == cudaSuccess) e = cudaMalloc(&m->bclass, (size_t)(tiles * nz));
+    if (e == cudaSuccess) e = cudaMalloc(&m->one_items, (size_t)(tiles * nz) * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&m->mixed_items, (size_t)(tiles * nz) * 4);
     if (e != cudaSuccess) {
-        if (m->tflag) cudaFree(m->tflag);
-        delete m;
+        fused_slab_destroy(m);
         return e;
     }
     *out = m;
@@ -514,7 +599,9 @@ cudaError_t fused_slab_create(FusedSlab **out, int nx, int ny, int nz, float *co
 
 void fused_slab_destroy(FusedSlab *m)
 {
-    if (m && m->tflag) cudaFree(m->tflag);
+    if (!m) return;
+    for (void *p : {(void *)m->tflag, (void *)m->bclass, (void *)m->one_items, (void *)m->mixed_items})
+        if (p) cudaFree(p);
     delete m;
 }
 
@@ -530,8 +617,38 @@ cudaError_t launch_fused_slab(const FusedArgs &a0, const FusedSlab *sm, int whic
     // one screen for the listed rare work: damage / ablation, and boiling
     float rare_thr = a.fc[FC_SCREEN];
     if (a.boil && a.fc[FC_TBOIL] < rare_thr) rare_thr = a.fc[FC_TBOIL];
-    return L.uniform >= 0 ? launch_slab_t<true>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, nullptr, s)
-                          : launch_slab_t<false>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, sm->tflag, s);
+    if (L.uniform >= 0)
+        return launch_slab_t<true>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, nullptr, 0, 0, false, s);
+    if (sm->list_zc != eff_zchunk(a.zchunk, a.nz))  // no lists for this z-chunk: the class kernel everywhere
+        return launch_slab_t<false>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, nullptr, 0, 0, false, s);
+    // two launches over disjoint blocks: the second may start as soon as the
+    // first one's blocks are placed (programmatic dependent launch), and the
+    // next step's launch waits for both.  The beam enters at the top face, so
+    // the top blocks carry the longest lists: the mixed blocks go first when
+    // they make up a quarter or more of the top three z-chunks (a layered
+    // grid whose thin top layers meet there: 50 against 62 us per
+    // 256 x 256 x 128 step), else the one-class blocks (a grid of scattered
+    // vessels: 78 against 84 us at 256^3)
+    cudaError_t e = cudaSuccess;
+    const bool both = sm->n_one > 0 && sm->n_mixed > 0;
+    auto mixed = [&](int early, bool overlap) {
+        return sm->n_mixed > 0 ? launch_slab_t<false>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, sm->mixed_items,
+                                                      sm->n_mixed, early, overlap, s)
+                               : cudaSuccess;
+    };
+    auto one = [&](int early, bool overlap) {
+        return sm->n_one > 0 ? launch_slab_t<true>(a, m, L, sm->cls_grid, sm->cls_pitch, rare_thr, sm->one_items,
+                                                   sm->n_one, early, overlap, s)
+                             : cudaSuccess;
+    };
+    if (sm->mixed_first) {
+        e = mixed(both ? 1 : 0, false);
+        if (e == cudaSuccess) e = one(0, both);
+    } else {
+        e = one(both ? 1 : 0, false);
+        if (e == cudaSuccess) e = mixed(0, both);
+    }
+    return e;
 }
 
 }  // namespace tam

@@ -13,10 +13,11 @@ namespace {
 // config-mode form; the stencil redone from global memory with its ghost
 // faces), the error word, then damage and ablation of the new temperature.
 // Ti / Ei: the step's input temperature and Kahan term; To / Eo: its output.
+// UNIFORM: every voxel around holds class `ucls` (default: the grid's one class).
 template <bool UNIFORM>
 __device__ __noinline__ void slab_fix(const FusedArgs &a, const ClassLut &L, const uint8_t *cls, int cpitch, int x,
                                       int y, int z, float Pdt, double t_new, unsigned &errbits, const float *Ti,
-                                      const float *Ei, float *To, float *Eo)
+                                      const float *Ei, float *To, float *Eo, int ucls = -1)
 {
     const int nx = a.nx, ny = a.ny, nz = a.nz;
     const int64_t sy = nx, sz = (int64_t)nx * ny, ni = sz * nz, v = x + sy * y + sz * z;
@@ -24,7 +25,7 @@ __device__ __noinline__ void slab_fix(const FusedArgs &a, const ClassLut &L, con
     float t = To[v], e = Eo[v];
     const int64_t cs = (int64_t)cpitch * ny;
     auto klass = [&](int xx, int yy, int zz) -> int {
-        return UNIFORM ? L.uniform : (cls[xx + (int64_t)cpitch * yy + cs * zz] & (MAX_MAT - 1));
+        return UNIFORM ? (ucls >= 0 ? ucls : L.uniform) : (cls[xx + (int64_t)cpitch * yy + cs * zz] & (MAX_MAT - 1));
     };
     const int k = klass(x, y, z);
     if (a.boil && tc >= a.fc[FC_TBOIL]) {

@@ -441,7 +441,7 @@ int set_thermal_classes(tam_ctx *ctx, int u)
     ctx->thermal_by_class = true;
     if (ctx->d_cls)
         CK(tam::launch_cls_from_mat(ctx->d_mat, nm, ctx->d_cls, ctx->nx, ctx->ny, ctx->nz, ctx->cls_pitch, ctx->stream));
-    if (ctx->d_cls && ctx->fslab) CK(tam::fused_slab_tile_flags(ctx->fslab, ctx->stream));
+    if (ctx->d_cls && ctx->fslab && u < 0) CK(tam::fused_slab_tile_flags(ctx->fslab, ctx->zchunk, ctx->stream));
     return TAM_OK;
 }
 
@@ -915,6 +915,15 @@ int staged_setup(tam_ctx *ctx)
     return TAM_OK;
 }
 
+// The slab form's per-block lists of a heterogeneous grid, for the context's
+// z-chunk (after a change of the z-chunk; synchronises the stream).
+int slab_lists(tam_ctx *ctx)
+{
+    if (!ctx->config || !ctx->d_cls || !ctx->fslab || ctx->cls_uniform >= 0) return TAM_OK;
+    CK(tam::fused_slab_tile_flags(ctx->fslab, ctx->zchunk, ctx->stream));
+    return TAM_OK;
+}
+
 // Forms of the config-mode heat step, by what the context's state allows.
 enum HeatForm { HF_CLS = 0, HF_STAGED, HF_TMA, HF_CPASYNC, HF_SLAB };
 
@@ -967,7 +976,8 @@ std::vector<unsigned char> graph_key(const tam_ctx *ctx, const tam::FusedArgs &a
     a.T_in = a.T_out = nullptr;
     a.Tc_in = nullptr;
     a.Tc_out = nullptr;
-    const int knobs[4] = {(int)form, ctx->cls_rows, ctx->zchunk, ctx->arr_fp64 ? 1 : 0};
+    const int knobs[5] = {(int)form, ctx->cls_rows, ctx->zchunk, ctx->arr_fp64 ? 1 : 0,
+                          (int)tam::fused_slab_generation(ctx->fslab)};  // the slab form's block lists
     std::vector<unsigned char> k(sizeof a + sizeof ctx->clut + sizeof knobs + 2 * sizeof(void *));
     unsigned char *p = k.data();
     std::memcpy(p, &a, sizeof a);
@@ -2853,6 +2863,8 @@ int tam_set_tuning(tam_ctx *ctx, const char *key, int64_t value)
     } else if (k == "heat.zchunk") {
         if (value < 0 || value > ctx->nz) return fail(ctx, TAM_E_INVALID, "heat.zchunk must be in 0..nz");
         ctx->zchunk = (int)value;
+        CK(cudaSetDevice(ctx->device));
+        RC(slab_lists(ctx));
     } else {
         return fail(ctx, TAM_E_INVALID, "unknown tuning key " + k);
     }
@@ -3042,7 +3054,8 @@ int tam_load_state(tam_ctx *ctx, const char *path)
         CK(cudaMemcpy(b.first, host.data(), n, cudaMemcpyHostToDevice));
     }
     // the slab form's tile flags follow the class grid just loaded
-    if (ctx->config && ctx->d_cls && ctx->fslab) CK(tam::fused_slab_tile_flags(ctx->fslab, ctx->stream));
+    if (ctx->config && ctx->d_cls && ctx->fslab && ctx->cls_uniform < 0)
+        CK(tam::fused_slab_tile_flags(ctx->fslab, ctx->zchunk, ctx->stream));
     set_scalars(ctx, S);
     std::memcpy(ctx->tally, tally, sizeof tally);
     ctx->tally_stale = false;
@@ -3156,6 +3169,7 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
         ctx->use_slab = slab0;
         (void)cudaGetLastError();
         (void)snap_restore(ctx, S);
+        (void)slab_lists(ctx);
         return code;
     };
     auto timed = [&](int ev0, int ev1) -> int {
@@ -3197,6 +3211,7 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
             for (int zc : zcs) {
                 if (zc > ctx->nz) continue;
                 ctx->zchunk = zc;
+                if ((r = slab_lists(ctx)) != TAM_OK) return undo(r);
                 ctx->use_slab = form == 2;
                 if (form != 2) ctx->cls_rows = form;
                 if ((r = cfg_heat(ctx, steps)) != TAM_OK || (r = timed(2, 3)) != TAM_OK ||
@@ -3211,6 +3226,7 @@ int tam_autotune(tam_ctx *ctx, int64_t packets, int32_t steps, int64_t *chosen, 
             }
         }
         ctx->zchunk = best_z;
+        if ((r = slab_lists(ctx)) != TAM_OK) return undo(r);
         ctx->cls_rows = best_r;
         ctx->use_slab = best_s;
     }

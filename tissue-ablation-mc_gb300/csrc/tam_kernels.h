@@ -314,10 +314,15 @@ bool fused_slab_supported(int nx, int ny, int nz);
 cudaError_t fused_slab_create(FusedSlab **out, int nx, int ny, int nz, float *const T[2], float *const Tc[2],
                               const float *J, const uint8_t *cls, int pitch);
 void fused_slab_destroy(FusedSlab *m);
-// Recompute the slab form's per-(tile, plane) one-class flags from the class
-// grid given at creation (after every change of that grid); until the first
-// call no tile counts as one-class.
-cudaError_t fused_slab_tile_flags(const FusedSlab *m, cudaStream_t s);
+// Heterogeneous grids: recompute the slab form's per-(tile, plane) one-class
+// flags from the class grid given at creation and, for the launch at
+// `zchunk`, the lists of blocks whose tile, rim and planes hold one class
+// (run by the one-class kernel with that class) and of the others (the class
+// kernel).  Call after every change of the class grid or of the z-chunk;
+// synchronises the stream.  Without lists for the launch's z-chunk the class
+// kernel takes every block.  fused_slab_generation counts the rebuilds.
+cudaError_t fused_slab_tile_flags(FusedSlab *m, int zchunk, cudaStream_t s);
+unsigned fused_slab_generation(const FusedSlab *m);
 cudaError_t launch_fused_slab(const FusedArgs &a, const FusedSlab *m, int which, const ClassLut &L, cudaStream_t s);
 
 // Batched FP32 heat step of many instances in one persistent cooperative

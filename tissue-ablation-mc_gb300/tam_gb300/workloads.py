@@ -287,13 +287,16 @@ def _run_layers(a) -> None:
 
 
 def _run_heat(a) -> None:
-    """The heat step of the homogeneous cube (configuration 2 at edge 200), or
-    of configuration 5's vessel grid (edge 512 at scale 1: the class-table
-    kernel): one MC pass for the absorbed-power field, then `steps` steps of
+    """The heat step of the homogeneous cube (configuration 2 at edge 200), of
+    configuration 5's vessel grid (edge 512 at scale 1) or of configuration
+    3's three-layer slab (edge 256 at scale 1; both heterogeneous: the
+    class-table kernels): one MC pass for the absorbed-power field, then `steps` steps of
     each requested form launched one by one (no graph replay), timed with the
     library's CUDA events; the form used by profiles of the heat kernels."""
     if a.geometry == "vessels":
         w = c5(scale=a.edge / 512.0, packets=a.packets)
+    elif a.geometry == "layers":
+        w = c3(scale=a.edge / 256.0, packets=a.packets)
     else:
         w = homogeneous(a.edge, a.packets, 2.0, 2.0, precision=1)
     with w.context() as ctx:
@@ -346,8 +349,9 @@ def parser():
     h.add_argument("--packets", type=int, default=1_000_000)
     h.add_argument("--steps", type=int, default=4)
     h.add_argument("--forms", default="slab,pair", help="comma list of slab / pair")
-    h.add_argument("--geometry", default="cube", choices=["cube", "vessels"],
-                   help="the homogeneous cube, or configuration 5's vessels and inclusions at this edge")
+    h.add_argument("--geometry", default="cube", choices=["cube", "vessels", "layers"],
+                   help="the homogeneous cube, configuration 5's vessels and inclusions at this edge, or "
+                        "configuration 3's three-layer slab (edge x edge x edge / 2)")
     return ap
 
 
