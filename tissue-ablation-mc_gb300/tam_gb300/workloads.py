@@ -276,14 +276,17 @@ def _run_layers(a) -> None:
 
     w = c3(scale=a.scale, packets=a.packets, steps=a.steps)
     with w.context() as ctx:
+        ctx.set_tuning("transport.bricks", a.bricks)
         t0 = time.perf_counter()
         ctx.step_coupled(a.steps, seed=a.seed)
         dt = time.perf_counter() - t0
         st = ctx.state()
         T = ctx.download(api._abi.TAM_F_TEMP)
+        tr, _, _ = ctx.timing()
         print(f"C3 three-layer slab {w.info['grid']}: {a.steps} heat steps of {st.delt:.3e} s (simulated "
               f"{st.time:.2f} s), {st.mc_passes} MC passes of {a.packets} packets, {st.n_ablated} voxels ablated, "
-              f"max T {T.max():.1f} K; wall {dt:.2f} s; device errors {ctx.device_errors()}", flush=True)
+              f"max T {T.max():.1f} K; wall {dt:.2f} s; last pass {tr:.1f} ms; device errors {ctx.device_errors()}",
+              flush=True)
 
 
 def _run_heat(a) -> None:
@@ -339,6 +342,8 @@ def parser():
     q.add_argument("--packets", type=int, default=100_000_000, help="packets per MC pass")
     q.add_argument("--steps", type=int, default=20_000, help="outer iterations (one heat step each)")
     q.add_argument("--seed", type=int, default=1)
+    q.add_argument("--bricks", type=int, default=-1, choices=[-1, 0, 1],
+                   help="material lookups through the brick table (transport.bricks)")
     r = sub.add_parser("pulsed", help="configuration 5: the whole pulsed coupled run on the vessel grid")
     r.add_argument("--scale", type=float, default=1.0, help="grid edge = 512 * scale")
     r.add_argument("--packets", type=int, default=1_000_000_000, help="packets per MC pass")
