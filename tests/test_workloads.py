@@ -60,6 +60,15 @@ def test_workload_command_line(tam):
     assert (a.cmd, a.scale, a.tally32, a.packets) == ("vessels", 0.6, 1, 10_000_000)
     with pytest.raises(SystemExit):
         p.parse_args(["vessels", "--tally32", "2"])
+    a = p.parse_args(["vessels", "--bricks", "0"])
+    assert (a.bricks, a.tally32) == (0, -1)
+    a = p.parse_args(["layers", "--bricks", "1", "--steps", "10"])
+    assert (a.cmd, a.bricks, a.steps, a.scale) == ("layers", 1, 10, 1.0)
+    a = p.parse_args(["heat", "--edge", "256", "--geometry", "layers", "--forms", "slab,pair"])
+    assert (a.edge, a.geometry, a.forms.split(",")) == (256, "layers", ["slab", "pair"])
+    assert p.parse_args(["heat"]).geometry == "cube"
+    with pytest.raises(SystemExit):
+        p.parse_args(["heat", "--geometry", "sphere"])
 
 
 # ------------------------------------------------------------------ GPU --
