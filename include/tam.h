@@ -290,7 +290,9 @@ int tam_get_timing(struct tam_ctx *ctx, double *transport_ms, double *heat_ms, i
  * up through a table of 8 x 8 x 8 bricks -- the one material of a brick, or
  * the grid itself inside mixed bricks -- for grids of 2^25 voxels or more, 0
  * never, 1 always; same walks either way), "heat.zchunk" (z planes per
- * thread column of the fused step, 0 = automatic), "heat.tma" (1: stage the
+ * thread column of the fused step, 0 = automatic; on a grid of several
+ * thermal classes a change rebuilds the slab form's lists of one-class and
+ * mixed blocks and synchronises the context's stream), "heat.tma" (1: stage the
  * FP32 fused step's planes with TMA where the row pitch allows, 0: cp.async),
  * "heat.cls" (1: while the thermal properties are those of the material
  * classes, look the face coefficients up per class pair instead of reading
