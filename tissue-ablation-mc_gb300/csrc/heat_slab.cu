@@ -517,12 +517,12 @@ cudaError_t fused_slab_tile_flags(FusedSlab *m, int zchunk, cudaStream_t s)
     const int tx = (m->nx + SW - 1) / SW, ty = (m->ny + SR - 1) / SR;
     const int zc = eff_zchunk(zchunk, m->nz), nzc = (m->nz + zc - 1) / zc;
     const int64_t tiles = (int64_t)tx * ty * m->nz, items = (int64_t)tx * ty * nzc;
-    if (items >= (int64_t)1 << 24) {  // list entries hold the block's index in 24 bits
-        m->n_one = m->n_mixed = 0;
-        m->list_zc = 0;  // the class kernel takes every block
-        ++m->gen;
-        return cudaSuccess;
-    }
+    // until the new lists are complete the class kernel takes every block
+    // (so a failure below leaves a correct step)
+    m->n_one = m->n_mixed = 0;
+    m->list_zc = 0;
+    ++m->gen;
+    if (items >= (int64_t)1 << 24) return cudaSuccess;  // list entries hold the block's index in 24 bits
     count_launch(2);
     slab_tile_flags_kernel<<<(unsigned)std::min<int64_t>((tiles + 7) / 8, 152 * 32), 256, 0, s>>>(
         m->cls_grid, m->cls_pitch, m->nx, m->ny, m->nz, m->tflag);
