@@ -38,6 +38,11 @@ extern "C" {
 
 #define TAM_ABI_VERSION 2
 
+/* The library's context (opaque).  Declared here, at file scope, so that
+ * every prototype below names this one type when the header is compiled as
+ * C (a struct first named inside a parameter list would be a new type). */
+struct tam_ctx;
+
 /* ---- status codes ---- */
 enum tam_status {
     TAM_OK = 0,
